@@ -1,0 +1,352 @@
+"""Benchmark: backward-Euler Newton steps/s of stable Neo-Hookean tets on one GB300.
+
+Workload (default ``beam1m``): the 1,020,000-tet beam (100x50x34 hex x 6 tets, h = 0.02), per-cell E
+log-uniform in [1e4, 1e6] (SplitMix64 seed 3), nu = 0.45, rho = 1000, left face fixed, gravity, dt =
+1e-2.  One step = prepare_step + Newton solve to |g| <= 1e-6 |g_0| + step_next.  ``value`` is the
+mixed-precision GPU path (FP32 Hessian / assembly / PCG, FP64 energy, gradient, state, reductions);
+the plain FP64 GPU path is timed in the same run on the same steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Under torchrun every rank runs an independent replica (the path does not shard); rank 0 prints one
+JSON line with the whole-job value.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton steps/s @1M tets: mixed vs FP64 plain at 1e-6 residual; adjoint ms/step"
+
+
+def newton_params(g):
+    """Solver settings shared by the mixed and FP64 GPU paths and the CPU baseline."""
+    return g.default_params(
+        stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-2, cg_eta_min=1e-3, cg_max_iters=5000,
+        max_newton_iters=100, cg_check_every=16,
+    )
+
+
+def make_scene(name):
+    from ssim_gb300 import scenes
+
+    if name == "beam1m":
+        return scenes.beam()
+    if name == "beam_small":
+        return scenes.beam(40, 20, 14, h=0.05)
+    if name == "cube10":
+        return scenes.cube10()
+    if name == "bar":
+        return scenes.bar()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload):
+    """DRAM bytes per launch of the PCG SpMV from the committed ncu summary of this workload, if any."""
+    p = os.path.join(ROOT, "profiles", f"pcg_spmv_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.dev = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_gpu_arm(args, scene):
+    import torch
+
+    import ssim_gb300 as g
+    from ssim_gb300 import scenes
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    params = newton_params(g)
+    result = {}
+    launches0 = g.launch_count()
+
+    ts = scenes.build_timestep(scene, precision="mixed", params=params)
+    ts.set_stream(stream.cuda_stream)
+    zeros = np.zeros_like(scene["X"])
+
+    def timed_run(precision, steps, warmup, profile=False):
+        # restart from rest: same initial state for every run
+        ts.set_precision(precision)
+        ts.reset("newton")
+        for f in ("deformation", "prev_deform", "velocity"):
+            ts.set(f, zeros if scene.get("u0") is None or f == "velocity" else scene["u0"])
+        for _ in range(warmup):
+            ts.step()
+        ts.profile(profile)
+        torch.cuda.synchronize()
+        stats = []
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = g.launch_count()
+        start.record(stream)
+        for _ in range(steps):
+            ts.step()
+            stats.append(ts.stats())
+        end.record(stream)
+        torch.cuda.synchronize()
+        ms = start.elapsed_time(end)
+        launches = g.launch_count() - l0
+        prof = ts.profile_read("pcg_spmv") if profile else None
+        ts.profile(False)
+        return ts, ms, stats, launches, prof
+
+    # ---- headline: mixed precision, inputs resident
+    with ClockSampler(dev) as clk:
+        ts, ms_mixed, st_mixed, launches, _ = timed_run("mixed", args.steps, args.warmup)
+    clocks = clk.summary()
+    # ---- roofline of the dominant kernel (PCG SpMV), events around each launch, same workload
+    _, _, _, _, prof = timed_run("mixed", min(args.steps, 3), 1, profile=True)
+    # ---- plain FP64 on the same steps
+    _, ms_fp64, st_fp64, _, _ = timed_run("fp64", args.steps, args.warmup)
+    # ---- e2e through the reference-facing API: per step h2d of the Dirichlet targets (pinned), the step,
+    # d2h of the deformation (pinned)
+    from ssim_gb300.libssim import fem
+
+    fixed = np.asarray(scene["fixed"], dtype=np.int32)
+    pin_targ = torch.zeros((3, fixed.size), dtype=torch.float64).pin_memory()
+    s = fem.tet_newton_cuda(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"],
+                            precision="mixed", params=params)
+    if scene.get("E_cells") is not None:
+        s.step_.set_material(scene["E_cells"], None)
+    s.add_gravity(scene["gravity"])
+    s.reset()
+    targ_np = pin_targ.numpy()
+    for _ in range(args.warmup):
+        s.mark_dirichlet_batched(fixed, targ_np)
+        s.step()
+        _ = s.deformation()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.mark_dirichlet_batched(fixed, targ_np)
+        s.step()
+        d = s.deformation()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    result.update(
+        ms_mixed=ms_mixed, ms_fp64=ms_fp64, st_mixed=st_mixed, st_fp64=st_fp64, launches=launches, prof=prof,
+        clocks=clocks, e2e_s=e2e_s, h2d=fixed.size * 3 * 8 + fixed.size * 4, d2h=d.size * 8,
+        total_launches=g.launch_count() - launches0,
+    )
+    return result
+
+
+def cpu_baseline(scene, max_seconds):
+    """The FP64 oracle on this host's cores: Newton steps of the same workload until max_seconds."""
+    from oracle import pyoracle
+    from ssim_gb300 import scenes
+
+    import ssim_gb300 as g
+
+    gp = newton_params(g)
+    op = pyoracle.default_params(stop_mode=1, rel_tol=gp.rel_tol, cg_forcing=1, cg_rtol=gp.cg_rtol,
+                                 cg_eta_min=gp.cg_eta_min, cg_max_iters=gp.cg_max_iters,
+                                 max_newton_iters=gp.max_newton_iters)
+    ot = scenes.build_oracle(scene)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        ot.prepare_step()
+        ot.compute_step("newton", op)
+        ot.step_next()
+        steps += 1
+        if time.perf_counter() - t0 >= max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": "steps/s", "cores": pyoracle.num_threads(), "kind": "port",
+            "sample": f"{steps} backward-Euler Newton step(s) of the same workload from rest, FP64 oracle "
+                      f"(C++/OpenMP restatement), {dt:.1f} s"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="beam1m")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+
+    scene = make_scene(args.workload)
+    T, V = scene["cells"].shape[0], scene["X"].shape[0]
+
+    if args.impl == "reference":
+        if rank == 0:
+            cb = cpu_baseline(scene, args.cpu_seconds)
+            line = {
+                "metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+                "config": {"workload": scene["name"], "tets": T, "vertices": V, "solver": "Newton + Jacobi-PCG, stop 1e-6 rel"},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            }
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import torch
+
+    r = run_gpu_arm(args, scene)
+    # max over ranks of the device time
+    t_mixed = r["ms_mixed"]
+    if dist:
+        import torch.distributed as tdist
+
+        t = torch.tensor([t_mixed, r["ms_fp64"], r["e2e_s"]], dtype=torch.float64)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        t_mixed, ms_fp64, e2e_s = t.tolist()
+    else:
+        ms_fp64, e2e_s = r["ms_fp64"], r["e2e_s"]
+    steps_total = args.steps * world
+    value = steps_total / (t_mixed / 1e3)
+    fp64_value = steps_total / (ms_fp64 / 1e3)
+    peak, peak_kind = load_peaks()
+    prof = r["prof"]
+    roofline = None
+    if prof and prof["launches"] > 0:
+        avg_s = prof["total_ms"] / prof["launches"] / 1e3
+        achieved = prof["bytes_per_launch"] / avg_s / 1e9
+        traffic = ncu_traffic(args.workload)
+        roofline = {"kernel": "pcg_spmv_kernel<float> (SELL-32 3x3-block SpMV + fused p update + FP64 p.q)",
+                    "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                    "algorithmic_bytes_per_launch": prof["bytes_per_launch"], "avg_launch_us": round(avg_s * 1e6, 2),
+                    "launches_timed": prof["launches"], "traffic": traffic}
+    st = r["st_mixed"]
+    stf = r["st_fp64"]
+    if rank == 0:
+        cb = None
+        if not args.no_cpu_baseline:
+            cb = cpu_baseline(scene, args.cpu_seconds)
+        line = {
+            "metric": METRIC,
+            "value": round(value, 4),
+            "unit": "steps/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(t_mixed / args.steps, 3),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32+f64",
+            "data": "synthetic (seeded SplitMix64 material)",
+            "config": {
+                "workload": scene["name"], "tets": T, "vertices": V, "dofs": 3 * V,
+                "solver": "Newton, stop |g| <= 1e-6 |g0|, Jacobi-PCG with forcing eta = min(1e-2, max(1e-3, |g|/|g0|))",
+                "precision": "mixed: FP32 Hessian/assembly/PCG vectors, FP64 energy/gradient/state/dots",
+                "parallelism": "replicas" if world > 1 else "1 GPU",
+                "l2": "working set per step ~1 GB > L2 (no explicit flush)",
+            },
+            "fp64_plain": {"value": round(fp64_value, 4), "unit": "steps/s", "ms_per_step": round(ms_fp64 / args.steps, 3),
+                           "newton_iters": [s["newton_iters"] for s in stf], "cg_iters": [s["cg_iters_total"] for s in stf]},
+            "mixed_over_fp64": round(value / fp64_value, 3),
+            "newton_iters": [s["newton_iters"] for s in st],
+            "cg_iters": [s["cg_iters_total"] for s in st],
+            "rel_residual": [s["grad_norm"] / s["grad_norm0"] if s["grad_norm0"] > 0 else 0.0 for s in st],
+            "tets_per_s": round(T * value, 1),
+            "adjoint_ms_per_step": None,
+            "e2e": {"value": round(steps_total / e2e_s, 4), "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"]},
+            "gpu_launches": r["launches"],
+            "roofline": roofline,
+            "cpu_baseline": cb,
+            "clocks": r["clocks"],
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

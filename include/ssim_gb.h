@@ -1,0 +1,204 @@
+/*
+ * ssim_gb.h -- C ABI of the GB300-native FEM time-stepping library (libssim_gb300.so).
+ *
+ * One handle is one ssim::fem::basic_time_step<double, cuda, 3, 4, stable_neohookean, ...> object
+ * (ssim/include/ssim/finite_elements/time_step.hpp:168-715) together with the stepper chosen at
+ * reset (Newton / L-BFGS / PD, stepper/backward_euler.hpp, stepper/projective_dynamics.hpp).  Every
+ * entry point takes plain pointers and sizes; host arrays use the reference's layouts:
+ *   vertices  [V,3] float64 row-major      (bindings/src/fem_host.cpp:56 VertNb)
+ *   cells     [T,4] int32 row-major         (bindings/src/fem_host.cpp:57 CellNb, index_t == int32)
+ *   per-vertex fields (deformation, velocity, forces ...) [V,3] float64
+ *   Dirichlet targets [n,3] float64 (the memory of Eigen::Matrix3Xd, fem_host.cpp:123)
+ *   CSR matrices: row_ptr [3V+1] int32, col_idx [nnz] int32, values [nnz] float64, full storage,
+ *   columns strictly ascending per row (global_composer.hpp:68-100)
+ * All functions return an ssim_gb_status; on failure ssim_gb_last_error(h) describes the cause.
+ * A handle is not thread-safe: calls on one handle must be serialised (the reference object is
+ * single-threaded too, time_step.hpp:679).  Different handles may run concurrently on different
+ * CUDA streams.  No entry point falls back to the CPU: with no usable CUDA device they fail with
+ * SSIM_GB_ERR_CUDA.
+ */
+#ifndef SSIM_GB_H
+#define SSIM_GB_H
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SSIM_GB_API __attribute__((visibility("default")))
+#else
+#define SSIM_GB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SSIM_GB_OK = 0,
+  SSIM_GB_ERR_INVALID_ARGUMENT = 1, /* where the reference throws std::invalid_argument */
+  SSIM_GB_ERR_NOT_CONVERGED = 2,    /* only returned when strict convergence is requested */
+  SSIM_GB_ERR_CUDA = 3,             /* CUDA runtime error (message in last_error) */
+  SSIM_GB_ERR_NUMERICAL = 4,        /* NaN/Inf in energy or gradient, or an inverted element */
+  SSIM_GB_ERR_STATE = 5,            /* call out of order (e.g. compute_step before prepare_step) */
+  SSIM_GB_ERR_OUT_OF_MEMORY = 6
+} ssim_gb_status;
+
+/* Precision of the Hessian, assembly and inner PCG.  Energy, gradient, state and every reduction are
+ * FP64 in both modes. */
+typedef enum { SSIM_GB_FP64 = 0, SSIM_GB_MIXED = 1 } ssim_gb_precision;
+
+typedef enum {
+  SSIM_GB_STEPPER_NEWTON = 0, /* time_step_solver_backward_euler<cg<diagonal>> (backward_euler.hpp:9-41) */
+  SSIM_GB_STEPPER_LBFGS = 1,  /* time_step_solver_lbfgs (backward_euler.hpp:43-67) */
+  SSIM_GB_STEPPER_PD = 2,     /* time_step_solver_pd (projective_dynamics.hpp:9-97) */
+  SSIM_GB_STEPPER_NONE = 3    /* time_step_solver_nothing (time_step.hpp:131-142) */
+} ssim_gb_stepper;
+
+typedef enum {
+  SSIM_GB_DEFORMATION = 0,
+  SSIM_GB_PREV_DEFORM = 1,
+  SSIM_GB_INERTIA_DEFORM = 2,
+  SSIM_GB_NEXT_DEFORM = 3,
+  SSIM_GB_VELOCITY = 4,
+  SSIM_GB_EXT_ACCEL = 5,
+  SSIM_GB_FORCES = 6,
+  SSIM_GB_DBC_VALUES = 7
+} ssim_gb_field;
+
+typedef enum { SSIM_GB_SYSMATRIX = 0, SSIM_GB_MASS = 1, SSIM_GB_MASS_FILTERED = 2 } ssim_gb_matrix;
+
+/* Solver settings.  Defaults (ssim_gb_default_params) follow the reference where it fixes a value:
+ * max 1000 Newton iterations and Armijo 0.3 (backward_euler.hpp:21-22), stopping rule
+ * |g| < rtol * sum|M| / 3 (time_step.hpp:490-491, 660-664), Jacobi-preconditioned CG
+ * (tests/fem_cu/main.cu:52-54). */
+typedef struct {
+  int32_t max_newton_iters;
+  double armijo;
+  double ls_shrink;
+  int32_t max_ls_iters;
+  int32_t cg_max_iters;
+  double cg_rtol;      /* PCG stop |r| <= eta |b| */
+  int32_t cg_forcing;  /* 0: eta = cg_rtol; 1: eta = min(cg_rtol, max(cg_eta_min, |g_k|/|g_0|)) */
+  double cg_eta_min;
+  int32_t stop_mode;   /* 0: |g| < rtol*sum|M|/3 (reference); 1: |g| <= rel_tol*|g_0| */
+  double rel_tol;
+  int32_t precond;     /* 0 none, 1 Jacobi */
+  int32_t lbfgs_history;
+  double lbfgs_armijo;
+  int32_t max_lbfgs_iters;
+  int32_t cg_check_every; /* PCG iterations launched between host convergence checks */
+} ssim_gb_params;
+
+/* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
+typedef struct {
+  int32_t converged;
+  int32_t newton_iters;
+  int32_t cg_iters_total;
+  int32_t ls_steps_total;
+  double grad_norm;
+  double grad_norm0;
+  double energy;
+  double last_change;
+  double elapsed_ms;
+} ssim_gb_step_stats;
+
+typedef struct ssim_gb_timestep ssim_gb_timestep;
+
+/* ---- library ---- */
+SSIM_GB_API const char* ssim_gb_version(void);
+/* count of CUDA kernels this library has launched in this process */
+SSIM_GB_API uint64_t ssim_gb_launch_count(void);
+SSIM_GB_API void ssim_gb_default_params(ssim_gb_params* p);
+SSIM_GB_API const char* ssim_gb_last_error(const ssim_gb_timestep* h);
+
+/* ---- mesh utilities (host only, no GPU needed) ---- */
+/* sizes / pattern of the Hessian CSR of a tet mesh, the pattern local_global_composer::hessian builds
+ * (global_composer.hpp:68-100): row_ptr [3V+1], col_idx [nnz] */
+SSIM_GB_API ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t num_cells, int32_t num_vertices, int64_t* nnz);
+SSIM_GB_API ssim_gb_status ssim_gb_mesh_csr_pattern(const int32_t* cells, int32_t num_cells, int32_t num_vertices,
+                                        int32_t* row_ptr, int32_t* col_idx);
+
+/* ---- construction: basic_time_step(mesh, dt, E, nu, rho) (time_step.hpp:260-265),
+ *      timestep_wrapper_cuda(vert, cell, time_step, youngs, poisson, density) (fem_cuda.cu:61-71) ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_create(const double* vertices, int32_t num_vertices, const int32_t* cells,
+                              int32_t num_cells, double time_step, double youngs, double poisson,
+                              double density, ssim_gb_timestep** out);
+SSIM_GB_API ssim_gb_status ssim_gb_destroy(ssim_gb_timestep* h);
+SSIM_GB_API ssim_gb_status ssim_gb_sizes(const ssim_gb_timestep* h, int32_t* num_vertices, int32_t* num_cells,
+                             int32_t* num_dofs, int64_t* nnz);
+/* use an existing CUDA stream (cudaStream_t); NULL restores the handle's own stream */
+SSIM_GB_API ssim_gb_status ssim_gb_set_stream(ssim_gb_timestep* h, void* stream);
+
+/* ---- setters (time_step.hpp:316-347); applied at the next reset() ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_set_time_step(ssim_gb_timestep* h, double dt);
+SSIM_GB_API ssim_gb_status ssim_gb_set_youngs(ssim_gb_timestep* h, double E);
+SSIM_GB_API ssim_gb_status ssim_gb_set_poisson(ssim_gb_timestep* h, double nu);
+SSIM_GB_API ssim_gb_status ssim_gb_set_density(ssim_gb_timestep* h, double rho);
+SSIM_GB_API ssim_gb_status ssim_gb_set_damping(ssim_gb_timestep* h, double damping);
+/* set_threshold (time_step.hpp:343-347) == set_rtol (fem_cuda.cu:132) */
+SSIM_GB_API ssim_gb_status ssim_gb_set_threshold(ssim_gb_timestep* h, double rtol);
+SSIM_GB_API ssim_gb_status ssim_gb_set_precision(ssim_gb_timestep* h, int32_t precision);
+SSIM_GB_API ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p);
+SSIM_GB_API ssim_gb_status ssim_gb_get_params(const ssim_gb_timestep* h, ssim_gb_params* p);
+/* per-element Young's modulus and Poisson ratio [T] (extension: the reference's elastic model has the
+ * per-call (lambda, mu) overloads of basic_elast.hpp:74-81 but the time step only uses uniform values);
+ * NULL restores the uniform material */
+SSIM_GB_API ssim_gb_status ssim_gb_set_material(ssim_gb_timestep* h, const double* youngs_per_cell,
+                                    const double* poisson_per_cell);
+
+/* ---- boundary conditions (fem_cuda.cu:115-150, boundary.hpp:13-106) ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_mark_dirichlet_batched(ssim_gb_timestep* h, const int32_t* verts, int32_t n,
+                                              const double* targ_deform /* [n,3] */);
+SSIM_GB_API ssim_gb_status ssim_gb_mark_general_batched(ssim_gb_timestep* h, const int32_t* verts, int32_t n);
+SSIM_GB_API ssim_gb_status ssim_gb_set_dof_type(ssim_gb_timestep* h, const int8_t* dof_type /* [V,3] */);
+SSIM_GB_API ssim_gb_status ssim_gb_get_dof_type(const ssim_gb_timestep* h, int8_t* dof_type /* [V,3] */);
+/* add_ext_force_dof (time_step.hpp:550-557); add_gravity (fem_cuda.cu:134-138) */
+SSIM_GB_API ssim_gb_status ssim_gb_add_ext_force_dof(ssim_gb_timestep* h, int32_t dof, double accel);
+SSIM_GB_API ssim_gb_status ssim_gb_add_gravity(ssim_gb_timestep* h, const double gravity[3]);
+
+/* ---- loop (time_step.hpp:363-543) ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_reset(ssim_gb_timestep* h, int32_t stepper);
+SSIM_GB_API ssim_gb_status ssim_gb_prepare_step(ssim_gb_timestep* h);
+/* compute_step: runs the stepper, re-evaluates the gradient, returns |g| (time_step.hpp:520-528) */
+SSIM_GB_API ssim_gb_status ssim_gb_compute_step(ssim_gb_timestep* h, double* residual_norm);
+SSIM_GB_API ssim_gb_status ssim_gb_step_next(ssim_gb_timestep* h);
+/* prepare + compute + next with the host wall time in ms (fem_cuda.cu:92-101) */
+SSIM_GB_API ssim_gb_status ssim_gb_step(ssim_gb_timestep* h, double* elapsed_ms);
+SSIM_GB_API ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h);
+SSIM_GB_API ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st);
+SSIM_GB_API ssim_gb_status ssim_gb_check_convergence(ssim_gb_timestep* h, int32_t* converged);
+SSIM_GB_API ssim_gb_status ssim_gb_threshold_abs(const ssim_gb_timestep* h, double* abs_tol);
+
+/* ---- energy / gradient / Hessian (time_step.hpp:577-658) ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_update_energy_and_gradients(ssim_gb_timestep* h, int32_t is_deform_grad_updated,
+                                                   double* energy);
+SSIM_GB_API ssim_gb_status ssim_gb_update_hessian(ssim_gb_timestep* h, int32_t is_deform_grad_updated, int32_t make_spsd,
+                                      int32_t filter_dbc);
+/* the incremental potential at an arbitrary displacement [V,3] (value only) */
+SSIM_GB_API ssim_gb_status ssim_gb_energy_at(ssim_gb_timestep* h, const double* deform, double* energy);
+
+/* ---- state and matrices (copies; views of time_step.hpp:275-311) ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_get_field(const ssim_gb_timestep* h, int32_t field, double* out /* [V,3] */);
+SSIM_GB_API ssim_gb_status ssim_gb_set_field(ssim_gb_timestep* h, int32_t field, const double* in /* [V,3] */);
+/* device address of a field ([V,3] float64 on the handle's device) for zero-copy interop */
+SSIM_GB_API ssim_gb_status ssim_gb_field_device_ptr(ssim_gb_timestep* h, int32_t field, void** dptr);
+SSIM_GB_API ssim_gb_status ssim_gb_get_csr_pattern(const ssim_gb_timestep* h, int32_t* row_ptr, int32_t* col_idx);
+SSIM_GB_API ssim_gb_status ssim_gb_get_matrix_values(ssim_gb_timestep* h, int32_t which, double* values /* [nnz] */);
+SSIM_GB_API ssim_gb_status ssim_gb_get_rest_volume(const ssim_gb_timestep* h, double* out /* [T] */);
+SSIM_GB_API ssim_gb_status ssim_gb_get_dminv(const ssim_gb_timestep* h, double* out /* [T,3,3] */);
+/* y = A x with the current system matrix (or mass) in the handle's precision, host buffers [V,3] */
+SSIM_GB_API ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, const double* x, double* y);
+/* PCG on the current system matrix: x [V,3] in/out (initial guess zero if x_is_guess == 0) */
+SSIM_GB_API ssim_gb_status ssim_gb_pcg(ssim_gb_timestep* h, const double* b, double* x, double rtol, int32_t max_iters,
+                           int32_t* iters, double* rel_residual);
+
+/* ---- profiling (CUDA events around the PCG SpMV launches, on the handle's stream) ---- */
+SSIM_GB_API ssim_gb_status ssim_gb_profile_enable(ssim_gb_timestep* h, int32_t enable);
+/* kernel: 0 = PCG SpMV, 1 = element Hessian, 2 = assembly, 3 = gradient element, 4 = PCG update */
+SSIM_GB_API ssim_gb_status ssim_gb_profile_read(ssim_gb_timestep* h, int32_t kernel, int64_t* launches, double* total_ms,
+                                    double* bytes_per_launch);
+SSIM_GB_API ssim_gb_status ssim_gb_synchronize(ssim_gb_timestep* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

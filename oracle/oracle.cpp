@@ -524,7 +524,7 @@ void element_mass(const double* Xv[4], double rho, double M[16]) {
     for (int k = 0; k < 3; ++k) J[r * 3 + k] = Xv[k + 1][r] - Xv[0][r];
   const double detJ = std::fabs(det3(J));
   for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) M[i * 4 + j] = rho * detJ * (i == j ? 1.0 / 60 : 1.0 / 120);
+    for (int j = 0; j < 4; ++j) M[i * 4 + j] = (detJ * (i == j ? 1.0 / 60 : 1.0 / 120)) * rho;
 }
 
 void element_laplace(const double* Xv[4], double alpha, double L[16]) {

@@ -1,0 +1,141 @@
+// common.cuh -- shared device/host helpers of the GB300 FEM library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <stdexcept>
+#include <string>
+
+#include "errors.h"
+
+namespace ssim_gb {
+
+#define SSIM_CUDA(expr)                                                                             \
+  do {                                                                                              \
+    cudaError_t _e = (expr);                                                                        \
+    if (_e != cudaSuccess) {                                                                        \
+      if (_e == cudaErrorMemoryAllocation) throw std::bad_alloc();                                  \
+      throw ::ssim_gb::cuda_error(std::string(#expr) + ": " + cudaGetErrorString(_e) + " at " +     \
+                                  __FILE__ + ":" + std::to_string(__LINE__));                       \
+    }                                                                                               \
+  } while (0)
+
+// every launch site calls this right after the <<<>>> so a launch error surfaces immediately and the
+// process-wide launch counter stays exact
+extern std::atomic<uint64_t> g_launches;
+inline void after_launch(const char* what) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw cuda_error(std::string("launch of ") + what + ": " + cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------- device vectors
+template <typename T>
+struct vec4 {};
+template <>
+struct vec4<float> {
+  using type = float4;
+};
+template <>
+struct vec4<double> {
+  using type = double4_32a;  // 32-byte aligned: one 256-bit load per vertex
+};
+
+inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// scalars shared by the reductions of one handle (device memory, one block per handle)
+struct DevScalars {
+  // gradient / energy
+  double energy_elastic;  // dt^2 * sum V_e Psi_e  (+ inertia, see kernels)
+  double energy;          // total incremental potential of the last evaluation
+  double gnorm2;          // |g|^2 (Dirichlet dofs zeroed)
+  double trial_energy;    // energy at u + alpha * d
+  double gd;              // g . d
+  double dnorm2;          // |d|^2
+  // PCG
+  double rz, rz_old, pq, rr, rr0, tol2;
+  int32_t iters;
+  int32_t done;
+  int32_t status;  // 0 ok, 1 breakdown (pq <= 0), 2 non-finite residual
+  int32_t pad;
+};
+
+// Deterministic grid reduction: every block writes its partial sums, the last block to finish (found
+// with a device-scope counter, the "threadFenceReduction" pattern of the CUDA samples) adds the
+// partials in block order and calls the epilogue.  No floating-point atomics: bitwise reproducible.
+template <int NV>
+struct BlockPartials {
+  double v[NV];
+};
+
+template <int NV, int BLOCK>
+__device__ __forceinline__ void block_sum(double (&vals)[NV], double (*sh)[NV]) {
+  // warp reduce then shared reduce; result valid in thread 0
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = vals[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    vals[k] = x;
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[warp][k] = vals[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0;
+      for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][k];
+      vals[k] = s;
+    }
+  }
+}
+
+// returns true in exactly one thread (thread 0 of the last block), with tot[] = sum of all partials
+template <int NV>
+__device__ __forceinline__ bool grid_sum_last(const double (&blockval)[NV], double* partials, unsigned int* counter,
+                                              double (&tot)[NV]) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[blockIdx.x * NV + k] = blockval[k];
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  // last block: sum partials in block order (all threads help, then fixed-order combine)
+  __shared__ double sh[NV][32];
+  const int lane = threadIdx.x;
+  if (lane < 32) {
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0;
+    for (unsigned int b = lane; b < gridDim.x; b += 32) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] += ((volatile double*)partials)[b * NV + k];
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k][lane] = acc[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0;
+      for (int l = 0; l < 32; ++l) s += sh[k][l];
+      tot[k] = s;
+    }
+    *counter = 0;  // ready for the next launch on this stream
+    __threadfence();
+    return true;
+  }
+  return false;
+}
+
+}  // namespace ssim_gb

@@ -1,0 +1,262 @@
+// elem_math.cuh -- per-tet math in registers: deformation gradient, stable Neo-Hookean energy / PK1,
+// and the SPD-projected 12x12 element stiffness through the analytic eigensystem of the 9x9 Hessian.
+//
+// Conventions (identical to the reference's views): F is the row-major deformation gradient
+// F(r, c) = sum_k Ds(r, k) Dminv(k, c) (def_grad.hpp:93-132); the 9x9 Hessian index is r*3 + c of F;
+// the 12x12 stiffness index is vertex*3 + dof (compute_pfpx_3, internal_physic.hpp:107-160).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace ssim_gb {
+
+template <typename S>
+__host__ __device__ __forceinline__ S det3(const S* A) {
+  return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+         A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+
+// dJ/dF: rows of cof(F) are cross products of rows of F (partial_determinant,
+// internal_physic.hpp:41-48, applied to the transposed matrix the model receives)
+template <typename S>
+__host__ __device__ __forceinline__ void cofactor(const S* F, S* C) {
+  C[0] = F[4] * F[8] - F[5] * F[7];
+  C[1] = F[5] * F[6] - F[3] * F[8];
+  C[2] = F[3] * F[7] - F[4] * F[6];
+  C[3] = F[7] * F[2] - F[8] * F[1];
+  C[4] = F[8] * F[0] - F[6] * F[2];
+  C[5] = F[6] * F[1] - F[7] * F[0];
+  C[6] = F[1] * F[5] - F[2] * F[4];
+  C[7] = F[2] * F[3] - F[0] * F[5];
+  C[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// stable Neo-Hookean, delta = 1 (stable_neohookean.hpp:23-62, 93-104):
+//   Psi = 1/2 [mu (Ic - 3) + lambda (J - alpha)^2 - mu log(Ic + 1)] - Psi0,  alpha = 1 + 3/4 mu/lambda
+//   P   = lambda (J - alpha) cof(F) + mu (1 - 1/(Ic + 1)) F
+template <typename S>
+__host__ __device__ __forceinline__ S snh_energy(const S* F, S lam, S mu) {
+  S Ic = 0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Ic += F[i] * F[i];
+  const S alpha = S(0.75) * mu / lam + S(1);
+  const S Jm = det3(F) - alpha;
+  const S zero_energy = S(0.5) * (lam * (S(1) - alpha) * (S(1) - alpha) - mu * log(S(4)));
+  return S(0.5) * (mu * (Ic - S(3)) + lam * Jm * Jm - mu * log(Ic + S(1))) - zero_energy;
+}
+
+template <typename S>
+__host__ __device__ __forceinline__ S snh_stress(const S* F, S lam, S mu, S* P) {
+  S Ic = 0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Ic += F[i] * F[i];
+  const S alpha = S(0.75) * mu / lam + S(1);
+  const S Jm = det3(F) - alpha;
+  S C[9];
+  cofactor(F, C);
+  const S s = mu * (S(1) - S(1) / (Ic + S(1)));
+  const S lj = lam * Jm;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) P[i] = lj * C[i] + s * F[i];
+  const S zero_energy = S(0.5) * (lam * (S(1) - alpha) * (S(1) - alpha) - mu * log(S(4)));
+  return S(0.5) * (mu * (Ic - S(3)) + lam * Jm * Jm - mu * log(Ic + S(1))) - zero_energy;
+}
+
+// ------------------------------------------------------------------ symmetric 3x3 eigen (cyclic Jacobi)
+// A (row-major, symmetric) is diagonalised in place; Q accumulates the rotations (eigenvectors as
+// columns).  Rotation of Golub & Van Loan Alg. 8.5.1 / Numerical Recipes 11.1.
+template <typename S>
+__host__ __device__ __forceinline__ void jacobi_rot(S* A, S* Q, int p, int q, int r) {
+  const S apq = A[p * 3 + q];
+  if (apq == S(0)) return;
+  const S tau = (A[q * 3 + q] - A[p * 3 + p]) / (S(2) * apq);
+  const S t = (tau >= S(0) ? S(1) : S(-1)) / (fabs(tau) + sqrt(S(1) + tau * tau));
+  const S c = S(1) / sqrt(S(1) + t * t), s = t * c;
+  A[p * 3 + p] -= t * apq;
+  A[q * 3 + q] += t * apq;
+  A[p * 3 + q] = A[q * 3 + p] = S(0);
+  const S arp = A[r * 3 + p], arq = A[r * 3 + q];
+  A[r * 3 + p] = A[p * 3 + r] = c * arp - s * arq;
+  A[r * 3 + q] = A[q * 3 + r] = s * arp + c * arq;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const S qkp = Q[k * 3 + p], qkq = Q[k * 3 + q];
+    Q[k * 3 + p] = c * qkp - s * qkq;
+    Q[k * 3 + q] = s * qkp + c * qkq;
+  }
+}
+
+template <typename S>
+__host__ __device__ __forceinline__ void sym_eig3(S* A, S* Q) {
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Q[i] = (i % 4 == 0) ? S(1) : S(0);
+  const S eps = sizeof(S) == 8 ? S(1e-32) : S(1e-14);  // squared relative off-diagonal target
+  for (int sweep = 0; sweep < 12; ++sweep) {
+    const S off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+    const S dia = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
+    if (!(off > eps * dia)) break;
+    jacobi_rot(A, Q, 0, 1, 2);
+    jacobi_rot(A, Q, 0, 2, 1);
+    jacobi_rot(A, Q, 1, 2, 0);
+  }
+}
+
+// Givens rotation on rows (i, j) zeroing B(j, c); U accumulates the transposes (B = U R).
+template <typename S>
+__host__ __device__ __forceinline__ void givens_qr(S* B, S* U, int i, int j, int c) {
+  const S a = B[i * 3 + c], b = B[j * 3 + c];
+  const S r = sqrt(a * a + b * b);
+  S cs = S(1), sn = S(0);
+  if (r > S(0)) {
+    cs = a / r;
+    sn = b / r;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const S bi = B[i * 3 + k], bj = B[j * 3 + k];
+    B[i * 3 + k] = cs * bi + sn * bj;
+    B[j * 3 + k] = -sn * bi + cs * bj;
+    const S ui = U[k * 3 + i], uj = U[k * 3 + j];
+    U[k * 3 + i] = cs * ui + sn * uj;
+    U[k * 3 + j] = -sn * ui + cs * uj;
+  }
+}
+
+template <typename S>
+__host__ __device__ __forceinline__ void swap_cols_keep_det(S* V, S* d, int i, int j) {
+  const S t = d[i];
+  d[i] = d[j];
+  d[j] = t;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const S a = V[k * 3 + i];
+    V[k * 3 + i] = V[k * 3 + j];
+    V[k * 3 + j] = -a;
+  }
+}
+
+// Rotation-variant SVD F = U diag(s) V^T with U, V in SO(3), s0 >= s1 >= |s2|, s2 < 0 for inverted F.
+// V from the Jacobi eigenvectors of F^T F, U and s from a Givens QR of F V (the approach of McAdams et
+// al., "Computing the SVD of 3x3 matrices with minimal branching", 2011, written here with exact
+// Jacobi rotations).
+template <typename S>
+__host__ __device__ __forceinline__ void svd3(const S* F, S* U, S* s, S* V) {
+  S A[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) A[i * 3 + j] = F[0 * 3 + i] * F[0 * 3 + j] + F[1 * 3 + i] * F[1 * 3 + j] + F[2 * 3 + i] * F[2 * 3 + j];
+  sym_eig3(A, V);
+  S d[3] = {A[0], A[4], A[8]};
+  if (d[0] < d[1]) swap_cols_keep_det(V, d, 0, 1);
+  if (d[0] < d[2]) swap_cols_keep_det(V, d, 0, 2);
+  if (d[1] < d[2]) swap_cols_keep_det(V, d, 1, 2);
+  S B[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) B[i * 3 + j] = F[i * 3 + 0] * V[0 * 3 + j] + F[i * 3 + 1] * V[1 * 3 + j] + F[i * 3 + 2] * V[2 * 3 + j];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) U[i] = (i % 4 == 0) ? S(1) : S(0);
+  givens_qr(B, U, 0, 1, 0);
+  givens_qr(B, U, 0, 2, 0);
+  givens_qr(B, U, 1, 2, 1);
+  s[0] = B[0];
+  s[1] = B[4];
+  s[2] = B[8];
+}
+
+// packed upper-triangular index of the 12x12 stiffness
+__host__ __device__ constexpr int kup(int i, int j) { return i * 12 - (i * (i - 1)) / 2 + (j - i); }
+
+template <typename S>
+__host__ __device__ __forceinline__ void rank1(S* K, S w, const S* g) {
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const S wi = w * g[i];
+#pragma unroll
+    for (int j = i; j < 12; ++j) K[kup(i, j)] += wi * g[j];
+  }
+}
+
+// 12x12 element stiffness K = pfpx^T H+ pfpx (time_step.hpp:23-60) where H is the 9x9 SNH Hessian
+// (stable_neohookean.hpp:64-91) and H+ = sum_m max(l_m, eps) e_m e_m^T (eps = 1e-3 absolute,
+// time_step.hpp:52) when spsd, else H itself.  The eigensystem is analytic: with F = U S V^T,
+//   a = mu (1 - 1/(I2 + 1)),  b = 2 mu / (I2 + 1)^2,  c = lambda (I3 - alpha)
+// the six off-diagonal modes U (e_i e_j^T -+ e_j e_i^T) V^T / sqrt2 have eigenvalues a +- c s_k
+// (k the third index), and the three scaling modes U diag(q) V^T come from the 3x3 block
+//   A3 = a I + b s s^T + lambda g g^T + c [[0,s2,s1],[s2,0,s0],[s1,s0,0]],  g = (s1 s2, s0 s2, s0 s1)
+// (the mode structure of Smith, de Goes & Kim, "Analytic Eigensystems for Isotropic Distortion
+// Energies", 2019, derived here for this energy's I2/I3 form).  Each mode contracts with the shape
+// gradients D (4x3) into a 12-vector G(v*3+a) = (E D^T)(a, v), and K accumulates l_m G G^T.
+// Output: packed upper triangle (78 entries), times `scale`.
+template <typename S>
+__host__ __device__ __forceinline__ void element_stiffness(const S* F, const S D[4][3], S lam, S mu, bool spsd, S scale,
+                                                  S* K) {
+  S U[9], s[3], V[9];
+  svd3(F, U, s, V);
+  const S I2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+  const S I3 = s[0] * s[1] * s[2];
+  const S alpha = S(0.75) * mu / lam + S(1);
+  const S a = mu * (S(1) - S(1) / (I2 + S(1)));
+  const S b = mu * (S(2) / ((I2 + S(1)) * (I2 + S(1))));
+  const S c = lam * (I3 - alpha);
+  const S eps = S(1e-3);
+  // W = D V : W[v][j] = sum_l D[v][l] V[l][j]
+  S W[4][3];
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) W[v][j] = D[v][0] * V[0 * 3 + j] + D[v][1] * V[1 * 3 + j] + D[v][2] * V[2 * 3 + j];
+#pragma unroll
+  for (int i = 0; i < 78; ++i) K[i] = S(0);
+  // twist / flip pairs (i, j) with remaining index k
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const int i = (m == 0) ? 1 : 0;
+    const int j = (m == 2) ? 1 : 2;
+    const int k = m;
+    S lt = a + c * s[k];
+    S lf = a - c * s[k];
+    if (spsd) {
+      lt = fmax(lt, eps);
+      lf = fmax(lf, eps);
+    }
+    S gt[12], gf[12];
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const S x = U[d * 3 + i] * W[v][j];
+        const S y = U[d * 3 + j] * W[v][i];
+        gt[v * 3 + d] = x - y;
+        gf[v * 3 + d] = x + y;
+      }
+    rank1(K, S(0.5) * lt * scale, gt);
+    rank1(K, S(0.5) * lf * scale, gf);
+  }
+  // scaling block
+  S A3[9], Q[9];
+  const S g0 = s[1] * s[2], g1 = s[0] * s[2], g2 = s[0] * s[1];
+  A3[0] = a + b * s[0] * s[0] + lam * g0 * g0;
+  A3[4] = a + b * s[1] * s[1] + lam * g1 * g1;
+  A3[8] = a + b * s[2] * s[2] + lam * g2 * g2;
+  A3[1] = A3[3] = b * s[0] * s[1] + lam * g0 * g1 + c * s[2];
+  A3[2] = A3[6] = b * s[0] * s[2] + lam * g0 * g2 + c * s[1];
+  A3[5] = A3[7] = b * s[1] * s[2] + lam * g1 * g2 + c * s[0];
+  sym_eig3(A3, Q);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    S l = A3[m * 4];
+    if (spsd) l = fmax(l, eps);
+    S g[12];
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        g[v * 3 + d] = Q[0 * 3 + m] * U[d * 3 + 0] * W[v][0] + Q[1 * 3 + m] * U[d * 3 + 1] * W[v][1] +
+                       Q[2 * 3 + m] * U[d * 3 + 2] * W[v][2];
+    rank1(K, l * scale, g);
+  }
+}
+
+}  // namespace ssim_gb

@@ -1,0 +1,116 @@
+// kernels.cuh -- launchers of the device kernels (definitions in kernels_elem.cu / kernels_sparse.cu).
+//
+// HBM layout of one time-step object (T tets, V vertices, S = float (mixed) or double (FP64)):
+//   cells        int4[T]                       vertex ids of each tet
+//   element SoA  dminv[9][T], vol[T], lam[T], mu[T]   (FP64, plus an FP32 copy for the mixed path)
+//   state        [V*3] FP64 in the reference layout (deformation, next, inertia, velocity, ...)
+//   xf           float4[V]  current positions X + u rounded to FP32 (mixed-path Hessian input)
+//   matrix       3x3-block SELL-32: slice s covers block rows 32s..32s+31; slot (s, k, lane) holds block
+//                (row = 32s+lane, col = sl_col[slot]); value c of a slot q sits at
+//                vals[9*(q & ~31) + 32*c + (q & 31)] so that every component load of a warp is one
+//                128-byte (FP32) or 256-byte (FP64) line
+//   Kbuf         S[T][10][9]  scaled element stiffness blocks (v <= w) awaiting assembly
+//   lf           double[T][4][3] scaled element forces awaiting the vertex gather
+//   vectors      vec4<S>[V]  CG vectors, one padded xyz triple per vertex
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ssim_gb {
+
+template <typename S>
+using V4 = typename vec4<S>::type;
+
+struct ElemFP64 {
+  int nt;
+  const int4* cells;
+  const double* dminv;  // SoA [9][nt]
+  const double* vol;
+  const double* lam;
+  const double* mu;
+};
+
+struct ElemFP32 {
+  int nt;
+  const int4* cells;
+  const float* dminv;  // SoA [9][nt]
+  const float* vol;
+  const float* lam;
+  const float* mu;
+};
+
+struct Reduce {
+  double* partials;       // [grid * 4] scratch
+  unsigned int* counter;  // zero-initialised, restored by the last block
+  DevScalars* sc;
+};
+
+struct SellMatrix {
+  int nv;
+  int nslots;
+  const int* sl_off;    // [nslices + 1] slot offset of each slice (multiple of 32)
+  const int* sl_col;    // [nslots] block column (vertex); own row for padding
+  const int* slot_row;  // [nslots] block row, -1 for padding
+};
+
+// ---------------- element kernels (FP64 energy / gradient) ----------------
+// lf[e] = dt^2 V_e * local elastic force + element inertia force M_e (u - x_tilde); energy reduced into
+// sc->energy.  When trial, u is replaced by u + alpha * d (no forces written; energy into sc->trial_energy).
+template <typename SD>
+void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* u, const double* xt,
+                             const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
+                             bool trial, const Reduce& red, cudaStream_t st);
+// g[v] = sum over incident (e, i) of lf[e][i], Dirichlet dofs zeroed; |g|^2 into sc->gnorm2
+void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
+                          double* g, const Reduce& red, cudaStream_t st);
+
+// ---------------- element Hessian ----------------
+template <typename S>
+void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
+                         const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
+
+// ---------------- assembly / sparse ----------------
+template <typename S>
+void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
+                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, cudaStream_t st);
+template <typename S>
+void launch_spmv(const SellMatrix& A, const S* vals, const V4<S>* x, V4<S>* y, cudaStream_t st);
+template <typename S>
+void launch_export_csr(const SellMatrix& A, const int* bptr, const S* vals, double* csr_vals, cudaStream_t st);
+
+// ---------------- PCG (fused) ----------------
+template <typename S>
+void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
+                      double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st);
+template <typename S>
+void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
+                     V4<S>* q, bool first, const Reduce& red, cudaStream_t st);
+template <typename S>
+void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
+                       int max_iters, const Reduce& red, cudaStream_t st);
+
+// ---------------- vector kernels ----------------
+template <typename S>
+void launch_dot_gd(int nv, const double* g, const V4<S>* d, const Reduce& red, cudaStream_t st);
+template <typename S>
+void launch_axpy_update(int nv, double alpha, const V4<S>* d, const double* X, double* u, float4* xf,
+                        cudaStream_t st);
+void launch_refresh_xf(int nv, const double* X, const double* u, float4* xf, cudaStream_t st);
+void launch_prepare_step(int n, double dt, const double* u, const double* v, const double* a,
+                         const int8_t* dof_type, const double* dbc, double* xt, double* next, cudaStream_t st);
+void launch_step_next(int n, double dt, double damping, double* prev, double* u, const double* next, double* v,
+                      cudaStream_t st);
+void launch_restore(int n, double dt, const int8_t* dof_type, const double* dbc, double* prev, double* u,
+                    double* v, cudaStream_t st);
+void launch_add_ext(int nv, int dof, double val, double* a, cudaStream_t st);
+void launch_mark_dofs(int n, const int* verts, const double* targ, int dirichlet, int8_t* dof_type, double* dbc,
+                      cudaStream_t st);
+void launch_build_mask(int nv, const int8_t* dof_type, uint8_t* mask, cudaStream_t st);
+template <typename S>
+void launch_to_vec4(int nv, const double* in, V4<S>* out, bool negate, cudaStream_t st);
+template <typename S>
+void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st);
+
+}  // namespace ssim_gb

@@ -1,0 +1,289 @@
+// kernels_elem.cu -- element-parallel kernels: FP64 energy / gradient (update_energy_and_gradients,
+// time_step.hpp:577-624), the vertex gather of element forces (global_composer.hpp:36-66 +
+// time_step.hpp:608-617) and the element Hessian (wrapped_pfpx, time_step.hpp:23-60, 626-651).
+#include "elem_math.cuh"
+#include "kernels.cuh"
+
+namespace ssim_gb {
+
+std::atomic<uint64_t> g_launches{0};
+
+namespace {
+
+constexpr int EB = 128;  // element block (energy / gradient)
+constexpr int HB = 64;   // element block (Hessian): 64 x 90 x sizeof(S) bytes of staging
+
+template <typename S>
+__device__ __forceinline__ S comp(const V4<S>& v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : v.z);
+}
+
+// One thread per tet.  x = X + u (+ alpha d), F = Ds Dminv (def_grad.hpp:108-126), PK1 and energy
+// (stable_neohookean.hpp:38-62), local forces P Dminv^T with row 0 = -sum (time_step.hpp:62-90), scaled
+// by dt^2 V_e (the composer's weight, global_composer.hpp:233-240, times alpha = dt^2), plus the
+// element's share of the consistent-mass inertia term: with M_e(i, j) = rho V_e / 20 (1 + delta_ij)
+// (bilinears.hpp:140-148), (M_e d)_i = rho V_e / 20 (d_i + sum_j d_j) and
+// 1/2 d^T M_e d = rho V_e / 40 (sum_i |d_i|^2 + |sum_i d_i|^2).  Summed over tets this is exactly the
+// unfiltered mass matrix product of time_step.hpp:589-592.
+template <typename SD, bool FORCES, bool TRIAL>
+__global__ void __launch_bounds__(EB)
+    elem_energy_grad_kernel(ElemFP64 el, const double* __restrict__ X, const double* __restrict__ u,
+                            const double* __restrict__ xt, const V4<SD>* __restrict__ d, double alpha, double dt2,
+                            double rho, double* __restrict__ lf, Reduce red) {
+  __shared__ double stage[FORCES ? EB * 12 : 1];
+  __shared__ double shred[EB / 32][1];
+  const int e0 = blockIdx.x * EB;
+  const int e = e0 + threadIdx.x;
+  double energy = 0;
+  double lfv[12];
+  if (e < el.nt) {
+    const int4 c = el.cells[e];
+    const int vid[4] = {c.x, c.y, c.z, c.w};
+    double x[4][3], dd[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      V4<SD> dv;
+      if (TRIAL) dv = d[vid[i]];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double uk = u[vid[i] * 3 + k];
+        if (TRIAL) uk += alpha * (double)comp<SD>(dv, k);
+        x[i][k] = X[vid[i] * 3 + k] + uk;
+        dd[i][k] = uk - xt[vid[i] * 3 + k];
+      }
+    }
+    double Dm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Dm[k] = el.dminv[(size_t)k * el.nt + e];
+    double Ds[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) Ds[r * 3 + k] = x[k + 1][r] - x[0][r];
+    double F[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        F[r * 3 + cc] = Ds[r * 3 + 0] * Dm[0 * 3 + cc] + Ds[r * 3 + 1] * Dm[1 * 3 + cc] + Ds[r * 3 + 2] * Dm[2 * 3 + cc];
+    const double lam = el.lam[e], mu = el.mu[e], V = el.vol[e];
+    const double m = rho * V * (1.0 / 20.0);
+    double sd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sd[k] = dd[0][k] + dd[1][k] + dd[2][k] + dd[3][k];
+    double q = sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q += dd[i][0] * dd[i][0] + dd[i][1] * dd[i][1] + dd[i][2] * dd[i][2];
+    double psi;
+    if (FORCES) {
+      double P[9];
+      psi = snh_stress<double>(F, lam, mu, P);
+      const double s = dt2 * V;
+      double tot[3] = {0, 0, 0};
+#pragma unroll
+      for (int i = 1; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const double h = P[j * 3 + 0] * Dm[(i - 1) * 3 + 0] + P[j * 3 + 1] * Dm[(i - 1) * 3 + 1] +
+                           P[j * 3 + 2] * Dm[(i - 1) * 3 + 2];
+          tot[j] += h;
+          lfv[i * 3 + j] = s * h + m * (dd[i][j] + sd[j]);
+        }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) lfv[j] = -s * tot[j] + m * (dd[0][j] + sd[j]);
+    } else {
+      psi = snh_energy<double>(F, lam, mu);
+    }
+    energy = dt2 * V * psi + 0.5 * m * q;
+  }
+  if (FORCES) {
+    if (e < el.nt) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) stage[threadIdx.x * 12 + k] = lfv[k];
+    }
+    __syncthreads();
+    const int nvalid = min(EB, el.nt - e0);
+    double* dst = lf + (size_t)e0 * 12;
+    for (int i = threadIdx.x; i < nvalid * 12; i += EB) dst[i] = stage[i];
+  }
+  double v1[1] = {energy};
+  block_sum<1, EB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1>(v1, red.partials, red.counter, tot)) {
+    if (TRIAL)
+      red.sc->trial_energy = tot[0];
+    else
+      red.sc->energy = tot[0];
+  }
+}
+
+constexpr int GB = 256;
+
+__global__ void __launch_bounds__(GB)
+    vertex_gather_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
+                         const double* __restrict__ lf, const uint8_t* __restrict__ mask, double* __restrict__ g,
+                         Reduce red) {
+  __shared__ double shred[GB / 32][1];
+  const int v = blockIdx.x * GB + threadIdx.x;
+  double part = 0;
+  if (v < nv) {
+    double a0 = 0, a1 = 0, a2 = 0;
+    const int k1 = vptr[v + 1];
+    for (int k = vptr[v]; k < k1; ++k) {
+      const double* s = lf + (size_t)vinc[k] * 3;
+      a0 += s[0];
+      a1 += s[1];
+      a2 += s[2];
+    }
+    const uint8_t m = mask[v];  // boundary_condition::grads (boundary.hpp:45-51)
+    if (m & 1) a0 = 0;
+    if (m & 2) a1 = 0;
+    if (m & 4) a2 = 0;
+    g[v * 3 + 0] = a0;
+    g[v * 3 + 1] = a1;
+    g[v * 3 + 2] = a2;
+    part = a0 * a0 + a1 * a1 + a2 * a2;
+  }
+  double v1[1] = {part};
+  block_sum<1, GB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+}
+
+// ------------------------------------------------------------------ element Hessian
+template <typename S>
+struct ElemSel;
+template <>
+struct ElemSel<float> {
+  __device__ static const float* dminv(const ElemFP64&, const ElemFP32& b) { return b.dminv; }
+  __device__ static float vol(const ElemFP64&, const ElemFP32& b, int e) { return b.vol[e]; }
+  __device__ static float lam(const ElemFP64&, const ElemFP32& b, int e) { return b.lam[e]; }
+  __device__ static float mu(const ElemFP64&, const ElemFP32& b, int e) { return b.mu[e]; }
+};
+template <>
+struct ElemSel<double> {
+  __device__ static const double* dminv(const ElemFP64& a, const ElemFP32&) { return a.dminv; }
+  __device__ static double vol(const ElemFP64& a, const ElemFP32&, int e) { return a.vol[e]; }
+  __device__ static double lam(const ElemFP64& a, const ElemFP32&, int e) { return a.lam[e]; }
+  __device__ static double mu(const ElemFP64& a, const ElemFP32&, int e) { return a.mu[e]; }
+};
+
+// One thread per tet: K_e = dt^2 V_e pfpx^T H+ pfpx (the gather weight V_e and alpha = dt^2 of
+// time_step.hpp:646-651 folded in), written as the 10 upper 3x3 vertex blocks, staged through shared
+// memory so the global writes are contiguous.
+template <typename S, bool XF>
+__global__ void __launch_bounds__(HB)
+    elem_hessian_kernel(ElemFP64 e64, ElemFP32 e32, const double* __restrict__ X, const double* __restrict__ u,
+                        const float4* __restrict__ xf, S dt2, int spsd, S* __restrict__ Kbuf) {
+  __shared__ S stage[HB * 90];
+  const int nt = e64.nt;
+  const int e0 = blockIdx.x * HB;
+  const int e = e0 + threadIdx.x;
+  if (e < nt) {
+    const int4 c = e64.cells[e];
+    const int vid[4] = {c.x, c.y, c.z, c.w};
+    S x[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (XF) {
+        const float4 p = xf[vid[i]];
+        x[i][0] = (S)p.x;
+        x[i][1] = (S)p.y;
+        x[i][2] = (S)p.z;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) x[i][k] = (S)(X[vid[i] * 3 + k] + u[vid[i] * 3 + k]);
+      }
+    }
+    const S* dm = ElemSel<S>::dminv(e64, e32);
+    S Dm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Dm[k] = dm[(size_t)k * nt + e];
+    S F[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        F[r * 3 + cc] = (x[1][r] - x[0][r]) * Dm[0 * 3 + cc] + (x[2][r] - x[0][r]) * Dm[1 * 3 + cc] +
+                        (x[3][r] - x[0][r]) * Dm[2 * 3 + cc];
+    S D[4][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      D[1][j] = Dm[0 * 3 + j];
+      D[2][j] = Dm[1 * 3 + j];
+      D[3][j] = Dm[2 * 3 + j];
+      D[0][j] = -(Dm[0 * 3 + j] + Dm[1 * 3 + j] + Dm[2 * 3 + j]);
+    }
+    S K[78];
+    element_stiffness<S>(F, D, ElemSel<S>::lam(e64, e32, e), ElemSel<S>::mu(e64, e32, e), spsd != 0,
+                         dt2 * ElemSel<S>::vol(e64, e32, e), K);
+    S* st = stage + threadIdx.x * 90;
+    int blk = 0;
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+      for (int w = v; w < 4; ++w) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            const int i = v * 3 + a, j = w * 3 + b;
+            st[blk * 9 + a * 3 + b] = (i <= j) ? K[kup(i, j)] : K[kup(j, i)];
+          }
+        ++blk;
+      }
+  }
+  __syncthreads();
+  const int nvalid = min(HB, nt - e0);
+  S* dst = Kbuf + (size_t)e0 * 90;
+  for (int i = threadIdx.x; i < nvalid * 90; i += HB) dst[i] = stage[i];
+}
+
+}  // namespace
+
+template <typename SD>
+void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* u, const double* xt,
+                             const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
+                             bool trial, const Reduce& red, cudaStream_t st) {
+  if (el.nt <= 0) return;
+  const int grid = div_up(el.nt, EB);
+  if (trial) {
+    elem_energy_grad_kernel<SD, false, true><<<grid, EB, 0, st>>>(el, X, u, xt, d, alpha, dt2, rho, lf, red);
+  } else if (with_forces) {
+    elem_energy_grad_kernel<SD, true, false><<<grid, EB, 0, st>>>(el, X, u, xt, d, alpha, dt2, rho, lf, red);
+  } else {
+    elem_energy_grad_kernel<SD, false, false><<<grid, EB, 0, st>>>(el, X, u, xt, d, alpha, dt2, rho, lf, red);
+  }
+  after_launch("elem_energy_grad");
+}
+template void launch_elem_energy_grad<float>(const ElemFP64&, const double*, const double*, const double*,
+                                             const float4*, double, double, double, double*, bool, bool,
+                                             const Reduce&, cudaStream_t);
+template void launch_elem_energy_grad<double>(const ElemFP64&, const double*, const double*, const double*,
+                                              const double4_32a*, double, double, double, double*, bool, bool,
+                                              const Reduce&, cudaStream_t);
+
+void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
+                          double* g, const Reduce& red, cudaStream_t st) {
+  if (nv <= 0) return;
+  vertex_gather_kernel<<<div_up(nv, GB), GB, 0, st>>>(nv, vptr, vinc, lf, mask, g, red);
+  after_launch("vertex_gather");
+}
+
+template <typename S>
+void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
+                         const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st) {
+  if (e64.nt <= 0) return;
+  const int grid = div_up(e64.nt, HB);
+  if (xf != nullptr)
+    elem_hessian_kernel<S, true><<<grid, HB, 0, st>>>(e64, e32, X, u, xf, (S)dt2, spsd ? 1 : 0, Kbuf);
+  else
+    elem_hessian_kernel<S, false><<<grid, HB, 0, st>>>(e64, e32, X, u, xf, (S)dt2, spsd ? 1 : 0, Kbuf);
+  after_launch("elem_hessian");
+}
+template void launch_elem_hessian<float>(const ElemFP64&, const ElemFP32&, const double*, const double*,
+                                         const float4*, double, bool, float*, cudaStream_t);
+template void launch_elem_hessian<double>(const ElemFP64&, const ElemFP32&, const double*, const double*,
+                                          const float4*, double, bool, double*, cudaStream_t);
+
+}  // namespace ssim_gb

@@ -1,0 +1,507 @@
+// kernels_sparse.cu -- CSR/SELL assembly, SpMV, the fused Jacobi-PCG and the state-update vector kernels.
+#include "kernels.cuh"
+
+namespace ssim_gb {
+namespace {
+
+constexpr int SB = 256;  // block of the slot / row / dof kernels (a multiple of the 32-row slice)
+
+template <typename S>
+__device__ __forceinline__ V4<S> mk4(S a, S b, S c) {
+  V4<S> r;
+  r.x = a;
+  r.y = b;
+  r.z = c;
+  r.w = S(0);
+  return r;
+}
+
+__device__ __forceinline__ size_t sell_base(int q) { return (size_t)9 * (size_t)(q & ~31) + (size_t)(q & 31); }
+
+// Assembly (update_hessian, time_step.hpp:631-657): each slot (one 3x3 vertex-pair block of the CSR)
+// adds its precomputed list of element blocks (global_composer.hpp:103-119 builds the same map entry
+// by entry) to the consistent-mass block, then applies the Dirichlet identity filter
+// (boundary.hpp:53-67).  One thread per slot, no atomics: deterministic.
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    assemble_kernel(SellMatrix A, const int* __restrict__ cptr, const int* __restrict__ csrc,
+                    const S* __restrict__ Kbuf, const S* __restrict__ slot_mass, const uint8_t* __restrict__ mask,
+                    int filter, S* __restrict__ vals, V4<S>* __restrict__ dinv) {
+  const int q = blockIdx.x * SB + threadIdx.x;
+  if (q >= A.nslots) return;
+  S acc[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) acc[i] = S(0);
+  if (Kbuf != nullptr) {
+    const int c1 = cptr[q + 1];
+    for (int c = cptr[q]; c < c1; ++c) {
+      const int code = csrc[c];
+      const S* k = Kbuf + (size_t)(code & 0x7fffffff) * 9;
+      S kv[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) kv[i] = k[i];
+      if (code >= 0) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) acc[i] += kv[i];
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) acc[a * 3 + b] += kv[b * 3 + a];
+      }
+    }
+  }
+  const int u = A.slot_row[q];
+  if (u >= 0) {
+    const S m = slot_mass[q];
+    acc[0] += m;
+    acc[4] += m;
+    acc[8] += m;
+    const int w = A.sl_col[q];
+    if (filter) {
+      const int mu = mask[u], mw = mask[w];
+      if (mu | mw) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            if (((mu >> a) & 1) || ((mw >> b) & 1)) acc[a * 3 + b] = (u == w && a == b) ? S(1) : S(0);
+      }
+    }
+    if (dinv != nullptr && u == w)
+      dinv[u] = mk4<S>(acc[0] != S(0) ? S(1) / acc[0] : S(1), acc[4] != S(0) ? S(1) / acc[4] : S(1),
+                       acc[8] != S(0) ? S(1) / acc[8] : S(1));
+  }
+  const size_t base = sell_base(q);
+#pragma unroll
+  for (int c = 0; c < 9; ++c) vals[base + 32 * c] = acc[c];
+}
+
+// SELL-32 3x3-block SpMV, one thread per block row; a warp walks one slice in lockstep so every value
+// load is one contiguous line.
+template <typename S>
+__device__ __forceinline__ void row_product(const SellMatrix& A, const S* __restrict__ vals, int u, const V4<S>* x0,
+                                            const V4<S>* x1, S beta, S& a0, S& a1, S& a2) {
+  const int lane = u & 31, s = u >> 5;
+  const int base = A.sl_off[s];
+  const int W = (A.sl_off[s + 1] - base) >> 5;
+  const S* vb = vals + (size_t)9 * base + lane;
+  const int* cb = A.sl_col + base + lane;
+  a0 = a1 = a2 = S(0);
+  for (int k = 0; k < W; ++k) {
+    const int col = cb[k * 32];
+    V4<S> xv = x0[col];
+    if (x1 != nullptr) {
+      const V4<S> pv = x1[col];
+      xv.x += beta * pv.x;
+      xv.y += beta * pv.y;
+      xv.z += beta * pv.z;
+    }
+    const S* v = vb + (size_t)k * 9 * 32;
+    a0 += v[0] * xv.x + v[32] * xv.y + v[64] * xv.z;
+    a1 += v[96] * xv.x + v[128] * xv.y + v[160] * xv.z;
+    a2 += v[192] * xv.x + v[224] * xv.y + v[256] * xv.z;
+  }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    spmv_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ x, V4<S>* __restrict__ y) {
+  const int u = blockIdx.x * SB + threadIdx.x;
+  if (u >= A.nv) return;
+  S a0, a1, a2;
+  row_product<S>(A, vals, u, x, nullptr, S(0), a0, a1, a2);
+  y[u] = mk4<S>(a0, a1, a2);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    export_csr_kernel(SellMatrix A, const int* __restrict__ bptr, const S* __restrict__ vals,
+                      double* __restrict__ out) {
+  const int q = blockIdx.x * SB + threadIdx.x;
+  if (q >= A.nslots) return;
+  const int u = A.slot_row[q];
+  if (u < 0) return;
+  const int k = (q - A.sl_off[u >> 5]) >> 5;
+  const long long b0 = bptr[u];
+  const int deg = bptr[u + 1] - bptr[u];
+  const size_t base = sell_base(q);
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) out[9 * b0 + 3LL * deg * a + 3 * k + b] = (double)vals[base + 32 * (a * 3 + b)];
+}
+
+// ------------------------------------------------------------------ PCG
+// Jacobi-PCG (the mathprim cg + diagonal_preconditioner the reference's Newton uses, fem_cu/main.cu:52-54),
+// two fused kernels per iteration.  FP64 dot products, vectors in S.  The search direction is
+// double-buffered: the SpMV kernel forms p_new = z + beta p_old on the fly for every neighbour it reads,
+// so the update of p needs no kernel of its own.
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    pcg_setup_kernel(int nv, const double* __restrict__ g, const V4<S>* __restrict__ dinv, V4<S>* __restrict__ x,
+                     V4<S>* __restrict__ r, V4<S>* __restrict__ z, V4<S>* __restrict__ p0, double rtol, int max_iters,
+                     int negate, Reduce red) {
+  __shared__ double shred[SB / 32][2];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part[2] = {0, 0};
+  if (u < nv) {
+    const double sg = negate ? -1.0 : 1.0;
+    const S r0 = (S)(sg * g[u * 3 + 0]), r1 = (S)(sg * g[u * 3 + 1]), r2 = (S)(sg * g[u * 3 + 2]);
+    const V4<S> di = dinv[u];
+    const S z0 = di.x * r0, z1 = di.y * r1, z2 = di.z * r2;
+    x[u] = mk4<S>(0, 0, 0);
+    r[u] = mk4<S>(r0, r1, r2);
+    z[u] = mk4<S>(z0, z1, z2);
+    p0[u] = mk4<S>(0, 0, 0);
+    part[0] = (double)r0 * z0 + (double)r1 * z1 + (double)r2 * z2;
+    part[1] = (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
+  }
+  block_sum<2, SB>(part, shred);
+  double tot[2];
+  if (grid_sum_last<2>(part, red.partials, red.counter, tot)) {
+    DevScalars* sc = red.sc;
+    sc->rz = tot[0];
+    sc->rz_old = 1.0;
+    sc->rr = tot[1];
+    sc->rr0 = tot[1];
+    sc->tol2 = rtol * rtol * tot[1];
+    sc->iters = 0;
+    sc->status = 0;
+    sc->done = (tot[1] <= sc->tol2 || tot[1] == 0.0 || max_iters <= 0) ? 1 : 0;
+  }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    pcg_spmv_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ z,
+                    const V4<S>* __restrict__ p_old, V4<S>* __restrict__ p_new, V4<S>* __restrict__ q, int first,
+                    Reduce red) {
+  if (*(volatile int*)&red.sc->done) return;
+  __shared__ double shred[SB / 32][1];
+  const S beta = first ? S(0) : (S)(red.sc->rz / red.sc->rz_old);
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part = 0;
+  if (u < A.nv) {
+    S a0, a1, a2;
+    row_product<S>(A, vals, u, z, p_old, beta, a0, a1, a2);
+    const V4<S> zu = z[u], pu = p_old[u];
+    const V4<S> pn = mk4<S>(zu.x + beta * pu.x, zu.y + beta * pu.y, zu.z + beta * pu.z);
+    p_new[u] = pn;
+    q[u] = mk4<S>(a0, a1, a2);
+    part = (double)pn.x * a0 + (double)pn.y * a1 + (double)pn.z * a2;
+  }
+  double v1[1] = {part};
+  block_sum<1, SB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1>(v1, red.partials, red.counter, tot)) {
+    red.sc->pq = tot[0];
+    if (!(tot[0] > 0.0)) {  // breakdown: not SPD along p (or non-finite)
+      red.sc->done = 1;
+      red.sc->status = 1;
+    }
+  }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    pcg_update_kernel(int nv, const V4<S>* __restrict__ p, const V4<S>* __restrict__ q,
+                      const V4<S>* __restrict__ dinv, V4<S>* __restrict__ x, V4<S>* __restrict__ r,
+                      V4<S>* __restrict__ z, int max_iters, Reduce red) {
+  if (*(volatile int*)&red.sc->done) return;
+  __shared__ double shred[SB / 32][2];
+  const S alpha = (S)(red.sc->rz / red.sc->pq);
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part[2] = {0, 0};
+  if (u < nv) {
+    const V4<S> pu = p[u], qu = q[u], di = dinv[u];
+    V4<S> xu = x[u], ru = r[u];
+    xu.x += alpha * pu.x;
+    xu.y += alpha * pu.y;
+    xu.z += alpha * pu.z;
+    ru.x -= alpha * qu.x;
+    ru.y -= alpha * qu.y;
+    ru.z -= alpha * qu.z;
+    const V4<S> zu = mk4<S>(di.x * ru.x, di.y * ru.y, di.z * ru.z);
+    x[u] = xu;
+    r[u] = ru;
+    z[u] = zu;
+    part[0] = (double)ru.x * zu.x + (double)ru.y * zu.y + (double)ru.z * zu.z;
+    part[1] = (double)ru.x * ru.x + (double)ru.y * ru.y + (double)ru.z * ru.z;
+  }
+  block_sum<2, SB>(part, shred);
+  double tot[2];
+  if (grid_sum_last<2>(part, red.partials, red.counter, tot)) {
+    DevScalars* sc = red.sc;
+    sc->rz_old = sc->rz;
+    sc->rz = tot[0];
+    sc->rr = tot[1];
+    sc->iters += 1;
+    if (!isfinite(tot[1])) {
+      sc->done = 1;
+      sc->status = 2;
+    } else if (tot[1] <= sc->tol2 || sc->iters >= max_iters || tot[0] == 0.0) {
+      sc->done = 1;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ vectors
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    dot_gd_kernel(int nv, const double* __restrict__ g, const V4<S>* __restrict__ d, Reduce red) {
+  __shared__ double shred[SB / 32][2];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part[2] = {0, 0};
+  if (u < nv) {
+    const V4<S> dv = d[u];
+    part[0] = g[u * 3 + 0] * (double)dv.x + g[u * 3 + 1] * (double)dv.y + g[u * 3 + 2] * (double)dv.z;
+    part[1] = (double)dv.x * dv.x + (double)dv.y * dv.y + (double)dv.z * dv.z;
+  }
+  block_sum<2, SB>(part, shred);
+  double tot[2];
+  if (grid_sum_last<2>(part, red.partials, red.counter, tot)) {
+    red.sc->gd = tot[0];
+    red.sc->dnorm2 = tot[1];
+  }
+}
+
+template <typename S>
+__global__ void axpy_update_kernel(int nv, double alpha, const V4<S>* __restrict__ d, const double* __restrict__ X,
+                                   double* __restrict__ u, float4* __restrict__ xf) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v >= nv) return;
+  const V4<S> dv = d[v];
+  const double u0 = u[v * 3 + 0] + alpha * (double)dv.x;
+  const double u1 = u[v * 3 + 1] + alpha * (double)dv.y;
+  const double u2 = u[v * 3 + 2] + alpha * (double)dv.z;
+  u[v * 3 + 0] = u0;
+  u[v * 3 + 1] = u1;
+  u[v * 3 + 2] = u2;
+  if (xf != nullptr)
+    xf[v] = make_float4((float)(X[v * 3 + 0] + u0), (float)(X[v * 3 + 1] + u1), (float)(X[v * 3 + 2] + u2), 0.f);
+}
+
+__global__ void refresh_xf_kernel(int nv, const double* __restrict__ X, const double* __restrict__ u,
+                                  float4* __restrict__ xf) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v >= nv) return;
+  xf[v] = make_float4((float)(X[v * 3 + 0] + u[v * 3 + 0]), (float)(X[v * 3 + 1] + u[v * 3 + 1]),
+                      (float)(X[v * 3 + 2] + u[v * 3 + 2]), 0.f);
+}
+
+// prepare_step (time_step.hpp:499-518): x~ = u + dt v + dt^2 a, Dirichlet values, next = x~
+__global__ void prepare_step_kernel(int n, double dt, const double* __restrict__ u, const double* __restrict__ v,
+                                    const double* __restrict__ a, const int8_t* __restrict__ dof_type,
+                                    const double* __restrict__ dbc, double* __restrict__ xt,
+                                    double* __restrict__ next) {
+  const int i = blockIdx.x * SB + threadIdx.x;
+  if (i >= n) return;
+  double x = u[i] + dt * v[i];
+  x = x + (dt * dt) * a[i];
+  if (dof_type[i] == 1) x = dbc[i];
+  xt[i] = x;
+  next[i] = x;
+}
+
+// step_next (time_step.hpp:530-543)
+__global__ void step_next_kernel(int n, double inv_dt, double keep, double* __restrict__ prev,
+                                 double* __restrict__ u, const double* __restrict__ next, double* __restrict__ v) {
+  const int i = blockIdx.x * SB + threadIdx.x;
+  if (i >= n) return;
+  const double uo = u[i], un = next[i];
+  prev[i] = uo;
+  u[i] = un;
+  v[i] = ((un - uo) * inv_dt) * keep;
+}
+
+// restore (time_step.hpp:560-569)
+__global__ void restore_kernel(int n, double inv_dt, const int8_t* __restrict__ dof_type,
+                               const double* __restrict__ dbc, double* __restrict__ prev, double* __restrict__ u,
+                               double* __restrict__ v) {
+  const int i = blockIdx.x * SB + threadIdx.x;
+  if (i >= n) return;
+  if (dof_type[i] == 1) {
+    prev[i] = dbc[i];
+    u[i] = dbc[i];
+  }
+  v[i] = (u[i] - prev[i]) * inv_dt;
+}
+
+__global__ void add_ext_kernel(int nv, int dof, double val, double* __restrict__ a) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v < nv) a[v * 3 + dof] += val;
+}
+
+// mark_dirichlet_batched / mark_general_batched (fem_cuda.cu:115-150)
+__global__ void mark_dofs_kernel(int n, const int* __restrict__ verts, const double* __restrict__ targ, int dirichlet,
+                                 int8_t* __restrict__ dof_type, double* __restrict__ dbc) {
+  const int i = blockIdx.x * SB + threadIdx.x;
+  if (i >= n) return;
+  const int v = verts[i];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dof_type[v * 3 + k] = dirichlet ? 1 : 0;
+    dbc[v * 3 + k] = dirichlet ? targ[i * 3 + k] : 0.0;
+  }
+}
+
+__global__ void build_mask_kernel(int nv, const int8_t* __restrict__ dof_type, uint8_t* __restrict__ mask) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v >= nv) return;
+  mask[v] = (uint8_t)((dof_type[v * 3 + 0] == 1 ? 1 : 0) | (dof_type[v * 3 + 1] == 1 ? 2 : 0) |
+                      (dof_type[v * 3 + 2] == 1 ? 4 : 0));
+}
+
+template <typename S>
+__global__ void to_vec4_kernel(int nv, const double* __restrict__ in, V4<S>* __restrict__ out, int negate) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v >= nv) return;
+  const double s = negate ? -1.0 : 1.0;
+  out[v] = mk4<S>((S)(s * in[v * 3 + 0]), (S)(s * in[v * 3 + 1]), (S)(s * in[v * 3 + 2]));
+}
+
+template <typename S>
+__global__ void from_vec4_kernel(int nv, const V4<S>* __restrict__ in, double* __restrict__ out) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v >= nv) return;
+  const V4<S> x = in[v];
+  out[v * 3 + 0] = (double)x.x;
+  out[v * 3 + 1] = (double)x.y;
+  out[v * 3 + 2] = (double)x.z;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+template <typename S>
+void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
+                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, cudaStream_t st) {
+  if (A.nslots <= 0) return;
+  assemble_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A, cptr, csrc, Kbuf, slot_mass, mask, filter ? 1 : 0,
+                                                          vals, dinv);
+  after_launch("assemble");
+}
+
+template <typename S>
+void launch_spmv(const SellMatrix& A, const S* vals, const V4<S>* x, V4<S>* y, cudaStream_t st) {
+  if (A.nv <= 0) return;
+  spmv_kernel<S><<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, x, y);
+  after_launch("spmv");
+}
+
+template <typename S>
+void launch_export_csr(const SellMatrix& A, const int* bptr, const S* vals, double* csr_vals, cudaStream_t st) {
+  if (A.nslots <= 0) return;
+  export_csr_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A, bptr, vals, csr_vals);
+  after_launch("export_csr");
+}
+
+template <typename S>
+void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
+                      double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st) {
+  pcg_setup_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, g, dinv, x, r, z, p0, rtol, max_iters, rhs_negate ? 1 : 0,
+                                                     red);
+  after_launch("pcg_setup");
+}
+
+template <typename S>
+void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
+                     V4<S>* q, bool first, const Reduce& red, cudaStream_t st) {
+  pcg_spmv_kernel<S><<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, z, p_old, p_new, q, first ? 1 : 0, red);
+  after_launch("pcg_spmv");
+}
+
+template <typename S>
+void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
+                       int max_iters, const Reduce& red, cudaStream_t st) {
+  pcg_update_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, p, q, dinv, x, r, z, max_iters, red);
+  after_launch("pcg_update");
+}
+
+template <typename S>
+void launch_dot_gd(int nv, const double* g, const V4<S>* d, const Reduce& red, cudaStream_t st) {
+  dot_gd_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, g, d, red);
+  after_launch("dot_gd");
+}
+
+template <typename S>
+void launch_axpy_update(int nv, double alpha, const V4<S>* d, const double* X, double* u, float4* xf,
+                        cudaStream_t st) {
+  axpy_update_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, alpha, d, X, u, xf);
+  after_launch("axpy_update");
+}
+
+void launch_refresh_xf(int nv, const double* X, const double* u, float4* xf, cudaStream_t st) {
+  if (nv <= 0) return;
+  refresh_xf_kernel<<<div_up(nv, SB), SB, 0, st>>>(nv, X, u, xf);
+  after_launch("refresh_xf");
+}
+
+void launch_prepare_step(int n, double dt, const double* u, const double* v, const double* a,
+                         const int8_t* dof_type, const double* dbc, double* xt, double* next, cudaStream_t st) {
+  prepare_step_kernel<<<div_up(n, SB), SB, 0, st>>>(n, dt, u, v, a, dof_type, dbc, xt, next);
+  after_launch("prepare_step");
+}
+
+void launch_step_next(int n, double dt, double damping, double* prev, double* u, const double* next, double* v,
+                      cudaStream_t st) {
+  step_next_kernel<<<div_up(n, SB), SB, 0, st>>>(n, 1.0 / dt, 1.0 - damping, prev, u, next, v);
+  after_launch("step_next");
+}
+
+void launch_restore(int n, double dt, const int8_t* dof_type, const double* dbc, double* prev, double* u,
+                    double* v, cudaStream_t st) {
+  restore_kernel<<<div_up(n, SB), SB, 0, st>>>(n, 1.0 / dt, dof_type, dbc, prev, u, v);
+  after_launch("restore");
+}
+
+void launch_add_ext(int nv, int dof, double val, double* a, cudaStream_t st) {
+  add_ext_kernel<<<div_up(nv, SB), SB, 0, st>>>(nv, dof, val, a);
+  after_launch("add_ext");
+}
+
+void launch_mark_dofs(int n, const int* verts, const double* targ, int dirichlet, int8_t* dof_type, double* dbc,
+                      cudaStream_t st) {
+  if (n <= 0) return;
+  mark_dofs_kernel<<<div_up(n, SB), SB, 0, st>>>(n, verts, targ, dirichlet, dof_type, dbc);
+  after_launch("mark_dofs");
+}
+
+void launch_build_mask(int nv, const int8_t* dof_type, uint8_t* mask, cudaStream_t st) {
+  build_mask_kernel<<<div_up(nv, SB), SB, 0, st>>>(nv, dof_type, mask);
+  after_launch("build_mask");
+}
+
+template <typename S>
+void launch_to_vec4(int nv, const double* in, V4<S>* out, bool negate, cudaStream_t st) {
+  to_vec4_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, in, out, negate ? 1 : 0);
+  after_launch("to_vec4");
+}
+
+template <typename S>
+void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st) {
+  from_vec4_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, in, out);
+  after_launch("from_vec4");
+}
+
+#define SSIM_INST(S)                                                                                              \
+  template void launch_assemble<S>(const SellMatrix&, const int*, const int*, const S*, const S*, const uint8_t*, \
+                                   bool, S*, V4<S>*, cudaStream_t);                                               \
+  template void launch_spmv<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, cudaStream_t);                 \
+  template void launch_export_csr<S>(const SellMatrix&, const int*, const S*, double*, cudaStream_t);            \
+  template void launch_pcg_setup<S>(int, const double*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, V4<S>*, double,   \
+                                    int, bool, const Reduce&, cudaStream_t);                                      \
+  template void launch_pcg_spmv<S>(const SellMatrix&, const S*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*,     \
+                                   bool, const Reduce&, cudaStream_t);                                            \
+  template void launch_pcg_update<S>(int, const V4<S>*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, int, \
+                                     const Reduce&, cudaStream_t);                                                \
+  template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
+  template void launch_axpy_update<S>(int, double, const V4<S>*, const double*, double*, float4*, cudaStream_t); \
+  template void launch_to_vec4<S>(int, const double*, V4<S>*, bool, cudaStream_t);                               \
+  template void launch_from_vec4<S>(int, const V4<S>*, double*, cudaStream_t);
+
+SSIM_INST(float)
+SSIM_INST(double)
+
+}  // namespace ssim_gb

@@ -1,0 +1,1075 @@
+// timestep.cu -- the time-step object (ssim::fem::basic_time_step, time_step.hpp:168-715, Device = cuda)
+// with its steppers, driving the kernels of kernels_elem.cu / kernels_sparse.cu, and the C ABI of
+// include/ssim_gb.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ssim_gb.h"
+#include "kernels.cuh"
+#include "topology.h"
+
+namespace ssim_gb {
+
+// ------------------------------------------------------------------ device buffer
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    SSIM_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  void zero(cudaStream_t st) {
+    if (p) SSIM_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+  }
+  void upload(const T* h, size_t count, cudaStream_t st) {
+    alloc(count);
+    if (count) SSIM_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+  }
+  void upload(const std::vector<T>& v, cudaStream_t st) { upload(v.data(), v.size(), st); }
+};
+
+template <typename S>
+struct Solver {
+  DBuf<S> K, vals, mvals;  // element blocks, system values, mass values (SELL)
+  DBuf<S> slot_mass;
+  DBuf<V4<S>> x, r, z, p0, p1, q, dinv, tmp;
+  void release() {
+    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass}) b->release();
+    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp}) b->release();
+  }
+};
+
+enum ProfileKernel { PK_SPMV = 0, PK_HESS = 1, PK_ASM = 2, PK_GRAD = 3, PK_UPD = 4, PK_COUNT = 5 };
+
+struct TimeStep {
+  // ---- configuration (time_step.hpp:683-708)
+  int nv = 0, nt = 0, n = 0;
+  double dt = 1e-3, E = 1e6, nu = 0.33, rho = 1e3, damping = 0.0, rtol = 1e-2, abs_tol = 1e-2;
+  int precision = SSIM_GB_FP64;
+  int stepper = SSIM_GB_STEPPER_NONE;
+  ssim_gb_params params{};
+  bool has_reset = false;
+  std::vector<double> E_elem, nu_elem;
+  std::vector<double> X;
+  std::vector<int32_t> cells;
+  std::vector<double> detJ, vol_h;
+  Topology topo;
+  bool topo_ready = false;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  std::string last_error;
+  ssim_gb_step_stats stats{};
+  // ---- device: mesh, element constants
+  DBuf<double> dX;
+  DBuf<int4> dcells;
+  DBuf<double> dminv, vol, lam, mu;
+  DBuf<float> fdminv, fvol, flam, fmu;
+  // ---- device: state [n] (time_step.hpp:668-679)
+  DBuf<double> deformation, prev_deform, inertia, next, velocity, ext_accel, forces, dbc_values, work;
+  DBuf<int8_t> dof_type;
+  DBuf<uint8_t> mask;
+  DBuf<float4> xf;
+  // ---- device: topology
+  DBuf<int32_t> vptr, vinc, sl_off, sl_col, slot_row, cptr, csrc, bptr;
+  DBuf<double> lf, csr_out;
+  // ---- device: solver
+  Solver<float> sf;
+  Solver<double> sd;
+  DBuf<double> partials;
+  DBuf<unsigned int> counter;
+  DBuf<DevScalars> sc;
+  DevScalars* hsc = nullptr;  // pinned
+  // ---- profiling
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev;
+  long long prof_launch[PK_COUNT] = {0};
+  double prof_ms[PK_COUNT] = {0};
+  double prof_bytes[PK_COUNT] = {0};
+
+  ~TimeStep() {
+    for (auto e : ev) cudaEventDestroy(e);
+    if (hsc) cudaFreeHost(hsc);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+
+  bool mixed() const { return precision == SSIM_GB_MIXED; }
+  Reduce red() { return Reduce{partials.p, counter.p, sc.p}; }
+  ElemFP64 e64() const { return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p}; }
+  ElemFP32 e32() const { return ElemFP32{nt, dcells.p, fdminv.p, fvol.p, flam.p, fmu.p}; }
+  SellMatrix A() const { return SellMatrix{nv, topo.nslots, sl_off.p, sl_col.p, slot_row.p}; }
+
+  void sync_scalars() {
+    SSIM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream));
+    SSIM_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // ------------------------------------------------------------------ construction
+  void create(const double* Xh, int nv_, const int32_t* cells_h, int nt_, double dt_, double E_, double nu_,
+              double rho_) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      throw cuda_error("no CUDA device available (this library has no CPU path)");
+    }
+    if (!Xh || !cells_h) throw invalid_argument("null mesh pointer");
+    nv = nv_;
+    nt = nt_;
+    n = 3 * nv;
+    dt = dt_;
+    E = E_;
+    nu = nu_;
+    rho = rho_;
+    X.assign(Xh, Xh + (size_t)n);
+    cells.assign(cells_h, cells_h + 4 * (size_t)nt);
+    build_topology(nv, nt, cells.data(), topo);  // validates indices
+    topo_ready = true;
+    ssim_gb_default_params(&params);
+    SSIM_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+    stream = own_stream;
+    SSIM_CUDA(cudaMallocHost((void**)&hsc, sizeof(DevScalars)));
+    // state buffers (zero_if_not_valid, time_step.hpp:396-413)
+    for (DBuf<double>* b : {&deformation, &prev_deform, &inertia, &next, &velocity, &ext_accel, &forces,
+                            &dbc_values, &work}) {
+      b->alloc(n);
+      b->zero(stream);
+    }
+    dof_type.alloc(n);
+    dof_type.zero(stream);
+    mask.alloc(nv);
+    mask.zero(stream);
+    xf.alloc(nv);
+    sc.alloc(1);
+    sc.zero(stream);
+    counter.alloc(1);
+    counter.zero(stream);
+    const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(nv, topo.nslots), 256)) + 1;
+    partials.alloc(maxgrid * 4);
+    dX.upload(X, stream);
+    std::vector<int4> c4(nt);
+    std::memcpy(c4.data(), cells.data(), sizeof(int4) * nt);
+    dcells.upload(c4, stream);
+    vptr.upload(topo.vptr, stream);
+    vinc.upload(topo.vinc, stream);
+    sl_off.upload(topo.sl_off, stream);
+    sl_col.upload(topo.sl_col, stream);
+    slot_row.upload(topo.slot_row, stream);
+    cptr.upload(topo.cptr, stream);
+    csrc.upload(topo.csrc, stream);
+    bptr.upload(topo.bptr, stream);
+    lf.alloc(12 * (size_t)nt);
+    // rest shape (dminv_task def_grad.hpp:56-91, rest_vol_task rest_vol.hpp:34-54)
+    std::vector<double> dm(9 * (size_t)nt);
+    detJ.assign(nt, 0);
+    vol_h.assign(nt, 0);
+    for (int e = 0; e < nt; ++e) {
+      const double* x0 = &X[3 * (size_t)cells[4 * e + 0]];
+      double D[9];
+      for (int k = 0; k < 3; ++k) {
+        const double* xk = &X[3 * (size_t)cells[4 * e + k + 1]];
+        for (int r = 0; r < 3; ++r) D[r * 3 + k] = xk[r] - x0[r];
+      }
+      const double det = D[0] * (D[4] * D[8] - D[5] * D[7]) - D[1] * (D[3] * D[8] - D[5] * D[6]) +
+                         D[2] * (D[3] * D[7] - D[4] * D[6]);
+      const double id = 1.0 / det;
+      const double B[9] = {(D[4] * D[8] - D[5] * D[7]) * id, (D[2] * D[7] - D[1] * D[8]) * id,
+                           (D[1] * D[5] - D[2] * D[4]) * id, (D[5] * D[6] - D[3] * D[8]) * id,
+                           (D[0] * D[8] - D[2] * D[6]) * id, (D[2] * D[3] - D[0] * D[5]) * id,
+                           (D[3] * D[7] - D[4] * D[6]) * id, (D[1] * D[6] - D[0] * D[7]) * id,
+                           (D[0] * D[4] - D[1] * D[3]) * id};
+      for (int k = 0; k < 9; ++k) dm[(size_t)k * nt + e] = B[k];
+      detJ[e] = std::fabs(det);
+      vol_h[e] = std::fabs(det / 6);
+    }
+    dminv.upload(dm, stream);
+    vol.upload(vol_h, stream);
+    std::vector<float> f(dm.begin(), dm.end());
+    fdminv.upload(f, stream);
+    std::vector<float> fv(vol_h.begin(), vol_h.end());
+    fvol.upload(fv, stream);
+    reset(SSIM_GB_STEPPER_NONE);  // the constructor calls reset() (time_step.hpp:260-265)
+  }
+
+  // ------------------------------------------------------------------ reset (time_step.hpp:363-494)
+  void reset(int stepper_kind) {
+    if (!(E >= 0)) throw invalid_argument("Young's modulus must be positive, got " + std::to_string(E));
+    if (!(nu > 0 && nu < 0.5)) throw invalid_argument("Poisson's ratio must be in (0, 0.5), got " + std::to_string(nu));
+    if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
+    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NONE) throw invalid_argument("unknown stepper");
+    if (stepper_kind == SSIM_GB_STEPPER_LBFGS || stepper_kind == SSIM_GB_STEPPER_PD)
+      throw invalid_argument("this build provides the Newton stepper; L-BFGS and PD are not built yet");
+    stepper = stepper_kind;
+    for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
+    // material: per element Lame parameters (basic_elast.hpp:10-20)
+    std::vector<double> l(nt), m(nt);
+    for (int e = 0; e < nt; ++e) {
+      const double Ee = E_elem.empty() ? E : E_elem[e];
+      const double ne = nu_elem.empty() ? nu : nu_elem[e];
+      m[e] = Ee / (2 * (1 + ne));
+      l[e] = Ee * ne / ((1 + ne) * (1 - 2 * ne));
+    }
+    lam.upload(l, stream);
+    mu.upload(m, stream);
+    std::vector<float> lf32(l.begin(), l.end()), mf32(m.begin(), m.end());
+    flam.upload(lf32, stream);
+    fmu.upload(mf32, stream);
+    // consistent mass per slot (time_step.hpp:437-461) and the threshold (time_step.hpp:490-491):
+    // rtol * asum(mass CSR values) / 3; each slot's scalar appears on the 3 diagonal dofs of its block
+    std::vector<double> smass;
+    slot_masses(topo, detJ, rho, smass);
+    double asum = 0;
+    for (double v : smass) asum += 3.0 * std::fabs(v);
+    abs_tol = asum / 3.0 * rtol;
+    if (mixed()) {
+      std::vector<float> sm(smass.begin(), smass.end());
+      sf.slot_mass.upload(sm, stream);
+      alloc_solver(sf);
+      sd.release();
+    } else {
+      sd.slot_mass.upload(smass, stream);
+      alloc_solver(sd);
+      sf.release();
+    }
+    launch_build_mask(nv, dof_type.p, mask.p, stream);
+    SSIM_CUDA(cudaStreamSynchronize(stream));
+    has_reset = true;
+  }
+
+  template <typename S>
+  void alloc_solver(Solver<S>& s) {
+    s.K.alloc(90 * (size_t)nt);
+    s.vals.alloc(9 * (size_t)topo.nslots);
+    s.vals.zero(stream);
+    s.mvals.release();
+    for (DBuf<V4<S>>* b : {&s.x, &s.r, &s.z, &s.p0, &s.p1, &s.q, &s.dinv, &s.tmp}) {
+      b->alloc(nv);
+      b->zero(stream);
+    }
+  }
+
+  // ------------------------------------------------------------------ loop
+  void prepare_step() {
+    if (!(0 <= damping && damping < 1)) throw invalid_argument("velocity damping must be in [0, 1).");
+    launch_prepare_step(n, dt, deformation.p, velocity.p, ext_accel.p, dof_type.p, dbc_values.p, inertia.p,
+                        next.p, stream);
+  }
+
+  void step_next() { launch_step_next(n, dt, damping, prev_deform.p, deformation.p, next.p, velocity.p, stream); }
+
+  void restore() { launch_restore(n, dt, dof_type.p, dbc_values.p, prev_deform.p, deformation.p, velocity.p, stream); }
+
+  // energy + gradient at next (update_energy_and_gradients, time_step.hpp:577-624); synchronous
+  double energy_grad() {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (profiling) prof_begin(e0, e1);
+    if (mixed())
+      launch_elem_energy_grad<float>(e64(), dX.p, next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
+                                     red(), stream);
+    else
+      launch_elem_energy_grad<double>(e64(), dX.p, next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
+                                      red(), stream);
+    if (profiling) prof_end(e0, e1, PK_GRAD, 0);
+    launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+    sync_scalars();
+    if (!std::isfinite(hsc->energy) || !std::isfinite(hsc->gnorm2))
+      throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
+    return hsc->energy;
+  }
+
+  double energy_at(const double* u_dev) {
+    // value only: trial kernel with alpha = 0 against an arbitrary displacement
+    if (mixed()) sf.tmp.zero(stream); else sd.tmp.zero(stream);
+    if (mixed())
+      launch_elem_energy_grad<float>(e64(), dX.p, u_dev, inertia.p, sf.tmp.p, 0.0, dt * dt, rho, nullptr, false,
+                                     true, red(), stream);
+    else
+      launch_elem_energy_grad<double>(e64(), dX.p, u_dev, inertia.p, sd.tmp.p, 0.0, dt * dt, rho, nullptr, false,
+                                      true, red(), stream);
+    sync_scalars();
+    return hsc->trial_energy;
+  }
+
+  template <typename S>
+  Solver<S>& solver();
+
+  // update_hessian (time_step.hpp:626-658)
+  template <typename S>
+  void hessian(bool spsd, bool filter) {
+    Solver<S>& s = solver<S>();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (profiling) prof_begin(e0, e1);
+    launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream);
+    if (profiling) prof_end(e0, e1, PK_HESS, 0);
+    if (profiling) prof_begin(e0, e1);
+    launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p, stream);
+    if (profiling) prof_end(e0, e1, PK_ASM, 0);
+  }
+
+  void hessian_any(bool spsd, bool filter) {
+    if (mixed()) {
+      launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+      hessian<float>(spsd, filter);
+    } else {
+      hessian<double>(spsd, filter);
+    }
+  }
+
+  // Jacobi-PCG on the current system values; rhs = (negate ? -b : b) with b an FP64 [n] device vector.
+  // Result in solver().x.  Returns iterations.
+  template <typename S>
+  int pcg(const double* b, bool negate, double eta, int max_iters, double* rel_res) {
+    Solver<S>& s = solver<S>();
+    if (params.precond == 0) {
+      std::vector<V4<S>> ones(nv);
+      for (auto& o : ones) o.x = o.y = o.z = S(1), o.w = S(0);
+      SSIM_CUDA(cudaMemcpyAsync(s.dinv.p, ones.data(), sizeof(V4<S>) * nv, cudaMemcpyHostToDevice, stream));
+    }
+    launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
+    int k = 0;
+    int chunk = std::max(1, params.cg_check_every);
+    const bool prof = profiling;
+    while (true) {
+      const int k0 = k;
+      for (int c = 0; c < chunk; ++c, ++k) {
+        V4<S>* pold = (k & 1) ? s.p1.p : s.p0.p;
+        V4<S>* pnew = (k & 1) ? s.p0.p : s.p1.p;
+        if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c], stream));
+        launch_pcg_spmv<S>(A(), s.vals.p, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream);
+        if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c + 1], stream));
+        launch_pcg_update<S>(nv, pnew, s.q.p, s.dinv.p, s.x.p, s.r.p, s.z.p, max_iters, red(), stream);
+      }
+      sync_scalars();
+      if (prof) {
+        const int valid = std::min(chunk, std::max(0, hsc->iters - k0));
+        for (int c = 0; c < valid; ++c) {
+          float ms = 0;
+          SSIM_CUDA(cudaEventElapsedTime(&ms, ev[2 * c], ev[2 * c + 1]));
+          prof_ms[PK_SPMV] += ms;
+          prof_launch[PK_SPMV] += 1;
+        }
+        prof_bytes[PK_SPMV] = spmv_bytes(sizeof(S));
+      }
+      if (hsc->done || hsc->iters >= max_iters) break;
+      chunk = std::min(chunk * 2, 64);
+    }
+    if (rel_res) *rel_res = hsc->rr0 > 0 ? std::sqrt(hsc->rr / hsc->rr0) : 0.0;
+    if (hsc->status == 2) throw numerical_error("PCG produced a non-finite residual");
+    return hsc->iters;
+  }
+
+  // algorithmic bytes of one SELL SpMV: values + block columns + x gathers (one 3-vector per block
+  // row, reused from cache) + y write.  Padding slots are counted (they are read).
+  double spmv_bytes(size_t s) const {
+    const double slots = topo.nslots;
+    return slots * (9.0 * s + 4.0) + (double)(topo.nslices + 1) * 4 + 2.0 * nv * 4 * s;
+  }
+
+  // ------------------------------------------------------------------ Newton stepper
+  // time_step_solver_backward_euler::solve_impl (backward_euler.hpp:15-33) over mathprim's
+  // newton_optimizer (absent from the reference tree; the definition used is the one restated by the
+  // oracle): evaluate; stop on the gradient test; H = update_hessian(true, make_spsd = true); d from
+  // Jacobi-PCG on H d = -g; backtracking Armijo line search from alpha = 1; x += alpha d.
+  template <typename S>
+  void newton(ssim_gb_step_stats& st) {
+    Solver<S>& s = solver<S>();
+    double E0 = energy_grad();
+    double gn = std::sqrt(hsc->gnorm2);
+    const double g0 = gn;
+    st.grad_norm0 = g0;
+    int it = 0;
+    for (;; ++it) {
+      st.grad_norm = gn;
+      st.energy = E0;
+      const bool ok = params.stop_mode == 0 ? (gn < abs_tol) : (gn <= params.rel_tol * g0);
+      if (ok) {
+        st.converged = 1;
+        break;
+      }
+      if (it >= params.max_newton_iters) break;
+      if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+      hessian<S>(true, true);
+      double eta = params.cg_rtol;
+      if (params.cg_forcing == 1 && g0 > 0) eta = std::min(params.cg_rtol, std::max(params.cg_eta_min, gn / g0));
+      double rr = 0;
+      st.cg_iters_total += pcg<S>(forces.p, true, eta, params.cg_max_iters, &rr);
+      launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
+      sync_scalars();
+      double gd = hsc->gd;
+      const double dn = std::sqrt(hsc->dnorm2);
+      if (!(gd < 0)) {  // not a descent direction: steepest descent
+        launch_to_vec4<S>(nv, forces.p, s.x.p, true, stream);
+        gd = -gn * gn;
+      }
+      double alpha = 1.0;
+      for (int ls = 0; ls < params.max_ls_iters; ++ls) {
+        launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, nullptr, false, true,
+                                   red(), stream);
+        sync_scalars();
+        st.ls_steps_total++;
+        if (hsc->trial_energy <= E0 + params.armijo * alpha * gd) break;
+        alpha *= params.ls_shrink;
+      }
+      launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, mixed() ? xf.p : nullptr, stream);
+      st.last_change = alpha * dn;
+      E0 = energy_grad();
+      gn = std::sqrt(hsc->gnorm2);
+    }
+    st.newton_iters = it;
+  }
+
+  // compute_step (time_step.hpp:520-528): run the stepper, then |g| at the result
+  double compute_step() {
+    if (!has_reset) throw state_error("compute_step() before reset()");
+    ssim_gb_step_stats st{};
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    if (stepper == SSIM_GB_STEPPER_NEWTON) {
+      if (mixed())
+        newton<float>(st);
+      else
+        newton<double>(st);
+    } else {
+      // time_step_solver_nothing: no solve; the gradient is still evaluated
+      st.energy = energy_grad();
+      st.grad_norm = st.grad_norm0 = std::sqrt(hsc->gnorm2);
+    }
+    const auto t1 = std::chrono::high_resolution_clock::now();
+    st.elapsed_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    stats = st;
+    return st.grad_norm;
+  }
+
+  // ------------------------------------------------------------------ profiling
+  void prof_begin(cudaEvent_t& a, cudaEvent_t& b) {
+    SSIM_CUDA(cudaEventCreate(&a));
+    SSIM_CUDA(cudaEventCreate(&b));
+    SSIM_CUDA(cudaEventRecord(a, stream));
+  }
+  void prof_end(cudaEvent_t a, cudaEvent_t b, int kind, double bytes) {
+    SSIM_CUDA(cudaEventRecord(b, stream));
+    SSIM_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    SSIM_CUDA(cudaEventElapsedTime(&ms, a, b));
+    prof_ms[kind] += ms;
+    prof_launch[kind] += 1;
+    if (bytes > 0) prof_bytes[kind] = bytes;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+  void set_profiling(bool on) {
+    profiling = on;
+    if (on && ev.empty()) {
+      ev.resize(128);
+      for (auto& e : ev) SSIM_CUDA(cudaEventCreate(&e));
+    }
+    for (int k = 0; k < PK_COUNT; ++k) {
+      prof_launch[k] = 0;
+      prof_ms[k] = 0;
+    }
+  }
+};
+
+template <>
+Solver<float>& TimeStep::solver<float>() {
+  return sf;
+}
+template <>
+Solver<double>& TimeStep::solver<double>() {
+  return sd;
+}
+
+}  // namespace ssim_gb
+
+// ==================================================================== C ABI
+using ssim_gb::TimeStep;
+
+struct ssim_gb_timestep {
+  TimeStep ts;
+};
+
+namespace {
+thread_local std::string g_global_error;
+
+ssim_gb_status fail(ssim_gb_timestep* h, ssim_gb_status s, const std::string& msg) {
+  if (h)
+    h->ts.last_error = msg;
+  else
+    g_global_error = msg;
+  return s;
+}
+}  // namespace
+
+#define API_TRY try {
+#define API_CATCH(h)                                                                             \
+  }                                                                                              \
+  catch (const std::invalid_argument& e) {                                                       \
+    return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, e.what());                                      \
+  }                                                                                              \
+  catch (const ssim_gb::state_error& e) {                                                        \
+    return fail(h, SSIM_GB_ERR_STATE, e.what());                                                 \
+  }                                                                                              \
+  catch (const ssim_gb::numerical_error& e) {                                                    \
+    return fail(h, SSIM_GB_ERR_NUMERICAL, e.what());                                             \
+  }                                                                                              \
+  catch (const ssim_gb::cuda_error& e) {                                                         \
+    return fail(h, SSIM_GB_ERR_CUDA, e.what());                                                  \
+  }                                                                                              \
+  catch (const std::bad_alloc&) {                                                                \
+    return fail(h, SSIM_GB_ERR_OUT_OF_MEMORY, "out of memory");                                  \
+  }                                                                                              \
+  catch (const std::exception& e) {                                                              \
+    return fail(h, SSIM_GB_ERR_CUDA, e.what());                                                  \
+  }                                                                                              \
+  return SSIM_GB_OK;
+
+#define CHECK_H(h) \
+  if (!(h)) return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, "null handle");
+
+static ssim_gb::DBuf<double>* field_buf(TimeStep& t, int f) {
+  switch (f) {
+    case SSIM_GB_DEFORMATION: return &t.deformation;
+    case SSIM_GB_PREV_DEFORM: return &t.prev_deform;
+    case SSIM_GB_INERTIA_DEFORM: return &t.inertia;
+    case SSIM_GB_NEXT_DEFORM: return &t.next;
+    case SSIM_GB_VELOCITY: return &t.velocity;
+    case SSIM_GB_EXT_ACCEL: return &t.ext_accel;
+    case SSIM_GB_FORCES: return &t.forces;
+    case SSIM_GB_DBC_VALUES: return &t.dbc_values;
+  }
+  return nullptr;
+}
+
+template <typename S>
+static void export_values(TimeStep& t, int which, double* out) {
+  ssim_gb::Solver<S>& s = t.solver<S>();
+  const S* src = s.vals.p;
+  if (which == SSIM_GB_MASS || which == SSIM_GB_MASS_FILTERED) {
+    s.mvals.alloc(9 * (size_t)t.topo.nslots);
+    ssim_gb::launch_assemble<S>(t.A(), t.cptr.p, t.csrc.p, nullptr, s.slot_mass.p, t.mask.p,
+                                which == SSIM_GB_MASS_FILTERED, s.mvals.p, nullptr, t.stream);
+    src = s.mvals.p;
+  }
+  t.csr_out.alloc(9 * (size_t)t.topo.nnzb);
+  ssim_gb::launch_export_csr<S>(t.A(), t.bptr.p, src, t.csr_out.p, t.stream);
+  SSIM_CUDA(cudaMemcpyAsync(out, t.csr_out.p, sizeof(double) * 9 * t.topo.nnzb, cudaMemcpyDeviceToHost, t.stream));
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+}
+
+template <typename S>
+static void do_spmv(TimeStep& t, int which, const double* x, double* y) {
+  ssim_gb::Solver<S>& s = t.solver<S>();
+  const S* vals = s.vals.p;
+  if (which == SSIM_GB_MASS || which == SSIM_GB_MASS_FILTERED) {
+    s.mvals.alloc(9 * (size_t)t.topo.nslots);
+    ssim_gb::launch_assemble<S>(t.A(), t.cptr.p, t.csrc.p, nullptr, s.slot_mass.p, t.mask.p,
+                                which == SSIM_GB_MASS_FILTERED, s.mvals.p, nullptr, t.stream);
+    vals = s.mvals.p;
+  }
+  SSIM_CUDA(cudaMemcpyAsync(t.work.p, x, sizeof(double) * t.n, cudaMemcpyHostToDevice, t.stream));
+  ssim_gb::launch_to_vec4<S>(t.nv, t.work.p, s.tmp.p, false, t.stream);
+  ssim_gb::launch_spmv<S>(t.A(), vals, s.tmp.p, s.q.p, t.stream);
+  ssim_gb::launch_from_vec4<S>(t.nv, s.q.p, t.work.p, t.stream);
+  SSIM_CUDA(cudaMemcpyAsync(y, t.work.p, sizeof(double) * t.n, cudaMemcpyDeviceToHost, t.stream));
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+}
+
+template <typename S>
+static int do_pcg(TimeStep& t, const double* b, double* x, double rtol, int max_iters, double* rr) {
+  SSIM_CUDA(cudaMemcpyAsync(t.work.p, b, sizeof(double) * t.n, cudaMemcpyHostToDevice, t.stream));
+  const int it = t.pcg<S>(t.work.p, false, rtol, max_iters, rr);
+  ssim_gb::launch_from_vec4<S>(t.nv, t.solver<S>().x.p, t.work.p, t.stream);
+  SSIM_CUDA(cudaMemcpyAsync(x, t.work.p, sizeof(double) * t.n, cudaMemcpyDeviceToHost, t.stream));
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  return it;
+}
+
+extern "C" {
+
+const char* ssim_gb_version(void) { return "ssim_gb300 0.1.0 (sm_103a)"; }
+
+uint64_t ssim_gb_launch_count(void) { return ssim_gb::g_launches.load(); }
+
+void ssim_gb_default_params(ssim_gb_params* p) {
+  if (!p) return;
+  p->max_newton_iters = 1000;
+  p->armijo = 0.3;
+  p->ls_shrink = 0.5;
+  p->max_ls_iters = 30;
+  p->cg_max_iters = 10000;
+  p->cg_rtol = 1e-8;
+  p->cg_forcing = 0;
+  p->cg_eta_min = 1e-6;
+  p->stop_mode = 0;
+  p->rel_tol = 1e-6;
+  p->precond = 1;
+  p->lbfgs_history = 8;
+  p->lbfgs_armijo = 1e-4;
+  p->max_lbfgs_iters = 1000;
+  p->cg_check_every = 8;
+}
+
+ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
+  API_TRY
+  if (!cells || !nnz) throw ssim_gb::invalid_argument("null pointer");
+  ssim_gb::Topology t;
+  ssim_gb::build_topology(nv, nt, cells, t);
+  *nnz = 9 * t.nnzb;
+  API_CATCH(nullptr)
+}
+
+ssim_gb_status ssim_gb_mesh_csr_pattern(const int32_t* cells, int32_t nt, int32_t nv, int32_t* row_ptr,
+                                        int32_t* col_idx) {
+  API_TRY
+  if (!cells || !row_ptr || !col_idx) throw ssim_gb::invalid_argument("null pointer");
+  ssim_gb::Topology t;
+  ssim_gb::build_topology(nv, nt, cells, t);
+  ssim_gb::csr_pattern(t, row_ptr, col_idx);
+  API_CATCH(nullptr)
+}
+
+const char* ssim_gb_last_error(const ssim_gb_timestep* h) {
+  return h ? h->ts.last_error.c_str() : g_global_error.c_str();
+}
+
+ssim_gb_status ssim_gb_create(const double* vertices, int32_t num_vertices, const int32_t* cells, int32_t num_cells,
+                              double time_step, double youngs, double poisson, double density,
+                              ssim_gb_timestep** out) {
+  if (!out) return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  std::unique_ptr<ssim_gb_timestep> h(new ssim_gb_timestep());
+  try {
+    h->ts.create(vertices, num_vertices, cells, num_cells, time_step, youngs, poisson, density);
+  } catch (const std::invalid_argument& e) {
+    return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, e.what());
+  } catch (const ssim_gb::cuda_error& e) {
+    return fail(nullptr, SSIM_GB_ERR_CUDA, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(nullptr, SSIM_GB_ERR_OUT_OF_MEMORY, "out of memory");
+  } catch (const std::exception& e) {
+    return fail(nullptr, SSIM_GB_ERR_CUDA, e.what());
+  }
+  *out = h.release();
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_destroy(ssim_gb_timestep* h) {
+  if (!h) return SSIM_GB_OK;
+  if (h->ts.stream) cudaStreamSynchronize(h->ts.stream);
+  delete h;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_sizes(const ssim_gb_timestep* h, int32_t* nv, int32_t* nt, int32_t* ndofs, int64_t* nnz) {
+  CHECK_H(h);
+  if (nv) *nv = h->ts.nv;
+  if (nt) *nt = h->ts.nt;
+  if (ndofs) *ndofs = h->ts.n;
+  if (nnz) *nnz = 9 * h->ts.topo.nnzb;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_set_stream(ssim_gb_timestep* h, void* stream) {
+  CHECK_H(h);
+  API_TRY
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  h->ts.stream = stream ? (cudaStream_t)stream : h->ts.own_stream;
+  API_CATCH(h)
+}
+
+#define SETTER(name, field, cond, msg)                                       \
+  ssim_gb_status name(ssim_gb_timestep* h, double v) {                       \
+    CHECK_H(h);                                                              \
+    if (!(cond)) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, msg);          \
+    h->ts.field = v;                                                         \
+    return SSIM_GB_OK;                                                       \
+  }
+// time_step.hpp:316-347
+SETTER(ssim_gb_set_time_step, dt, v > 0, "Time step must be positive.")
+SETTER(ssim_gb_set_youngs, E, v > 0, "Young's modulus must be positive.")
+SETTER(ssim_gb_set_poisson, nu, v > 0 && v < 0.5, "Poisson's ratio must be in (0, 0.5).")
+SETTER(ssim_gb_set_density, rho, v > 0, "Density must be positive.")
+SETTER(ssim_gb_set_damping, damping, 0 <= v && v < 1, "Damping must be in [0, 1).")
+SETTER(ssim_gb_set_threshold, rtol, 0 < v && v < 1, "Threshold must be positive.")
+
+ssim_gb_status ssim_gb_set_precision(ssim_gb_timestep* h, int32_t precision) {
+  CHECK_H(h);
+  if (precision != SSIM_GB_FP64 && precision != SSIM_GB_MIXED)
+    return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "precision must be SSIM_GB_FP64 or SSIM_GB_MIXED");
+  if (precision != h->ts.precision) {
+    h->ts.precision = precision;
+    h->ts.has_reset = false;  // buffers of the other precision are allocated at reset()
+  }
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) {
+  CHECK_H(h);
+  if (!p) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null params");
+  if (p->max_newton_iters < 0 || p->cg_max_iters < 0 || p->max_ls_iters < 1 || !(p->ls_shrink > 0 && p->ls_shrink < 1) ||
+      !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
+    return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
+  h->ts.params = *p;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_get_params(const ssim_gb_timestep* h, ssim_gb_params* p) {
+  CHECK_H(h);
+  if (p) *p = h->ts.params;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_set_material(ssim_gb_timestep* h, const double* Ee, const double* ne) {
+  CHECK_H(h);
+  TimeStep& t = h->ts;
+  if (Ee) {
+    for (int e = 0; e < t.nt; ++e)
+      if (!(Ee[e] > 0)) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "Young's modulus must be positive.");
+    t.E_elem.assign(Ee, Ee + t.nt);
+  } else {
+    t.E_elem.clear();
+  }
+  if (ne) {
+    for (int e = 0; e < t.nt; ++e)
+      if (!(ne[e] > 0 && ne[e] < 0.5)) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "Poisson's ratio must be in (0, 0.5).");
+    t.nu_elem.assign(ne, ne + t.nt);
+  } else {
+    t.nu_elem.clear();
+  }
+  t.has_reset = false;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_mark_dirichlet_batched(ssim_gb_timestep* h, const int32_t* verts, int32_t n,
+                                              const double* targ) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (n < 0 || (n > 0 && (!verts || !targ))) throw ssim_gb::invalid_argument("invalid vertex list");
+  for (int i = 0; i < n; ++i)
+    if (verts[i] < 0 || verts[i] >= t.nv) throw ssim_gb::invalid_argument("vertex index out of range");
+  if (n == 0) return SSIM_GB_OK;
+  ssim_gb::DBuf<int32_t> dv;
+  ssim_gb::DBuf<double> dt_;
+  dv.upload(verts, n, t.stream);
+  dt_.upload(targ, 3 * (size_t)n, t.stream);
+  ssim_gb::launch_mark_dofs(n, dv.p, dt_.p, 1, t.dof_type.p, t.dbc_values.p, t.stream);
+  ssim_gb::launch_build_mask(t.nv, t.dof_type.p, t.mask.p, t.stream);
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_mark_general_batched(ssim_gb_timestep* h, const int32_t* verts, int32_t n) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (n < 0 || (n > 0 && !verts)) throw ssim_gb::invalid_argument("invalid vertex list");
+  for (int i = 0; i < n; ++i)
+    if (verts[i] < 0 || verts[i] >= t.nv) throw ssim_gb::invalid_argument("vertex index out of range");
+  if (n == 0) return SSIM_GB_OK;
+  ssim_gb::DBuf<int32_t> dv;
+  dv.upload(verts, n, t.stream);
+  ssim_gb::launch_mark_dofs(n, dv.p, nullptr, 0, t.dof_type.p, t.dbc_values.p, t.stream);
+  ssim_gb::launch_build_mask(t.nv, t.dof_type.p, t.mask.p, t.stream);
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_set_dof_type(ssim_gb_timestep* h, const int8_t* types) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!types) throw ssim_gb::invalid_argument("null dof types");
+  for (int i = 0; i < t.n; ++i)
+    if (types[i] != 0 && types[i] != 1) throw ssim_gb::invalid_argument("dof type must be 0 (general) or 1 (dirichlet)");
+  SSIM_CUDA(cudaMemcpyAsync(t.dof_type.p, types, t.n, cudaMemcpyHostToDevice, t.stream));
+  ssim_gb::launch_build_mask(t.nv, t.dof_type.p, t.mask.p, t.stream);
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_get_dof_type(const ssim_gb_timestep* hc, int8_t* types) {
+  ssim_gb_timestep* h = const_cast<ssim_gb_timestep*>(hc);
+  CHECK_H(h);
+  API_TRY
+  if (!types) throw ssim_gb::invalid_argument("null output");
+  SSIM_CUDA(cudaMemcpyAsync(types, h->ts.dof_type.p, h->ts.n, cudaMemcpyDeviceToHost, h->ts.stream));
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_add_ext_force_dof(ssim_gb_timestep* h, int32_t dof, double a) {
+  CHECK_H(h);
+  API_TRY
+  // time_step.hpp:550-557
+  if (!(-3 < dof && dof < 3)) throw ssim_gb::invalid_argument("|dof_idx| must be less than PhysicalDim.");
+  if (dof < 0) dof += 3;
+  ssim_gb::launch_add_ext(h->ts.nv, dof, a, h->ts.ext_accel.p, h->ts.stream);
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_add_gravity(ssim_gb_timestep* h, const double g[3]) {
+  CHECK_H(h);
+  if (!g) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null gravity");
+  for (int d = 0; d < 3; ++d) {
+    ssim_gb_status s = ssim_gb_add_ext_force_dof(h, d, g[d]);
+    if (s != SSIM_GB_OK) return s;
+  }
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_reset(ssim_gb_timestep* h, int32_t stepper) {
+  CHECK_H(h);
+  API_TRY
+  h->ts.reset(stepper);
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_prepare_step(ssim_gb_timestep* h) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!t.has_reset) {
+    // fem_cuda.cu:78-86: the wrapper resets with a warning when prepare_step comes first
+    fprintf(stderr, "Warning: prepare_step() called before reset(), bad logic.\n");
+    t.reset(t.stepper);
+  }
+  t.prepare_step();
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_compute_step(ssim_gb_timestep* h, double* residual) {
+  CHECK_H(h);
+  API_TRY
+  const double r = h->ts.compute_step();
+  if (residual) *residual = r;
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_step_next(ssim_gb_timestep* h) {
+  CHECK_H(h);
+  API_TRY
+  h->ts.step_next();
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_step(ssim_gb_timestep* h, double* elapsed_ms) {
+  CHECK_H(h);
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  ssim_gb_status s = ssim_gb_prepare_step(h);
+  if (s != SSIM_GB_OK) return s;
+  s = ssim_gb_compute_step(h, nullptr);
+  if (s != SSIM_GB_OK) return s;
+  s = ssim_gb_step_next(h);
+  if (s != SSIM_GB_OK) return s;
+  API_TRY
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  const auto t1 = std::chrono::high_resolution_clock::now();
+  if (elapsed_ms) *elapsed_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h) {
+  CHECK_H(h);
+  API_TRY
+  h->ts.restore();
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st) {
+  CHECK_H(h);
+  if (st) *st = h->ts.stats;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_check_convergence(ssim_gb_timestep* h, int32_t* converged) {
+  CHECK_H(h);
+  API_TRY
+  // time_step.hpp:660-664, on the forces of the last evaluation
+  TimeStep& t = h->ts;
+  std::vector<double> f(t.n);
+  SSIM_CUDA(cudaMemcpyAsync(f.data(), t.forces.p, sizeof(double) * t.n, cudaMemcpyDeviceToHost, t.stream));
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  double s = 0;
+  for (double v : f) s += v * v;
+  if (converged) *converged = std::sqrt(s) < t.abs_tol ? 1 : 0;
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_threshold_abs(const ssim_gb_timestep* h, double* abs_tol) {
+  CHECK_H(h);
+  if (abs_tol) *abs_tol = h->ts.abs_tol;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_update_energy_and_gradients(ssim_gb_timestep* h, int32_t, double* energy) {
+  CHECK_H(h);
+  API_TRY
+  const double E = h->ts.energy_grad();
+  if (energy) *energy = E;
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_update_hessian(ssim_gb_timestep* h, int32_t, int32_t make_spsd, int32_t filter_dbc) {
+  CHECK_H(h);
+  API_TRY
+  if (!h->ts.has_reset) throw ssim_gb::state_error("update_hessian() before reset()");
+  h->ts.hessian_any(make_spsd != 0, filter_dbc != 0);
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_energy_at(ssim_gb_timestep* h, const double* deform, double* energy) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!deform) throw ssim_gb::invalid_argument("null deformation");
+  SSIM_CUDA(cudaMemcpyAsync(t.work.p, deform, sizeof(double) * t.n, cudaMemcpyHostToDevice, t.stream));
+  const double E = t.energy_at(t.work.p);
+  if (energy) *energy = E;
+  API_CATCH(h)
+}
+
+
+ssim_gb_status ssim_gb_get_field(const ssim_gb_timestep* hc, int32_t field, double* out) {
+  ssim_gb_timestep* h = const_cast<ssim_gb_timestep*>(hc);
+  CHECK_H(h);
+  API_TRY
+  auto* b = field_buf(h->ts, field);
+  if (!b || !out) throw ssim_gb::invalid_argument("unknown field or null output");
+  SSIM_CUDA(cudaMemcpyAsync(out, b->p, sizeof(double) * h->ts.n, cudaMemcpyDeviceToHost, h->ts.stream));
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_set_field(ssim_gb_timestep* h, int32_t field, const double* in) {
+  CHECK_H(h);
+  API_TRY
+  auto* b = field_buf(h->ts, field);
+  if (!b || !in) throw ssim_gb::invalid_argument("unknown field or null input");
+  SSIM_CUDA(cudaMemcpyAsync(b->p, in, sizeof(double) * h->ts.n, cudaMemcpyHostToDevice, h->ts.stream));
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_field_device_ptr(ssim_gb_timestep* h, int32_t field, void** dptr) {
+  CHECK_H(h);
+  auto* b = field_buf(h->ts, field);
+  if (!b || !dptr) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "unknown field or null output");
+  *dptr = b->p;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_get_csr_pattern(const ssim_gb_timestep* h, int32_t* row_ptr, int32_t* col_idx) {
+  CHECK_H(h);
+  if (!row_ptr || !col_idx) return fail(const_cast<ssim_gb_timestep*>(h), SSIM_GB_ERR_INVALID_ARGUMENT, "null output");
+  ssim_gb::csr_pattern(h->ts.topo, row_ptr, col_idx);
+  return SSIM_GB_OK;
+}
+
+
+ssim_gb_status ssim_gb_get_matrix_values(ssim_gb_timestep* h, int32_t which, double* values) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!values || which < 0 || which > 2) throw ssim_gb::invalid_argument("invalid matrix or null output");
+  if (!t.has_reset) throw ssim_gb::state_error("matrix values before reset()");
+  if (t.mixed())
+    export_values<float>(t, which, values);
+  else
+    export_values<double>(t, which, values);
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_get_rest_volume(const ssim_gb_timestep* h, double* out) {
+  CHECK_H(h);
+  if (!out) return fail(const_cast<ssim_gb_timestep*>(h), SSIM_GB_ERR_INVALID_ARGUMENT, "null output");
+  std::copy(h->ts.vol_h.begin(), h->ts.vol_h.end(), out);
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_get_dminv(const ssim_gb_timestep* hc, double* out) {
+  ssim_gb_timestep* h = const_cast<ssim_gb_timestep*>(hc);
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!out) throw ssim_gb::invalid_argument("null output");
+  std::vector<double> soa(9 * (size_t)t.nt);
+  SSIM_CUDA(cudaMemcpyAsync(soa.data(), t.dminv.p, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost, t.stream));
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  for (int e = 0; e < t.nt; ++e)
+    for (int k = 0; k < 9; ++k) out[9 * (size_t)e + k] = soa[(size_t)k * t.nt + e];
+  API_CATCH(h)
+}
+
+
+ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, const double* x, double* y) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!x || !y || which < 0 || which > 2) throw ssim_gb::invalid_argument("invalid matrix or null buffer");
+  if (!t.has_reset) throw ssim_gb::state_error("spmv before reset()");
+  if (t.mixed())
+    do_spmv<float>(t, which, x, y);
+  else
+    do_spmv<double>(t, which, x, y);
+  API_CATCH(h)
+}
+
+
+ssim_gb_status ssim_gb_pcg(ssim_gb_timestep* h, const double* b, double* x, double rtol, int32_t max_iters,
+                           int32_t* iters, double* rel_residual) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!b || !x) throw ssim_gb::invalid_argument("null buffer");
+  if (!t.has_reset) throw ssim_gb::state_error("pcg before reset()");
+  double rr = 0;
+  const int it = t.mixed() ? do_pcg<float>(t, b, x, rtol, max_iters, &rr) : do_pcg<double>(t, b, x, rtol, max_iters, &rr);
+  if (iters) *iters = it;
+  if (rel_residual) *rel_residual = rr;
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_profile_enable(ssim_gb_timestep* h, int32_t enable) {
+  CHECK_H(h);
+  API_TRY
+  h->ts.set_profiling(enable != 0);
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_profile_read(ssim_gb_timestep* h, int32_t kernel, int64_t* launches, double* total_ms,
+                                    double* bytes_per_launch) {
+  CHECK_H(h);
+  if (kernel < 0 || kernel >= ssim_gb::PK_COUNT) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "unknown kernel id");
+  if (launches) *launches = h->ts.prof_launch[kernel];
+  if (total_ms) *total_ms = h->ts.prof_ms[kernel];
+  if (bytes_per_launch) *bytes_per_launch = h->ts.prof_bytes[kernel];
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_synchronize(ssim_gb_timestep* h) {
+  CHECK_H(h);
+  API_TRY
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  API_CATCH(h)
+}
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+"""Seeded synthetic workloads with the shapes, sizes and value distributions of the benchmark configs.
+
+Each scene returns a dict with the mesh, the material, the boundary and the
+time-stepping settings; ``build_timestep`` turns it into a GPU ``TimeStep`` and
+the tests feed the same dict to the oracle.  No public dataset is involved.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import mesh
+
+
+def cube10():
+    """Plain FP64 cube: [0,1]^3, 10^3 hex x 6 tets (6,000 tets, 1,331 vertices), E=1e5, nu=0.45,
+    rho=1000, top face (z=1) fixed, gravity -9.8 e_z, dt=1e-2, 10 steps, Newton + Jacobi-PCG 1e-8."""
+    X, T = mesh.kuhn_box((10, 10, 10))
+    return dict(
+        name="cube10_kuhn_6000tets",
+        X=X,
+        cells=T,
+        dt=1e-2,
+        E=1e5,
+        nu=0.45,
+        rho=1000.0,
+        fixed=np.where(X[:, 2] == 1.0)[0],
+        gravity=(0.0, 0.0, -9.8),
+        steps=10,
+        u0=None,
+        E_cells=None,
+    )
+
+
+def reference_box(nx=11):
+    """The reference's own CPU scene shape (tests/fem_time_step/main.cpp:39-67) on unit_box(nx,nx,nx):
+    x = 0 face fixed, gravity -9.8 on y, E=1e6, nu=0.4, rho=10, dt=1e-2."""
+    X, T = mesh.unit_box(nx, nx, nx)
+    return dict(
+        name=f"unit_box{nx}_5tet",
+        X=X,
+        cells=T,
+        dt=1e-2,
+        E=1e6,
+        nu=0.4,
+        rho=10.0,
+        fixed=np.where(X[:, 0] == 0.0)[0],
+        gravity=(0.0, -9.8, 0.0),
+        steps=10,
+        u0=None,
+        E_cells=None,
+    )
+
+
+def bar(nx=80, ny=20, nz=20, seed=2):
+    """Single large bar: 80x20x20 hex over [0,4]x[0,1]^2 (h=0.05) x 6 = 192,000 tets; interior vertices
+    jittered U(-0.1h, 0.1h) (SplitMix64 seed 2); E=1e6, nu=0.4, rho=1000; initial state stretched 1.5x
+    along x (u0 = 0.5 X_x e_x); left face (x=0) fixed; dt=5e-3; 20 steps; stop at 1e-6 relative residual."""
+    h = 4.0 / nx
+    X, T = mesh.kuhn_box((nx, ny, nz), (4.0, ny * h, nz * h))
+    X = mesh.jitter_interior(X, 0.1 * h, seed)
+    u0 = np.zeros_like(X)
+    u0[:, 0] = 0.5 * X[:, 0]
+    return dict(
+        name=f"bar_{nx}x{ny}x{nz}_{T.shape[0]}tets",
+        X=X,
+        cells=T,
+        dt=5e-3,
+        E=1e6,
+        nu=0.4,
+        rho=1000.0,
+        fixed=np.where(X[:, 0] == 0.0)[0],
+        gravity=(0.0, 0.0, 0.0),
+        steps=20,
+        u0=u0,
+        E_cells=None,
+    )
+
+
+def beam(nx=100, ny=50, nz=34, h=0.02, seed=3):
+    """1.02M-tet beam: 100x50x34 hex (h=0.02, [0,2]x[0,1]x[0,0.68]) x 6 tets; per-cell E log-uniform in
+    [1e4, 1e6] (SplitMix64 seed 3), nu=0.45, rho=1000; left face (x=0) fixed; gravity -9.8 e_z; dt=1e-2."""
+    X, T = mesh.kuhn_box((nx, ny, nz), (nx * h, ny * h, nz * h))
+    E_cells = 10.0 ** mesh.uniform(seed, T.shape[0], 4.0, 6.0)
+    return dict(
+        name=f"beam_{nx}x{ny}x{nz}_{T.shape[0]}tets",
+        X=X,
+        cells=T,
+        dt=1e-2,
+        E=1e5,
+        nu=0.45,
+        rho=1000.0,
+        fixed=np.where(X[:, 0] == 0.0)[0],
+        gravity=(0.0, 0.0, -9.8),
+        steps=10,
+        u0=None,
+        E_cells=E_cells,
+    )
+
+
+def build_timestep(scene, precision="fp64", stepper="newton", params=None, rtol=None):
+    """A GPU TimeStep set up for ``scene`` (material, Dirichlet face, gravity, initial state)."""
+    from .timestep import TimeStep
+
+    ts = TimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
+    ts.set_precision(precision)
+    if scene.get("E_cells") is not None:
+        ts.set_material(scene["E_cells"], None)
+    if len(scene["fixed"]):
+        ts.mark_dirichlet_batched(scene["fixed"], np.zeros((len(scene["fixed"]), 3)))
+    if any(scene["gravity"]):
+        ts.add_gravity(scene["gravity"])
+    if rtol is not None:
+        ts.set_threshold(rtol)
+    if params is not None:
+        ts.set_params(params)
+    ts.reset(stepper)
+    if scene.get("u0") is not None:
+        ts.set("deformation", scene["u0"])
+        ts.set("prev_deform", scene["u0"])
+    return ts
+
+
+def build_oracle(scene, rtol=None):
+    """The same scene on the FP64 CPU oracle (test infrastructure)."""
+    from oracle import pyoracle
+
+    ts = pyoracle.OracleTimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
+    if scene.get("E_cells") is not None:
+        ts.set_material(scene["E_cells"], None)
+    if len(scene["fixed"]):
+        ts.mark_dirichlet(scene["fixed"])
+    if any(scene["gravity"]):
+        ts.add_gravity(scene["gravity"])
+    if rtol is not None:
+        ts.set_threshold(rtol)
+    ts.reset()
+    if scene.get("u0") is not None:
+        ts.set("deformation", scene["u0"])
+        ts.set("prev_deform", scene["u0"])
+    return ts

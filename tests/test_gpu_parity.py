@@ -1,0 +1,252 @@
+"""GPU parity: the CUDA library (through the C ABI) against the FP64 oracle on identical seeded inputs.
+
+Bars: integer / index data bit-exact; plain FP64 path <= 1e-10 relative (per kernel output and on
+tightly-solved trajectories); mixed FP32/FP64 path: Newton residual <= 1e-6 relative and its state
+error against the FP64 oracle stated in the test.
+"""
+import numpy as np
+import pytest
+
+import ssim_gb300 as g
+from ssim_gb300 import mesh, scenes
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    den = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() / den
+
+
+def _pair(X, T, dt=1e-2, E=1e6, nu=0.33, rho=1e3, precision="fp64"):
+    ts = g.TimeStep(X, T, dt, E, nu, rho)
+    ts.set_precision(precision)
+    ts.reset("none")
+    from oracle import pyoracle
+
+    ot = pyoracle.OracleTimeStep(X, T, dt, E, nu, rho)
+    return ts, ot
+
+
+def _meshes():
+    X7, T7 = mesh.unit_box(7, 7, 7)
+    Xk, Tk = mesh.kuhn_box((6, 5, 4), (1.2, 1.0, 0.8))
+    Xj = mesh.jitter_interior(Xk, 0.02, 11)
+    return {"tetra": mesh.tetra(), "unit_box7": (X7, T7), "kuhn_jitter": (Xj, Tk)}
+
+
+@pytest.mark.parametrize("name", ["tetra", "unit_box7", "kuhn_jitter"])
+def test_rest_shape(name):
+    X, T = _meshes()[name]
+    ts, ot = _pair(X, T)
+    assert rel(ts.rest_volume(), ot.rest_vol()) == 0.0
+    assert rel(ts.dminv(), ot.dminv()) == 0.0
+    rp, ci = ts.csr_pattern()
+    rpo, cio = ot.csr_pattern()
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+
+
+@pytest.mark.parametrize("name", ["tetra", "unit_box7", "kuhn_jitter"])
+def test_energy_gradient(name):
+    X, T = _meshes()[name]
+    ts, ot = _pair(X, T, rho=10.0)
+    rng = np.random.default_rng(5)
+    u = rng.uniform(-1, 1, X.shape) * 0.1
+    xt = rng.uniform(-1, 1, X.shape) * 0.05
+    for t in (ts, ot):
+        t.prepare_step()
+        t.set("inertia_deform", xt)
+        t.set("next_deform", u)
+    e = ts.update_energy_and_gradients()
+    eo = ot.update_energy_and_gradients()
+    assert abs(e - eo) <= FP64_RTOL * abs(eo)
+    assert rel(ts.get("forces"), ot.get("forces")) <= FP64_RTOL
+    # value-only evaluation at another state
+    u2 = u + 0.01 * rng.normal(size=X.shape)
+    assert abs(ts.energy_at(u2) - ot.energy_at(u2)) <= FP64_RTOL * abs(ot.energy_at(u2))
+
+
+@pytest.mark.parametrize("name", ["tetra", "unit_box7", "kuhn_jitter"])
+@pytest.mark.parametrize("spsd", [False, True])
+@pytest.mark.parametrize("filt", [False, True])
+def test_hessian_values(name, spsd, filt):
+    X, T = _meshes()[name]
+    ts, ot = _pair(X, T, E=1e5, nu=0.45, rho=1000.0)
+    fixed = np.where(X[:, 0] == X[:, 0].min())[0]
+    ts.mark_dirichlet_batched(fixed, np.zeros((fixed.size, 3)))
+    ot.mark_dirichlet(fixed)
+    u = np.random.default_rng(6).uniform(-1, 1, X.shape) * 0.15
+    ts.set("next_deform", u)
+    ot.set("next_deform", u)
+    ts.update_hessian(False, spsd, filt)
+    ot.update_hessian(False, spsd, filt)
+    assert rel(ts.values("sysmatrix"), ot.values("sysmatrix")) <= FP64_RTOL
+
+
+def test_mass_matrices():
+    X, T = _meshes()["kuhn_jitter"]
+    ts, ot = _pair(X, T, rho=700.0)
+    fixed = np.arange(0, X.shape[0], 7)
+    ts.mark_dirichlet_batched(fixed, np.zeros((fixed.size, 3)))
+    ot.mark_dirichlet(fixed)
+    ot.reset()
+    assert rel(ts.values("mass"), ot.values("mass")) <= 1e-15
+    assert rel(ts.values("mass_filtered"), ot.values("mass_filtered")) <= 1e-15
+    assert abs(ts.threshold_abs - ot.threshold_abs) <= 1e-14 * ot.threshold_abs
+
+
+def test_spmv_and_pcg():
+    X, T = _meshes()["kuhn_jitter"]
+    ts, ot = _pair(X, T, E=1e5, nu=0.45, rho=1000.0)
+    u = np.random.default_rng(7).uniform(-1, 1, X.shape) * 0.05
+    for t in (ts, ot):
+        t.set("next_deform", u)
+        t.update_hessian(False, True, True)
+    x = np.random.default_rng(8).normal(size=X.shape)
+    assert rel(ts.spmv(x), ot.spmv(x).reshape(-1, 3)) <= FP64_RTOL
+    assert rel(ts.spmv(x, "mass"), ot.spmv(x, "mass").reshape(-1, 3)) <= FP64_RTOL
+    xs, it, rr = ts.pcg(x, rtol=1e-12, max_iters=5000)
+    xo, ito, rro = ot.pcg(x, rtol=1e-12, max_iters=5000)
+    assert abs(it - ito) <= 1
+    assert rr <= 1e-12 and rro <= 1e-12
+    assert rel(xs, xo.reshape(-1, 3)) <= 1e-9
+
+
+def test_mixed_kernels_close_to_fp64():
+    """FP32 Hessian / assembly against the FP64 oracle: relative error stated (<= 1e-5)."""
+    X, T = _meshes()["kuhn_jitter"]
+    ts, ot = _pair(X, T, E=1e5, nu=0.45, rho=1000.0, precision="mixed")
+    u = np.random.default_rng(9).uniform(-1, 1, X.shape) * 0.1
+    for t in (ts, ot):
+        t.set("next_deform", u)
+        t.update_hessian(False, True, True)
+    assert rel(ts.values("sysmatrix"), ot.values("sysmatrix")) <= 1e-5
+    # energy / gradient stay FP64 in the mixed path
+    for t in (ts, ot):
+        t.prepare_step()
+        t.set("next_deform", u)
+    e, eo = ts.update_energy_and_gradients(), ot.update_energy_and_gradients()
+    assert abs(e - eo) <= FP64_RTOL * abs(eo)
+    assert rel(ts.get("forces"), ot.get("forces")) <= FP64_RTOL
+
+
+def _run(scene, precision, params, oracle_params, steps, rtol=None):
+    ts = scenes.build_timestep(scene, precision=precision, params=params, rtol=rtol)
+    ot = scenes.build_oracle(scene, rtol=rtol)
+    hist = []
+    for _ in range(steps):
+        ts.prepare_step()
+        r = ts.compute_step()
+        st = ts.stats()
+        ts.step_next()
+        ot.prepare_step()
+        ro, sto = ot.compute_step("newton", oracle_params)
+        ot.step_next()
+        hist.append((r, ro, st, sto))
+    return ts, ot, hist
+
+
+def test_newton_trajectory_fp64_tight():
+    """Plain FP64 Newton on the 6,000-tet cube (top fixed, gravity) for 10 steps, solved tightly:
+    the trajectory matches the oracle to 1e-10 relative."""
+    scene = scenes.cube10()
+    params = g.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-12, cg_max_iters=20000)
+    from oracle import pyoracle
+
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-12, cg_max_iters=20000)
+    ts, ot, hist = _run(scene, "fp64", params, op, 10)
+    for r, ro, st, sto in hist:
+        assert st["converged"] == 1, st
+        assert sto["converged"] == 1, sto
+        assert abs(st["newton_iters"] - sto["newton_iters"]) <= 1
+    u, uo = ts.get("deformation"), ot.get("deformation")
+    assert rel(u, uo) <= FP64_RTOL
+    assert rel(ts.get("velocity"), ot.get("velocity")) <= 1e-8
+    assert np.all(u[scene["fixed"]] == 0.0)
+
+
+def test_newton_reference_settings_fp64():
+    """Reference settings (stop |g| < rtol*sum|M|/3 with rtol 1e-2 default, PCG 1e-8): both converge every
+    step and agree to the solver tolerance."""
+    scene = scenes.cube10()
+    from oracle import pyoracle
+
+    ts, ot, hist = _run(scene, "fp64", g.default_params(), pyoracle.default_params(), 5)
+    for r, ro, st, sto in hist:
+        assert st["converged"] == 1 and sto["converged"] == 1
+        assert r < ts.threshold_abs
+    assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-3
+
+
+def test_newton_mixed_residual():
+    """Mixed precision Newton reaches 1e-6 relative residual each step; state error vs the FP64 oracle
+    solved to the same residual is below 1e-5 relative."""
+    scene = scenes.cube10()
+    params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-2, cg_eta_min=1e-4)
+    from oracle import pyoracle
+
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12)
+    ts, ot, hist = _run(scene, "mixed", params, op, 5)
+    for r, ro, st, sto in hist:
+        assert st["converged"] == 1
+        assert st["grad_norm"] <= 1e-6 * st["grad_norm0"]
+    assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-5
+
+
+def test_determinism_bitwise():
+    scene = scenes.cube10()
+    outs = []
+    for _ in range(2):
+        ts = scenes.build_timestep(scene, precision="mixed", params=g.default_params(stop_mode=1, rel_tol=1e-6))
+        for _ in range(2):
+            ts.step()
+        outs.append(ts.get("deformation"))
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_errors_like_reference():
+    X, T = mesh.unit_box(3, 3, 3)
+    ts = g.TimeStep(X, T, 1e-2)
+    with pytest.raises(ValueError):
+        ts.set_poisson(0.5)
+    with pytest.raises(ValueError):
+        ts.set_time_step(0.0)
+    with pytest.raises(ValueError):
+        ts.set_threshold(1.0)
+    with pytest.raises(ValueError):
+        ts.add_ext_force_dof(3, 1.0)
+    with pytest.raises(ValueError):
+        ts.mark_dirichlet_batched([X.shape[0]], np.zeros((1, 3)))
+    bad = T.copy()
+    bad[0, 0] = -1
+    with pytest.raises(ValueError):
+        g.TimeStep(X, bad, 1e-2)
+    with pytest.raises(ValueError):
+        g.TimeStep(X, T, 1e-2, 1e6, 0.6)  # reset() checks the Poisson ratio (time_step.hpp:371-372)
+
+
+def test_pyssim_facade_matches_oracle():
+    from ssim_gb300.pyssim.fem import TetFiniteElementSolver_Cuda, unit_box
+
+    v, c = unit_box(6, 4, 4)
+    vert, elem = v.T.copy(), c.T.copy()
+    s = TetFiniteElementSolver_Cuda(vert, elem, 1e-2, 1e5, 0.4, 100.0, "newton")
+    s.set_rtol(1e-4)
+    fixed = np.where(vert[:, 0] == 0)[0].astype(np.int32)
+    s.mark_dirichlet_batched(fixed, np.zeros((3, fixed.size)))
+    s.add_gravity(np.array([0, 0, -9.81]))
+    s.reset()
+    for _ in range(3):
+        ms = s.step()
+        assert ms > 0
+    d = s.deformation()
+    assert d.shape == (3, vert.shape[0])
+    assert np.abs(d[:, fixed]).max() == 0.0 and d[2].min() < 0
+    s.update_hessian(True)
+    H = s.hessian()
+    assert H.shape == (3 * vert.shape[0],) * 2
+    assert abs(H - H.T).max() <= 1e-9 * abs(H).max()
+    assert s.mass_matrix().nnz == H.nnz
