@@ -33,7 +33,7 @@ def newton_params(g):
     """Solver settings shared by the mixed and FP64 GPU paths and the CPU baseline."""
     return g.default_params(
         stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-2, cg_eta_min=1e-3, cg_max_iters=5000,
-        max_newton_iters=100, cg_check_every=16,
+        max_newton_iters=100, cg_check_every=16, precond=2,
     )
 
 
@@ -169,6 +169,9 @@ def run_gpu_arm(args, scene):
     with ClockSampler(dev) as clk:
         ts, ms_mixed, st_mixed, launches, _ = timed_run("mixed", args.steps, args.warmup)
     clocks = clk.summary()
+    if args.arms == "mixed":
+        return dict(ms_mixed=ms_mixed, ms_fp64=float("nan"), st_mixed=st_mixed, st_fp64=[], launches=launches,
+                    prof=None, clocks=clocks, e2e_s=float("nan"), h2d=0, d2h=0, total_launches=0)
     # ---- roofline of the dominant kernel (PCG SpMV), events around each launch, same workload
     _, _, _, _, prof = timed_run("mixed", min(args.steps, 3), 1, profile=True)
     # ---- plain FP64 on the same steps
@@ -206,8 +209,9 @@ def run_gpu_arm(args, scene):
     return result
 
 
-def cpu_baseline(scene, max_seconds):
-    """The FP64 oracle on this host's cores: Newton steps of the same workload until max_seconds."""
+def cpu_baseline_inproc(scene, max_seconds, max_steps):
+    """The FP64 oracle on this host's cores: whole Newton steps of the same workload from rest, as many as
+    fit in ``max_seconds`` (at least one, at most ``max_steps``)."""
     from oracle import pyoracle
     from ssim_gb300 import scenes
 
@@ -216,7 +220,7 @@ def cpu_baseline(scene, max_seconds):
     gp = newton_params(g)
     op = pyoracle.default_params(stop_mode=1, rel_tol=gp.rel_tol, cg_forcing=1, cg_rtol=gp.cg_rtol,
                                  cg_eta_min=gp.cg_eta_min, cg_max_iters=gp.cg_max_iters,
-                                 max_newton_iters=gp.max_newton_iters)
+                                 max_newton_iters=gp.max_newton_iters, precond=gp.precond)
     ot = scenes.build_oracle(scene)
     t0 = time.perf_counter()
     steps = 0
@@ -225,12 +229,26 @@ def cpu_baseline(scene, max_seconds):
         ot.compute_step("newton", op)
         ot.step_next()
         steps += 1
-        if time.perf_counter() - t0 >= max_seconds:
+        if steps >= max_steps or time.perf_counter() - t0 >= max_seconds:
             break
     dt = time.perf_counter() - t0
     return {"value": steps / dt, "unit": "steps/s", "cores": pyoracle.num_threads(), "kind": "port",
             "sample": f"{steps} backward-Euler Newton step(s) of the same workload from rest, FP64 oracle "
-                      f"(C++/OpenMP restatement), {dt:.1f} s"}
+                      f"(C++/OpenMP restatement of the reference path), {dt:.1f} s, no warm-up (CPU)"}
+
+
+def cpu_baseline(workload, max_seconds, max_steps):
+    """Runs the CPU baseline in a fresh process so its OpenMP pool does not share the process with torch."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
+           "--cpu-seconds", str(max_seconds), "--steps", str(max_steps), "--warmup", "0"]
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    for line in r.stdout.splitlines()[::-1]:
+        if line.startswith("{"):
+            return json.loads(line)["cpu_baseline"]
+    return {"value": None, "unavailable": (r.stderr or "no output")[-300:]}
 
 
 def main():
@@ -240,8 +258,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam1m")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -259,12 +278,12 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            cb = cpu_baseline(scene, args.cpu_seconds)
+            cb = cpu_baseline_inproc(scene, args.cpu_seconds, max(1, args.steps))
             line = {
                 "metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-                "config": {"workload": scene["name"], "tets": T, "vertices": V, "solver": "Newton + Jacobi-PCG, stop 1e-6 rel"},
+                "config": {"workload": scene["name"], "tets": T, "vertices": V, "solver": "Newton + block-Jacobi PCG, stop 1e-6 rel"},
                 "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             }
@@ -306,7 +325,7 @@ def main():
     if rank == 0:
         cb = None
         if not args.no_cpu_baseline:
-            cb = cpu_baseline(scene, args.cpu_seconds)
+            cb = cpu_baseline(args.workload, args.cpu_seconds, args.steps)
         line = {
             "metric": METRIC,
             "value": round(value, 4),
@@ -322,7 +341,7 @@ def main():
             "data": "synthetic (seeded SplitMix64 material)",
             "config": {
                 "workload": scene["name"], "tets": T, "vertices": V, "dofs": 3 * V,
-                "solver": "Newton, stop |g| <= 1e-6 |g0|, Jacobi-PCG with forcing eta = min(1e-2, max(1e-3, |g|/|g0|))",
+                "solver": "Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-2, max(1e-3, |g|/|g0|))",
                 "precision": "mixed: FP32 Hessian/assembly/PCG vectors, FP64 energy/gradient/state/dots",
                 "parallelism": "replicas" if world > 1 else "1 GPU",
                 "l2": "working set per step ~1 GB > L2 (no explicit flush)",

@@ -81,11 +81,13 @@ typedef struct {
   double cg_eta_min;
   int32_t stop_mode;   /* 0: |g| < rtol*sum|M|/3 (reference); 1: |g| <= rel_tol*|g_0| */
   double rel_tol;
-  int32_t precond;     /* 0 none, 1 Jacobi */
+  int32_t precond;     /* 0 none, 1 Jacobi (the reference's diagonal preconditioner), 2 block-Jacobi (3x3) */
   int32_t lbfgs_history;
   double lbfgs_armijo;
   int32_t max_lbfgs_iters;
   int32_t cg_check_every; /* PCG iterations launched between host convergence checks */
+  double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack |E| (round-off floor of E) */
+  int32_t pd_kappa_mode;  /* PD matrix diffusivity: 0 as ssim builds it (time_step.hpp:356), 1 from Lame */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

@@ -471,15 +471,44 @@ void update_hessian(orc_ts& s, bool F_updated, bool make_spsd, bool filter) {
 int pcg(const orc_ts& s, const Vec& vals, const double* b, double* x, double rtol, int max_iters, int precond,
         double* rel_res) {
   const int n = s.n;
-  Vec r(n), z(n), p(n), q(n), dinv(n, 1.0);
-  if (precond) {
-    for (int i = 0; i < n; ++i) {
-      double d = 0;
-      for (int k = s.row_ptr[i]; k < s.row_ptr[i + 1]; ++k)
-        if (s.col_idx[k] == i) d = vals[k];
-      dinv[i] = d != 0.0 ? 1.0 / d : 1.0;
+  Vec r(n), z(n), p(n), q(n);
+  // preconditioner as one 3x3 block per vertex: 0 identity, 1 Jacobi (diagonal), 2 block-Jacobi
+  Vec P(9 * (size_t)s.nv, 0.0);
+  for (int u = 0; u < s.nv; ++u) {
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int k = s.row_ptr[3 * u + i]; k < s.row_ptr[3 * u + i + 1]; ++k) {
+        const int c = s.col_idx[k];
+        if (c >= 3 * u && c < 3 * u + 3) a[i * 3 + (c - 3 * u)] = vals[k];
+      }
+    double* m = &P[9 * (size_t)u];
+    int mode = precond;
+    if (mode == 2) {
+      const double det = det3(a);
+      if (det > 0 && std::isfinite(det)) {
+        inv3(a, m);
+        const double m01 = 0.5 * (m[1] + m[3]), m02 = 0.5 * (m[2] + m[6]), m12 = 0.5 * (m[5] + m[7]);
+        m[1] = m[3] = m01;
+        m[2] = m[6] = m02;
+        m[5] = m[7] = m12;
+      } else {
+        mode = 1;
+      }
+    }
+    if (mode == 1) {
+      for (int i = 0; i < 3; ++i) m[i * 4] = a[i * 4] != 0.0 ? 1.0 / a[i * 4] : 1.0;
+    } else if (mode == 0) {
+      for (int i = 0; i < 3; ++i) m[i * 4] = 1.0;
     }
   }
+  auto apply = [&](const Vec& in, Vec& out) {
+#pragma omp parallel for schedule(static)
+    for (int u = 0; u < s.nv; ++u) {
+      const double* m = &P[9 * (size_t)u];
+      for (int i = 0; i < 3; ++i)
+        out[3 * u + i] = m[i * 3] * in[3 * u] + m[i * 3 + 1] * in[3 * u + 1] + m[i * 3 + 2] * in[3 * u + 2];
+    }
+  };
   spmv(s, vals, x, q.data());
   for (int i = 0; i < n; ++i) r[i] = b[i] - q[i];
   Vec bv(b, b + n);
@@ -488,7 +517,7 @@ int pcg(const orc_ts& s, const Vec& vals, const double* b, double* x, double rto
     if (rel_res) *rel_res = 0;
     return 0;
   }
-  for (int i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+  apply(r, z);
   p = z;
   double rz = dot(r, z);
   int k = 0;
@@ -499,15 +528,12 @@ int pcg(const orc_ts& s, const Vec& vals, const double* b, double* x, double rto
     const double pq = dot(p, q);
     if (pq <= 0) break;
     const double alpha = rz / pq;
-    double rr = 0, rzn = 0;
-#pragma omp parallel for reduction(+ : rr, rzn) schedule(static)
     for (int i = 0; i < n; ++i) {
       x[i] += alpha * p[i];
       r[i] -= alpha * q[i];
-      z[i] = dinv[i] * r[i];
-      rr += r[i] * r[i];
-      rzn += r[i] * z[i];
     }
+    apply(r, z);
+    const double rr = dot(r, r), rzn = dot(r, z);
     rn = std::sqrt(rr);
     const double beta = rzn / rz;
     rz = rzn;
@@ -665,6 +691,7 @@ void orc_default_params(orc_params* p) {
   p->lbfgs_history = 8;
   p->lbfgs_armijo = 1e-4;
   p->max_lbfgs_iters = 1000;
+  p->ls_energy_slack = 1e-12;
 }
 
 orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double dt, double E, double nu,
@@ -807,7 +834,9 @@ void orc_update_hessian(orc_ts* s, int F_updated, int make_spsd, int filter_dbc)
 // mathprim's newton_optimizer (not in the reference tree; definition restated here):
 //   loop: evaluate E, g; stop if the gradient test passes; H = update_hessian(true, make_spsd=true)
 //   (variational_problem::eval_hessian_impl, time_step.hpp:764-768); d from Jacobi-PCG on H d = -g;
-//   backtracking line search from alpha = 1, shrink `ls_shrink`, Armijo constant `armijo`; x += alpha d.
+//   backtracking line search from alpha = 1, shrink `ls_shrink`, Armijo constant `armijo`, accepting
+//   E(x + a d) <= E + armijo a g.d + ls_energy_slack |E| (the slack is the round-off floor of the summed
+//   energy: without it the test cannot pass once the Newton decrement falls below that floor); x += a d.
 // Then compute_step (time_step.hpp:520-528) re-evaluates the gradient and returns its norm.
 double orc_compute_step_newton(orc_ts* s, const orc_params* p, orc_stats* st) {
   orc_stats loc{};
@@ -844,7 +873,7 @@ double orc_compute_step_newton(orc_ts* s, const orc_params* p, orc_stats* st) {
       for (int i = 0; i < s->n; ++i) xt[i] = s->next[i] + alpha * d[i];
       const double Et = energy_only(*s, xt);
       loc.ls_steps_total++;
-      if (Et <= E + p->armijo * alpha * gd) break;
+      if (Et <= E + p->armijo * alpha * gd + p->ls_energy_slack * std::fabs(E)) break;
       alpha *= p->ls_shrink;
     }
     double ch = 0;
@@ -918,7 +947,7 @@ static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, bool pd)
       for (int k = 0; k < n; ++k) xt[k] = s->next[k] + alpha * z[k];
       const double Et = energy_only(*s, xt);
       loc.ls_steps_total++;
-      if (Et <= E + p->lbfgs_armijo * alpha * gd) break;
+      if (Et <= E + p->lbfgs_armijo * alpha * gd + p->ls_energy_slack * std::fabs(E)) break;
       alpha *= p->ls_shrink;
     }
     Vec sv(n), yv(n);

@@ -73,10 +73,11 @@ typedef struct {
   double cg_eta_min;     /* lower clamp of the adaptive forcing term */
   int stop_mode;         /* 0: |g| < rtol*sum|M|/3 (reference); 1: |g| <= rel_tol*|g_0| */
   double rel_tol;        /* used when stop_mode == 1 */
-  int precond;           /* 0: none, 1: Jacobi (diagonal) */
+  int precond;           /* 0: none, 1: Jacobi (diagonal), 2: block-Jacobi (3x3) */
   int lbfgs_history;     /* L-BFGS memory m */
   double lbfgs_armijo;   /* L-BFGS Armijo constant */
   int max_lbfgs_iters;
+  double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack |E| (energy round-off floor) */
 } orc_params;
 
 typedef struct {

@@ -50,6 +50,7 @@ class OrcParams(C.Structure):
         ("lbfgs_history", C.c_int),
         ("lbfgs_armijo", C.c_double),
         ("max_lbfgs_iters", C.c_int),
+        ("ls_energy_slack", C.c_double),
     ]
 
 

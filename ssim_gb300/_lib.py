@@ -50,6 +50,8 @@ class Params(C.Structure):
         ("lbfgs_armijo", C.c_double),
         ("max_lbfgs_iters", C.c_int32),
         ("cg_check_every", C.c_int32),
+        ("ls_energy_slack", C.c_double),
+        ("pd_kappa_mode", C.c_int32),
     ]
 
     def as_dict(self):

@@ -95,11 +95,14 @@ __device__ __forceinline__ void block_sum(double (&vals)[NV], double (*sh)[NV]) 
   }
 }
 
-// returns true in exactly one thread (thread 0 of the last block), with tot[] = sum of all partials
-template <int NV>
+// returns true in exactly one thread (thread 0 of the last block), with tot[] = sum of all partials.
+// The last block reads the partials with every thread at once (L2-coherent loads) and combines them in a
+// fixed order, so the result depends only on the grid and block sizes.
+template <int NV, int BLOCK>
 __device__ __forceinline__ bool grid_sum_last(const double (&blockval)[NV], double* partials, unsigned int* counter,
                                               double (&tot)[NV]) {
   __shared__ bool am_last;
+  __shared__ double sh[BLOCK / 32][NV];
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) partials[blockIdx.x * NV + k] = blockval[k];
@@ -109,28 +112,18 @@ __device__ __forceinline__ bool grid_sum_last(const double (&blockval)[NV], doub
   }
   __syncthreads();
   if (!am_last) return false;
-  // last block: sum partials in block order (all threads help, then fixed-order combine)
-  __shared__ double sh[NV][32];
-  const int lane = threadIdx.x;
-  if (lane < 32) {
-    double acc[NV];
+  __threadfence();
+  double acc[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = 0;
-    for (unsigned int b = lane; b < gridDim.x; b += 32) {
+  for (int k = 0; k < NV; ++k) acc[k] = 0;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += BLOCK) {
 #pragma unroll
-      for (int k = 0; k < NV; ++k) acc[k] += ((volatile double*)partials)[b * NV + k];
-    }
-#pragma unroll
-    for (int k = 0; k < NV; ++k) sh[k][lane] = acc[k];
+    for (int k = 0; k < NV; ++k) acc[k] += __ldcg(partials + b * NV + k);
   }
-  __syncthreads();
+  block_sum<NV, BLOCK>(acc, sh);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s = 0;
-      for (int l = 0; l < 32; ++l) s += sh[k][l];
-      tot[k] = s;
-    }
+    for (int k = 0; k < NV; ++k) tot[k] = acc[k];
     *counter = 0;  // ready for the next launch on this stream
     __threadfence();
     return true;

@@ -5,10 +5,11 @@
 //   element SoA  dminv[9][T], vol[T], lam[T], mu[T]   (FP64, plus an FP32 copy for the mixed path)
 //   state        [V*3] FP64 in the reference layout (deformation, next, inertia, velocity, ...)
 //   xf           float4[V]  current positions X + u rounded to FP32 (mixed-path Hessian input)
-//   matrix       3x3-block SELL-32: slice s covers block rows 32s..32s+31; slot (s, k, lane) holds block
-//                (row = 32s+lane, col = sl_col[slot]); value c of a slot q sits at
-//                vals[9*(q & ~31) + 32*c + (q & 31)] so that every component load of a warp is one
-//                128-byte (FP32) or 256-byte (FP64) line
+//   matrix       symmetric 3x3-block SELL-32: slice s covers block rows 32s..32s+31; upper slot
+//                (s, k, lane) holds block (row = 32s+lane, col = sl_col[slot] >= row); value c of a slot q
+//                sits at vals[9*(q & ~31) + 32*c + (q & 31)] so that every component load of a warp is one
+//                128-byte (FP32) or 256-byte (FP64) line; lower blocks are transposed upper slots
+//   dinv         vec4<S>[3V]  rows of the inverse 3x3 diagonal block (block-Jacobi preconditioner)
 //   Kbuf         S[T][10][9]  scaled element stiffness blocks (v <= w) awaiting assembly
 //   lf           double[T][4][3] scaled element forces awaiting the vertex gather
 //   vectors      vec4<S>[V]  CG vectors, one padded xyz triple per vertex
@@ -47,17 +48,23 @@ struct Reduce {
   DevScalars* sc;
 };
 
+// Symmetric 3x3-block matrix: upper blocks (w >= u) in SELL-32 slots; the lower blocks of row u are read
+// as transposes of upper slots of other rows through a second SELL-32 index.
 struct SellMatrix {
   int nv;
   int nslots;
   const int* sl_off;    // [nslices + 1] slot offset of each slice (multiple of 32)
   const int* sl_col;    // [nslots] block column (vertex); own row for padding
   const int* slot_row;  // [nslots] block row, -1 for padding
+  const int* lo_off;    // [nslices + 1]
+  const int* lo_src;    // [nlslots] upper slot holding the transposed block, -1 for padding
+  const int* lo_col;    // [nlslots] block column (own row for padding)
 };
 
 // ---------------- element kernels (FP64 energy / gradient) ----------------
 // lf[e] = dt^2 V_e * local elastic force + element inertia force M_e (u - x_tilde); energy reduced into
-// sc->energy.  When trial, u is replaced by u + alpha * d (no forces written; energy into sc->trial_energy).
+// sc->energy.  When trial, u is replaced by u + alpha * d and the energy goes to sc->trial_energy (forces
+// at the trial point are written when with_forces: an accepted line-search trial is the next gradient).
 template <typename SD>
 void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* u, const double* xt,
                              const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
@@ -72,13 +79,15 @@ void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double*
                          const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
 
 // ---------------- assembly / sparse ----------------
+// precond: 0 identity, 1 Jacobi (diagonal of the diagonal block), 2 block-Jacobi (inverse 3x3 block)
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
-                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, cudaStream_t st);
+                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st);
 template <typename S>
 void launch_spmv(const SellMatrix& A, const S* vals, const V4<S>* x, V4<S>* y, cudaStream_t st);
 template <typename S>
-void launch_export_csr(const SellMatrix& A, const int* bptr, const S* vals, double* csr_vals, cudaStream_t st);
+void launch_export_csr(const SellMatrix& A, const int* bptr, const int* slot_k, const int* slot_kt, const S* vals,
+                       double* csr_vals, cudaStream_t st);
 
 // ---------------- PCG (fused) ----------------
 template <typename S>
@@ -110,6 +119,19 @@ void launch_mark_dofs(int n, const int* verts, const double* targ, int dirichlet
 void launch_build_mask(int nv, const int8_t* dof_type, uint8_t* mask, cudaStream_t st);
 template <typename S>
 void launch_to_vec4(int nv, const double* in, V4<S>* out, bool negate, cudaStream_t st);
+// FP64 dot of two S vectors into *out (device), deterministic
+template <typename S>
+void launch_vdot(int nv, const V4<S>* a, const V4<S>* b, double* out, const Reduce& red, cudaStream_t st);
+// y = alpha * y + beta * x
+template <typename S>
+void launch_vaxpby(int nv, double alpha, V4<S>* y, double beta, const V4<S>* x, cudaStream_t st);
+// y = (S)(a - b) for FP64 [3V] a, b
+template <typename S>
+void launch_vdiff(int nv, const double* a, const double* b, V4<S>* y, cudaStream_t st);
+// PCG setup from an S right-hand side (the PD stepper's inner solve)
+template <typename S>
+void launch_pcg_setup_v(int nv, const V4<S>* b, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
+                        double rtol, int max_iters, const Reduce& red, cudaStream_t st);
 template <typename S>
 void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st);
 

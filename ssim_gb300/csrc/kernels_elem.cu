@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(EB)
   double v1[1] = {energy};
   block_sum<1, EB>(v1, shred);
   double tot[1];
-  if (grid_sum_last<1>(v1, red.partials, red.counter, tot)) {
+  if (grid_sum_last<1, EB>(v1, red.partials, red.counter, tot)) {
     if (TRIAL)
       red.sc->trial_energy = tot[0];
     else
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(GB)
   double v1[1] = {part};
   block_sum<1, GB>(v1, shred);
   double tot[1];
-  if (grid_sum_last<1>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+  if (grid_sum_last<1, GB>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
 }
 
 // ------------------------------------------------------------------ element Hessian
@@ -247,7 +247,9 @@ void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* 
                              bool trial, const Reduce& red, cudaStream_t st) {
   if (el.nt <= 0) return;
   const int grid = div_up(el.nt, EB);
-  if (trial) {
+  if (trial && with_forces) {
+    elem_energy_grad_kernel<SD, true, true><<<grid, EB, 0, st>>>(el, X, u, xt, d, alpha, dt2, rho, lf, red);
+  } else if (trial) {
     elem_energy_grad_kernel<SD, false, true><<<grid, EB, 0, st>>>(el, X, u, xt, d, alpha, dt2, rho, lf, red);
   } else if (with_forces) {
     elem_energy_grad_kernel<SD, true, false><<<grid, EB, 0, st>>>(el, X, u, xt, d, alpha, dt2, rho, lf, red);

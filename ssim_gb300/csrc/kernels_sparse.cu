@@ -18,15 +18,57 @@ __device__ __forceinline__ V4<S> mk4(S a, S b, S c) {
 
 __device__ __forceinline__ size_t sell_base(int q) { return (size_t)9 * (size_t)(q & ~31) + (size_t)(q & 31); }
 
-// Assembly (update_hessian, time_step.hpp:631-657): each slot (one 3x3 vertex-pair block of the CSR)
-// adds its precomputed list of element blocks (global_composer.hpp:103-119 builds the same map entry
-// by entry) to the consistent-mass block, then applies the Dirichlet identity filter
+// 3x3 preconditioner rows from a diagonal block a (row-major): 0 identity, 1 Jacobi, 2 block-Jacobi
+// (inverse of the symmetric block by its adjugate; falls back to Jacobi if the block is singular).
+template <typename S>
+__device__ __forceinline__ void precond_rows(const S* a, int precond, V4<S>* out) {
+  S m[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m[i] = S(0);
+  if (precond == 2) {
+    const S c0 = a[4] * a[8] - a[5] * a[7], c1 = a[5] * a[6] - a[3] * a[8], c2 = a[3] * a[7] - a[4] * a[6];
+    const S det = a[0] * c0 + a[1] * c1 + a[2] * c2;
+    if (det > S(0) && isfinite(det)) {
+      const S id = S(1) / det;
+      m[0] = c0 * id;
+      m[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+      m[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+      m[3] = c1 * id;
+      m[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+      m[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+      m[6] = c2 * id;
+      m[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+      m[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+      // symmetrise (the block is symmetric; keeps the preconditioner exactly symmetric)
+      const S m01 = S(0.5) * (m[1] + m[3]), m02 = S(0.5) * (m[2] + m[6]), m12 = S(0.5) * (m[5] + m[7]);
+      m[1] = m[3] = m01;
+      m[2] = m[6] = m02;
+      m[5] = m[7] = m12;
+    } else {
+      precond = 1;
+    }
+  }
+  if (precond == 1) {
+    m[0] = a[0] != S(0) ? S(1) / a[0] : S(1);
+    m[4] = a[4] != S(0) ? S(1) / a[4] : S(1);
+    m[8] = a[8] != S(0) ? S(1) / a[8] : S(1);
+  } else if (precond == 0) {
+    m[0] = m[4] = m[8] = S(1);
+  }
+  out[0] = mk4<S>(m[0], m[1], m[2]);
+  out[1] = mk4<S>(m[3], m[4], m[5]);
+  out[2] = mk4<S>(m[6], m[7], m[8]);
+}
+
+// Assembly (update_hessian, time_step.hpp:631-657): each upper slot (one 3x3 vertex-pair block of the
+// symmetric matrix) adds its precomputed list of element blocks (global_composer.hpp:103-119 builds the
+// same map entry by entry) to the consistent-mass block, then applies the Dirichlet identity filter
 // (boundary.hpp:53-67).  One thread per slot, no atomics: deterministic.
 template <typename S>
 __global__ void __launch_bounds__(SB)
     assemble_kernel(SellMatrix A, const int* __restrict__ cptr, const int* __restrict__ csrc,
                     const S* __restrict__ Kbuf, const S* __restrict__ slot_mass, const uint8_t* __restrict__ mask,
-                    int filter, S* __restrict__ vals, V4<S>* __restrict__ dinv) {
+                    int filter, S* __restrict__ vals, V4<S>* __restrict__ dinv, int precond) {
   const int q = blockIdx.x * SB + threadIdx.x;
   if (q >= A.nslots) return;
   S acc[9];
@@ -68,39 +110,63 @@ __global__ void __launch_bounds__(SB)
             if (((mu >> a) & 1) || ((mw >> b) & 1)) acc[a * 3 + b] = (u == w && a == b) ? S(1) : S(0);
       }
     }
-    if (dinv != nullptr && u == w)
-      dinv[u] = mk4<S>(acc[0] != S(0) ? S(1) / acc[0] : S(1), acc[4] != S(0) ? S(1) / acc[4] : S(1),
-                       acc[8] != S(0) ? S(1) / acc[8] : S(1));
+    if (dinv != nullptr && u == w) precond_rows<S>(acc, precond, dinv + 3 * (size_t)u);
   }
   const size_t base = sell_base(q);
 #pragma unroll
   for (int c = 0; c < 9; ++c) vals[base + 32 * c] = acc[c];
 }
 
-// SELL-32 3x3-block SpMV, one thread per block row; a warp walks one slice in lockstep so every value
-// load is one contiguous line.
+// Symmetric SELL-32 3x3-block SpMV, one thread per block row; a warp walks one slice in lockstep so every
+// upper value load is one contiguous line.  The lower blocks are the transposed upper slots of earlier
+// rows; for meshes numbered along a grid the slots read by neighbouring lanes are neighbours too.
+template <typename S>
+__device__ __forceinline__ V4<S> load_x(const V4<S>* x0, const V4<S>* x1, S beta, int col) {
+  V4<S> xv = x0[col];
+  if (x1 != nullptr) {
+    const V4<S> pv = x1[col];
+    xv.x += beta * pv.x;
+    xv.y += beta * pv.y;
+    xv.z += beta * pv.z;
+  }
+  return xv;
+}
+
 template <typename S>
 __device__ __forceinline__ void row_product(const SellMatrix& A, const S* __restrict__ vals, int u, const V4<S>* x0,
                                             const V4<S>* x1, S beta, S& a0, S& a1, S& a2) {
   const int lane = u & 31, s = u >> 5;
-  const int base = A.sl_off[s];
-  const int W = (A.sl_off[s + 1] - base) >> 5;
-  const S* vb = vals + (size_t)9 * base + lane;
-  const int* cb = A.sl_col + base + lane;
   a0 = a1 = a2 = S(0);
-  for (int k = 0; k < W; ++k) {
-    const int col = cb[k * 32];
-    V4<S> xv = x0[col];
-    if (x1 != nullptr) {
-      const V4<S> pv = x1[col];
-      xv.x += beta * pv.x;
-      xv.y += beta * pv.y;
-      xv.z += beta * pv.z;
+  {
+    const int base = A.sl_off[s];
+    const int W = (A.sl_off[s + 1] - base) >> 5;
+    const S* vb = vals + (size_t)9 * base + lane;
+    const int* cb = A.sl_col + base + lane;
+#pragma unroll 2
+    for (int k = 0; k < W; ++k) {
+      const V4<S> xv = load_x<S>(x0, x1, beta, cb[k * 32]);
+      const S* v = vb + (size_t)k * 9 * 32;
+      a0 += v[0] * xv.x + v[32] * xv.y + v[64] * xv.z;
+      a1 += v[96] * xv.x + v[128] * xv.y + v[160] * xv.z;
+      a2 += v[192] * xv.x + v[224] * xv.y + v[256] * xv.z;
     }
-    const S* v = vb + (size_t)k * 9 * 32;
-    a0 += v[0] * xv.x + v[32] * xv.y + v[64] * xv.z;
-    a1 += v[96] * xv.x + v[128] * xv.y + v[160] * xv.z;
-    a2 += v[192] * xv.x + v[224] * xv.y + v[256] * xv.z;
+  }
+  {
+    const int base = A.lo_off[s];
+    const int W = (A.lo_off[s + 1] - base) >> 5;
+    const int* sb = A.lo_src + base + lane;
+    const int* cb = A.lo_col + base + lane;
+#pragma unroll 2
+    for (int k = 0; k < W; ++k) {
+      const int q = sb[k * 32];
+      if (q < 0) continue;
+      const V4<S> xv = load_x<S>(x0, x1, beta, cb[k * 32]);
+      const S* v = vals + sell_base(q);
+      // (A_wu)^T x_w: column a of the stored block times x
+      a0 += v[0] * xv.x + v[96] * xv.y + v[192] * xv.z;
+      a1 += v[32] * xv.x + v[128] * xv.y + v[224] * xv.z;
+      a2 += v[64] * xv.x + v[160] * xv.y + v[256] * xv.z;
+    }
   }
 }
 
@@ -114,22 +180,34 @@ __global__ void __launch_bounds__(SB)
   y[u] = mk4<S>(a0, a1, a2);
 }
 
+// Symmetric storage -> the reference's full CSR: each upper slot writes its block into row u (position
+// slot_k) and, off the diagonal, its transpose into row w (position slot_kt).
 template <typename S>
 __global__ void __launch_bounds__(SB)
-    export_csr_kernel(SellMatrix A, const int* __restrict__ bptr, const S* __restrict__ vals,
-                      double* __restrict__ out) {
+    export_csr_kernel(SellMatrix A, const int* __restrict__ bptr, const int* __restrict__ slot_k,
+                      const int* __restrict__ slot_kt, const S* __restrict__ vals, double* __restrict__ out) {
   const int q = blockIdx.x * SB + threadIdx.x;
   if (q >= A.nslots) return;
   const int u = A.slot_row[q];
   if (u < 0) return;
-  const int k = (q - A.sl_off[u >> 5]) >> 5;
-  const long long b0 = bptr[u];
-  const int deg = bptr[u + 1] - bptr[u];
+  const int w = A.sl_col[q];
   const size_t base = sell_base(q);
+  {
+    const long long b0 = bptr[u];
+    const int deg = bptr[u + 1] - bptr[u], k = slot_k[q];
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) out[9 * b0 + 3LL * deg * a + 3 * k + b] = (double)vals[base + 32 * (a * 3 + b)];
+      for (int b = 0; b < 3; ++b) out[9 * b0 + 3LL * deg * a + 3 * k + b] = (double)vals[base + 32 * (a * 3 + b)];
+  }
+  if (w != u) {
+    const long long b0 = bptr[w];
+    const int deg = bptr[w + 1] - bptr[w], k = slot_kt[q];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) out[9 * b0 + 3LL * deg * a + 3 * k + b] = (double)vals[base + 32 * (b * 3 + a)];
+  }
 }
 
 // ------------------------------------------------------------------ PCG
@@ -148,8 +226,10 @@ __global__ void __launch_bounds__(SB)
   if (u < nv) {
     const double sg = negate ? -1.0 : 1.0;
     const S r0 = (S)(sg * g[u * 3 + 0]), r1 = (S)(sg * g[u * 3 + 1]), r2 = (S)(sg * g[u * 3 + 2]);
-    const V4<S> di = dinv[u];
-    const S z0 = di.x * r0, z1 = di.y * r1, z2 = di.z * r2;
+    const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
+    const S z0 = d0.x * r0 + d0.y * r1 + d0.z * r2;
+    const S z1 = d1.x * r0 + d1.y * r1 + d1.z * r2;
+    const S z2 = d2.x * r0 + d2.y * r1 + d2.z * r2;
     x[u] = mk4<S>(0, 0, 0);
     r[u] = mk4<S>(r0, r1, r2);
     z[u] = mk4<S>(z0, z1, z2);
@@ -159,7 +239,7 @@ __global__ void __launch_bounds__(SB)
   }
   block_sum<2, SB>(part, shred);
   double tot[2];
-  if (grid_sum_last<2>(part, red.partials, red.counter, tot)) {
+  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
     DevScalars* sc = red.sc;
     sc->rz = tot[0];
     sc->rz_old = 1.0;
@@ -194,7 +274,7 @@ __global__ void __launch_bounds__(SB)
   double v1[1] = {part};
   block_sum<1, SB>(v1, shred);
   double tot[1];
-  if (grid_sum_last<1>(v1, red.partials, red.counter, tot)) {
+  if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) {
     red.sc->pq = tot[0];
     if (!(tot[0] > 0.0)) {  // breakdown: not SPD along p (or non-finite)
       red.sc->done = 1;
@@ -214,7 +294,8 @@ __global__ void __launch_bounds__(SB)
   const int u = blockIdx.x * SB + threadIdx.x;
   double part[2] = {0, 0};
   if (u < nv) {
-    const V4<S> pu = p[u], qu = q[u], di = dinv[u];
+    const V4<S> pu = p[u], qu = q[u];
+    const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
     V4<S> xu = x[u], ru = r[u];
     xu.x += alpha * pu.x;
     xu.y += alpha * pu.y;
@@ -222,7 +303,8 @@ __global__ void __launch_bounds__(SB)
     ru.x -= alpha * qu.x;
     ru.y -= alpha * qu.y;
     ru.z -= alpha * qu.z;
-    const V4<S> zu = mk4<S>(di.x * ru.x, di.y * ru.y, di.z * ru.z);
+    const V4<S> zu = mk4<S>(d0.x * ru.x + d0.y * ru.y + d0.z * ru.z, d1.x * ru.x + d1.y * ru.y + d1.z * ru.z,
+                            d2.x * ru.x + d2.y * ru.y + d2.z * ru.z);
     x[u] = xu;
     r[u] = ru;
     z[u] = zu;
@@ -231,7 +313,7 @@ __global__ void __launch_bounds__(SB)
   }
   block_sum<2, SB>(part, shred);
   double tot[2];
-  if (grid_sum_last<2>(part, red.partials, red.counter, tot)) {
+  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
     DevScalars* sc = red.sc;
     sc->rz_old = sc->rz;
     sc->rz = tot[0];
@@ -260,7 +342,7 @@ __global__ void __launch_bounds__(SB)
   }
   block_sum<2, SB>(part, shred);
   double tot[2];
-  if (grid_sum_last<2>(part, red.partials, red.counter, tot)) {
+  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
     red.sc->gd = tot[0];
     red.sc->dnorm2 = tot[1];
   }
@@ -354,6 +436,77 @@ __global__ void build_mask_kernel(int nv, const int8_t* __restrict__ dof_type, u
 }
 
 template <typename S>
+__global__ void __launch_bounds__(SB)
+    vdot_kernel(int nv, const V4<S>* __restrict__ a, const V4<S>* __restrict__ b, double* out, Reduce red) {
+  __shared__ double shred[SB / 32][1];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part = 0;
+  if (u < nv) {
+    const V4<S> x = a[u], y = b[u];
+    part = (double)x.x * y.x + (double)x.y * y.y + (double)x.z * y.z;
+  }
+  double v1[1] = {part};
+  block_sum<1, SB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) *out = tot[0];
+}
+
+template <typename S>
+__global__ void vaxpby_kernel(int nv, S alpha, V4<S>* __restrict__ y, S beta, const V4<S>* __restrict__ x) {
+  const int u = blockIdx.x * SB + threadIdx.x;
+  if (u >= nv) return;
+  const V4<S> xv = x[u];
+  V4<S> yv = y[u];
+  yv.x = alpha * yv.x + beta * xv.x;
+  yv.y = alpha * yv.y + beta * xv.y;
+  yv.z = alpha * yv.z + beta * xv.z;
+  y[u] = yv;
+}
+
+template <typename S>
+__global__ void vdiff_kernel(int nv, const double* __restrict__ a, const double* __restrict__ b, V4<S>* __restrict__ y) {
+  const int u = blockIdx.x * SB + threadIdx.x;
+  if (u >= nv) return;
+  y[u] = mk4<S>((S)(a[3 * u] - b[3 * u]), (S)(a[3 * u + 1] - b[3 * u + 1]), (S)(a[3 * u + 2] - b[3 * u + 2]));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    pcg_setup_v_kernel(int nv, const V4<S>* __restrict__ bv, const V4<S>* __restrict__ dinv, V4<S>* __restrict__ x,
+                       V4<S>* __restrict__ r, V4<S>* __restrict__ z, V4<S>* __restrict__ p0, double rtol,
+                       int max_iters, Reduce red) {
+  __shared__ double shred[SB / 32][2];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part[2] = {0, 0};
+  if (u < nv) {
+    const V4<S> rb = bv[u];
+    const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
+    const S z0 = d0.x * rb.x + d0.y * rb.y + d0.z * rb.z;
+    const S z1 = d1.x * rb.x + d1.y * rb.y + d1.z * rb.z;
+    const S z2 = d2.x * rb.x + d2.y * rb.y + d2.z * rb.z;
+    x[u] = mk4<S>(0, 0, 0);
+    r[u] = mk4<S>(rb.x, rb.y, rb.z);
+    z[u] = mk4<S>(z0, z1, z2);
+    p0[u] = mk4<S>(0, 0, 0);
+    part[0] = (double)rb.x * z0 + (double)rb.y * z1 + (double)rb.z * z2;
+    part[1] = (double)rb.x * rb.x + (double)rb.y * rb.y + (double)rb.z * rb.z;
+  }
+  block_sum<2, SB>(part, shred);
+  double tot[2];
+  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
+    DevScalars* sc = red.sc;
+    sc->rz = tot[0];
+    sc->rz_old = 1.0;
+    sc->rr = tot[1];
+    sc->rr0 = tot[1];
+    sc->tol2 = rtol * rtol * tot[1];
+    sc->iters = 0;
+    sc->status = 0;
+    sc->done = (tot[1] <= sc->tol2 || tot[1] == 0.0 || max_iters <= 0) ? 1 : 0;
+  }
+}
+
+template <typename S>
 __global__ void to_vec4_kernel(int nv, const double* __restrict__ in, V4<S>* __restrict__ out, int negate) {
   const int v = blockIdx.x * SB + threadIdx.x;
   if (v >= nv) return;
@@ -376,10 +529,10 @@ __global__ void from_vec4_kernel(int nv, const V4<S>* __restrict__ in, double* _
 // ------------------------------------------------------------------ launchers
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
-                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, cudaStream_t st) {
+                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st) {
   if (A.nslots <= 0) return;
   assemble_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A, cptr, csrc, Kbuf, slot_mass, mask, filter ? 1 : 0,
-                                                          vals, dinv);
+                                                          vals, dinv, precond);
   after_launch("assemble");
 }
 
@@ -391,9 +544,10 @@ void launch_spmv(const SellMatrix& A, const S* vals, const V4<S>* x, V4<S>* y, c
 }
 
 template <typename S>
-void launch_export_csr(const SellMatrix& A, const int* bptr, const S* vals, double* csr_vals, cudaStream_t st) {
+void launch_export_csr(const SellMatrix& A, const int* bptr, const int* slot_k, const int* slot_kt, const S* vals,
+                       double* csr_vals, cudaStream_t st) {
   if (A.nslots <= 0) return;
-  export_csr_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A, bptr, vals, csr_vals);
+  export_csr_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A, bptr, slot_k, slot_kt, vals, csr_vals);
   after_launch("export_csr");
 }
 
@@ -485,11 +639,37 @@ void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st) {
   after_launch("from_vec4");
 }
 
+template <typename S>
+void launch_vdot(int nv, const V4<S>* a, const V4<S>* b, double* out, const Reduce& red, cudaStream_t st) {
+  vdot_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, a, b, out, red);
+  after_launch("vdot");
+}
+
+template <typename S>
+void launch_vaxpby(int nv, double alpha, V4<S>* y, double beta, const V4<S>* x, cudaStream_t st) {
+  vaxpby_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, (S)alpha, y, (S)beta, x);
+  after_launch("vaxpby");
+}
+
+template <typename S>
+void launch_vdiff(int nv, const double* a, const double* b, V4<S>* y, cudaStream_t st) {
+  vdiff_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, a, b, y);
+  after_launch("vdiff");
+}
+
+template <typename S>
+void launch_pcg_setup_v(int nv, const V4<S>* b, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
+                        double rtol, int max_iters, const Reduce& red, cudaStream_t st) {
+  pcg_setup_v_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, b, dinv, x, r, z, p0, rtol, max_iters, red);
+  after_launch("pcg_setup_v");
+}
+
 #define SSIM_INST(S)                                                                                              \
   template void launch_assemble<S>(const SellMatrix&, const int*, const int*, const S*, const S*, const uint8_t*, \
-                                   bool, S*, V4<S>*, cudaStream_t);                                               \
+                                   bool, S*, V4<S>*, int, cudaStream_t);                                          \
   template void launch_spmv<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, cudaStream_t);                 \
-  template void launch_export_csr<S>(const SellMatrix&, const int*, const S*, double*, cudaStream_t);            \
+  template void launch_export_csr<S>(const SellMatrix&, const int*, const int*, const int*, const S*, double*,   \
+                                     cudaStream_t);                                                               \
   template void launch_pcg_setup<S>(int, const double*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, V4<S>*, double,   \
                                     int, bool, const Reduce&, cudaStream_t);                                      \
   template void launch_pcg_spmv<S>(const SellMatrix&, const S*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*,     \
@@ -499,7 +679,12 @@ void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st) {
   template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
   template void launch_axpy_update<S>(int, double, const V4<S>*, const double*, double*, float4*, cudaStream_t); \
   template void launch_to_vec4<S>(int, const double*, V4<S>*, bool, cudaStream_t);                               \
-  template void launch_from_vec4<S>(int, const V4<S>*, double*, cudaStream_t);
+  template void launch_from_vec4<S>(int, const V4<S>*, double*, cudaStream_t);                                  \
+  template void launch_vdot<S>(int, const V4<S>*, const V4<S>*, double*, const Reduce&, cudaStream_t);          \
+  template void launch_vaxpby<S>(int, double, V4<S>*, double, const V4<S>*, cudaStream_t);                      \
+  template void launch_vdiff<S>(int, const double*, const double*, V4<S>*, cudaStream_t);                       \
+  template void launch_pcg_setup_v<S>(int, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, V4<S>*, double,  \
+                                      int, const Reduce&, cudaStream_t);
 
 SSIM_INST(float)
 SSIM_INST(double)

@@ -53,9 +53,16 @@ struct Solver {
   DBuf<S> K, vals, mvals;  // element blocks, system values, mass values (SELL)
   DBuf<S> slot_mass;
   DBuf<V4<S>> x, r, z, p0, p1, q, dinv, tmp;
+  // L-BFGS / PD: direction, two-loop work vector, history ring, PD matrix and its preconditioner
+  DBuf<V4<S>> ld, lq;
+  std::vector<std::unique_ptr<DBuf<V4<S>>>> hs, hy;
+  DBuf<S> pd_vals, slot_pd;
+  DBuf<V4<S>> pd_dinv;
   void release() {
-    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass}) b->release();
-    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp}) b->release();
+    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd}) b->release();
+    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &ld, &lq, &pd_dinv}) b->release();
+    hs.clear();
+    hy.clear();
   }
 };
 
@@ -90,7 +97,7 @@ struct TimeStep {
   DBuf<uint8_t> mask;
   DBuf<float4> xf;
   // ---- device: topology
-  DBuf<int32_t> vptr, vinc, sl_off, sl_col, slot_row, cptr, csrc, bptr;
+  DBuf<int32_t> vptr, vinc, sl_off, sl_col, slot_row, cptr, csrc, bptr, slot_k, slot_kt, lo_off, lo_src, lo_col;
   DBuf<double> lf, csr_out;
   // ---- device: solver
   Solver<float> sf;
@@ -99,6 +106,8 @@ struct TimeStep {
   DBuf<unsigned int> counter;
   DBuf<DevScalars> sc;
   DevScalars* hsc = nullptr;  // pinned
+  DBuf<double> gprev, dscal;   // previous gradient (L-BFGS), device scalars of vdot
+  double* hscal = nullptr;     // pinned mirror of dscal
   // ---- profiling
   bool profiling = false;
   std::vector<cudaEvent_t> ev;
@@ -109,6 +118,7 @@ struct TimeStep {
   ~TimeStep() {
     for (auto e : ev) cudaEventDestroy(e);
     if (hsc) cudaFreeHost(hsc);
+    if (hscal) cudaFreeHost(hscal);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -116,7 +126,9 @@ struct TimeStep {
   Reduce red() { return Reduce{partials.p, counter.p, sc.p}; }
   ElemFP64 e64() const { return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p}; }
   ElemFP32 e32() const { return ElemFP32{nt, dcells.p, fdminv.p, fvol.p, flam.p, fmu.p}; }
-  SellMatrix A() const { return SellMatrix{nv, topo.nslots, sl_off.p, sl_col.p, slot_row.p}; }
+  SellMatrix A() const {
+    return SellMatrix{nv, topo.nslots, sl_off.p, sl_col.p, slot_row.p, lo_off.p, lo_src.p, lo_col.p};
+  }
 
   void sync_scalars() {
     SSIM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream));
@@ -147,6 +159,9 @@ struct TimeStep {
     SSIM_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
     stream = own_stream;
     SSIM_CUDA(cudaMallocHost((void**)&hsc, sizeof(DevScalars)));
+    SSIM_CUDA(cudaMallocHost((void**)&hscal, 8 * sizeof(double)));
+    dscal.alloc(8);
+    gprev.alloc(n);
     // state buffers (zero_if_not_valid, time_step.hpp:396-413)
     for (DBuf<double>* b : {&deformation, &prev_deform, &inertia, &next, &velocity, &ext_accel, &forces,
                             &dbc_values, &work}) {
@@ -162,7 +177,7 @@ struct TimeStep {
     sc.zero(stream);
     counter.alloc(1);
     counter.zero(stream);
-    const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(nv, topo.nslots), 256)) + 1;
+    const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(3 * nv, topo.nslots), 256)) + 1;
     partials.alloc(maxgrid * 4);
     dX.upload(X, stream);
     std::vector<int4> c4(nt);
@@ -176,6 +191,11 @@ struct TimeStep {
     cptr.upload(topo.cptr, stream);
     csrc.upload(topo.csrc, stream);
     bptr.upload(topo.bptr, stream);
+    slot_k.upload(topo.slot_k, stream);
+    slot_kt.upload(topo.slot_kt, stream);
+    lo_off.upload(topo.lo_off, stream);
+    lo_src.upload(topo.lo_src, stream);
+    lo_col.upload(topo.lo_col, stream);
     lf.alloc(12 * (size_t)nt);
     // rest shape (dminv_task def_grad.hpp:56-91, rest_vol_task rest_vol.hpp:34-54)
     std::vector<double> dm(9 * (size_t)nt);
@@ -215,8 +235,6 @@ struct TimeStep {
     if (!(nu > 0 && nu < 0.5)) throw invalid_argument("Poisson's ratio must be in (0, 0.5), got " + std::to_string(nu));
     if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
     if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NONE) throw invalid_argument("unknown stepper");
-    if (stepper_kind == SSIM_GB_STEPPER_LBFGS || stepper_kind == SSIM_GB_STEPPER_PD)
-      throw invalid_argument("this build provides the Newton stepper; L-BFGS and PD are not built yet");
     stepper = stepper_kind;
     for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
     // material: per element Lame parameters (basic_elast.hpp:10-20)
@@ -250,8 +268,36 @@ struct TimeStep {
       sf.release();
     }
     launch_build_mask(nv, dof_type.p, mask.p, stream);
+    if (stepper == SSIM_GB_STEPPER_PD) {
+      if (mixed())
+        pd_setup<float>(sf);
+      else
+        pd_setup<double>(sd);
+    }
     SSIM_CUDA(cudaStreamSynchronize(stream));
     has_reset = true;
+  }
+
+  // time_step_solver_pd::reset_impl (projective_dynamics.hpp:53-93): (mass(rho) + laplace(dt^2 kappa)) (x) I3
+  // with the Dirichlet identity filter, assembled once into the symmetric block store.  kappa is
+  // approximated_diffusivity (stable_neohookean.hpp:106-111) of uniform_elasticity() (time_step.hpp:356),
+  // which builds the model as ElastModel{E, nu}, i.e. with (E, nu) in its (lambda, mu) slots; mode 1 uses the
+  // Lame parameters instead.
+  template <typename S>
+  void pd_setup(Solver<S>& s) {
+    double lam_slot = E, mu_slot = nu;
+    if (params.pd_kappa_mode == 1) {
+      mu_slot = E / (2 * (1 + nu));
+      lam_slot = E * nu / ((1 + nu) * (1 - 2 * nu));
+    }
+    const double kappa = (lam_slot + 5.0 / 6.0 * mu_slot) + 2.0 * (4.0 / 3.0 * mu_slot);
+    std::vector<double> pd;
+    slot_pd_values(topo, cells.data(), X.data(), detJ, rho, dt * dt * kappa, pd);
+    std::vector<S> pds(pd.begin(), pd.end());
+    s.slot_pd.upload(pds, stream);
+    s.pd_vals.alloc(9 * (size_t)topo.nslots);
+    s.pd_dinv.alloc(3 * (size_t)nv);
+    launch_assemble<S>(A(), cptr.p, csrc.p, nullptr, s.slot_pd.p, mask.p, true, s.pd_vals.p, s.pd_dinv.p, 2, stream);
   }
 
   template <typename S>
@@ -260,9 +306,21 @@ struct TimeStep {
     s.vals.alloc(9 * (size_t)topo.nslots);
     s.vals.zero(stream);
     s.mvals.release();
-    for (DBuf<V4<S>>* b : {&s.x, &s.r, &s.z, &s.p0, &s.p1, &s.q, &s.dinv, &s.tmp}) {
+    for (DBuf<V4<S>>* b : {&s.x, &s.r, &s.z, &s.p0, &s.p1, &s.q, &s.tmp}) {
       b->alloc(nv);
       b->zero(stream);
+    }
+    s.dinv.alloc(3 * (size_t)nv);
+    s.dinv.zero(stream);
+    s.ld.alloc(nv);
+    s.lq.alloc(nv);
+    s.hs.clear();
+    s.hy.clear();
+    for (int i = 0; i < params.lbfgs_history; ++i) {
+      s.hs.emplace_back(new DBuf<V4<S>>());
+      s.hy.emplace_back(new DBuf<V4<S>>());
+      s.hs.back()->alloc(nv);
+      s.hy.back()->alloc(nv);
     }
   }
 
@@ -320,7 +378,8 @@ struct TimeStep {
     launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream);
     if (profiling) prof_end(e0, e1, PK_HESS, 0);
     if (profiling) prof_begin(e0, e1);
-    launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p, stream);
+    launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
+                       params.precond, stream);
     if (profiling) prof_end(e0, e1, PK_ASM, 0);
   }
 
@@ -338,24 +397,35 @@ struct TimeStep {
   template <typename S>
   int pcg(const double* b, bool negate, double eta, int max_iters, double* rel_res) {
     Solver<S>& s = solver<S>();
-    if (params.precond == 0) {
-      std::vector<V4<S>> ones(nv);
-      for (auto& o : ones) o.x = o.y = o.z = S(1), o.w = S(0);
-      SSIM_CUDA(cudaMemcpyAsync(s.dinv.p, ones.data(), sizeof(V4<S>) * nv, cudaMemcpyHostToDevice, stream));
-    }
     launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
+    return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true);
+  }
+
+  // PCG on another matrix of the same block pattern (the PD matrix) with an S right-hand side
+  template <typename S>
+  int pcg_on(const S* vals, const V4<S>* dinv, const V4<S>* b, double eta, int max_iters, double* rel_res) {
+    Solver<S>& s = solver<S>();
+    launch_pcg_setup_v<S>(nv, b, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, red(), stream);
+    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false);
+  }
+
+  template <typename S>
+  int pcg_loop(const S* vals, const V4<S>* dinv, int max_iters, double* rel_res, bool profile_spmv) {
+    Solver<S>& s = solver<S>();
     int k = 0;
     int chunk = std::max(1, params.cg_check_every);
-    const bool prof = profiling;
+    const bool prof = profiling && profile_spmv;
+    int it_prev = 0;
+    double rr_prev = 0;
     while (true) {
       const int k0 = k;
       for (int c = 0; c < chunk; ++c, ++k) {
         V4<S>* pold = (k & 1) ? s.p1.p : s.p0.p;
         V4<S>* pnew = (k & 1) ? s.p0.p : s.p1.p;
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c], stream));
-        launch_pcg_spmv<S>(A(), s.vals.p, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream);
+        launch_pcg_spmv<S>(A(), vals, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream);
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c + 1], stream));
-        launch_pcg_update<S>(nv, pnew, s.q.p, s.dinv.p, s.x.p, s.r.p, s.z.p, max_iters, red(), stream);
+        launch_pcg_update<S>(nv, pnew, s.q.p, dinv, s.x.p, s.r.p, s.z.p, max_iters, red(), stream);
       }
       sync_scalars();
       if (prof) {
@@ -369,25 +439,140 @@ struct TimeStep {
         prof_bytes[PK_SPMV] = spmv_bytes(sizeof(S));
       }
       if (hsc->done || hsc->iters >= max_iters) break;
-      chunk = std::min(chunk * 2, 64);
+      // next chunk: the iterations still needed at the observed convergence rate (plus a margin), so few
+      // launches run past convergence and few host round trips are spent
+      const int it_now = hsc->iters;
+      const double rr_now = hsc->rr;
+      if (it_prev == 0) rr_prev = hsc->rr0;
+      int next_chunk = 2 * chunk;
+      if (it_now > it_prev && rr_now > 0 && rr_prev > 0 && rr_now < rr_prev && hsc->tol2 > 0) {
+        const double rate = std::log(rr_now / rr_prev) / (it_now - it_prev);  // log decrease per iteration
+        const double need = std::log(hsc->tol2 / rr_now) / rate;
+        if (std::isfinite(need)) next_chunk = (int)std::ceil(1.1 * need) + 2;
+      }
+      it_prev = it_now;
+      rr_prev = rr_now;
+      chunk = std::max(4, std::min(next_chunk, 256));
+      if ((int)ev.size() < 2 * chunk && prof) chunk = (int)ev.size() / 2;
     }
     if (rel_res) *rel_res = hsc->rr0 > 0 ? std::sqrt(hsc->rr / hsc->rr0) : 0.0;
     if (hsc->status == 2) throw numerical_error("PCG produced a non-finite residual");
     return hsc->iters;
   }
 
-  // algorithmic bytes of one SELL SpMV: values + block columns + x gathers (one 3-vector per block
-  // row, reused from cache) + y write.  Padding slots are counted (they are read).
+  template <typename S>
+  double vdot(const V4<S>* a, const V4<S>* b) {
+    launch_vdot<S>(nv, a, b, dscal.p, red(), stream);
+    SSIM_CUDA(cudaMemcpyAsync(hscal, dscal.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SSIM_CUDA(cudaStreamSynchronize(stream));
+    return hscal[0];
+  }
+
+  // L-BFGS stepper (backward_euler.hpp:43-67) over mathprim's l_bfgs_optimizer (absent from the reference
+  // tree; the definition used is the oracle's: two-loop recursion, initial scaling s.y / y.y (1/|g| before
+  // any history), backtracking Armijo line search).  With pd, the initial inverse Hessian is the PD matrix
+  // solve (projective_dynamics.hpp:31-34), done here by PCG to pd tolerance instead of a factorisation.
+  template <typename S>
+  void lbfgs(ssim_gb_step_stats& st, bool pd) {
+    Solver<S>& s = solver<S>();
+    const int m = std::max(1, std::min(params.lbfgs_history, (int)s.hs.size()));
+    std::vector<double> rho_h(m, 0.0), al(m, 0.0);
+    int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
+    double E0 = energy_grad();
+    double gn = std::sqrt(hsc->gnorm2);
+    const double g0 = gn;
+    st.grad_norm0 = g0;
+    SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    const double pd_tol = mixed() ? std::max(params.cg_rtol, 1e-6) : params.cg_rtol;
+    int it = 0;
+    for (;; ++it) {
+      st.grad_norm = gn;
+      st.energy = E0;
+      const bool ok = params.stop_mode == 0 ? (gn < abs_tol) : (gn <= params.rel_tol * g0);
+      if (ok) {
+        st.converged = 1;
+        break;
+      }
+      if (it >= params.max_lbfgs_iters) break;
+      launch_to_vec4<S>(nv, forces.p, s.lq.p, false, stream);  // q = g
+      for (int j = hsize - 1; j >= 0; --j) {
+        const int i = (head - hsize + j + m) % m;
+        al[i] = rho_h[i] * vdot<S>(s.hs[i]->p, s.lq.p);
+        launch_vaxpby<S>(nv, 1.0, s.lq.p, -al[i], s.hy[i]->p, stream);
+      }
+      if (pd) {
+        double rr = 0;
+        st.cg_iters_total += pcg_on<S>(s.pd_vals.p, s.pd_dinv.p, s.lq.p, pd_tol, params.cg_max_iters, &rr);
+        launch_vaxpby<S>(nv, 0.0, s.ld.p, 1.0, s.x.p, stream);  // z = A^-1 q
+      } else {
+        double gamma = 1.0 / std::max(gn, 1e-300);
+        if (hsize > 0) {
+          const int i = (head - 1 + m) % m;
+          gamma = vdot<S>(s.hs[i]->p, s.hy[i]->p) / vdot<S>(s.hy[i]->p, s.hy[i]->p);
+        }
+        launch_vaxpby<S>(nv, 0.0, s.ld.p, gamma, s.lq.p, stream);
+      }
+      for (int j = 0; j < hsize; ++j) {
+        const int i = (head - hsize + j + m) % m;
+        const double bb = rho_h[i] * vdot<S>(s.hy[i]->p, s.ld.p);
+        launch_vaxpby<S>(nv, 1.0, s.ld.p, al[i] - bb, s.hs[i]->p, stream);
+      }
+      launch_vaxpby<S>(nv, -1.0, s.ld.p, 0.0, s.ld.p, stream);  // d = -z
+      launch_dot_gd<S>(nv, forces.p, s.ld.p, red(), stream);
+      sync_scalars();
+      double gd = hsc->gd;
+      if (!(gd < 0)) {  // not a descent direction: drop the history, normalised steepest descent
+        hsize = 0;
+        launch_to_vec4<S>(nv, forces.p, s.ld.p, false, stream);
+        launch_vaxpby<S>(nv, -1.0 / std::max(gn, 1e-300), s.ld.p, 0.0, s.ld.p, stream);
+        launch_dot_gd<S>(nv, forces.p, s.ld.p, red(), stream);
+        sync_scalars();
+        gd = hsc->gd;
+      }
+      const double dn = std::sqrt(hsc->dnorm2);
+      double alpha = 1.0;
+      for (int ls = 0; ls < params.max_ls_iters; ++ls) {
+        launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.ld.p, alpha, dt * dt, rho, nullptr, false, true,
+                                   red(), stream);
+        sync_scalars();
+        st.ls_steps_total++;
+        if (hsc->trial_energy <= E0 + params.lbfgs_armijo * alpha * gd + params.ls_energy_slack * std::fabs(E0)) break;
+        alpha *= params.ls_shrink;
+      }
+      launch_axpy_update<S>(nv, alpha, s.ld.p, dX.p, next.p, nullptr, stream);
+      st.last_change = alpha * dn;
+      E0 = energy_grad();
+      gn = std::sqrt(hsc->gnorm2);
+      // s = alpha d, y = g_new - g_old
+      const int slot = head;
+      launch_vaxpby<S>(nv, 0.0, s.hs[slot]->p, alpha, s.ld.p, stream);
+      launch_vdiff<S>(nv, forces.p, gprev.p, s.hy[slot]->p, stream);
+      SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+      const double sy = vdot<S>(s.hs[slot]->p, s.hy[slot]->p);
+      if (sy > 1e-300) {
+        rho_h[slot] = 1.0 / sy;
+        head = (head + 1) % m;
+        hsize = std::min(hsize + 1, m);
+      }
+    }
+    st.newton_iters = it;
+  }
+
+  // algorithmic bytes of one symmetric SELL SpMV: upper values + block columns, lower slot/column indices
+  // and the values they read (the transposed blocks: a second read of upper slots), x gathers (one
+  // 3-vector per block row, reused from cache) + y write.  Padding slots are counted (they are read).
   double spmv_bytes(size_t s) const {
-    const double slots = topo.nslots;
-    return slots * (9.0 * s + 4.0) + (double)(topo.nslices + 1) * 4 + 2.0 * nv * 4 * s;
+    const double up = topo.nslots, lo = topo.nlslots;
+    const double lo_real = (double)topo.nnzb - (double)(topo.nnzb + nv) / 2.0;
+    return up * (9.0 * s + 4.0) + lo * 8.0 + lo_real * 9.0 * s + 2.0 * (topo.nslices + 1) * 4 + 2.0 * nv * 4 * s;
   }
 
   // ------------------------------------------------------------------ Newton stepper
   // time_step_solver_backward_euler::solve_impl (backward_euler.hpp:15-33) over mathprim's
   // newton_optimizer (absent from the reference tree; the definition used is the one restated by the
   // oracle): evaluate; stop on the gradient test; H = update_hessian(true, make_spsd = true); d from
-  // Jacobi-PCG on H d = -g; backtracking Armijo line search from alpha = 1; x += alpha d.
+  // Jacobi-PCG on H d = -g; backtracking Armijo line search from alpha = 1 (with the energy round-off
+  // slack ls_energy_slack |E|); x += alpha d.
   template <typename S>
   void newton(ssim_gb_step_stats& st) {
     Solver<S>& s = solver<S>();
@@ -419,18 +604,26 @@ struct TimeStep {
         launch_to_vec4<S>(nv, forces.p, s.x.p, true, stream);
         gd = -gn * gn;
       }
+      // backtracking line search; each trial evaluates energy and forces at u + alpha d in one element
+      // pass, so the accepted trial's forces are the next gradient (no separate evaluation)
       double alpha = 1.0;
+      double Et = 0;
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
-        launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, nullptr, false, true,
+        launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
                                    red(), stream);
         sync_scalars();
         st.ls_steps_total++;
-        if (hsc->trial_energy <= E0 + params.armijo * alpha * gd) break;
-        alpha *= params.ls_shrink;
+        Et = hsc->trial_energy;
+        if (Et <= E0 + params.armijo * alpha * gd + params.ls_energy_slack * std::fabs(E0)) break;
+        if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
-      launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, mixed() ? xf.p : nullptr, stream);
+      launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
+      launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+      sync_scalars();
+      if (!std::isfinite(Et) || !std::isfinite(hsc->gnorm2))
+        throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
       st.last_change = alpha * dn;
-      E0 = energy_grad();
+      E0 = Et;
       gn = std::sqrt(hsc->gnorm2);
     }
     st.newton_iters = it;
@@ -446,6 +639,11 @@ struct TimeStep {
         newton<float>(st);
       else
         newton<double>(st);
+    } else if (stepper == SSIM_GB_STEPPER_LBFGS || stepper == SSIM_GB_STEPPER_PD) {
+      if (mixed())
+        lbfgs<float>(st, stepper == SSIM_GB_STEPPER_PD);
+      else
+        lbfgs<double>(st, stepper == SSIM_GB_STEPPER_PD);
     } else {
       // time_step_solver_nothing: no solve; the gradient is still evaluated
       st.energy = energy_grad();
@@ -477,7 +675,7 @@ struct TimeStep {
   void set_profiling(bool on) {
     profiling = on;
     if (on && ev.empty()) {
-      ev.resize(128);
+      ev.resize(512);
       for (auto& e : ev) SSIM_CUDA(cudaEventCreate(&e));
     }
     for (int k = 0; k < PK_COUNT; ++k) {
@@ -564,11 +762,11 @@ static void export_values(TimeStep& t, int which, double* out) {
   if (which == SSIM_GB_MASS || which == SSIM_GB_MASS_FILTERED) {
     s.mvals.alloc(9 * (size_t)t.topo.nslots);
     ssim_gb::launch_assemble<S>(t.A(), t.cptr.p, t.csrc.p, nullptr, s.slot_mass.p, t.mask.p,
-                                which == SSIM_GB_MASS_FILTERED, s.mvals.p, nullptr, t.stream);
+                                which == SSIM_GB_MASS_FILTERED, s.mvals.p, nullptr, 0, t.stream);
     src = s.mvals.p;
   }
   t.csr_out.alloc(9 * (size_t)t.topo.nnzb);
-  ssim_gb::launch_export_csr<S>(t.A(), t.bptr.p, src, t.csr_out.p, t.stream);
+  ssim_gb::launch_export_csr<S>(t.A(), t.bptr.p, t.slot_k.p, t.slot_kt.p, src, t.csr_out.p, t.stream);
   SSIM_CUDA(cudaMemcpyAsync(out, t.csr_out.p, sizeof(double) * 9 * t.topo.nnzb, cudaMemcpyDeviceToHost, t.stream));
   SSIM_CUDA(cudaStreamSynchronize(t.stream));
 }
@@ -580,7 +778,7 @@ static void do_spmv(TimeStep& t, int which, const double* x, double* y) {
   if (which == SSIM_GB_MASS || which == SSIM_GB_MASS_FILTERED) {
     s.mvals.alloc(9 * (size_t)t.topo.nslots);
     ssim_gb::launch_assemble<S>(t.A(), t.cptr.p, t.csrc.p, nullptr, s.slot_mass.p, t.mask.p,
-                                which == SSIM_GB_MASS_FILTERED, s.mvals.p, nullptr, t.stream);
+                                which == SSIM_GB_MASS_FILTERED, s.mvals.p, nullptr, 0, t.stream);
     vals = s.mvals.p;
   }
   SSIM_CUDA(cudaMemcpyAsync(t.work.p, x, sizeof(double) * t.n, cudaMemcpyHostToDevice, t.stream));
@@ -624,6 +822,8 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->lbfgs_armijo = 1e-4;
   p->max_lbfgs_iters = 1000;
   p->cg_check_every = 8;
+  p->ls_energy_slack = 1e-12;
+  p->pd_kappa_mode = 0;
 }
 
 ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
@@ -724,6 +924,7 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
   CHECK_H(h);
   if (!p) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null params");
   if (p->max_newton_iters < 0 || p->cg_max_iters < 0 || p->max_ls_iters < 1 || !(p->ls_shrink > 0 && p->ls_shrink < 1) ||
+      !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 1 ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;

@@ -1,12 +1,26 @@
-// topology.cpp -- host set-up of the CSR pattern, SELL-32 slot layout, assembly lists and incidence.
+// topology.cpp -- host set-up of the CSR pattern, the symmetric SELL-32 slot layout, the assembly lists
+// and the vertex incidence.
 #include "topology.h"
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 
 #include "errors.h"
 
 namespace ssim_gb {
+
+namespace {
+// local upper block id -> (v, w)
+constexpr int kBlkV[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3};
+constexpr int kBlkW[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+
+int find_pos(const Topology& t, int u, int w) {
+  const int32_t* nb = t.bcol.data() + t.bptr[u];
+  const int deg = t.bptr[u + 1] - t.bptr[u];
+  return (int)(std::lower_bound(nb, nb + deg, w) - nb);
+}
+}  // namespace
 
 void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
   if (nv <= 0 || nt <= 0) throw invalid_argument("mesh must have at least one vertex and one cell");
@@ -45,64 +59,97 @@ void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
   }
   t.nnzb = t.bptr[nv];
   if (9LL * t.nnzb >= (1LL << 31)) throw invalid_argument("matrix too large for 32-bit CSR indices");
-  // SELL-32
+  // lower / upper degree of every row.  Vertices used by no cell have an empty row; they still get one
+  // (zero) diagonal slot so every row owns a slot.
+  std::vector<int32_t> lo_deg(nv), up_deg(nv);
+  for (int u = 0; u < nv; ++u) {
+    const int k = find_pos(t, u, u);
+    lo_deg[u] = k;
+    up_deg[u] = (t.bptr[u + 1] - t.bptr[u]) - k;
+  }
   t.nslices = (nv + 31) / 32;
   t.sl_off.assign(t.nslices + 1, 0);
+  t.lo_off.assign(t.nslices + 1, 0);
   for (int s = 0; s < t.nslices; ++s) {
-    int w = 0;
-    for (int u = 32 * s; u < std::min(nv, 32 * s + 32); ++u) w = std::max(w, t.bptr[u + 1] - t.bptr[u]);
-    t.sl_off[s + 1] = t.sl_off[s] + 32 * w;
+    int wu = 1, wl = 0;
+    for (int u = 32 * s; u < std::min(nv, 32 * s + 32); ++u) {
+      wu = std::max(wu, up_deg[u]);
+      wl = std::max(wl, lo_deg[u]);
+    }
+    t.sl_off[s + 1] = t.sl_off[s] + 32 * wu;
+    t.lo_off[s + 1] = t.lo_off[s] + 32 * wl;
   }
   t.nslots = t.sl_off[t.nslices];
+  t.nlslots = t.lo_off[t.nslices];
   t.sl_col.assign(t.nslots, 0);
   t.slot_row.assign(t.nslots, -1);
+  t.slot_k.assign(t.nslots, 0);
+  t.slot_kt.assign(t.nslots, 0);
+  auto slot_of = [&](int u, int kk) { return t.sl_off[u >> 5] + 32 * kk + (u & 31); };
   for (int s = 0; s < t.nslices; ++s) {
     const int W = (t.sl_off[s + 1] - t.sl_off[s]) / 32;
     for (int lane = 0; lane < 32; ++lane) {
       const int u = 32 * s + lane;
-      const int deg = u < nv ? t.bptr[u + 1] - t.bptr[u] : 0;
-      for (int k = 0; k < W; ++k) {
-        const int q = t.sl_off[s] + 32 * k + lane;
-        if (k < deg) {
-          t.sl_col[q] = t.bcol[t.bptr[u] + k];
+      const int k0 = u < nv ? lo_deg[u] : 0;
+      const int du = u < nv ? up_deg[u] : 0;
+      for (int kk = 0; kk < W; ++kk) {
+        const int q = t.sl_off[s] + 32 * kk + lane;
+        if (kk < du) {
+          const int w = t.bcol[t.bptr[u] + k0 + kk];
+          t.sl_col[q] = w;
           t.slot_row[q] = u;
+          t.slot_k[q] = k0 + kk;
+          t.slot_kt[q] = find_pos(t, w, u);
         } else {
           t.sl_col[q] = u < nv ? u : 0;  // padding: a valid column, zero values
-          t.slot_row[q] = -1;
         }
       }
     }
   }
-  // assembly lists (global_composer.hpp:103-119 at block granularity), stable in element order
-  std::vector<int32_t> slot_of(16LL * nt);
-  std::vector<int32_t> ccnt(t.nslots + 1, 0);
-  for (int e = 0; e < nt; ++e)
-    for (int v = 0; v < 4; ++v) {
-      const int u = cells[4 * e + v];
-      const int32_t* nb = t.bcol.data() + t.bptr[u];
-      const int deg = t.bptr[u + 1] - t.bptr[u];
-      for (int w = 0; w < 4; ++w) {
-        const int x = cells[4 * e + w];
-        const int k = (int)(std::lower_bound(nb, nb + deg, x) - nb);
-        const int q = t.sl_off[u >> 5] + 32 * k + (u & 31);
-        slot_of[16LL * e + 4 * v + w] = q;
-        ccnt[q + 1]++;
+  t.lo_src.assign(t.nlslots, -1);
+  t.lo_col.assign(t.nlslots, 0);
+  for (int s = 0; s < t.nslices; ++s) {
+    const int W = (t.lo_off[s + 1] - t.lo_off[s]) / 32;
+    for (int lane = 0; lane < 32; ++lane) {
+      const int u = 32 * s + lane;
+      const int dl = u < nv ? lo_deg[u] : 0;
+      for (int kk = 0; kk < W; ++kk) {
+        const int q = t.lo_off[s] + 32 * kk + lane;
+        if (kk < dl) {
+          const int w = t.bcol[t.bptr[u] + kk];  // w < u
+          t.lo_src[q] = slot_of(w, find_pos(t, w, u) - lo_deg[w]);
+          t.lo_col[q] = w;
+        } else {
+          t.lo_col[q] = u < nv ? u : 0;
+        }
       }
     }
-  for (int q = 0; q < t.nslots; ++q) ccnt[q + 1] += ccnt[q];
-  t.cptr = ccnt;
-  t.csrc.assign(16LL * nt, 0);
-  {
-    std::vector<int32_t> fill(ccnt.begin(), ccnt.end() - 1);
+  }
+  // assembly lists (global_composer.hpp:103-119 at block granularity, upper blocks only), stable in
+  // element order.  A local pair (v, w) lands in global block (cells[v], cells[w]); pairs whose global
+  // block is a lower one are the transposes of pairs already counted, except on the diagonal (a cell
+  // repeating a vertex) where both orientations add, as they do in the reference's full gather.
+  std::vector<int32_t> ccnt(t.nslots + 1, 0);
+  auto visit = [&](auto&& fn) {
     for (int e = 0; e < nt; ++e)
       for (int v = 0; v < 4; ++v)
         for (int w = 0; w < 4; ++w) {
-          const int q = slot_of[16LL * e + 4 * v + w];
+          const int gu = cells[4 * e + v], gw = cells[4 * e + w];
+          if (gu > gw) continue;
+          const int q = slot_of(gu, find_pos(t, gu, gw) - lo_deg[gu]);
           const int lo = std::min(v, w), hi = std::max(v, w);
           int32_t code = (int32_t)(10 * e + upper_block_id(lo, hi));
           if (v > w) code = (int32_t)((uint32_t)code | 0x80000000u);
-          t.csrc[fill[q]++] = code;
+          fn(q, code);
         }
+  };
+  visit([&](int q, int32_t) { ccnt[q + 1]++; });
+  for (int q = 0; q < t.nslots; ++q) ccnt[q + 1] += ccnt[q];
+  t.cptr = ccnt;
+  t.csrc.assign(ccnt[t.nslots], 0);
+  {
+    std::vector<int32_t> fill(ccnt.begin(), ccnt.end() - 1);
+    visit([&](int q, int32_t code) { t.csrc[fill[q]++] = code; });
   }
   // vertex incidence (global_composer.hpp:36-66)
   t.vptr.assign(nv + 1, 0);
@@ -137,8 +184,54 @@ void slot_masses(const Topology& t, const std::vector<double>& detJ, double rho,
       const uint32_t code = (uint32_t)t.csrc[c];
       const int eb = (int)(code & 0x7fffffffu);
       const int e = eb / 10, blk = eb % 10;
-      const bool diag = (blk == 0 || blk == 4 || blk == 7 || blk == 9);
+      const bool diag = kBlkV[blk] == kBlkW[blk];
       m += (detJ[e] * (diag ? 1.0 / 60 : 1.0 / 120)) * rho;  // (|det J| p_ij) * alpha as bilinears.hpp:236,249
+    }
+    out[q] = m;
+  }
+}
+
+void slot_pd_values(const Topology& t, const int32_t* cells, const double* X, const std::vector<double>& detJ,
+                    double rho, double alpha, std::vector<double>& out) {
+  // per element: grad phi_i from the inverse Jacobian (bilinears.hpp:158-167 summed over k = l)
+  std::vector<double> lap(10 * (size_t)t.nt);
+  for (int e = 0; e < t.nt; ++e) {
+    const double* x0 = X + 3 * (size_t)cells[4 * e];
+    double J[9];
+    for (int k = 0; k < 3; ++k) {
+      const double* xk = X + 3 * (size_t)cells[4 * e + k + 1];
+      for (int r = 0; r < 3; ++r) J[r * 3 + k] = xk[r] - x0[r];
+    }
+    const double d = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+    const double id = 1.0 / d;
+    const double B[9] = {(J[4] * J[8] - J[5] * J[7]) * id, (J[2] * J[7] - J[1] * J[8]) * id,
+                         (J[1] * J[5] - J[2] * J[4]) * id, (J[5] * J[6] - J[3] * J[8]) * id,
+                         (J[0] * J[8] - J[2] * J[6]) * id, (J[2] * J[3] - J[0] * J[5]) * id,
+                         (J[3] * J[7] - J[4] * J[6]) * id, (J[1] * J[6] - J[0] * J[7]) * id,
+                         (J[0] * J[4] - J[1] * J[3]) * id};
+    double g[4][3];
+    for (int k = 0; k < 3; ++k) {
+      g[1][k] = B[0 * 3 + k];
+      g[2][k] = B[1 * 3 + k];
+      g[3][k] = B[2 * 3 + k];
+      g[0][k] = -(g[1][k] + g[2][k] + g[3][k]);
+    }
+    for (int b = 0; b < 10; ++b) {
+      const int v = kBlkV[b], w = kBlkW[b];
+      lap[10 * (size_t)e + b] =
+          (detJ[e] / 6.0 * (g[v][0] * g[w][0] + g[v][1] * g[w][1] + g[v][2] * g[w][2])) * alpha;
+    }
+  }
+  out.assign(t.nslots, 0.0);
+  for (int q = 0; q < t.nslots; ++q) {
+    double m = 0;
+    for (int c = t.cptr[q]; c < t.cptr[q + 1]; ++c) {
+      const uint32_t code = (uint32_t)t.csrc[c];
+      const int eb = (int)(code & 0x7fffffffu);
+      const int e = eb / 10, blk = eb % 10;
+      const bool diag = kBlkV[blk] == kBlkW[blk];
+      m += (detJ[e] * (diag ? 1.0 / 60 : 1.0 / 120)) * rho + lap[eb];
     }
     out[q] = m;
   }
