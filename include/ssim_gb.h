@@ -86,7 +86,7 @@ typedef struct {
   double lbfgs_armijo;
   int32_t max_lbfgs_iters;
   int32_t cg_check_every; /* PCG iterations launched between host convergence checks */
-  double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack |E| (round-off floor of E) */
+  double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack * sum|energy terms| (round-off) */
   int32_t pd_kappa_mode;  /* PD matrix diffusivity: 0 as ssim builds it (time_step.hpp:356), 1 from Lame */
 } ssim_gb_params;
 

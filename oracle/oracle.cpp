@@ -91,6 +91,18 @@ inline double snh_stress(const double* F, double lambda, double mu, double* P) {
   return 0.5 * (mu * (Ic - 3.0) + lambda * Jm * Jm - mu * std::log(Ic + kDelta)) - zero_energy;
 }
 
+// sum of the magnitudes of the terms of snh_energy: the scale of its absolute round-off (the terms are
+// O(mu) and cancel to O(mu strain^2), so the round-off of Psi is relative to this, not to Psi)
+inline double snh_energy_scale(const double* F, double lambda, double mu) {
+  double Ic = 0;
+  for (int i = 0; i < 9; ++i) Ic += F[i] * F[i];
+  const double alpha = snh_alpha(lambda, mu);
+  const double Jm = det3(F) - alpha;
+  const double zero_energy = 0.5 * (lambda * (1 - alpha) * (1 - alpha) - mu * std::log(3.0 + kDelta));
+  return 0.5 * (mu * std::fabs(Ic - 3.0) + lambda * Jm * Jm + mu * std::fabs(std::log(Ic + kDelta))) +
+         std::fabs(zero_energy);
+}
+
 // x_hat (internal_physic.hpp:59-63): the cross-product matrix [v]x.
 inline void xhat(const double* v, double s, double* M) {
   M[0] = 0;
@@ -266,6 +278,7 @@ struct orc_ts {
   std::vector<int32_t> fcon_ptr, fcon_src;  // per vertex, the (elem*4+i) that add into it
   bool has_reset = false;
   bool pd_ready = false;
+  double energy_scale = 0;  // sum of term magnitudes of the last energy evaluation (line-search slack)
 
   double lam(int e) const {
     const double Ee = E_elem.empty() ? E : E_elem[e];
@@ -388,10 +401,14 @@ double inertia_term(const orc_ts& s, const Vec& u, Vec* f_out) {
   return e;
 }
 
-double elastic_energy(orc_ts& s) {
-  double sum = 0;
-#pragma omp parallel for reduction(+ : sum) schedule(static)
-  for (int e = 0; e < s.nt; ++e) sum += snh_energy(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+double elastic_energy(orc_ts& s, double* scale) {
+  double sum = 0, sc = 0;
+#pragma omp parallel for reduction(+ : sum, sc) schedule(static)
+  for (int e = 0; e < s.nt; ++e) {
+    sum += snh_energy(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+    sc += snh_energy_scale(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+  }
+  if (scale) *scale = sc * s.dt * s.dt;
   return sum * s.dt * s.dt;
 }
 
@@ -435,15 +452,19 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
   for (int i = 0; i < s.n; ++i)
     if (s.dbc(i)) f[i] = 0;
   s.forces = std::move(f);
-  double elast = 0;
-  for (int e = 0; e < s.nt; ++e) elast += s.local_energy[e] * s.vol[e];
+  double elast = 0, sc = 0;
+  for (int e = 0; e < s.nt; ++e) {
+    elast += s.local_energy[e] * s.vol[e];
+    sc += snh_energy_scale(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+  }
+  s.energy_scale = inertia_energy + sc * s.dt * s.dt;
   return inertia_energy + elast * s.dt * s.dt;
 }
 
 double energy_only(orc_ts& s, const Vec& u) {
   update_def_grad(s, u);
   const double ei = inertia_term(s, u, nullptr);
-  return ei + elastic_energy(s);
+  return ei + elastic_energy(s, nullptr);
 }
 
 // update_hessian (time_step.hpp:626-658)
@@ -691,7 +712,7 @@ void orc_default_params(orc_params* p) {
   p->lbfgs_history = 8;
   p->lbfgs_armijo = 1e-4;
   p->max_lbfgs_iters = 1000;
-  p->ls_energy_slack = 1e-12;
+  p->ls_energy_slack = 1e-14;
 }
 
 orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double dt, double E, double nu,
@@ -835,8 +856,9 @@ void orc_update_hessian(orc_ts* s, int F_updated, int make_spsd, int filter_dbc)
 //   loop: evaluate E, g; stop if the gradient test passes; H = update_hessian(true, make_spsd=true)
 //   (variational_problem::eval_hessian_impl, time_step.hpp:764-768); d from Jacobi-PCG on H d = -g;
 //   backtracking line search from alpha = 1, shrink `ls_shrink`, Armijo constant `armijo`, accepting
-//   E(x + a d) <= E + armijo a g.d + ls_energy_slack |E| (the slack is the round-off floor of the summed
-//   energy: without it the test cannot pass once the Newton decrement falls below that floor); x += a d.
+//   E(x + a d) <= E + armijo a g.d + ls_energy_slack S_E, with S_E the sum of the magnitudes of the
+//   energy's terms (the scale of its round-off: without the slack the test cannot pass once the Newton
+//   decrement falls below that floor); x += a d.
 // Then compute_step (time_step.hpp:520-528) re-evaluates the gradient and returns its norm.
 double orc_compute_step_newton(orc_ts* s, const orc_params* p, orc_stats* st) {
   orc_stats loc{};
@@ -869,11 +891,12 @@ double orc_compute_step_newton(orc_ts* s, const orc_params* p, orc_stats* st) {
       gd = -gn * gn;
     }
     double alpha = 1.0;
+    const double Escale = s->energy_scale;
     for (int ls = 0; ls < p->max_ls_iters; ++ls) {
       for (int i = 0; i < s->n; ++i) xt[i] = s->next[i] + alpha * d[i];
       const double Et = energy_only(*s, xt);
       loc.ls_steps_total++;
-      if (Et <= E + p->armijo * alpha * gd + p->ls_energy_slack * std::fabs(E)) break;
+      if (Et <= E + p->armijo * alpha * gd + p->ls_energy_slack * Escale) break;
       alpha *= p->ls_shrink;
     }
     double ch = 0;
@@ -943,11 +966,12 @@ static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, bool pd)
       gd = dot(g, z);
     }
     double alpha = 1.0;
+    const double Escale = s->energy_scale;
     for (int ls = 0; ls < p->max_ls_iters; ++ls) {
       for (int k = 0; k < n; ++k) xt[k] = s->next[k] + alpha * z[k];
       const double Et = energy_only(*s, xt);
       loc.ls_steps_total++;
-      if (Et <= E + p->lbfgs_armijo * alpha * gd + p->ls_energy_slack * std::fabs(E)) break;
+      if (Et <= E + p->lbfgs_armijo * alpha * gd + p->ls_energy_slack * Escale) break;
       alpha *= p->ls_shrink;
     }
     Vec sv(n), yv(n);

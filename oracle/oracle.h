@@ -77,7 +77,7 @@ typedef struct {
   int lbfgs_history;     /* L-BFGS memory m */
   double lbfgs_armijo;   /* L-BFGS Armijo constant */
   int max_lbfgs_iters;
-  double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack |E| (energy round-off floor) */
+  double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack S_E, S_E = sum of |energy terms| */
 } orc_params;
 
 typedef struct {

@@ -51,10 +51,13 @@ struct DevScalars {
   double energy;          // total incremental potential of the last evaluation
   double gnorm2;          // |g|^2 (Dirichlet dofs zeroed)
   double trial_energy;    // energy at u + alpha * d
+  double energy_scale;    // sum of |energy terms| of the last evaluation (round-off scale)
+  double trial_energy_scale;
   double gd;              // g . d
   double dnorm2;          // |d|^2
   // PCG
   double rz, rz_old, pq, rr, rr0, tol2;
+  double alpha, beta;  // rz / pq and rz / rz_old, formed once by the reducing block
   int32_t iters;
   int32_t done;
   int32_t status;  // 0 ok, 1 breakdown (pq <= 0), 2 non-finite residual

@@ -61,6 +61,19 @@ __host__ __device__ __forceinline__ S snh_stress(const S* F, S lam, S mu, S* P) 
   return S(0.5) * (mu * (Ic - S(3)) + lam * Jm * Jm - mu * log(Ic + S(1))) - zero_energy;
 }
 
+// sum of the magnitudes of the terms of snh_energy: the scale of its absolute round-off (the terms are
+// O(mu) and cancel to O(mu strain^2) near rest); the line search compares energies only above it
+template <typename S>
+__host__ __device__ __forceinline__ S snh_energy_scale(const S* F, S lam, S mu) {
+  S Ic = 0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Ic += F[i] * F[i];
+  const S alpha = S(0.75) * mu / lam + S(1);
+  const S Jm = det3(F) - alpha;
+  const S zero_energy = S(0.5) * (lam * (S(1) - alpha) * (S(1) - alpha) - mu * log(S(4)));
+  return S(0.5) * (mu * fabs(Ic - S(3)) + lam * Jm * Jm + mu * fabs(log(Ic + S(1)))) + fabs(zero_energy);
+}
+
 // ------------------------------------------------------------------ symmetric 3x3 eigen (cyclic Jacobi)
 // A (row-major, symmetric) is diagonalised in place; Q accumulates the rotations (eigenvectors as
 // columns).  Rotation of Golub & Van Loan Alg. 8.5.1 / Numerical Recipes 11.1.

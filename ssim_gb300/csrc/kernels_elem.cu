@@ -31,10 +31,10 @@ __global__ void __launch_bounds__(EB)
                             const double* __restrict__ xt, const V4<SD>* __restrict__ d, double alpha, double dt2,
                             double rho, double* __restrict__ lf, Reduce red) {
   __shared__ double stage[FORCES ? EB * 12 : 1];
-  __shared__ double shred[EB / 32][1];
+  __shared__ double shred[EB / 32][2];
   const int e0 = blockIdx.x * EB;
   const int e = e0 + threadIdx.x;
-  double energy = 0;
+  double energy = 0, escale = 0;
   double lfv[12];
   if (e < el.nt) {
     const int4 c = el.cells[e];
@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(EB)
       psi = snh_energy<double>(F, lam, mu);
     }
     energy = dt2 * V * psi + 0.5 * m * q;
+    escale = dt2 * V * snh_energy_scale<double>(F, lam, mu) + 0.5 * m * q;
   }
   if (FORCES) {
     if (e < el.nt) {
@@ -106,14 +107,17 @@ __global__ void __launch_bounds__(EB)
     double* dst = lf + (size_t)e0 * 12;
     for (int i = threadIdx.x; i < nvalid * 12; i += EB) dst[i] = stage[i];
   }
-  double v1[1] = {energy};
-  block_sum<1, EB>(v1, shred);
-  double tot[1];
-  if (grid_sum_last<1, EB>(v1, red.partials, red.counter, tot)) {
-    if (TRIAL)
+  double v2[2] = {energy, escale};
+  block_sum<2, EB>(v2, shred);
+  double tot[2];
+  if (grid_sum_last<2, EB>(v2, red.partials, red.counter, tot)) {
+    if (TRIAL) {
       red.sc->trial_energy = tot[0];
-    else
+      red.sc->trial_energy_scale = tot[1];
+    } else {
       red.sc->energy = tot[0];
+      red.sc->energy_scale = tot[1];
+    }
   }
 }
 

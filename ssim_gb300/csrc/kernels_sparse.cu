@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(SB)
                     Reduce red) {
   if (*(volatile int*)&red.sc->done) return;
   __shared__ double shred[SB / 32][1];
-  const S beta = first ? S(0) : (S)(red.sc->rz / red.sc->rz_old);
+  const S beta = first ? S(0) : (S)red.sc->beta;
   const int u = blockIdx.x * SB + threadIdx.x;
   double part = 0;
   if (u < A.nv) {
@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(SB)
   double tot[1];
   if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) {
     red.sc->pq = tot[0];
+    red.sc->alpha = red.sc->rz / tot[0];
     if (!(tot[0] > 0.0)) {  // breakdown: not SPD along p (or non-finite)
       red.sc->done = 1;
       red.sc->status = 1;
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(SB)
                       V4<S>* __restrict__ z, int max_iters, Reduce red) {
   if (*(volatile int*)&red.sc->done) return;
   __shared__ double shred[SB / 32][2];
-  const S alpha = (S)(red.sc->rz / red.sc->pq);
+  const S alpha = (S)red.sc->alpha;
   const int u = blockIdx.x * SB + threadIdx.x;
   double part[2] = {0, 0};
   if (u < nv) {
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(SB)
     DevScalars* sc = red.sc;
     sc->rz_old = sc->rz;
     sc->rz = tot[0];
+    sc->beta = tot[0] / sc->rz_old;
     sc->rr = tot[1];
     sc->iters += 1;
     if (!isfinite(tot[1])) {

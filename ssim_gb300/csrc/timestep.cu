@@ -484,6 +484,7 @@ struct TimeStep {
     st.grad_norm0 = g0;
     SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
     const double pd_tol = mixed() ? std::max(params.cg_rtol, 1e-6) : params.cg_rtol;
+    double E0_scale = hsc->energy_scale;
     int it = 0;
     for (;; ++it) {
       st.grad_norm = gn;
@@ -530,18 +531,20 @@ struct TimeStep {
         gd = hsc->gd;
       }
       const double dn = std::sqrt(hsc->dnorm2);
+      const double Escale = E0_scale;
       double alpha = 1.0;
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
         launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.ld.p, alpha, dt * dt, rho, nullptr, false, true,
                                    red(), stream);
         sync_scalars();
         st.ls_steps_total++;
-        if (hsc->trial_energy <= E0 + params.lbfgs_armijo * alpha * gd + params.ls_energy_slack * std::fabs(E0)) break;
+        if (hsc->trial_energy <= E0 + params.lbfgs_armijo * alpha * gd + params.ls_energy_slack * Escale) break;
         alpha *= params.ls_shrink;
       }
       launch_axpy_update<S>(nv, alpha, s.ld.p, dX.p, next.p, nullptr, stream);
       st.last_change = alpha * dn;
       E0 = energy_grad();
+      E0_scale = hsc->energy_scale;
       gn = std::sqrt(hsc->gnorm2);
       // s = alpha d, y = g_new - g_old
       const int slot = head;
@@ -572,11 +575,12 @@ struct TimeStep {
   // newton_optimizer (absent from the reference tree; the definition used is the one restated by the
   // oracle): evaluate; stop on the gradient test; H = update_hessian(true, make_spsd = true); d from
   // Jacobi-PCG on H d = -g; backtracking Armijo line search from alpha = 1 (with the energy round-off
-  // slack ls_energy_slack |E|); x += alpha d.
+  // slack ls_energy_slack * sum of |energy terms|); x += alpha d.
   template <typename S>
   void newton(ssim_gb_step_stats& st) {
     Solver<S>& s = solver<S>();
     double E0 = energy_grad();
+    double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
     st.grad_norm0 = g0;
@@ -607,14 +611,15 @@ struct TimeStep {
       // backtracking line search; each trial evaluates energy and forces at u + alpha d in one element
       // pass, so the accepted trial's forces are the next gradient (no separate evaluation)
       double alpha = 1.0;
-      double Et = 0;
+      double Et = 0, Et_scale = 0;
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
         launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
                                    red(), stream);
         sync_scalars();
         st.ls_steps_total++;
         Et = hsc->trial_energy;
-        if (Et <= E0 + params.armijo * alpha * gd + params.ls_energy_slack * std::fabs(E0)) break;
+        Et_scale = hsc->trial_energy_scale;
+        if (Et <= E0 + params.armijo * alpha * gd + params.ls_energy_slack * Escale) break;
         if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
       launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
@@ -624,6 +629,7 @@ struct TimeStep {
         throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
       st.last_change = alpha * dn;
       E0 = Et;
+      Escale = Et_scale;
       gn = std::sqrt(hsc->gnorm2);
     }
     st.newton_iters = it;
@@ -822,7 +828,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->lbfgs_armijo = 1e-4;
   p->max_lbfgs_iters = 1000;
   p->cg_check_every = 8;
-  p->ls_energy_slack = 1e-12;
+  p->ls_energy_slack = 1e-14;
   p->pd_kappa_mode = 0;
 }
 
