@@ -193,6 +193,27 @@ SSIM_GB_API ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, cons
 SSIM_GB_API ssim_gb_status ssim_gb_pcg(ssim_gb_timestep* h, const double* b, double* x, double rtol, int32_t max_iters,
                            int32_t* iters, double* rel_residual);
 
+/* ---- allocation-free energy (no counterpart in the reference) ----
+ * The incremental potential 1/2 |u - x~|^2_M + dt^2 sum_e V_e Psi(F_e) (the value update_energy_and_gradients
+ * returns, time_step.hpp:577-624) of a tet mesh given entirely by caller-owned device arrays, computed
+ * without allocating device memory.  For callers that cannot call cudaMalloc: code whose device memory is
+ * all owned by another allocator (a framework's caching allocator, a fixed budget taken at start-up) or a
+ * loop that must not pay an allocation's latency or risk its failure.
+ * Inputs (device): X, u, x_tilde [V,3] float64; cells [T,4] int32, 16-byte aligned; dminv [T,3,3] (rows of
+ * Dm^-1, ssim_gb_get_dminv's layout); rest_volume, lambda, mu [T].  Output: *energy_out (device, one
+ * double), written on `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * Scratch: a fixed 128 KiB array inside the library, held by every GPU that loads it until the process
+ * exits.  num_cells above SSIM_GB_NOALLOC_MAX_CELLS is rejected (SSIM_GB_ERR_INVALID_ARGUMENT).  The first
+ * call on a device looks up that array's device address; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (different streams, or different host threads
+ * without ordering) race and give wrong results; calls queued on one stream are safe. */
+#define SSIM_GB_NOALLOC_MAX_CELLS (1 << 20)
+SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, const double* u, const double* x_tilde,
+                                                  const int32_t* cells, const double* dminv,
+                                                  const double* rest_volume, const double* lambda_,
+                                                  const double* mu, int32_t num_cells, double time_step,
+                                                  double density, void* stream, double* energy_out);
+
 /* ---- profiling (CUDA events around the PCG SpMV launches, on the handle's stream) ---- */
 SSIM_GB_API ssim_gb_status ssim_gb_profile_enable(ssim_gb_timestep* h, int32_t enable);
 /* kernel: 0 = PCG SpMV, 1 = element Hessian, 2 = assembly, 3 = gradient element, 4 = PCG update */

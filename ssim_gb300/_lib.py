@@ -139,6 +139,10 @@ _SIGS = {
     "ssim_gb_get_dminv": (C.c_int, [_H, _D]),
     "ssim_gb_spmv": (C.c_int, [_H, C.c_int32, _D, _D]),
     "ssim_gb_pcg": (C.c_int, [_H, _D, _D, C.c_double, C.c_int32, _I, _D]),
+    "ssim_gb_energy_noalloc": (
+        C.c_int,
+        [C.c_void_p] * 8 + [C.c_int32, C.c_double, C.c_double, C.c_void_p, C.c_void_p],
+    ),
     "ssim_gb_profile_enable": (C.c_int, [_H, C.c_int32]),
     "ssim_gb_profile_read": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), _D, _D]),
     "ssim_gb_synchronize": (C.c_int, [_H]),

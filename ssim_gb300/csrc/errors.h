@@ -19,4 +19,7 @@ struct numerical_error : std::runtime_error {
   explicit numerical_error(const std::string& s) : std::runtime_error(s) {}
 };
 
+// message returned by ssim_gb_last_error(NULL) on this thread (entry points without a handle)
+void set_global_error(const std::string& msg);
+
 }  // namespace ssim_gb

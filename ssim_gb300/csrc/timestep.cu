@@ -712,6 +712,11 @@ struct ssim_gb_timestep {
 namespace {
 thread_local std::string g_global_error;
 
+}  // namespace
+
+void ssim_gb::set_global_error(const std::string& msg) { g_global_error = msg; }
+
+namespace {
 ssim_gb_status fail(ssim_gb_timestep* h, ssim_gb_status s, const std::string& msg) {
   if (h)
     h->ts.last_error = msg;
