@@ -50,7 +50,9 @@ typedef enum {
   SSIM_GB_STEPPER_NEWTON = 0, /* time_step_solver_backward_euler<cg<diagonal>> (backward_euler.hpp:9-41) */
   SSIM_GB_STEPPER_LBFGS = 1,  /* time_step_solver_lbfgs (backward_euler.hpp:43-67) */
   SSIM_GB_STEPPER_PD = 2,     /* time_step_solver_pd (projective_dynamics.hpp:9-97) */
-  SSIM_GB_STEPPER_NONE = 3    /* time_step_solver_nothing (time_step.hpp:131-142) */
+  SSIM_GB_STEPPER_NONE = 3,   /* time_step_solver_nothing (time_step.hpp:131-142) */
+  SSIM_GB_STEPPER_FORWARD_EULER = 4, /* time_step_solver_forward_euler (time_step.hpp:717-736) */
+  SSIM_GB_STEPPER_H0 = 5      /* time_step_solver_h0 (projective_dynamics.hpp:100-150) */
 } ssim_gb_stepper;
 
 typedef enum {
@@ -192,6 +194,27 @@ SSIM_GB_API ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, cons
 /* PCG on the current system matrix: x [V,3] in/out (initial guess zero if x_is_guess == 0) */
 SSIM_GB_API ssim_gb_status ssim_gb_pcg(ssim_gb_timestep* h, const double* b, double* x, double rtol, int32_t max_iters,
                            int32_t* iters, double* rel_residual);
+
+/* ---- batched instances (extension; SURVEY config 4): the mesh handed to ssim_gb_create is a disjoint
+ * union of independent meshes whose vertices occupy the contiguous ranges vertex_offsets[i] ..
+ * vertex_offsets[i+1]-1 (num_instances + 1 offsets, first 0, last V).  Every kernel runs over the whole
+ * union; with stop_mode 1 each instance must meet |g_i| <= rel_tol |g_i0| on its own. */
+SSIM_GB_API ssim_gb_status ssim_gb_set_instances(ssim_gb_timestep* h, const int32_t* vertex_offsets,
+                                                 int32_t num_instances);
+/* per-instance |g_i| of the last gradient and |g_i0| at the start of the last compute_step [num_instances] */
+SSIM_GB_API ssim_gb_status ssim_gb_get_instance_residuals(ssim_gb_timestep* h, double* grad_norm, double* grad_norm0);
+
+/* ---- adjoint of one backward-Euler step (extension: the reference has no differentiation) ----
+ * The handle's next_deform must hold u_{n+1}, the state after forward step n.  ubar, vbar (device [V,3]
+ * float64) hold dL/du_{n+1}, dL/dv_{n+1} on entry and dL/du_n, dL/dv_n on exit; ebar (device [T] float64)
+ * accumulates dL/dE_e (Young's modulus per cell).  The linear solve H lambda = ubar uses the exact filtered
+ * Hessian at u_{n+1} and PCG to rtol; *projected = 1 reports a fall-back to the SPD-projected Hessian. */
+SSIM_GB_API ssim_gb_status ssim_gb_adjoint_step(ssim_gb_timestep* h, double* ubar, double* vbar, double* ebar,
+                                                double rtol, int32_t max_iters, int32_t* cg_iters,
+                                                int32_t* projected);
+/* device-to-device copies of a field ([V,3] float64 device buffers), ordered on the handle's stream */
+SSIM_GB_API ssim_gb_status ssim_gb_get_field_device(ssim_gb_timestep* h, int32_t field, double* dst);
+SSIM_GB_API ssim_gb_status ssim_gb_set_field_device(ssim_gb_timestep* h, int32_t field, const double* src);
 
 /* ---- allocation-free energy (no counterpart in the reference) ----
  * The incremental potential 1/2 |u - x~|^2_M + dt^2 sum_e V_e Psi(F_e) (the value update_energy_and_gradients

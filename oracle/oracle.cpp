@@ -916,7 +916,15 @@ double orc_compute_step_newton(orc_ts* s, const orc_params* p, orc_stats* st) {
 // L-BFGS stepper (backward_euler.hpp:43-67) over mathprim's l_bfgs_optimizer (restated here as the
 // two-loop recursion of Nocedal & Wright, Alg. 7.4, with backtracking Armijo line search).  When
 // `Ainv` is set, the initial inverse Hessian is that solve (projective_dynamics.hpp:31-34).
-static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, bool pd) {
+// mode: 0 plain L-BFGS, 1 PD (initial inverse Hessian = PD matrix solve), 2 H0 (= solve with the projected
+// Hessian at the start of the step, time_step_solver_h0, projective_dynamics.hpp:100-150)
+static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, int mode) {
+  const bool pd = mode != 0;
+  Vec h0_vals;
+  if (mode == 2) {
+    update_hessian(*s, false, true, true);  // s.update_hessian(false, true) at the step start
+    h0_vals = s->sys_vals;
+  }
   orc_stats loc{};
   const int n = s->n, m = std::max(1, p->lbfgs_history);
   std::vector<Vec> S, Y;
@@ -946,7 +954,7 @@ static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, bool pd)
     if (pd) {
       std::fill(z.begin(), z.end(), 0.0);
       double rr;
-      pcg(*s, s->pd_vals, q.data(), z.data(), 1e-12, 100000, 1, &rr);
+      pcg(*s, mode == 2 ? h0_vals : s->pd_vals, q.data(), z.data(), 1e-12, 100000, 1, &rr);
     } else {
       double gamma = 1.0 / std::max(gn, 1e-300);
       if (h > 0) gamma = dot(S[h - 1], Y[h - 1]) / dot(Y[h - 1], Y[h - 1]);
@@ -1000,7 +1008,24 @@ static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, bool pd)
   return nrm2(s->forces);
 }
 
-double orc_compute_step_lbfgs(orc_ts* s, const orc_params* p, orc_stats* st) { return lbfgs_core(s, p, st, false); }
+double orc_compute_step_lbfgs(orc_ts* s, const orc_params* p, orc_stats* st) { return lbfgs_core(s, p, st, 0); }
+
+double orc_compute_step_h0(orc_ts* s, const orc_params* p, orc_stats* st) { return lbfgs_core(s, p, st, 2); }
+
+// time_step_solver_forward_euler (time_step.hpp:717-736): evaluate, then next += dt^2/2 * forces (the
+// gradient of the incremental potential, as the reference adds it); compute_step then re-evaluates
+double orc_compute_step_forward_euler(orc_ts* s, const orc_params*, orc_stats* st) {
+  energy_and_gradients(*s, false);
+  const double a = 0.5 * s->dt * s->dt;
+  for (int i = 0; i < s->n; ++i) s->next[i] += a * s->forces[i];
+  const double E = energy_and_gradients(*s, false);
+  if (st) {
+    *st = orc_stats{};
+    st->energy = E;
+    st->grad_norm = nrm2(s->forces);
+  }
+  return nrm2(s->forces);
+}
 
 // PD matrix (projective_dynamics.hpp:53-93): (mass(rho) + laplace(dt^2 * kappa)) (x) I3 with the DBC
 // identity filter.  kappa = approximated_diffusivity (stable_neohookean.hpp:106-111) of
@@ -1031,7 +1056,7 @@ void orc_pd_matrix_values(orc_ts* s, double* out) {
 
 double orc_compute_step_pd(orc_ts* s, const orc_params* p, orc_stats* st) {
   if (!s->pd_ready) orc_pd_matrix_values(s, nullptr);
-  return lbfgs_core(s, p, st, true);
+  return lbfgs_core(s, p, st, 1);
 }
 
 // step_next (time_step.hpp:530-543)

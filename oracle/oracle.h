@@ -126,6 +126,8 @@ void orc_update_hessian(orc_ts* ts, int F_updated, int make_spsd, int filter_dbc
 double orc_compute_step_newton(orc_ts* ts, const orc_params* p, orc_stats* st);
 double orc_compute_step_lbfgs(orc_ts* ts, const orc_params* p, orc_stats* st);
 double orc_compute_step_pd(orc_ts* ts, const orc_params* p, orc_stats* st);
+double orc_compute_step_h0(orc_ts* ts, const orc_params* p, orc_stats* st);
+double orc_compute_step_forward_euler(orc_ts* ts, const orc_params* p, orc_stats* st);
 void orc_step_next(orc_ts* ts);
 void orc_restore(orc_ts* ts);
 int orc_check_convergence(orc_ts* ts);

@@ -130,6 +130,8 @@ def lib():
         "orc_compute_step_newton": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_compute_step_lbfgs": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_compute_step_pd": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
+        "orc_compute_step_h0": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
+        "orc_compute_step_forward_euler": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_step_next": (None, [vp]),
         "orc_restore": (None, [vp]),
         "orc_check_convergence": (C.c_int, [vp]),
@@ -350,6 +352,8 @@ class OracleTimeStep:
             "newton": self._L.orc_compute_step_newton,
             "lbfgs": self._L.orc_compute_step_lbfgs,
             "pd": self._L.orc_compute_step_pd,
+            "h0": self._L.orc_compute_step_h0,
+            "forward_euler": self._L.orc_compute_step_forward_euler,
         }[method]
         r = fn(self._h, C.byref(p), C.byref(st))
         return r, st.as_dict()

@@ -143,6 +143,11 @@ _SIGS = {
         C.c_int,
         [C.c_void_p] * 8 + [C.c_int32, C.c_double, C.c_double, C.c_void_p, C.c_void_p],
     ),
+    "ssim_gb_set_instances": (C.c_int, [_H, _I, C.c_int32]),
+    "ssim_gb_get_instance_residuals": (C.c_int, [_H, _D, _D]),
+    "ssim_gb_adjoint_step": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, _I, _I]),
+    "ssim_gb_get_field_device": (C.c_int, [_H, C.c_int32, C.c_void_p]),
+    "ssim_gb_set_field_device": (C.c_int, [_H, C.c_int32, C.c_void_p]),
     "ssim_gb_profile_enable": (C.c_int, [_H, C.c_int32]),
     "ssim_gb_profile_read": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), _D, _D]),
     "ssim_gb_synchronize": (C.c_int, [_H]),

@@ -98,6 +98,30 @@ __device__ __forceinline__ void block_sum(double (&vals)[NV], double (*sh)[NV]) 
   }
 }
 
+// Block sum of per-thread values of type S: the warp-level tree runs in S (FP32 on the mixed path, so the
+// scarce FP64 pipe is not used per element), each warp's sum is widened to FP64 and the warps are added in
+// FP64 in a fixed order.  Result (FP64) valid in thread 0.
+template <int NV, int BLOCK, typename S>
+__device__ __forceinline__ void block_sum_s(const S (&vals)[NV], double (&out)[NV], double (*sh)[NV]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    S x = vals[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[warp][k] = (double)x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0;
+      for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][k];
+      out[k] = s;
+    }
+  }
+}
+
 // returns true in exactly one thread (thread 0 of the last block), with tot[] = sum of all partials.
 // The last block reads the partials with every thread at once (L2-coherent loads) and combines them in a
 // fixed order, so the result depends only on the grid and block sizes.

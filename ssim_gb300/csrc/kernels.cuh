@@ -119,6 +119,8 @@ void launch_mark_dofs(int n, const int* verts, const double* targ, int dirichlet
 void launch_build_mask(int nv, const int8_t* dof_type, uint8_t* mask, cudaStream_t st);
 template <typename S>
 void launch_to_vec4(int nv, const double* in, V4<S>* out, bool negate, cudaStream_t st);
+// y += a x on FP64 [n] vectors
+void launch_axpy_d(int n, double a, const double* x, double* y, cudaStream_t st);
 // FP64 dot of two S vectors into *out (device), deterministic
 template <typename S>
 void launch_vdot(int nv, const V4<S>* a, const V4<S>* b, double* out, const Reduce& red, cudaStream_t st);
@@ -128,11 +130,23 @@ void launch_vaxpby(int nv, double alpha, V4<S>* y, double beta, const V4<S>* x, 
 // y = (S)(a - b) for FP64 [3V] a, b
 template <typename S>
 void launch_vdiff(int nv, const double* a, const double* b, V4<S>* y, cudaStream_t st);
+// per-instance |g|^2 over contiguous vertex ranges voff[i]..voff[i+1] (one block per instance, fixed order)
+void launch_instance_norms(int ninst, const int* voff, const double* g, double* out, cudaStream_t st);
 // PCG setup from an S right-hand side (the PD stepper's inner solve)
 template <typename S>
 void launch_pcg_setup_v(int nv, const V4<S>* b, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
                         double rtol, int max_iters, const Reduce& red, cudaStream_t st);
 template <typename S>
 void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st);
+
+// ---------------- adjoint (kernels_adjoint.cu) ----------------
+void launch_adj_prep(int n, double kdt, const double* ubar, const double* vbar, const int8_t* dof_type, double* ub,
+                     double* ubp, cudaStream_t st);
+template <typename S>
+void launch_adj_finish(int nv, double dt, const V4<S>* mlam, const int8_t* dof_type, const double* ubp, double* ubar,
+                       double* vbar, cudaStream_t st);
+template <typename S>
+void launch_adj_material(const ElemFP64& el, const double* X, const double* u, const V4<S>* lam_adj, double dt2,
+                         double* Ebar, cudaStream_t st);
 
 }  // namespace ssim_gb

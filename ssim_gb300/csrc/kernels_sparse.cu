@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(SB)
 
 // ------------------------------------------------------------------ PCG
 // Jacobi-PCG (the mathprim cg + diagonal_preconditioner the reference's Newton uses, fem_cu/main.cu:52-54),
-// two fused kernels per iteration.  FP64 dot products, vectors in S.  The search direction is
+// two fused kernels per iteration.  Vectors in S; dot products summed in S within a warp (32 rows) and in
+// FP64 across warps, blocks and the grid.  The search direction is
 // double-buffered: the SpMV kernel forms p_new = z + beta p_old on the fly for every neighbour it reads,
 // so the update of p needs no kernel of its own.
 template <typename S>
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(SB)
                      int negate, Reduce red) {
   __shared__ double shred[SB / 32][2];
   const int u = blockIdx.x * SB + threadIdx.x;
-  double part[2] = {0, 0};
+  S part[2] = {S(0), S(0)};
   if (u < nv) {
     const double sg = negate ? -1.0 : 1.0;
     const S r0 = (S)(sg * g[u * 3 + 0]), r1 = (S)(sg * g[u * 3 + 1]), r2 = (S)(sg * g[u * 3 + 2]);
@@ -234,12 +235,13 @@ __global__ void __launch_bounds__(SB)
     r[u] = mk4<S>(r0, r1, r2);
     z[u] = mk4<S>(z0, z1, z2);
     p0[u] = mk4<S>(0, 0, 0);
-    part[0] = (double)r0 * z0 + (double)r1 * z1 + (double)r2 * z2;
-    part[1] = (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
+    part[0] = r0 * z0 + r1 * z1 + r2 * z2;
+    part[1] = r0 * r0 + r1 * r1 + r2 * r2;
   }
-  block_sum<2, SB>(part, shred);
+  double bs[2];
+  block_sum_s<2, SB, S>(part, bs, shred);
   double tot[2];
-  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
+  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) {
     DevScalars* sc = red.sc;
     sc->rz = tot[0];
     sc->rz_old = 1.0;
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(SB)
   __shared__ double shred[SB / 32][1];
   const S beta = first ? S(0) : (S)red.sc->beta;
   const int u = blockIdx.x * SB + threadIdx.x;
-  double part = 0;
+  S part[1] = {S(0)};
   if (u < A.nv) {
     S a0, a1, a2;
     row_product<S>(A, vals, u, z, p_old, beta, a0, a1, a2);
@@ -269,10 +271,10 @@ __global__ void __launch_bounds__(SB)
     const V4<S> pn = mk4<S>(zu.x + beta * pu.x, zu.y + beta * pu.y, zu.z + beta * pu.z);
     p_new[u] = pn;
     q[u] = mk4<S>(a0, a1, a2);
-    part = (double)pn.x * a0 + (double)pn.y * a1 + (double)pn.z * a2;
+    part[0] = pn.x * a0 + pn.y * a1 + pn.z * a2;
   }
-  double v1[1] = {part};
-  block_sum<1, SB>(v1, shred);
+  double v1[1];
+  block_sum_s<1, SB, S>(part, v1, shred);
   double tot[1];
   if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) {
     red.sc->pq = tot[0];
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(SB)
   __shared__ double shred[SB / 32][2];
   const S alpha = (S)red.sc->alpha;
   const int u = blockIdx.x * SB + threadIdx.x;
-  double part[2] = {0, 0};
+  S part[2] = {S(0), S(0)};
   if (u < nv) {
     const V4<S> pu = p[u], qu = q[u];
     const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
@@ -309,12 +311,13 @@ __global__ void __launch_bounds__(SB)
     x[u] = xu;
     r[u] = ru;
     z[u] = zu;
-    part[0] = (double)ru.x * zu.x + (double)ru.y * zu.y + (double)ru.z * zu.z;
-    part[1] = (double)ru.x * ru.x + (double)ru.y * ru.y + (double)ru.z * ru.z;
+    part[0] = ru.x * zu.x + ru.y * zu.y + ru.z * zu.z;
+    part[1] = ru.x * ru.x + ru.y * ru.y + ru.z * ru.z;
   }
-  block_sum<2, SB>(part, shred);
+  double bs[2];
+  block_sum_s<2, SB, S>(part, bs, shred);
   double tot[2];
-  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
+  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) {
     DevScalars* sc = red.sc;
     sc->rz_old = sc->rz;
     sc->rz = tot[0];
@@ -412,6 +415,11 @@ __global__ void restore_kernel(int n, double inv_dt, const int8_t* __restrict__ 
   v[i] = (u[i] - prev[i]) * inv_dt;
 }
 
+__global__ void axpy_d_kernel(int n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  const int i = blockIdx.x * SB + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
 __global__ void add_ext_kernel(int nv, int dof, double val, double* __restrict__ a) {
   const int v = blockIdx.x * SB + threadIdx.x;
   if (v < nv) a[v * 3 + dof] += val;
@@ -442,13 +450,13 @@ __global__ void __launch_bounds__(SB)
     vdot_kernel(int nv, const V4<S>* __restrict__ a, const V4<S>* __restrict__ b, double* out, Reduce red) {
   __shared__ double shred[SB / 32][1];
   const int u = blockIdx.x * SB + threadIdx.x;
-  double part = 0;
+  S part[1] = {S(0)};
   if (u < nv) {
     const V4<S> x = a[u], y = b[u];
-    part = (double)x.x * y.x + (double)x.y * y.y + (double)x.z * y.z;
+    part[0] = x.x * y.x + x.y * y.y + x.z * y.z;
   }
-  double v1[1] = {part};
-  block_sum<1, SB>(v1, shred);
+  double v1[1];
+  block_sum_s<1, SB, S>(part, v1, shred);
   double tot[1];
   if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) *out = tot[0];
 }
@@ -479,7 +487,7 @@ __global__ void __launch_bounds__(SB)
                        int max_iters, Reduce red) {
   __shared__ double shred[SB / 32][2];
   const int u = blockIdx.x * SB + threadIdx.x;
-  double part[2] = {0, 0};
+  S part[2] = {S(0), S(0)};
   if (u < nv) {
     const V4<S> rb = bv[u];
     const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
@@ -490,12 +498,13 @@ __global__ void __launch_bounds__(SB)
     r[u] = mk4<S>(rb.x, rb.y, rb.z);
     z[u] = mk4<S>(z0, z1, z2);
     p0[u] = mk4<S>(0, 0, 0);
-    part[0] = (double)rb.x * z0 + (double)rb.y * z1 + (double)rb.z * z2;
-    part[1] = (double)rb.x * rb.x + (double)rb.y * rb.y + (double)rb.z * rb.z;
+    part[0] = rb.x * z0 + rb.y * z1 + rb.z * z2;
+    part[1] = rb.x * rb.x + rb.y * rb.y + rb.z * rb.z;
   }
-  block_sum<2, SB>(part, shred);
+  double bs[2];
+  block_sum_s<2, SB, S>(part, bs, shred);
   double tot[2];
-  if (grid_sum_last<2, SB>(part, red.partials, red.counter, tot)) {
+  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) {
     DevScalars* sc = red.sc;
     sc->rz = tot[0];
     sc->rz_old = 1.0;
@@ -506,6 +515,18 @@ __global__ void __launch_bounds__(SB)
     sc->status = 0;
     sc->done = (tot[1] <= sc->tol2 || tot[1] == 0.0 || max_iters <= 0) ? 1 : 0;
   }
+}
+
+__global__ void __launch_bounds__(SB)
+    instance_norms_kernel(const int* __restrict__ voff, const double* __restrict__ g, double* __restrict__ out) {
+  __shared__ double shred[SB / 32][1];
+  const int i = blockIdx.x;
+  const long long a = 3LL * voff[i], b = 3LL * voff[i + 1];
+  double part = 0;
+  for (long long k = a + threadIdx.x; k < b; k += SB) part += g[k] * g[k];
+  double v1[1] = {part};
+  block_sum<1, SB>(v1, shred);
+  if (threadIdx.x == 0) out[i] = v1[0];
 }
 
 template <typename S>
@@ -612,6 +633,11 @@ void launch_restore(int n, double dt, const int8_t* dof_type, const double* dbc,
   after_launch("restore");
 }
 
+void launch_axpy_d(int n, double a, const double* x, double* y, cudaStream_t st) {
+  axpy_d_kernel<<<div_up(n, SB), SB, 0, st>>>(n, a, x, y);
+  after_launch("axpy_d");
+}
+
 void launch_add_ext(int nv, int dof, double val, double* a, cudaStream_t st) {
   add_ext_kernel<<<div_up(nv, SB), SB, 0, st>>>(nv, dof, val, a);
   after_launch("add_ext");
@@ -664,6 +690,12 @@ void launch_pcg_setup_v(int nv, const V4<S>* b, const V4<S>* dinv, V4<S>* x, V4<
                         double rtol, int max_iters, const Reduce& red, cudaStream_t st) {
   pcg_setup_v_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, b, dinv, x, r, z, p0, rtol, max_iters, red);
   after_launch("pcg_setup_v");
+}
+
+void launch_instance_norms(int ninst, const int* voff, const double* g, double* out, cudaStream_t st) {
+  if (ninst <= 0) return;
+  instance_norms_kernel<<<ninst, SB, 0, st>>>(voff, g, out);
+  after_launch("instance_norms");
 }
 
 #define SSIM_INST(S)                                                                                              \

@@ -107,6 +107,13 @@ struct TimeStep {
   DBuf<DevScalars> sc;
   DevScalars* hsc = nullptr;  // pinned
   DBuf<double> gprev, dscal;   // previous gradient (L-BFGS), device scalars of vdot
+  // batched instances: the mesh is a disjoint union of independent meshes with contiguous vertex ranges;
+  // with stop_mode 1 every instance must meet |g_i| <= rel_tol |g_i0| on its own
+  int ninst = 0;
+  std::vector<int32_t> inst_off_h;
+  DBuf<int32_t> inst_off;
+  DBuf<double> inst_g2;
+  std::vector<double> inst_g2_h, inst_g0_h;
   double* hscal = nullptr;     // pinned mirror of dscal
   // ---- profiling
   bool profiling = false;
@@ -234,7 +241,7 @@ struct TimeStep {
     if (!(E >= 0)) throw invalid_argument("Young's modulus must be positive, got " + std::to_string(E));
     if (!(nu > 0 && nu < 0.5)) throw invalid_argument("Poisson's ratio must be in (0, 0.5), got " + std::to_string(nu));
     if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
-    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NONE) throw invalid_argument("unknown stepper");
+    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_H0) throw invalid_argument("unknown stepper");
     stepper = stepper_kind;
     for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
     // material: per element Lame parameters (basic_elast.hpp:10-20)
@@ -254,8 +261,9 @@ struct TimeStep {
     // rtol * asum(mass CSR values) / 3; each slot's scalar appears on the 3 diagonal dofs of its block
     std::vector<double> smass;
     slot_masses(topo, detJ, rho, smass);
-    double asum = 0;
-    for (double v : smass) asum += 3.0 * std::fabs(v);
+    double asum = 0;  // the full CSR holds every off-diagonal block twice (the store keeps the upper one)
+    for (int q = 0; q < topo.nslots; ++q)
+      if (topo.slot_row[q] >= 0) asum += (topo.sl_col[q] == topo.slot_row[q] ? 3.0 : 6.0) * std::fabs(smass[q]);
     abs_tol = asum / 3.0 * rtol;
     if (mixed()) {
       std::vector<float> sm(smass.begin(), smass.end());
@@ -460,6 +468,28 @@ struct TimeStep {
     return hsc->iters;
   }
 
+  // per-instance |g_i|^2 of the current forces (host copy in inst_g2_h)
+  void instance_norms() {
+    launch_instance_norms(ninst, inst_off.p, forces.p, inst_g2.p, stream);
+    SSIM_CUDA(cudaMemcpyAsync(inst_g2_h.data(), inst_g2.p, sizeof(double) * ninst, cudaMemcpyDeviceToHost, stream));
+    SSIM_CUDA(cudaStreamSynchronize(stream));
+  }
+  void start_instances() {
+    if (ninst <= 1 || params.stop_mode != 1) return;
+    instance_norms();
+    for (int i = 0; i < ninst; ++i) inst_g0_h[i] = std::sqrt(inst_g2_h[i]);
+  }
+  // the stopping test: the reference's absolute rule (stop_mode 0), the relative rule on the whole vector,
+  // or, for a batch, the relative rule on every instance
+  bool stop_test(double gn, double g0) {
+    if (params.stop_mode == 0) return gn < abs_tol;
+    if (ninst <= 1) return gn <= params.rel_tol * g0;
+    instance_norms();
+    for (int i = 0; i < ninst; ++i)
+      if (std::sqrt(inst_g2_h[i]) > params.rel_tol * inst_g0_h[i]) return false;
+    return true;
+  }
+
   template <typename S>
   double vdot(const V4<S>* a, const V4<S>* b) {
     launch_vdot<S>(nv, a, b, dscal.p, red(), stream);
@@ -473,8 +503,21 @@ struct TimeStep {
   // any history), backtracking Armijo line search).  With pd, the initial inverse Hessian is the PD matrix
   // solve (projective_dynamics.hpp:31-34), done here by PCG to pd tolerance instead of a factorisation.
   template <typename S>
-  void lbfgs(ssim_gb_step_stats& st, bool pd) {
+  void lbfgs(ssim_gb_step_stats& st, bool pd, bool h0 = false) {
     Solver<S>& s = solver<S>();
+    if (h0) {
+      // time_step_solver_h0 (projective_dynamics.hpp:100-150): the projected Hessian at the step start is
+      // the initial inverse Hessian (the reference factorises it; here it is applied by PCG)
+      if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+      hessian<S>(true, true);
+      s.pd_vals.alloc(9 * (size_t)topo.nslots);
+      s.pd_dinv.alloc(3 * (size_t)nv);
+      SSIM_CUDA(cudaMemcpyAsync(s.pd_vals.p, s.vals.p, sizeof(S) * 9 * (size_t)topo.nslots, cudaMemcpyDeviceToDevice,
+                                stream));
+      SSIM_CUDA(cudaMemcpyAsync(s.pd_dinv.p, s.dinv.p, sizeof(V4<S>) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice,
+                                stream));
+      pd = true;
+    }
     const int m = std::max(1, std::min(params.lbfgs_history, (int)s.hs.size()));
     std::vector<double> rho_h(m, 0.0), al(m, 0.0);
     int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
@@ -482,6 +525,7 @@ struct TimeStep {
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
     st.grad_norm0 = g0;
+    start_instances();
     SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
     const double pd_tol = mixed() ? std::max(params.cg_rtol, 1e-6) : params.cg_rtol;
     double E0_scale = hsc->energy_scale;
@@ -489,8 +533,7 @@ struct TimeStep {
     for (;; ++it) {
       st.grad_norm = gn;
       st.energy = E0;
-      const bool ok = params.stop_mode == 0 ? (gn < abs_tol) : (gn <= params.rel_tol * g0);
-      if (ok) {
+      if (stop_test(gn, g0)) {
         st.converged = 1;
         break;
       }
@@ -570,6 +613,35 @@ struct TimeStep {
     return up * (9.0 * s + 4.0) + lo * 8.0 + lo_real * 9.0 * s + 2.0 * (topo.nslices + 1) * 4 + 2.0 * nv * 4 * s;
   }
 
+  // ------------------------------------------------------------------ adjoint of one step
+  // The handle's next_deform holds u_{n+1}.  ubar, vbar (device [n]) hold the adjoint of (u_{n+1}, v_{n+1}) on
+  // entry and of (u_n, v_n) on exit; ebar (device [T]) accumulates dL/dE_e.  Returns the PCG iterations;
+  // *projected = 1 when the exact Hessian was not positive definite along the CG directions and the solve
+  // fell back to the SPD-projected one.
+  template <typename S>
+  int adjoint_step(double* ubar, double* vbar, double* ebar, double rtol, int max_iters, int* projected) {
+    Solver<S>& s = solver<S>();
+    if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+    hessian<S>(false, true);
+    launch_adj_prep(n, (1.0 - damping) / dt, ubar, vbar, dof_type.p, work.p, gprev.p, stream);
+    double rr = 0;
+    int it = pcg<S>(work.p, false, rtol, max_iters, &rr);
+    int proj = 0;
+    if (hsc->status == 1) {  // indefinite along a CG direction: use the projected Hessian
+      hessian<S>(true, true);
+      it += pcg<S>(work.p, false, rtol, max_iters, &rr);
+      proj = 1;
+    }
+    if (projected) *projected = proj;
+    s.mvals.alloc(9 * (size_t)topo.nslots);
+    launch_assemble<S>(A(), cptr.p, csrc.p, nullptr, s.slot_mass.p, mask.p, false, s.mvals.p, nullptr, 0, stream);
+    launch_spmv<S>(A(), s.mvals.p, s.x.p, s.q.p, stream);
+    launch_adj_finish<S>(nv, dt, s.q.p, dof_type.p, gprev.p, ubar, vbar, stream);
+    launch_adj_material<S>(e64(), dX.p, next.p, s.x.p, dt * dt, ebar, stream);
+    SSIM_CUDA(cudaStreamSynchronize(stream));
+    return it;
+  }
+
   // ------------------------------------------------------------------ Newton stepper
   // time_step_solver_backward_euler::solve_impl (backward_euler.hpp:15-33) over mathprim's
   // newton_optimizer (absent from the reference tree; the definition used is the one restated by the
@@ -584,12 +656,12 @@ struct TimeStep {
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
     st.grad_norm0 = g0;
+    start_instances();
     int it = 0;
     for (;; ++it) {
       st.grad_norm = gn;
       st.energy = E0;
-      const bool ok = params.stop_mode == 0 ? (gn < abs_tol) : (gn <= params.rel_tol * g0);
-      if (ok) {
+      if (stop_test(gn, g0)) {
         st.converged = 1;
         break;
       }
@@ -650,6 +722,19 @@ struct TimeStep {
         lbfgs<float>(st, stepper == SSIM_GB_STEPPER_PD);
       else
         lbfgs<double>(st, stepper == SSIM_GB_STEPPER_PD);
+    } else if (stepper == SSIM_GB_STEPPER_H0) {
+      if (mixed())
+        lbfgs<float>(st, false, true);
+      else
+        lbfgs<double>(st, false, true);
+    } else if (stepper == SSIM_GB_STEPPER_FORWARD_EULER) {
+      // time_step_solver_forward_euler (time_step.hpp:717-736): evaluate, next += dt^2 / 2 * forces; then
+      // the re-evaluation of compute_step
+      energy_grad();
+      launch_axpy_d(n, 0.5 * dt * dt, forces.p, next.p, stream);
+      st.energy = energy_grad();
+      st.grad_norm = st.grad_norm0 = std::sqrt(hsc->gnorm2);
+      st.converged = 1;
     } else {
       // time_step_solver_nothing: no solve; the gradient is still evaluated
       st.energy = energy_grad();
@@ -1257,6 +1342,76 @@ ssim_gb_status ssim_gb_pcg(ssim_gb_timestep* h, const double* b, double* x, doub
   const int it = t.mixed() ? do_pcg<float>(t, b, x, rtol, max_iters, &rr) : do_pcg<double>(t, b, x, rtol, max_iters, &rr);
   if (iters) *iters = it;
   if (rel_residual) *rel_residual = rr;
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_set_instances(ssim_gb_timestep* h, const int32_t* vertex_offsets, int32_t num_instances) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (num_instances < 0 || (num_instances > 0 && !vertex_offsets)) throw ssim_gb::invalid_argument("invalid instances");
+  if (num_instances > 0) {
+    if (vertex_offsets[0] != 0 || vertex_offsets[num_instances] != t.nv)
+      throw ssim_gb::invalid_argument("instance offsets must run from 0 to the number of vertices");
+    for (int i = 0; i < num_instances; ++i)
+      if (vertex_offsets[i + 1] <= vertex_offsets[i]) throw ssim_gb::invalid_argument("instance offsets must increase");
+  }
+  t.ninst = num_instances;
+  t.inst_off_h.assign(vertex_offsets, vertex_offsets + (num_instances > 0 ? num_instances + 1 : 0));
+  t.inst_off.upload(t.inst_off_h, t.stream);
+  t.inst_g2.alloc(std::max(1, num_instances));
+  t.inst_g2_h.assign(std::max(1, num_instances), 0.0);
+  t.inst_g0_h.assign(std::max(1, num_instances), 0.0);
+  SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_get_instance_residuals(ssim_gb_timestep* h, double* grad_norm, double* grad_norm0) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (t.ninst <= 0) throw ssim_gb::state_error("no instances set");
+  t.instance_norms();
+  for (int i = 0; i < t.ninst; ++i) {
+    if (grad_norm) grad_norm[i] = std::sqrt(t.inst_g2_h[i]);
+    if (grad_norm0) grad_norm0[i] = t.inst_g0_h[i];
+  }
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_adjoint_step(ssim_gb_timestep* h, double* ubar, double* vbar, double* ebar, double rtol,
+                                    int32_t max_iters, int32_t* cg_iters, int32_t* projected) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!ubar || !vbar || !ebar) throw ssim_gb::invalid_argument("null adjoint buffer");
+  if (!(rtol > 0) || max_iters <= 0) throw ssim_gb::invalid_argument("invalid adjoint solve tolerance");
+  if (!t.has_reset) throw ssim_gb::state_error("adjoint_step() before reset()");
+  int proj = 0;
+  const int it = t.mixed() ? t.adjoint_step<float>(ubar, vbar, ebar, rtol, max_iters, &proj)
+                           : t.adjoint_step<double>(ubar, vbar, ebar, rtol, max_iters, &proj);
+  if (cg_iters) *cg_iters = it;
+  if (projected) *projected = proj;
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_get_field_device(ssim_gb_timestep* h, int32_t field, double* dst) {
+  CHECK_H(h);
+  API_TRY
+  auto* b = field_buf(h->ts, field);
+  if (!b || !dst) throw ssim_gb::invalid_argument("unknown field or null output");
+  SSIM_CUDA(cudaMemcpyAsync(dst, b->p, sizeof(double) * h->ts.n, cudaMemcpyDeviceToDevice, h->ts.stream));
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
+  API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_set_field_device(ssim_gb_timestep* h, int32_t field, const double* src) {
+  CHECK_H(h);
+  API_TRY
+  auto* b = field_buf(h->ts, field);
+  if (!b || !src) throw ssim_gb::invalid_argument("unknown field or null input");
+  SSIM_CUDA(cudaMemcpyAsync(b->p, src, sizeof(double) * h->ts.n, cudaMemcpyDeviceToDevice, h->ts.stream));
+  SSIM_CUDA(cudaStreamSynchronize(h->ts.stream));
   API_CATCH(h)
 }
 

@@ -138,3 +138,63 @@ def build_oracle(scene, rtol=None):
         ts.set("deformation", scene["u0"])
         ts.set("prev_deform", scene["u0"])
     return ts
+
+
+def batch_cubes(n=256, kmin=4, kmax=24, seed=4, dt=1e-2, rho=1000.0):
+    """Batched instances: n unit cubes with per-side hex counts k ~ U{kmin..kmax} (6 tets per hex), E
+    log-uniform in [1e4, 1e6], nu ~ U[0.3, 0.48] and one initial velocity per cube with N(0, 0.5^2)
+    components (SplitMix64 stream ``seed``); bottom face (z = 0) fixed; no gravity; dt = 1e-2."""
+    ks = kmin + np.floor(mesh.uniform(seed, n, 0.0, 1.0) * (kmax - kmin + 1)).astype(int)
+    E = 10.0 ** mesh.uniform(seed, n, 4.0, 6.0, offset=n)
+    nu = mesh.uniform(seed, n, 0.3, 0.48, offset=2 * n)
+    v0 = 0.5 * mesh.normal(seed, 3 * n, offset=3 * n).reshape(n, 3)
+    Xs, Ts, voff, E_cells, nu_cells, fixed, vel = [], [], [0], [], [], [], []
+    for i, k in enumerate(ks):
+        X, T = mesh.kuhn_box((int(k), int(k), int(k)))
+        Ts.append(T + voff[-1])
+        Xs.append(X)
+        fixed.append(np.where(X[:, 2] == 0.0)[0] + voff[-1])
+        vel.append(np.tile(v0[i], (X.shape[0], 1)))
+        E_cells.append(np.full(T.shape[0], E[i]))
+        nu_cells.append(np.full(T.shape[0], nu[i]))
+        voff.append(voff[-1] + X.shape[0])
+    return dict(
+        name=f"batch{n}_cubes_k{kmin}-{kmax}",
+        X=np.concatenate(Xs), cells=np.concatenate(Ts).astype(np.int32), vertex_offsets=np.array(voff, dtype=np.int32),
+        k=ks, E_inst=E, nu_inst=nu, v0_inst=v0, E_cells=np.concatenate(E_cells), nu_cells=np.concatenate(nu_cells),
+        fixed=np.concatenate(fixed), velocity=np.concatenate(vel), dt=dt, E=1e5, nu=0.4, rho=rho,
+        gravity=(0.0, 0.0, 0.0), steps=10, u0=None,
+    )
+
+
+def build_batch_timestep(batch, precision="mixed", params=None):
+    """One GPU TimeStep over the disjoint union of the batch's cubes (per-cell material, per-instance
+    stopping test)."""
+    from .timestep import TimeStep
+
+    ts = TimeStep(batch["X"], batch["cells"], batch["dt"], batch["E"], batch["nu"], batch["rho"])
+    ts.set_precision(precision)
+    ts.set_material(batch["E_cells"], batch["nu_cells"])
+    ts.mark_dirichlet_batched(batch["fixed"], np.zeros((len(batch["fixed"]), 3)))
+    ts.set_instances(batch["vertex_offsets"])
+    if params is not None:
+        ts.set_params(params)
+    ts.reset("newton")
+    ts.set("velocity", batch["velocity"])
+    return ts
+
+
+def batch_instance_oracle(batch, i):
+    """Instance i of the batch on the FP64 oracle (test infrastructure)."""
+    from oracle import pyoracle
+
+    a, b = batch["vertex_offsets"][i], batch["vertex_offsets"][i + 1]
+    X = batch["X"][a:b]
+    cells = batch["cells"]
+    sel = (cells[:, 0] >= a) & (cells[:, 0] < b)
+    T = cells[sel] - a
+    ot = pyoracle.OracleTimeStep(X, T, batch["dt"], batch["E_inst"][i], batch["nu_inst"][i], batch["rho"])
+    ot.mark_dirichlet(np.where(X[:, 2] == 0.0)[0])
+    ot.reset()
+    ot.set("velocity", batch["velocity"][a:b])
+    return ot

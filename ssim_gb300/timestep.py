@@ -153,7 +153,7 @@ class TimeStep:
     # ---------------------------------------------------------------- loop
     def reset(self, stepper: int | str | None = None):
         if isinstance(stepper, str):
-            stepper = {"newton": 0, "lbfgs": 1, "pd": 2, "none": 3}[stepper]
+            stepper = {"newton": 0, "lbfgs": 1, "pd": 2, "none": 3, "forward_euler": 4, "h0": 5}[stepper]
         if stepper is not None:
             self._stepper = int(stepper)
         self._c(self._L.ssim_gb_reset(self._h, self._stepper))
@@ -285,6 +285,18 @@ class TimeStep:
         it, rr = C.c_int32(), C.c_double()
         self._c(self._L.ssim_gb_pcg(self._h, dptr(bv), dptr(x), rtol, max_iters, C.byref(it), C.byref(rr)))
         return x.reshape(-1, 3), it.value, rr.value
+
+    # ---------------------------------------------------------------- batched instances
+    def set_instances(self, vertex_offsets):
+        off = np.ascontiguousarray(vertex_offsets, dtype=np.int32).reshape(-1)
+        self._c(self._L.ssim_gb_set_instances(self._h, iptr(off), off.size - 1))
+        self._ninst = off.size - 1
+
+    def instance_residuals(self):
+        g = np.zeros(self._ninst)
+        g0 = np.zeros(self._ninst)
+        self._c(self._L.ssim_gb_get_instance_residuals(self._h, dptr(g), dptr(g0)))
+        return g, g0
 
     # ---------------------------------------------------------------- profiling
     def profile(self, enable: bool = True):

@@ -320,3 +320,43 @@ def test_lbfgs_mixed_reaches_residual():
         ts.step()
         st = ts.stats()
         assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"]
+
+
+def test_forward_euler_matches_oracle():
+    """time_step_solver_forward_euler (time_step.hpp:717-736) restated: one explicit update per step."""
+    from oracle import pyoracle
+
+    scene = scenes.cube10()
+    ts = scenes.build_timestep(scene, precision="fp64", stepper="forward_euler")
+    ot = scenes.build_oracle(scene)
+    for _ in range(3):
+        ts.prepare_step()
+        r = ts.compute_step()
+        ts.step_next()
+        ot.prepare_step()
+        ro, _ = ot.compute_step("forward_euler", pyoracle.default_params())
+        ot.step_next()
+        assert abs(r - ro) <= 1e-9 * abs(ro)
+    assert rel(ts.get("deformation"), ot.get("deformation")) <= FP64_RTOL
+
+
+def test_h0_stepper_fp64():
+    """time_step_solver_h0 (projective_dynamics.hpp:100-150): L-BFGS preconditioned by the projected
+    Hessian at the start of the step; converged state equals the oracle's."""
+    from oracle import pyoracle
+
+    scene = scenes.cube10()
+    params = g.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-11, max_lbfgs_iters=5000, precond=2)
+    ts = scenes.build_timestep(scene, precision="fp64", stepper="h0", params=params)
+    ot = scenes.build_oracle(scene)
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=5000)
+    for _ in range(3):
+        ts.prepare_step()
+        ts.compute_step()
+        st = ts.stats()
+        ts.step_next()
+        ot.prepare_step()
+        _, sto = ot.compute_step("h0", op)
+        ot.step_next()
+        assert st["converged"] == 1 and sto["converged"] == 1
+    assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6
