@@ -74,7 +74,7 @@ def ncu_traffic(workload):
 
 
 class ClockSampler:
-    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    """nvidia-smi sampled every 100 ms while the timed region runs."""
 
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
 
@@ -86,11 +86,12 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"],
+                 "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
             )
         except FileNotFoundError:
             self.proc = None
+        time.sleep(1.0)  # let nvidia-smi start sampling before the timed region
         return self
 
     def __exit__(self, *a):
@@ -140,6 +141,12 @@ def run_gpu_arm(args, scene):
     ts.set_stream(stream.cuda_stream)
     zeros = np.zeros_like(scene["X"])
 
+    import torch.distributed as tdist
+
+    def barrier():
+        if tdist.is_available() and tdist.is_initialized():
+            tdist.barrier()
+
     def timed_run(precision, steps, warmup, profile=False):
         # restart from rest: same initial state for every run
         ts.set_precision(precision)
@@ -150,6 +157,7 @@ def run_gpu_arm(args, scene):
             ts.step()
         ts.profile(profile)
         torch.cuda.synchronize()
+        barrier()
         stats = []
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = g.launch_count()
@@ -159,6 +167,7 @@ def run_gpu_arm(args, scene):
             stats.append(ts.stats())
         end.record(stream)
         torch.cuda.synchronize()
+        barrier()
         ms = start.elapsed_time(end)
         launches = g.launch_count() - l0
         prof = ts.profile_read("pcg_spmv") if profile else None
@@ -194,6 +203,7 @@ def run_gpu_arm(args, scene):
         s.step()
         _ = s.deformation()
     torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         s.mark_dirichlet_batched(fixed, targ_np)
@@ -201,12 +211,50 @@ def run_gpu_arm(args, scene):
         d = s.deformation()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    barrier()
     result.update(
         ms_mixed=ms_mixed, ms_fp64=ms_fp64, st_mixed=st_mixed, st_fp64=st_fp64, launches=launches, prof=prof,
         clocks=clocks, e2e_s=e2e_s, h2d=fixed.size * 3 * 8 + fixed.size * 4, d2h=d.size * 8,
-        total_launches=g.launch_count() - launches0,
+        total_launches=g.launch_count() - launches0, nnz=ts.nnz,
     )
+    if args.adjoint:
+        result["adjoint"] = [run_adjoint("mixed"), run_adjoint("fp64")]
     return result
+
+
+def run_adjoint(precision, n=32, steps=40, checkpoint_every=8):
+    """Differentiable rollout (32^3 hex x 6 = 196,608 tets, 40 steps, checkpoints every 8): wall time of the
+    forward rollout and of the backward pass (segment recomputation + one adjoint solve per step), per
+    step, with the headline Newton settings and the adjoint PCG at the same 1e-6 relative tolerance."""
+    import torch
+
+    import ssim_gb300 as g
+    from ssim_gb300 import adjoint, scenes
+
+    sc = scenes.rollout_cube(n)
+    eng = adjoint.RolloutEngine(sc["X"], sc["cells"], sc["fixed"], dt=sc["dt"], nu=sc["nu"], rho=sc["rho"],
+                                precision=precision, params=newton_params(g), adjoint_rtol=1e-6)
+    E = torch.tensor(sc["E_cells"], dtype=torch.float64, device="cuda", requires_grad=True)
+    v0 = torch.tensor(sc["v0"], dtype=torch.float64, device="cuda", requires_grad=True)
+    Xt = torch.tensor(sc["X"], dtype=torch.float64, device="cuda")
+    target = torch.tensor(sc["target"], dtype=torch.float64, device="cuda")
+    # one untimed short rollout (allocations, first-use costs)
+    adjoint.rollout(E, v0, eng, 2, checkpoint_every)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = adjoint.rollout(E, v0, eng, steps, checkpoint_every)
+    loss = ((Xt + u - target) ** 2).sum()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    it0 = eng.cg_iters
+    loss.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"precision": precision, "workload": sc["name"], "steps": steps, "checkpoint_every": checkpoint_every,
+            "forward_ms_per_step": round((t1 - t0) * 1e3 / steps, 3),
+            "adjoint_ms_per_step": round((t2 - t1) * 1e3 / steps, 3),
+            "adjoint_cg_iters_per_step": round((eng.cg_iters - it0) / steps, 1),
+            "grad_finite": bool(torch.isfinite(E.grad).all().item() and torch.isfinite(v0.grad).all().item())}
 
 
 def cpu_baseline_inproc(scene, max_seconds, max_steps):
@@ -254,13 +302,15 @@ def cpu_baseline(workload, max_seconds, max_steps):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam1m")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="skip the differentiable-rollout timing (32^3 cube, 40 steps)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -313,13 +363,19 @@ def main():
     roofline = None
     if prof and prof["launches"] > 0:
         avg_s = prof["total_ms"] / prof["launches"] / 1e3
-        achieved = prof["bytes_per_launch"] / avg_s / 1e9
-        traffic = ncu_traffic(args.workload)
-        roofline = {"kernel": "pcg_spmv_kernel<float> (SELL-32 3x3-block SpMV + fused p update + FP64 p.q)",
+        # algorithmic bytes of one SpMV of the system matrix as a scalar CSR in FP32 (the reference's
+        # format): nnz (value + column) + row pointers + x read + y written
+        s_b, nnz, n = 4, r["nnz"], 3 * V
+        algo = nnz * (s_b + 4) + 4 * (n + 1) + 2 * s_b * n
+        achieved = algo / avg_s / 1e9
+        fmt = prof["bytes_per_launch"]
+        roofline = {"kernel": "pcg_spmv_kernel<float> (SELL-32 3x3-block symmetric SpMV + fused p update + p.q)",
                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                    "algorithmic_bytes_per_launch": prof["bytes_per_launch"], "avg_launch_us": round(avg_s * 1e6, 2),
-                    "launches_timed": prof["launches"], "traffic": traffic}
+                    "algorithmic_bytes_per_launch": algo, "avg_launch_us": round(avg_s * 1e6, 2),
+                    "launches_timed": prof["launches"], "traffic": ncu_traffic(args.workload),
+                    "format_bytes_per_launch": round(fmt),
+                    "format_frac": round(fmt / avg_s / 1e9 / peak, 4)}
     st = r["st_mixed"]
     stf = r["st_fp64"]
     if rank == 0:
@@ -353,7 +409,8 @@ def main():
             "cg_iters": [s["cg_iters_total"] for s in st],
             "rel_residual": [s["grad_norm"] / s["grad_norm0"] if s["grad_norm0"] > 0 else 0.0 for s in st],
             "tets_per_s": round(T * value, 1),
-            "adjoint_ms_per_step": None,
+            "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
+            "adjoint": r.get("adjoint"),
             "e2e": {"value": round(steps_total / e2e_s, 4), "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": r["launches"],

@@ -167,6 +167,24 @@ def batch_cubes(n=256, kmin=4, kmax=24, seed=4, dt=1e-2, rho=1000.0):
     )
 
 
+def rollout_cube(n=32, seed=5, v0_seed=6):
+    """Differentiable rollout: [0,1]^3 with n^3 hex x 6 tets (n = 32: 196,608 tets), per-cell E log-uniform
+    in [1e4, 1e6] (SplitMix64 seed 5), nu = 0.45, rho = 1000, bottom face (z = 0) fixed, initial vertex
+    velocities N(0, 0.5^2) per component (seed 6, zero on the fixed face), dt = 1e-2, 40 steps; the loss
+    target is the rest shape displaced by 0.1 sin(2 pi x) e_z."""
+    X, T = mesh.kuhn_box((n, n, n))
+    fixed = np.where(X[:, 2] == 0.0)[0]
+    v0 = 0.5 * mesh.normal(v0_seed, X.size).reshape(X.shape)
+    v0[fixed] = 0.0
+    target = X.copy()
+    target[:, 2] += 0.1 * np.sin(2 * np.pi * X[:, 0])
+    return dict(
+        name=f"rollout_cube{n}_{T.shape[0]}tets", X=X, cells=T, fixed=fixed, dt=1e-2, nu=0.45, rho=1000.0,
+        E_cells=10.0 ** mesh.uniform(seed, T.shape[0], 4.0, 6.0), v0=v0, target=target, steps=40,
+        checkpoint_every=8,
+    )
+
+
 def build_batch_timestep(batch, precision="mixed", params=None):
     """One GPU TimeStep over the disjoint union of the batch's cubes (per-cell material, per-instance
     stopping test)."""
