@@ -39,7 +39,8 @@ typedef enum {
   SSIM_GB_ERR_CUDA = 3,             /* CUDA runtime error (message in last_error) */
   SSIM_GB_ERR_NUMERICAL = 4,        /* NaN/Inf in energy or gradient, or an inverted element */
   SSIM_GB_ERR_STATE = 5,            /* call out of order (e.g. compute_step before prepare_step) */
-  SSIM_GB_ERR_OUT_OF_MEMORY = 6
+  SSIM_GB_ERR_OUT_OF_MEMORY = 6,
+  SSIM_GB_ERR_DEVICE_TIMEOUT = 7    /* a bounded device-side wait gave up; the CUDA context stays usable */
 } ssim_gb_status;
 
 /* Precision of the Hessian, assembly and inner PCG.  Energy, gradient, state and every reduction are
@@ -90,6 +91,16 @@ typedef struct {
   int32_t cg_check_every; /* PCG iterations launched between host convergence checks */
   double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack * sum|energy terms| (round-off) */
   int32_t pd_kappa_mode;  /* PD matrix diffusivity: 0 as ssim builds it (time_step.hpp:356), 1 from Lame */
+  int32_t pcg_persistent; /* 0: two launches per PCG iteration, host checks every cg_check_every iterations;
+                             1: the same PCG in one cooperative launch per solve (grid barriers, no host
+                             round trips; bitwise the iterates of 0); 2: Chronopoulos-Gear PCG in one
+                             launch (one reduction per iteration; equal to 0 up to rounding);
+                             3 (default): 2 in mixed precision, 0 in FP64 (the faster on GB300) */
+  int64_t pcg_spin_limit; /* polls before a grid-barrier wait gives up (SSIM_GB_ERR_DEVICE_TIMEOUT); 0 = default
+                             (2^25 polls, about a second) */
+  int32_t pcg_barrier_extra; /* test hook: arrivals a grid barrier waits for beyond the grid; 0 in normal use,
+                                > 0 makes every wait run out after pcg_spin_limit polls */
+  int32_t pcg_max_blocks; /* cap on the persistent PCG grid (0: as many 256-thread blocks as are resident) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
@@ -237,9 +248,10 @@ SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, const double*
                                                   const double* mu, int32_t num_cells, double time_step,
                                                   double density, void* stream, double* energy_out);
 
-/* ---- profiling (CUDA events around the PCG SpMV launches, on the handle's stream) ---- */
+/* ---- profiling (CUDA events on the handle's stream around the element, assembly and PCG launches) ---- */
 SSIM_GB_API ssim_gb_status ssim_gb_profile_enable(ssim_gb_timestep* h, int32_t enable);
-/* kernel: 0 = PCG SpMV, 1 = element Hessian, 2 = assembly, 3 = gradient element, 4 = PCG update */
+/* kernel: 0 = PCG SpMV, 1 = element Hessian, 2 = assembly, 3 = gradient element, 4 = PCG update (the
+ * two-launch PCG), 5 = persistent PCG: launches = iterations, total_ms over all solves, bytes per iteration */
 SSIM_GB_API ssim_gb_status ssim_gb_profile_read(ssim_gb_timestep* h, int32_t kernel, int64_t* launches, double* total_ms,
                                     double* bytes_per_launch);
 SSIM_GB_API ssim_gb_status ssim_gb_synchronize(ssim_gb_timestep* h);

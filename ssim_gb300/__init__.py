@@ -6,8 +6,9 @@ holds its Python binding (``TimeStep``), the reference-shaped ``libssim`` / ``py
 mesh generators and the benchmark scenes.
 """
 from . import mesh
-from ._lib import default_params, launch_count, lib, mesh_csr_pattern
+from ._lib import DeviceTimeout, NumericalError, SsimGbError, default_params, launch_count, lib, mesh_csr_pattern
 from .timestep import TimeStep
 
-__all__ = ["TimeStep", "mesh", "lib", "default_params", "launch_count", "mesh_csr_pattern"]
+__all__ = ["TimeStep", "mesh", "lib", "default_params", "launch_count", "mesh_csr_pattern", "SsimGbError",
+           "NumericalError", "DeviceTimeout"]
 __version__ = "0.1.0"

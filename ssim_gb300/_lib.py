@@ -16,7 +16,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libssim_gb300.so")
 HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "ssim_gb.h")
 
-OK, ERR_INVALID_ARGUMENT, ERR_NOT_CONVERGED, ERR_CUDA, ERR_NUMERICAL, ERR_STATE, ERR_OUT_OF_MEMORY = range(7)
+(OK, ERR_INVALID_ARGUMENT, ERR_NOT_CONVERGED, ERR_CUDA, ERR_NUMERICAL, ERR_STATE, ERR_OUT_OF_MEMORY,
+ ERR_DEVICE_TIMEOUT) = range(8)
 FP64, MIXED = 0, 1
 STEPPER_NEWTON, STEPPER_LBFGS, STEPPER_PD, STEPPER_NONE = 0, 1, 2, 3
 FIELDS = {
@@ -30,7 +31,7 @@ FIELDS = {
     "dbc_values": 7,
 }
 MATRICES = {"sysmatrix": 0, "mass": 1, "mass_filtered": 2}
-PROFILE_KERNELS = {"pcg_spmv": 0, "elem_hessian": 1, "assemble": 2, "elem_grad": 3, "pcg_update": 4}
+PROFILE_KERNELS = {"pcg_spmv": 0, "elem_hessian": 1, "assemble": 2, "elem_grad": 3, "pcg_update": 4, "pcg_iteration": 5}
 
 
 class Params(C.Structure):
@@ -52,6 +53,10 @@ class Params(C.Structure):
         ("cg_check_every", C.c_int32),
         ("ls_energy_slack", C.c_double),
         ("pd_kappa_mode", C.c_int32),
+        ("pcg_persistent", C.c_int32),
+        ("pcg_spin_limit", C.c_int64),
+        ("pcg_barrier_extra", C.c_int32),
+        ("pcg_max_blocks", C.c_int32),
     ]
 
     def as_dict(self):
@@ -81,6 +86,10 @@ class SsimGbError(RuntimeError):
 
 class NumericalError(ArithmeticError):
     """Non-finite energy / gradient / residual reported by the library."""
+
+
+class DeviceTimeout(SsimGbError):
+    """A bounded wait inside a kernel (a grid barrier) gave up; the CUDA context is still usable."""
 
 
 _lib = None
@@ -193,6 +202,8 @@ def check(status: int, handle=None):
         raise NumericalError(msg)
     if status == ERR_OUT_OF_MEMORY:
         raise MemoryError(msg)
+    if status == ERR_DEVICE_TIMEOUT:
+        raise DeviceTimeout(msg)
     raise SsimGbError(f"status {status}: {msg}")
 
 

@@ -61,7 +61,7 @@ struct DevScalars {
   int32_t iters;
   int32_t done;
   int32_t status;  // 0 ok, 1 breakdown (pq <= 0), 2 non-finite residual
-  int32_t pad;
+  int32_t wait_failed;  // set by a persistent kernel whose grid-barrier wait gave up
 };
 
 // Deterministic grid reduction: every block writes its partial sums, the last block to finish (found
@@ -143,9 +143,23 @@ __device__ __forceinline__ bool grid_sum_last(const double (&blockval)[NV], doub
   double acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) acc[k] = 0;
-  for (unsigned int b = threadIdx.x; b < gridDim.x; b += BLOCK) {
+  // four partials per value in flight at once, added in the same order as one at a time
+  const int nparts = (int)gridDim.x;
+  for (int b0 = threadIdx.x; b0 < nparts; b0 += 4 * BLOCK) {
+    double v[4][NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] += __ldcg(partials + b * NV + k);
+    for (int j = 0; j < 4; ++j) {
+      const int b = b0 + j * BLOCK;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[j][k] = b < nparts ? __ldcg(partials + b * NV + k) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (b0 + j * BLOCK < nparts) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += v[j][k];
+      }
+    }
   }
   block_sum<NV, BLOCK>(acc, sh);
   if (threadIdx.x == 0) {

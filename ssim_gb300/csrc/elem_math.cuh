@@ -61,6 +61,42 @@ __host__ __device__ __forceinline__ S snh_stress(const S* F, S lam, S mu, S* P) 
   return S(0.5) * (mu * (Ic - S(3)) + lam * Jm * Jm - mu * log(Ic + S(1))) - zero_energy;
 }
 
+// Energy, first Piola-Kirchhoff stress (when STRESS) and the sum of the magnitudes of the energy's terms
+// in one pass sharing I_c, J and log(I_c + 1); alpha = 1 + 3/4 mu / lambda and psi0 = the energy's value
+// at F = I (stable_neohookean.hpp:34,60) come precomputed per element.  Same formulas as snh_stress /
+// snh_energy / snh_energy_scale.
+template <typename S, bool STRESS>
+__host__ __device__ __forceinline__ S snh_eval(const S* F, S lam, S mu, S alpha, S psi0, S* P, S& scale) {
+  S Ic = 0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Ic += F[i] * F[i];
+  S C[9];
+  S J;
+  if (STRESS) {
+    cofactor(F, C);
+    J = F[0] * C[0] + F[1] * C[1] + F[2] * C[2];
+  } else {
+    J = det3(F);
+  }
+  const S Jm = J - alpha;
+  if (STRESS) {
+    const S sF = mu * (S(1) - S(1) / (Ic + S(1)));
+    const S lj = lam * Jm;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) P[i] = lj * C[i] + sF * F[i];
+  }
+  const S t1 = mu * (Ic - S(3)), t2 = lam * Jm * Jm, t3 = mu * log(Ic + S(1));
+  scale = S(0.5) * (fabs(t1) + t2 + fabs(t3)) + fabs(psi0);
+  return S(0.5) * (t1 + t2 - t3) - psi0;
+}
+
+// per-element constants of snh_eval
+template <typename S>
+__host__ __device__ __forceinline__ void snh_constants(S lam, S mu, S& alpha, S& psi0) {
+  alpha = S(0.75) * mu / lam + S(1);
+  psi0 = S(0.5) * (lam * (S(1) - alpha) * (S(1) - alpha) - mu * log(S(4)));
+}
+
 // sum of the magnitudes of the terms of snh_energy: the scale of its absolute round-off (the terms are
 // O(mu) and cancel to O(mu strain^2) near rest); the line search compares energies only above it
 template <typename S>

@@ -18,6 +18,9 @@ struct state_error : std::runtime_error {
 struct numerical_error : std::runtime_error {
   explicit numerical_error(const std::string& s) : std::runtime_error(s) {}
 };
+struct device_timeout : std::runtime_error {
+  explicit device_timeout(const std::string& s) : std::runtime_error(s) {}
+};
 
 // message returned by ssim_gb_last_error(NULL) on this thread (entry points without a handle)
 void set_global_error(const std::string& msg);

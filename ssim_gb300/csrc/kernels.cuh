@@ -31,6 +31,8 @@ struct ElemFP64 {
   const double* vol;
   const double* lam;
   const double* mu;
+  const double* alpha;  // 1 + 3/4 mu / lambda
+  const double* psi0;   // stable Neo-Hookean energy at F = I
 };
 
 struct ElemFP32 {
@@ -96,6 +98,13 @@ void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S
 template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
                      V4<S>* q, bool first, const Reduce& red, cudaStream_t st);
+// the whole PCG loop (after launch_pcg_setup*) in one cooperative launch: variant 1 standard PCG (bitwise
+// the two-launch iterates), 2 Chronopoulos-Gear PCG; false if the device cannot launch it cooperatively
+// (the caller then runs the two-launch loop)
+template <typename S>
+bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
+                           V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned int* gsync,
+                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st);
 template <typename S>
 void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                        int max_iters, const Reduce& red, cudaStream_t st);

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(EB)
   if (e < el.nt) {
     const int4 c = el.cells[e];
     const int vid[4] = {c.x, c.y, c.z, c.w};
-    double x[4][3], dd[4][3];
+    double uu[4][3], dd[4][3];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       V4<SD> dv;
@@ -48,24 +48,27 @@ __global__ void __launch_bounds__(EB)
       for (int k = 0; k < 3; ++k) {
         double uk = u[vid[i] * 3 + k];
         if (TRIAL) uk += alpha * (double)comp<SD>(dv, k);
-        x[i][k] = X[vid[i] * 3 + k] + uk;
+        uu[i][k] = uk;
         dd[i][k] = uk - xt[vid[i] * 3 + k];
       }
     }
     double Dm[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) Dm[k] = el.dminv[(size_t)k * el.nt + e];
-    double Ds[9];
+    // F = Ds Dm^-1 with Ds = [x1-x0, x2-x0, x3-x0] (def_grad.hpp:108-126); the rest edges times Dm^-1 are
+    // the identity, so F = I + [u1-u0, u2-u0, u3-u0] Dm^-1, which keeps the displacement's digits
+    double Du[9];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) Ds[r * 3 + k] = x[k + 1][r] - x[0][r];
+      for (int k = 0; k < 3; ++k) Du[r * 3 + k] = uu[k + 1][r] - uu[0][r];
     double F[9];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int cc = 0; cc < 3; ++cc)
-        F[r * 3 + cc] = Ds[r * 3 + 0] * Dm[0 * 3 + cc] + Ds[r * 3 + 1] * Dm[1 * 3 + cc] + Ds[r * 3 + 2] * Dm[2 * 3 + cc];
+        F[r * 3 + cc] = (r == cc ? 1.0 : 0.0) + (Du[r * 3 + 0] * Dm[0 * 3 + cc] + Du[r * 3 + 1] * Dm[1 * 3 + cc] +
+                                                 Du[r * 3 + 2] * Dm[2 * 3 + cc]);
     const double lam = el.lam[e], mu = el.mu[e], V = el.vol[e];
     const double m = rho * V * (1.0 / 20.0);
     double sd[3];
@@ -74,10 +77,9 @@ __global__ void __launch_bounds__(EB)
     double q = sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2];
 #pragma unroll
     for (int i = 0; i < 4; ++i) q += dd[i][0] * dd[i][0] + dd[i][1] * dd[i][1] + dd[i][2] * dd[i][2];
-    double psi;
+    double P[9], sc;
+    const double psi = snh_eval<double, FORCES>(F, lam, mu, el.alpha[e], el.psi0[e], P, sc);
     if (FORCES) {
-      double P[9];
-      psi = snh_stress<double>(F, lam, mu, P);
       const double s = dt2 * V;
       double tot[3] = {0, 0, 0};
 #pragma unroll
@@ -91,11 +93,9 @@ __global__ void __launch_bounds__(EB)
         }
 #pragma unroll
       for (int j = 0; j < 3; ++j) lfv[j] = -s * tot[j] + m * (dd[0][j] + sd[j]);
-    } else {
-      psi = snh_energy<double>(F, lam, mu);
     }
     energy = dt2 * V * psi + 0.5 * m * q;
-    escale = dt2 * V * snh_energy_scale<double>(F, lam, mu) + 0.5 * m * q;
+    escale = dt2 * V * sc + 0.5 * m * q;
   }
   if (FORCES) {
     if (e < el.nt) {

@@ -1,4 +1,6 @@
 // kernels_sparse.cu -- CSR/SELL assembly, SpMV, the fused Jacobi-PCG and the state-update vector kernels.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace ssim_gb {
@@ -132,42 +134,110 @@ __device__ __forceinline__ V4<S> load_x(const V4<S>* x0, const V4<S>* x1, S beta
   return xv;
 }
 
+// y_u = sum over the upper slots of A_uw x_w + sum over the lower slots of (A_wu)^T x_w, accumulated slot
+// by slot in chunks of two (indices first, then the two slots' x gathers and 18 values, then the FMAs);
+// lower padding entries point at an all-zero slot, so no branch stops the loads from being hoisted.
+template <typename S, int U>
+__device__ __forceinline__ void upper_chunk(const S* __restrict__ vb, const int (&c)[U], const V4<S>* x0,
+                                            const V4<S>* x1, S beta, int k, S& a0, S& a1, S& a2) {
+  S v[U][9];
+#pragma unroll
+  for (int j = 0; j < U; ++j)
+#pragma unroll
+    for (int m = 0; m < 9; ++m) v[j][m] = vb[(size_t)(k + j) * 288 + 32 * m];
+  V4<S> xv[U];
+#pragma unroll
+  for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
+#pragma unroll
+  for (int j = 0; j < U; ++j) {
+    a0 += v[j][0] * xv[j].x + v[j][1] * xv[j].y + v[j][2] * xv[j].z;
+    a1 += v[j][3] * xv[j].x + v[j][4] * xv[j].y + v[j][5] * xv[j].z;
+    a2 += v[j][6] * xv[j].x + v[j][7] * xv[j].y + v[j][8] * xv[j].z;
+  }
+}
+
+template <typename S, int U>
+__device__ __forceinline__ void lower_chunk(const S* __restrict__ vals, const int (&q)[U], const int (&c)[U],
+                                            const V4<S>* x0, const V4<S>* x1, S beta, S& a0, S& a1, S& a2) {
+  S v[U][9];
+#pragma unroll
+  for (int j = 0; j < U; ++j) {
+    const S* p = vals + sell_base(q[j]);
+#pragma unroll
+    for (int m = 0; m < 9; ++m) v[j][m] = p[32 * m];
+  }
+  V4<S> xv[U];
+#pragma unroll
+  for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
+  // (A_wu)^T x_w: column a of the stored block times x
+#pragma unroll
+  for (int j = 0; j < U; ++j) {
+    a0 += v[j][0] * xv[j].x + v[j][3] * xv[j].y + v[j][6] * xv[j].z;
+    a1 += v[j][1] * xv[j].x + v[j][4] * xv[j].y + v[j][7] * xv[j].z;
+    a2 += v[j][2] * xv[j].x + v[j][5] * xv[j].y + v[j][8] * xv[j].z;
+  }
+}
+
+// Index source of one row: straight from global memory, or from a per-warp shared-memory copy of the
+// slice's first ST_UP upper columns and ST_LO lower (slot, column) pairs, filled with cp.async in one
+// round trip so the value and x loads of every chunk depend only on fast shared loads.
+constexpr int ST_UP = 12, ST_LO = 10, ST_K = ST_UP + 2 * ST_LO;
+
+__device__ __forceinline__ void cp_async4(int* dst, const int* src) {
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+template <typename S, bool STAGED>
+__device__ __forceinline__ void row_product_t(const SellMatrix& A, const S* __restrict__ vals, int u, const V4<S>* x0,
+                                              const V4<S>* x1, S beta, int (*sidx)[32], S& a0, S& a1, S& a2) {
+  const int lane = u & 31, s = u >> 5;
+  const int ub = A.sl_off[s], Wu = (A.sl_off[s + 1] - ub) >> 5;
+  const int lb = A.lo_off[s], Wl = (A.lo_off[s + 1] - lb) >> 5;
+  const int* cb = A.sl_col + ub + lane;
+  const int* sb = A.lo_src + lb + lane;
+  const int* lcb = A.lo_col + lb + lane;
+  if (STAGED) {
+    const int nu = min(Wu, ST_UP), nl = min(Wl, ST_LO);
+    for (int k = 0; k < nu; ++k) cp_async4(&sidx[k][lane], cb + k * 32);
+    for (int k = 0; k < nl; ++k) {
+      cp_async4(&sidx[ST_UP + 2 * k][lane], sb + k * 32);
+      cp_async4(&sidx[ST_UP + 2 * k + 1][lane], lcb + k * 32);
+    }
+    cp_async_wait_all();
+  }
+  auto ucol = [&](int k) { return (STAGED && k < ST_UP) ? sidx[k][lane] : cb[k * 32]; };
+  auto lsrc = [&](int k) { return (STAGED && k < ST_LO) ? sidx[ST_UP + 2 * k][lane] : sb[k * 32]; };
+  auto lcol = [&](int k) { return (STAGED && k < ST_LO) ? sidx[ST_UP + 2 * k + 1][lane] : lcb[k * 32]; };
+  a0 = a1 = a2 = S(0);
+  const S* vb = vals + (size_t)9 * ub + lane;
+  int k = 0;
+  for (; k + 2 <= Wu; k += 2) {
+    const int c[2] = {ucol(k), ucol(k + 1)};
+    upper_chunk<S, 2>(vb, c, x0, x1, beta, k, a0, a1, a2);
+  }
+  if (k < Wu) {
+    const int c[1] = {ucol(k)};
+    upper_chunk<S, 1>(vb, c, x0, x1, beta, k, a0, a1, a2);
+  }
+  k = 0;
+  for (; k + 2 <= Wl; k += 2) {
+    const int qq[2] = {lsrc(k), lsrc(k + 1)}, c[2] = {lcol(k), lcol(k + 1)};
+    lower_chunk<S, 2>(vals, qq, c, x0, x1, beta, a0, a1, a2);
+  }
+  if (k < Wl) {
+    const int qq[1] = {lsrc(k)}, c[1] = {lcol(k)};
+    lower_chunk<S, 1>(vals, qq, c, x0, x1, beta, a0, a1, a2);
+  }
+}
+
 template <typename S>
 __device__ __forceinline__ void row_product(const SellMatrix& A, const S* __restrict__ vals, int u, const V4<S>* x0,
                                             const V4<S>* x1, S beta, S& a0, S& a1, S& a2) {
-  const int lane = u & 31, s = u >> 5;
-  a0 = a1 = a2 = S(0);
-  {
-    const int base = A.sl_off[s];
-    const int W = (A.sl_off[s + 1] - base) >> 5;
-    const S* vb = vals + (size_t)9 * base + lane;
-    const int* cb = A.sl_col + base + lane;
-#pragma unroll 2
-    for (int k = 0; k < W; ++k) {
-      const V4<S> xv = load_x<S>(x0, x1, beta, cb[k * 32]);
-      const S* v = vb + (size_t)k * 9 * 32;
-      a0 += v[0] * xv.x + v[32] * xv.y + v[64] * xv.z;
-      a1 += v[96] * xv.x + v[128] * xv.y + v[160] * xv.z;
-      a2 += v[192] * xv.x + v[224] * xv.y + v[256] * xv.z;
-    }
-  }
-  {
-    const int base = A.lo_off[s];
-    const int W = (A.lo_off[s + 1] - base) >> 5;
-    const int* sb = A.lo_src + base + lane;
-    const int* cb = A.lo_col + base + lane;
-#pragma unroll 2
-    for (int k = 0; k < W; ++k) {
-      const int q = sb[k * 32];
-      if (q < 0) continue;
-      const V4<S> xv = load_x<S>(x0, x1, beta, cb[k * 32]);
-      const S* v = vals + sell_base(q);
-      // (A_wu)^T x_w: column a of the stored block times x
-      a0 += v[0] * xv.x + v[96] * xv.y + v[192] * xv.z;
-      a1 += v[32] * xv.x + v[128] * xv.y + v[224] * xv.z;
-      a2 += v[64] * xv.x + v[160] * xv.y + v[256] * xv.z;
-    }
-  }
+  row_product_t<S, false>(A, vals, u, x0, x1, beta, nullptr, a0, a1, a2);
 }
 
 template <typename S>
@@ -254,6 +324,70 @@ __global__ void __launch_bounds__(SB)
   }
 }
 
+// One row of the fused PCG SpMV: p_new = z + beta p_old (formed on the fly for the gathered columns),
+// q = A p_new; returns the row's share of p_new . q.
+template <typename S>
+__device__ __forceinline__ S pcg_spmv_row(const SellMatrix& A, const S* __restrict__ vals, const V4<S>* z,
+                                          const V4<S>* p_old, V4<S>* p_new, V4<S>* q, S beta, int u,
+                                          int (*sidx)[32]) {
+  if (u >= A.nv) return S(0);
+  S a0, a1, a2;
+  row_product_t<S, true>(A, vals, u, z, p_old, beta, sidx, a0, a1, a2);
+  const V4<S> zu = z[u], pu = p_old[u];
+  const V4<S> pn = mk4<S>(zu.x + beta * pu.x, zu.y + beta * pu.y, zu.z + beta * pu.z);
+  p_new[u] = pn;
+  q[u] = mk4<S>(a0, a1, a2);
+  return pn.x * a0 + pn.y * a1 + pn.z * a2;
+}
+
+// One row of the PCG update: x += alpha p, r -= alpha q, z = D^-1 r; shares of r.z and r.r in part.
+template <typename S>
+__device__ __forceinline__ void pcg_update_row(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* __restrict__ dinv,
+                                               V4<S>* x, V4<S>* r, V4<S>* z, S alpha, int u, S (&part)[2]) {
+  part[0] = part[1] = S(0);
+  if (u >= nv) return;
+  const V4<S> pu = p[u], qu = q[u];
+  const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
+  V4<S> xu = x[u], ru = r[u];
+  xu.x += alpha * pu.x;
+  xu.y += alpha * pu.y;
+  xu.z += alpha * pu.z;
+  ru.x -= alpha * qu.x;
+  ru.y -= alpha * qu.y;
+  ru.z -= alpha * qu.z;
+  const V4<S> zu = mk4<S>(d0.x * ru.x + d0.y * ru.y + d0.z * ru.z, d1.x * ru.x + d1.y * ru.y + d1.z * ru.z,
+                          d2.x * ru.x + d2.y * ru.y + d2.z * ru.z);
+  x[u] = xu;
+  r[u] = ru;
+  z[u] = zu;
+  part[0] = ru.x * zu.x + ru.y * zu.y + ru.z * zu.z;
+  part[1] = ru.x * ru.x + ru.y * ru.y + ru.z * ru.z;
+}
+
+// the scalar epilogues shared by the two-launch and the persistent PCG
+__device__ __forceinline__ void pcg_after_pq(DevScalars* sc, double pq) {
+  sc->pq = pq;
+  sc->alpha = sc->rz / pq;
+  if (!(pq > 0.0)) {  // breakdown: not SPD along p (or non-finite)
+    sc->done = 1;
+    sc->status = 1;
+  }
+}
+
+__device__ __forceinline__ void pcg_after_rz(DevScalars* sc, double rz, double rr, int max_iters) {
+  sc->rz_old = sc->rz;
+  sc->rz = rz;
+  sc->beta = rz / sc->rz_old;
+  sc->rr = rr;
+  sc->iters += 1;
+  if (!isfinite(rr)) {
+    sc->done = 1;
+    sc->status = 2;
+  } else if (rr <= sc->tol2 || sc->iters >= max_iters || rz == 0.0) {
+    sc->done = 1;
+  }
+}
+
 template <typename S>
 __global__ void __launch_bounds__(SB)
     pcg_spmv_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ z,
@@ -261,29 +395,14 @@ __global__ void __launch_bounds__(SB)
                     Reduce red) {
   if (*(volatile int*)&red.sc->done) return;
   __shared__ double shred[SB / 32][1];
+  __shared__ int sidx[SB / 32][ST_K][32];
   const S beta = first ? S(0) : (S)red.sc->beta;
-  const int u = blockIdx.x * SB + threadIdx.x;
-  S part[1] = {S(0)};
-  if (u < A.nv) {
-    S a0, a1, a2;
-    row_product<S>(A, vals, u, z, p_old, beta, a0, a1, a2);
-    const V4<S> zu = z[u], pu = p_old[u];
-    const V4<S> pn = mk4<S>(zu.x + beta * pu.x, zu.y + beta * pu.y, zu.z + beta * pu.z);
-    p_new[u] = pn;
-    q[u] = mk4<S>(a0, a1, a2);
-    part[0] = pn.x * a0 + pn.y * a1 + pn.z * a2;
-  }
+  S part[1] = {pcg_spmv_row<S>(A, vals, z, p_old, p_new, q, beta, blockIdx.x * SB + threadIdx.x,
+                               sidx[threadIdx.x >> 5])};
   double v1[1];
   block_sum_s<1, SB, S>(part, v1, shred);
   double tot[1];
-  if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) {
-    red.sc->pq = tot[0];
-    red.sc->alpha = red.sc->rz / tot[0];
-    if (!(tot[0] > 0.0)) {  // breakdown: not SPD along p (or non-finite)
-      red.sc->done = 1;
-      red.sc->status = 1;
-    }
-  }
+  if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) pcg_after_pq(red.sc, tot[0]);
 }
 
 template <typename S>
@@ -294,43 +413,309 @@ __global__ void __launch_bounds__(SB)
   if (*(volatile int*)&red.sc->done) return;
   __shared__ double shred[SB / 32][2];
   const S alpha = (S)red.sc->alpha;
-  const int u = blockIdx.x * SB + threadIdx.x;
-  S part[2] = {S(0), S(0)};
-  if (u < nv) {
-    const V4<S> pu = p[u], qu = q[u];
-    const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
-    V4<S> xu = x[u], ru = r[u];
-    xu.x += alpha * pu.x;
-    xu.y += alpha * pu.y;
-    xu.z += alpha * pu.z;
-    ru.x -= alpha * qu.x;
-    ru.y -= alpha * qu.y;
-    ru.z -= alpha * qu.z;
-    const V4<S> zu = mk4<S>(d0.x * ru.x + d0.y * ru.y + d0.z * ru.z, d1.x * ru.x + d1.y * ru.y + d1.z * ru.z,
-                            d2.x * ru.x + d2.y * ru.y + d2.z * ru.z);
-    x[u] = xu;
-    r[u] = ru;
-    z[u] = zu;
-    part[0] = ru.x * zu.x + ru.y * zu.y + ru.z * zu.z;
-    part[1] = ru.x * ru.x + ru.y * ru.y + ru.z * ru.z;
-  }
+  S part[2];
+  pcg_update_row<S>(nv, p, q, dinv, x, r, z, alpha, blockIdx.x * SB + threadIdx.x, part);
   double bs[2];
   block_sum_s<2, SB, S>(part, bs, shred);
   double tot[2];
-  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) {
-    DevScalars* sc = red.sc;
-    sc->rz_old = sc->rz;
-    sc->rz = tot[0];
-    sc->beta = tot[0] / sc->rz_old;
-    sc->rr = tot[1];
-    sc->iters += 1;
-    if (!isfinite(tot[1])) {
-      sc->done = 1;
-      sc->status = 2;
-    } else if (tot[1] <= sc->tol2 || sc->iters >= max_iters || tot[0] == 0.0) {
-      sc->done = 1;
+  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) pcg_after_rz(red.sc, tot[0], tot[1], max_iters);
+}
+
+// ------------------------------------------------------------------ persistent PCG
+// The whole PCG loop in one cooperative launch (every block resident).  Work is split into 256-row
+// "virtual blocks", each block taking virtual blocks blockIdx.x, blockIdx.x + gridDim.x, ...; every virtual
+// block writes its partial sums, and at the reducing grid barrier the LAST block to arrive adds them in
+// grid_sum_last's order and runs the scalar epilogue into the device scalars before it releases the
+// others, who then read alpha / beta / done from there.  The result does not depend on the grid size, and
+// the FP64 reduction runs once per barrier (the FP64 pipe is narrow on GB300).  Arrays written inside the
+// loop are read with plain loads only after a barrier, whose acquire side orders them after the writers'
+// release (the cooperative-groups grid sync pattern); the scalars are read with L2 loads.
+struct GridSync {
+  unsigned int* count;  // arrivals in the current phase
+  unsigned int* gen;    // completed phases
+  unsigned int extra;   // arrivals beyond the grid (test hook; 0 in normal use)
+  long long spin_limit;
+};
+
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier; the last block to arrive runs last_fn() with all its threads before releasing the rest.
+// Returns false in every thread of a block whose wait gave up after spin_limit polls.
+template <typename F>
+__device__ __forceinline__ bool grid_barrier_last(const GridSync& gs, F&& last_fn) {
+  __shared__ int role;  // 0 released, 1 last arriver, 2 gave up
+  __shared__ unsigned int gen0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gen0 = ld_acquire_gpu(gs.gen);
+    __threadfence();
+    role = (atomicAdd(gs.count, 1u) == gridDim.x + gs.extra - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (role == 1) {
+    __threadfence();
+    last_fn();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      atomicExch(gs.count, 0u);
+      __threadfence();
+      atomicAdd(gs.gen, 1u);
+    }
+    __syncthreads();
+    return true;
+  }
+  if (threadIdx.x == 0) {
+    long long n = 0;
+    int r = 0;
+    while (ld_acquire_gpu(gs.gen) == gen0) {
+      if (++n > gs.spin_limit) {
+        r = 2;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    role = r;
+  }
+  __syncthreads();
+  return role != 2;
+}
+
+// grid_sum_last's final sum, run by one whole block: partials of nparts virtual blocks (stride NV)
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double* partials, int nparts, double (*sh)[NV], double (&tot)[NV]) {
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) acc[k] = 0;
+  // four partials per value in flight at once, added in the same order as one at a time
+  for (int b0 = threadIdx.x; b0 < nparts; b0 += 4 * SB) {
+    double v[4][NV];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int b = b0 + j * SB;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[j][k] = b < nparts ? __ldcg(partials + b * NV + k) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (b0 + j * SB < nparts) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += v[j][k];
+      }
     }
   }
+  block_sum<NV, SB>(acc, sh);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = acc[k];  // valid in thread 0
+}
+
+// Chronopoulos-Gear PCG (Chronopoulos & Gear, J. Comput. Appl. Math. 25, 1989): the same iterates as
+// PCG in exact arithmetic, with s = A p carried by its own recurrence so one reduction per iteration
+// gives all scalars.  With u = M r and w = A u:
+//   phase A:  w = A u;  gamma = (r, u), delta = (w, u), rr = (r, r)          -> one grid reduction
+//   scalars:  beta = gamma / gamma_old, alpha = gamma / (delta - beta gamma / alpha_old)  (first: 0, gamma/delta)
+//   phase B:  p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = M r   (per vertex)
+// The SpMV gathers one vector (u) instead of forming z + beta p for every neighbour; the barrier after
+// phase B only orders u's writes before the next gathers.  Vectors: u = z, w = q, p = p0, s = p1.
+template <typename S>
+__device__ __forceinline__ void cgcg_spmv_row(const SellMatrix& A, const S* __restrict__ vals, const V4<S>* z,
+                                              const V4<S>* r, V4<S>* q, int u, int (*sidx)[32], S (&part)[3]) {
+  part[0] = part[1] = part[2] = S(0);
+  if (u >= A.nv) return;
+  S a0, a1, a2;
+  row_product_t<S, true>(A, vals, u, z, nullptr, S(0), sidx, a0, a1, a2);
+  q[u] = mk4<S>(a0, a1, a2);
+  const V4<S> uu = z[u], ru = r[u];
+  part[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
+  part[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
+  part[2] = ru.x * ru.x + ru.y * ru.y + ru.z * ru.z;
+}
+
+template <typename S>
+__device__ __forceinline__ void cgcg_update_row(int nv, bool first, S alpha, S beta, const V4<S>* __restrict__ dinv,
+                                                V4<S>* z, const V4<S>* q, V4<S>* p, V4<S>* sv, V4<S>* x, V4<S>* r,
+                                                int u) {
+  if (u >= nv) return;
+  const V4<S> uu = z[u], ww = q[u];
+  V4<S> pu = uu, su = ww;
+  if (!first) {
+    const V4<S> po = p[u], so = sv[u];
+    pu = mk4<S>(uu.x + beta * po.x, uu.y + beta * po.y, uu.z + beta * po.z);
+    su = mk4<S>(ww.x + beta * so.x, ww.y + beta * so.y, ww.z + beta * so.z);
+  }
+  const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
+  V4<S> xu = x[u], ru = r[u];
+  xu.x += alpha * pu.x;
+  xu.y += alpha * pu.y;
+  xu.z += alpha * pu.z;
+  ru.x -= alpha * su.x;
+  ru.y -= alpha * su.y;
+  ru.z -= alpha * su.z;
+  p[u] = pu;
+  sv[u] = su;
+  x[u] = xu;
+  r[u] = ru;
+  z[u] = mk4<S>(d0.x * ru.x + d0.y * ru.y + d0.z * ru.z, d1.x * ru.x + d1.y * ru.y + d1.z * ru.z,
+                d2.x * ru.x + d2.y * ru.y + d2.z * ru.z);
+}
+
+// scalar epilogue after phase A (one thread): stop tests on the residual of the current x, then the
+// step lengths.  iters counts the x updates; rr is |r|^2 of the current x.
+__device__ __forceinline__ void cgcg_after(DevScalars* sc, double g, double d, double rr, int max_iters) {
+  sc->rr = rr;
+  if (!isfinite(rr)) {
+    sc->done = 1;
+    sc->status = 2;
+    return;
+  }
+  if (rr <= sc->tol2 || g == 0.0 || sc->iters >= max_iters) {
+    sc->done = 1;
+    return;
+  }
+  double beta = 0.0, den = d;
+  if (sc->iters > 0) {
+    beta = g / sc->rz;
+    den = d - beta * g / sc->alpha;
+  }
+  if (!(den > 0.0)) {  // breakdown: not SPD along p (or non-finite)
+    sc->done = 1;
+    sc->status = 1;
+    return;
+  }
+  sc->rz_old = sc->rz;
+  sc->rz = g;
+  sc->pq = den;
+  sc->beta = beta;
+  sc->alpha = g / den;
+  sc->iters += 1;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
+    cgcg_persistent_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ dinv, V4<S>* x,
+                           V4<S>* r, V4<S>* z, V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, Reduce red,
+                           GridSync gs) {
+  __shared__ double shred[SB / 32][3];
+  __shared__ int sidx[SB / 32][ST_K][32];
+  __shared__ double s_alpha, s_beta;
+  __shared__ int s_done;
+  DevScalars* sc = red.sc;
+  if (threadIdx.x == 0) s_done = *(volatile int*)&sc->done;
+  __syncthreads();
+  if (s_done) return;
+  const int nvb = (A.nv + SB - 1) / SB;
+  double* part = red.partials;
+  bool ok = true;
+  for (int k = 0;; ++k) {
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      S pr[3];
+      cgcg_spmv_row<S>(A, vals, z, r, q, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5], pr);
+      double bs[3];
+      block_sum_s<3, SB, S>(pr, bs, shred);
+      if (threadIdx.x == 0) {
+        part[3 * vb] = bs[0];
+        part[3 * vb + 1] = bs[1];
+        part[3 * vb + 2] = bs[2];
+      }
+      __syncthreads();
+    }
+    ok = grid_barrier_last(gs, [&] {
+      double tot[3];
+      sum_partials<3>(part, nvb, shred, tot);
+      if (threadIdx.x == 0) cgcg_after(sc, tot[0], tot[1], tot[2], max_iters);
+    });
+    if (!ok) break;
+    if (threadIdx.x == 0) {
+      s_done = __ldcg(&sc->done);
+      s_alpha = __ldcg(&sc->alpha);
+      s_beta = __ldcg(&sc->beta);
+    }
+    __syncthreads();
+    if (s_done) break;
+    const S alpha = (S)s_alpha, beta = (S)s_beta;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x)
+      cgcg_update_row<S>(A.nv, k == 0, alpha, beta, dinv, z, q, p0, p1, x, r, vb * SB + threadIdx.x);
+    ok = grid_barrier_last(gs, [] {});
+    if (!ok) break;
+  }
+  // a barrier wait gave up: flag it (the host clears the flag before the launch) and leave
+  if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
+}
+
+// Standard PCG in one launch: the two-launch loop's phases (SpMV forming p = z + beta p_old, then the
+// update) separated by reducing grid barriers; the last block runs the same reductions and epilogues as
+// the two-launch kernels, so the iterates are bitwise theirs.
+template <typename S>
+__global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
+    pcg_persistent_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ dinv, V4<S>* x,
+                          V4<S>* r, V4<S>* z, V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, Reduce red,
+                          GridSync gs) {
+  __shared__ double shred[SB / 32][2];
+  __shared__ int sidx[SB / 32][ST_K][32];
+  __shared__ double s_coef;  // beta for the SpMV phase, alpha for the update phase
+  __shared__ int s_done;
+  DevScalars* sc = red.sc;
+  if (threadIdx.x == 0) s_done = *(volatile int*)&sc->done;
+  __syncthreads();
+  if (s_done) return;
+  const int nvb = (A.nv + SB - 1) / SB;
+  double* part_pq = red.partials;
+  double* part_rz = red.partials + 2 * (size_t)nvb;
+  bool ok = true;
+  for (int k = 0;; ++k) {
+    V4<S>* pold = (k & 1) ? p1 : p0;
+    V4<S>* pnew = (k & 1) ? p0 : p1;
+    const S beta = k == 0 ? S(0) : (S)s_coef;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      S part[1] = {pcg_spmv_row<S>(A, vals, z, pold, pnew, q, beta, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5])};
+      double v1[1];
+      block_sum_s<1, SB, S>(part, v1, reinterpret_cast<double(*)[1]>(shred));
+      if (threadIdx.x == 0) part_pq[vb] = v1[0];
+      __syncthreads();
+    }
+    ok = grid_barrier_last(gs, [&] {
+      double tot[1];
+      sum_partials<1>(part_pq, nvb, reinterpret_cast<double(*)[1]>(shred), tot);
+      if (threadIdx.x == 0) pcg_after_pq(sc, tot[0]);
+    });
+    if (!ok) break;
+    if (threadIdx.x == 0) {
+      s_done = __ldcg(&sc->done);
+      s_coef = __ldcg(&sc->alpha);
+    }
+    __syncthreads();
+    if (s_done) break;
+    const S alpha = (S)s_coef;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      S part[2];
+      pcg_update_row<S>(A.nv, pnew, q, dinv, x, r, z, alpha, vb * SB + threadIdx.x, part);
+      double bs[2];
+      block_sum_s<2, SB, S>(part, bs, shred);
+      if (threadIdx.x == 0) {
+        part_rz[2 * vb] = bs[0];
+        part_rz[2 * vb + 1] = bs[1];
+      }
+      __syncthreads();
+    }
+    ok = grid_barrier_last(gs, [&] {
+      double tot[2];
+      sum_partials<2>(part_rz, nvb, shred, tot);
+      if (threadIdx.x == 0) pcg_after_rz(sc, tot[0], tot[1], max_iters);
+    });
+    if (!ok) break;
+    if (threadIdx.x == 0) {
+      s_done = __ldcg(&sc->done);
+      s_coef = __ldcg(&sc->beta);
+    }
+    __syncthreads();
+    if (s_done) break;
+  }
+  // a barrier wait gave up: flag it (the host clears the flag before the launch) and leave
+  if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
 }
 
 // ------------------------------------------------------------------ vectors
@@ -590,6 +975,33 @@ void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V
 }
 
 template <typename S>
+bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
+                           V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned int* gsync,
+                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st) {
+  int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+  SSIM_CUDA(cudaGetDevice(&dev));
+  SSIM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) return false;
+  SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const void* fn = variant == 2 ? (const void*)cgcg_persistent_kernel<S> : (const void*)pcg_persistent_kernel<S>;
+  SSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SB, 0));
+  if (per_sm < 1) return false;
+  int grid = std::min(div_up(A.nv, SB), per_sm * nsm);
+  if (max_blocks > 0) grid = std::min(grid, max_blocks);
+  if (grid < 1) return true;
+  SSIM_CUDA(cudaMemsetAsync(gsync, 0, 2 * sizeof(unsigned int), st));
+  SSIM_CUDA(cudaMemsetAsync(&red.sc->wait_failed, 0, sizeof(int32_t), st));
+  GridSync gs{gsync, gsync + 1, (unsigned int)extra, spin_limit > 0 ? spin_limit : (1LL << 25)};
+  SellMatrix a = A;
+  Reduce rd = red;
+  void* args[] = {(void*)&a,  (void*)&vals, (void*)&dinv, (void*)&x,         (void*)&r,  (void*)&z,
+                  (void*)&p0, (void*)&p1,   (void*)&q,    (void*)&max_iters, (void*)&rd, (void*)&gs};
+  SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), args, 0, st));
+  after_launch("pcg_persistent");
+  return true;
+}
+
+template <typename S>
 void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                        int max_iters, const Reduce& red, cudaStream_t st) {
   pcg_update_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, p, q, dinv, x, r, z, max_iters, red);
@@ -710,6 +1122,9 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
                                    bool, const Reduce&, cudaStream_t);                                            \
   template void launch_pcg_update<S>(int, const V4<S>*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, int, \
                                      const Reduce&, cudaStream_t);                                                \
+  template bool launch_pcg_persistent<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*,       \
+                                         V4<S>*, V4<S>*, V4<S>*, int, const Reduce&, unsigned int*, long long,   \
+                                         int, int, int, cudaStream_t);                                            \
   template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
   template void launch_axpy_update<S>(int, double, const V4<S>*, const double*, double*, float4*, cudaStream_t); \
   template void launch_to_vec4<S>(int, const double*, V4<S>*, bool, cudaStream_t);                               \

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/ssim_gb.h"
+#include "elem_math.cuh"
 #include "kernels.cuh"
 #include "topology.h"
 
@@ -66,7 +67,9 @@ struct Solver {
   }
 };
 
-enum ProfileKernel { PK_SPMV = 0, PK_HESS = 1, PK_ASM = 2, PK_GRAD = 3, PK_UPD = 4, PK_COUNT = 5 };
+// PK_PCG counts iterations of the persistent PCG kernel (one launch per solve), so total / count is the
+// time of one PCG iteration
+enum ProfileKernel { PK_SPMV = 0, PK_HESS = 1, PK_ASM = 2, PK_GRAD = 3, PK_UPD = 4, PK_PCG = 5, PK_COUNT = 6 };
 
 struct TimeStep {
   // ---- configuration (time_step.hpp:683-708)
@@ -89,7 +92,7 @@ struct TimeStep {
   // ---- device: mesh, element constants
   DBuf<double> dX;
   DBuf<int4> dcells;
-  DBuf<double> dminv, vol, lam, mu;
+  DBuf<double> dminv, vol, lam, mu, snh_alpha, snh_psi0;
   DBuf<float> fdminv, fvol, flam, fmu;
   // ---- device: state [n] (time_step.hpp:668-679)
   DBuf<double> deformation, prev_deform, inertia, next, velocity, ext_accel, forces, dbc_values, work;
@@ -104,6 +107,7 @@ struct TimeStep {
   Solver<double> sd;
   DBuf<double> partials;
   DBuf<unsigned int> counter;
+  DBuf<unsigned int> gsync;  // grid-barrier state of the persistent PCG (count, generation)
   DBuf<DevScalars> sc;
   DevScalars* hsc = nullptr;  // pinned
   DBuf<double> gprev, dscal;   // previous gradient (L-BFGS), device scalars of vdot
@@ -131,7 +135,7 @@ struct TimeStep {
 
   bool mixed() const { return precision == SSIM_GB_MIXED; }
   Reduce red() { return Reduce{partials.p, counter.p, sc.p}; }
-  ElemFP64 e64() const { return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p}; }
+  ElemFP64 e64() const { return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p, snh_alpha.p, snh_psi0.p}; }
   ElemFP32 e32() const { return ElemFP32{nt, dcells.p, fdminv.p, fvol.p, flam.p, fmu.p}; }
   SellMatrix A() const {
     return SellMatrix{nv, topo.nslots, sl_off.p, sl_col.p, slot_row.p, lo_off.p, lo_src.p, lo_col.p};
@@ -184,6 +188,8 @@ struct TimeStep {
     sc.zero(stream);
     counter.alloc(1);
     counter.zero(stream);
+    gsync.alloc(2);
+    gsync.zero(stream);
     const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(3 * nv, topo.nslots), 256)) + 1;
     partials.alloc(maxgrid * 4);
     dX.upload(X, stream);
@@ -254,6 +260,10 @@ struct TimeStep {
     }
     lam.upload(l, stream);
     mu.upload(m, stream);
+    std::vector<double> al(nt), p0(nt);
+    for (int e = 0; e < nt; ++e) snh_constants<double>(l[e], m[e], al[e], p0[e]);
+    snh_alpha.upload(al, stream);
+    snh_psi0.upload(p0, stream);
     std::vector<float> lf32(l.begin(), l.end()), mf32(m.begin(), m.end());
     flam.upload(lf32, stream);
     fmu.upload(mf32, stream);
@@ -420,6 +430,30 @@ struct TimeStep {
   template <typename S>
   int pcg_loop(const S* vals, const V4<S>* dinv, int max_iters, double* rel_res, bool profile_spmv) {
     Solver<S>& s = solver<S>();
+    int variant = params.pcg_persistent;
+    if (variant == 3) variant = sizeof(S) == 4 ? 2 : 0;
+    if (variant) {
+      const bool prof = profiling && profile_spmv;
+      if (prof) SSIM_CUDA(cudaEventRecord(ev[0], stream));
+      const bool ran = launch_pcg_persistent<S>(A(), vals, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters,
+                                                red(), gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra,
+                                                params.pcg_max_blocks, variant, stream);
+      if (ran) {
+        if (prof) SSIM_CUDA(cudaEventRecord(ev[1], stream));
+        sync_scalars();
+        if (hsc->wait_failed) throw device_timeout("a grid-barrier wait of the persistent PCG kernel gave up");
+        if (prof) {
+          float ms = 0;
+          SSIM_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+          prof_ms[PK_PCG] += ms;
+          prof_launch[PK_PCG] += hsc->iters;
+          prof_bytes[PK_PCG] = spmv_bytes(sizeof(S)) + update_bytes(sizeof(S));
+        }
+        if (rel_res) *rel_res = hsc->rr0 > 0 ? std::sqrt(hsc->rr / hsc->rr0) : 0.0;
+        if (hsc->status == 2) throw numerical_error("PCG produced a non-finite residual");
+        return hsc->iters;
+      }
+    }
     int k = 0;
     int chunk = std::max(1, params.cg_check_every);
     const bool prof = profiling && profile_spmv;
@@ -604,14 +638,17 @@ struct TimeStep {
     st.newton_iters = it;
   }
 
-  // algorithmic bytes of one symmetric SELL SpMV: upper values + block columns, lower slot/column indices
-  // and the values they read (the transposed blocks: a second read of upper slots), x gathers (one
-  // 3-vector per block row, reused from cache) + y write.  Padding slots are counted (they are read).
+  // bytes one PCG SpMV launch must move in this storage format, each array counted once: upper values
+  // + block columns (padding slots included: they are read), lower slot/column indices, slice offsets,
+  // z and p_old read, p_new and q written (4-wide vectors).  The transposed re-reads of upper blocks for
+  // the lower triangle and the repeated x gathers are cache traffic, not counted.
   double spmv_bytes(size_t s) const {
     const double up = topo.nslots, lo = topo.nlslots;
-    const double lo_real = (double)topo.nnzb - (double)(topo.nnzb + nv) / 2.0;
-    return up * (9.0 * s + 4.0) + lo * 8.0 + lo_real * 9.0 * s + 2.0 * (topo.nslices + 1) * 4 + 2.0 * nv * 4 * s;
+    return up * (9.0 * s + 4.0) + lo * 8.0 + 2.0 * (topo.nslices + 1) * 4 + 4.0 * nv * 4 * s;
   }
+
+  // bytes one PCG update pass moves: p, q, x, r read, x, r, z written, the 3x3 preconditioner blocks
+  double update_bytes(size_t s) const { return 7.0 * nv * 4 * s + 3.0 * nv * 4 * s; }
 
   // ------------------------------------------------------------------ adjoint of one step
   // The handle's next_deform holds u_{n+1}.  ubar, vbar (device [n]) hold the adjoint of (u_{n+1}, v_{n+1}) on
@@ -823,6 +860,9 @@ ssim_gb_status fail(ssim_gb_timestep* h, ssim_gb_status s, const std::string& ms
   catch (const ssim_gb::numerical_error& e) {                                                    \
     return fail(h, SSIM_GB_ERR_NUMERICAL, e.what());                                             \
   }                                                                                              \
+  catch (const ssim_gb::device_timeout& e) {                                                     \
+    return fail(h, SSIM_GB_ERR_DEVICE_TIMEOUT, e.what());                                        \
+  }                                                                                              \
   catch (const ssim_gb::cuda_error& e) {                                                         \
     return fail(h, SSIM_GB_ERR_CUDA, e.what());                                                  \
   }                                                                                              \
@@ -920,6 +960,10 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->cg_check_every = 8;
   p->ls_energy_slack = 1e-14;
   p->pd_kappa_mode = 0;
+  p->pcg_persistent = 3;
+  p->pcg_spin_limit = 0;
+  p->pcg_barrier_extra = 0;
+  p->pcg_max_blocks = 0;
 }
 
 ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
@@ -1021,6 +1065,8 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
   if (!p) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null params");
   if (p->max_newton_iters < 0 || p->cg_max_iters < 0 || p->max_ls_iters < 1 || !(p->ls_shrink > 0 && p->ls_shrink < 1) ||
       !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 1 ||
+      p->pcg_persistent < 0 || p->pcg_persistent > 3 || p->pcg_spin_limit < 0 || p->pcg_barrier_extra < 0 ||
+      p->pcg_max_blocks < 0 ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;

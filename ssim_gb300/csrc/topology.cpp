@@ -79,7 +79,10 @@ void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
     t.sl_off[s + 1] = t.sl_off[s] + 32 * wu;
     t.lo_off[s + 1] = t.lo_off[s] + 32 * wl;
   }
-  t.nslots = t.sl_off[t.nslices];
+  // one slice of padding slots after the last row slice: never assembled into, always zero; the lower
+  // index points its padding entries at the first of them, so the SpMV needs no branch on padding
+  t.zero_slot = t.sl_off[t.nslices];
+  t.nslots = t.sl_off[t.nslices] + 32;
   t.nlslots = t.lo_off[t.nslices];
   t.sl_col.assign(t.nslots, 0);
   t.slot_row.assign(t.nslots, -1);
@@ -106,7 +109,7 @@ void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
       }
     }
   }
-  t.lo_src.assign(t.nlslots, -1);
+  t.lo_src.assign(t.nlslots, t.zero_slot);
   t.lo_col.assign(t.nlslots, 0);
   for (int s = 0; s < t.nslices; ++s) {
     const int W = (t.lo_off[s + 1] - t.lo_off[s]) / 32;

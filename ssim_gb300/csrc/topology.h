@@ -16,7 +16,8 @@ struct Topology {
   int max_deg = 0;
   // The matrix is symmetric; only the upper blocks (w >= u) are stored, in SELL-32: slice s = block rows
   // 32s..32s+31, width = the slice's largest upper degree.
-  int nslices = 0, nslots = 0;
+  int nslices = 0, nslots = 0;  // nslots = sl_off[nslices] + 32 (a trailing all-padding slice)
+  int zero_slot = 0;             // first slot of the trailing slice: values always zero
   std::vector<int32_t> sl_off;    // [nslices+1] multiples of 32
   std::vector<int32_t> sl_col;    // [nslots] block column w (own row for padding)
   std::vector<int32_t> slot_row;  // [nslots] block row u, -1 for padding
@@ -25,7 +26,7 @@ struct Topology {
   // lower blocks of row u are the transposes of upper slots of other rows, listed in SELL-32 too
   int nlslots = 0;
   std::vector<int32_t> lo_off;  // [nslices+1]
-  std::vector<int32_t> lo_src;  // [nlslots] upper slot holding block (w, u), -1 for padding
+  std::vector<int32_t> lo_src;  // [nlslots] upper slot holding block (w, u), zero_slot for padding
   std::vector<int32_t> lo_col;  // [nlslots] w (own row for padding)
   // assembly lists: per upper slot, codes (e*10 + local upper block id) | (bit 31 if that element block
   // enters transposed)

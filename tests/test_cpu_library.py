@@ -110,3 +110,24 @@ def test_libssim_unit_box_layout():
     v, c = fem.unit_box(4, 3, 2)
     assert v.shape == (3, 24) and c.shape == (4, 5 * 3 * 2 * 1)
     assert v.dtype == np.float64 and c.dtype == np.int32
+
+
+def _header_struct_fields(name):
+    """(type, field) pairs of the typedef struct ``name`` in include/ssim_gb.h."""
+    import re
+
+    text = open(_lib.HEADER_PATH).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    m = re.search(r"typedef struct \{([^{}]*)\}\s*" + name + ";", text)
+    assert m, name
+    return re.findall(r"^\s*(int32_t|int64_t|double)\s+(\w+);", m.group(1), flags=re.M)
+
+
+@pytest.mark.parametrize("cname, pycls", [("ssim_gb_params", _lib.Params), ("ssim_gb_step_stats", _lib.StepStats)])
+def test_ctypes_structs_mirror_header(cname, pycls):
+    ctype = {"int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64, "double": ctypes.c_double}
+    hdr = [(f, ctype[t]) for t, f in _header_struct_fields(cname)]
+    assert hdr == list(pycls._fields_)
+    # the library's defaults round-trip through the Python struct
+    p = g.default_params()
+    assert p.pcg_persistent == 3 and p.pcg_barrier_extra == 0 and p.pcg_spin_limit == 0

@@ -360,3 +360,102 @@ def test_h0_stepper_fp64():
         ot.step_next()
         assert st["converged"] == 1 and sto["converged"] == 1
     assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6
+
+
+def _pcg_case(precision):
+    X, T = mesh.kuhn_box((12, 10, 9), (1.2, 1.0, 0.9))
+    X = mesh.jitter_interior(X, 0.01, 21)
+    ts, _ = _pair(X, T, E=1e5, nu=0.45, rho=1000.0, precision=precision)
+    ts.set_params(precond=2)
+    u = np.random.default_rng(3).uniform(-1, 1, X.shape) * 0.05
+    ts.set("next_deform", u)
+    ts.update_hessian(False, True, True)
+    b = np.random.default_rng(4).normal(size=X.shape)
+    return ts, b
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_persistent_pcg_bitwise_equals_two_launch(precision):
+    """Standard PCG in one cooperative launch (grid barriers; the last block to arrive runs the two-launch
+    path's reductions and epilogues) reproduces the two-launch loop bit for bit, also under an iteration cap."""
+    ts, b = _pcg_case(precision)
+    ts.set_params(pcg_persistent=0)
+    x0, it0, rr0 = ts.pcg(b, rtol=1e-6, max_iters=5000)
+    xc0, itc0, _ = ts.pcg(b, rtol=1e-12, max_iters=7)
+    ts.set_params(pcg_persistent=1)
+    x1, it1, rr1 = ts.pcg(b, rtol=1e-6, max_iters=5000)
+    xc1, itc1, _ = ts.pcg(b, rtol=1e-12, max_iters=7)
+    assert it0 == it1 and it0 > 10 and rr0 == rr1 and np.array_equal(x0, x1)
+    assert itc0 == itc1 == 7 and np.array_equal(xc0, xc1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_chronopoulos_gear_pcg_matches_two_launch(precision):
+    """Chronopoulos-Gear PCG in one launch and the two-launch PCG give the same iterates up to rounding:
+    iteration counts within 2, both true residuals at the tolerance, the solutions close; an iteration cap
+    stops both at the same iterate up to rounding."""
+    ts, b = _pcg_case(precision)
+    ts.set_params(pcg_persistent=0)
+    x0, it0, rr0 = ts.pcg(b, rtol=1e-6, max_iters=5000)
+    ts.set_params(pcg_persistent=2)
+    x1, it1, rr1 = ts.pcg(b, rtol=1e-6, max_iters=5000)
+    assert it0 > 10 and abs(it0 - it1) <= 2
+    bn = np.linalg.norm(b)
+    for x in (x0, x1):
+        assert np.linalg.norm(b - ts.spmv(x)) <= 1.5e-6 * bn
+    assert rel(x1, x0) <= (1e-9 if precision == "fp64" else 1e-4)
+    ts.set_params(pcg_persistent=0)
+    xc0, itc0, _ = ts.pcg(b, rtol=1e-12, max_iters=7)
+    ts.set_params(pcg_persistent=2)
+    xc1, itc1, _ = ts.pcg(b, rtol=1e-12, max_iters=7)
+    assert itc0 == itc1 == 7
+    assert rel(xc1, xc0) <= (1e-12 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("variant", [1, 2])
+def test_persistent_pcg_independent_of_grid(precision, variant):
+    """Partial sums are formed per 256-row virtual block and added in a fixed order by whichever block
+    arrives last, so the result is bitwise the same whether each block owns one virtual block or several."""
+    ts, b = _pcg_case(precision)
+    outs = []
+    for mb in (0, 3, 1):
+        ts.set_params(pcg_persistent=variant, pcg_max_blocks=mb)
+        outs.append(ts.pcg(b, rtol=1e-6, max_iters=5000))
+    for x, it, rr in outs[1:]:
+        assert it == outs[0][1] and rr == outs[0][2] and np.array_equal(x, outs[0][0])
+
+
+def test_persistent_newton_steps_match_two_launch():
+    scene = scenes.cube10()
+    outs = []
+    for pers in (0, 1, 2):
+        ts = scenes.build_timestep(scene, precision="mixed",
+                                   params=g.default_params(stop_mode=1, rel_tol=1e-6, pcg_persistent=pers))
+        for _ in range(2):
+            ts.step()
+            st = ts.stats()
+            assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"]
+        outs.append(ts.get("deformation"))
+    assert np.array_equal(outs[1], outs[0])
+    assert rel(outs[2], outs[0]) <= 1e-5
+
+
+def test_grid_barrier_wait_gives_up_and_context_survives():
+    """A barrier told to wait for one block more than the grid has (a flag nothing sets) gives up after
+    pcg_spin_limit polls: the call fails with DeviceTimeout, and the next solve on the same handle works."""
+    X, T = mesh.kuhn_box((6, 5, 4), (1.2, 1.0, 0.8))
+    ts, _ = _pair(X, T, E=1e5, nu=0.45, rho=1000.0)
+    u = np.random.default_rng(7).uniform(-1, 1, X.shape) * 0.05
+    ts.set("next_deform", u)
+    ts.update_hessian(False, True, True)
+    b = np.random.default_rng(8).normal(size=X.shape)
+    for variant in (1, 2):
+        ts.set_params(pcg_persistent=variant)
+        ref, it_ref, _ = ts.pcg(b, rtol=1e-10, max_iters=5000)
+        ts.set_params(pcg_barrier_extra=1, pcg_spin_limit=2000)
+        with pytest.raises(g.DeviceTimeout):
+            ts.pcg(b, rtol=1e-10, max_iters=5000)
+        ts.set_params(pcg_barrier_extra=0, pcg_spin_limit=0)
+        x, it, _ = ts.pcg(b, rtol=1e-10, max_iters=5000)
+        assert it == it_ref and np.array_equal(x, ref)
