@@ -179,9 +179,11 @@ def run_gpu_arm(args, scene):
     with ClockSampler(dev) as clk:
         ts, ms_mixed, st_mixed, launches, _ = timed_run("mixed", args.steps, args.warmup)
     clocks = clk.summary()
+    solve_log = ts.solve_log()
     if args.arms == "mixed":
         return dict(ms_mixed=ms_mixed, ms_fp64=float("nan"), st_mixed=st_mixed, st_fp64=[], launches=launches,
-                    prof=None, clocks=clocks, e2e_s=float("nan"), h2d=0, d2h=0, total_launches=0)
+                    prof=None, clocks=clocks, e2e_s=float("nan"), h2d=0, d2h=0, total_launches=0,
+                    solve_log=solve_log)
     # ---- roofline of the dominant kernel (PCG SpMV), events around each launch, same workload
     _, _, _, _, prof = timed_run("mixed", min(args.steps, 3), 1, profile=True)
     # ---- plain FP64 on the same steps
@@ -216,7 +218,7 @@ def run_gpu_arm(args, scene):
     result.update(
         ms_mixed=ms_mixed, ms_fp64=ms_fp64, st_mixed=st_mixed, st_fp64=st_fp64, launches=launches, prof=prof,
         clocks=clocks, e2e_s=e2e_s, h2d=fixed.size * 3 * 8 + fixed.size * 4, d2h=d.size * 8,
-        total_launches=g.launch_count() - launches0, nnz=ts.nnz,
+        total_launches=g.launch_count() - launches0, nnz=ts.nnz, solve_log=solve_log,
     )
     if args.adjoint:
         result["adjoint"] = [run_adjoint("mixed"), run_adjoint("fp64")]
@@ -426,6 +428,7 @@ def main():
             "e2e": {"value": round(steps_total / e2e_s, 4), "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": r["launches"],
+            "pcg_iters_per_solve_from_reset": r.get("solve_log"),
             "roofline": roofline,
             "cpu_baseline": cb,
             "clocks": r["clocks"],

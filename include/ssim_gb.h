@@ -180,6 +180,10 @@ SSIM_GB_API ssim_gb_status ssim_gb_step_next(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_step(ssim_gb_timestep* h, double* elapsed_ms);
 SSIM_GB_API ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st);
+/* PCG iteration counts of every solve since the last reset, oldest first: *count = number logged, the
+ * first min(count, capacity) copied to iters (diagnostics; no reference counterpart) */
+SSIM_GB_API ssim_gb_status ssim_gb_get_solve_log(const ssim_gb_timestep* h, int32_t* iters, int32_t capacity,
+                                                 int32_t* count);
 SSIM_GB_API ssim_gb_status ssim_gb_check_convergence(ssim_gb_timestep* h, int32_t* converged);
 SSIM_GB_API ssim_gb_status ssim_gb_threshold_abs(const ssim_gb_timestep* h, double* abs_tol);
 

@@ -134,6 +134,7 @@ _SIGS = {
     "ssim_gb_step": (C.c_int, [_H, _D]),
     "ssim_gb_restore": (C.c_int, [_H]),
     "ssim_gb_get_step_stats": (C.c_int, [_H, C.POINTER(StepStats)]),
+    "ssim_gb_get_solve_log": (C.c_int, [_H, _I, C.c_int32, _I]),
     "ssim_gb_check_convergence": (C.c_int, [_H, _I]),
     "ssim_gb_threshold_abs": (C.c_int, [_H, _D]),
     "ssim_gb_update_energy_and_gradients": (C.c_int, [_H, C.c_int32, _D]),

@@ -58,6 +58,7 @@ struct DevScalars {
   // PCG
   double rz, rz_old, pq, rr, rr0, tol2;
   double alpha, beta;  // rz / pq and rz / rz_old, formed once by the reducing block
+  double inv_rz, inv_alpha;  // 1 / rz and 1 / alpha of the last Chronopoulos-Gear step
   int32_t iters;
   int32_t done;
   int32_t status;  // 0 ok, 1 breakdown (pq <= 0), 2 non-finite residual
@@ -75,13 +76,13 @@ struct BlockPartials {
 template <int NV, int BLOCK>
 __device__ __forceinline__ void block_sum(double (&vals)[NV], double (*sh)[NV]) {
   // warp reduce then shared reduce; result valid in thread 0
+  // the NV sums advance level by level together, so their FP64 latency chains overlap (FP64 latency is
+  // long on GB300); each sum's order of additions is that of a per-value tree
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double x = vals[k];
+  for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    vals[k] = x;
+    for (int k = 0; k < NV; ++k) vals[k] += __shfl_down_sync(0xffffffffu, vals[k], o);
   }
   if (lane == 0) {
 #pragma unroll
@@ -89,12 +90,16 @@ __device__ __forceinline__ void block_sum(double (&vals)[NV], double (*sh)[NV]) 
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    double s[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s = 0;
-      for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][k];
-      vals[k] = s;
+    for (int k = 0; k < NV; ++k) s[k] = 0;
+#pragma unroll
+    for (int w = 0; w < BLOCK / 32; ++w) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) s[k] += sh[w][k];
     }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) vals[k] = s[k];
   }
 }
 
@@ -104,21 +109,30 @@ __device__ __forceinline__ void block_sum(double (&vals)[NV], double (*sh)[NV]) 
 template <int NV, int BLOCK, typename S>
 __device__ __forceinline__ void block_sum_s(const S (&vals)[NV], double (&out)[NV], double (*sh)[NV]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  S x[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    S x = vals[k];
+  for (int k = 0; k < NV; ++k) x[k] = vals[k];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[warp][k] = (double)x;
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[warp][k] = (double)x[k];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    double s[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s = 0;
-      for (int w = 0; w < BLOCK / 32; ++w) s += sh[w][k];
-      out[k] = s;
+    for (int k = 0; k < NV; ++k) s[k] = 0;
+#pragma unroll
+    for (int w = 0; w < BLOCK / 32; ++w) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) s[k] += sh[w][k];
     }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = s[k];
   }
 }
 

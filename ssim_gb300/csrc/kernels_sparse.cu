@@ -453,11 +453,12 @@ __device__ __forceinline__ bool grid_barrier_last(const GridSync& gs, F&& last_f
   if (threadIdx.x == 0) {
     gen0 = ld_acquire_gpu(gs.gen);
     __threadfence();
-    role = (atomicAdd(gs.count, 1u) == gridDim.x + gs.extra - 1) ? 1 : 0;
+    const bool last = atomicAdd(gs.count, 1u) == gridDim.x + gs.extra - 1;
+    if (last) __threadfence();  // acquire side of the other blocks' arrivals; the block follows via bar.sync
+    role = last ? 1 : 0;
   }
   __syncthreads();
   if (role == 1) {
-    __threadfence();
     last_fn();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -576,21 +577,26 @@ __device__ __forceinline__ void cgcg_after(DevScalars* sc, double g, double d, d
     sc->done = 1;
     return;
   }
+  // beta = g / g_old and den = d - beta g / alpha_old from the reciprocals kept by the previous step, so
+  // only two independent divisions remain on this serial path (FP64 divisions are slow on GB300)
   double beta = 0.0, den = d;
   if (sc->iters > 0) {
-    beta = g / sc->rz;
-    den = d - beta * g / sc->alpha;
+    beta = g * sc->inv_rz;
+    den = d - beta * g * sc->inv_alpha;
   }
   if (!(den > 0.0)) {  // breakdown: not SPD along p (or non-finite)
     sc->done = 1;
     sc->status = 1;
     return;
   }
+  const double inv_den = 1.0 / den, inv_g = 1.0 / g;
   sc->rz_old = sc->rz;
   sc->rz = g;
   sc->pq = den;
   sc->beta = beta;
-  sc->alpha = g / den;
+  sc->alpha = g * inv_den;
+  sc->inv_rz = inv_g;
+  sc->inv_alpha = den * inv_g;
   sc->iters += 1;
 }
 

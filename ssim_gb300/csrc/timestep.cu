@@ -122,6 +122,7 @@ struct TimeStep {
   // ---- profiling
   bool profiling = false;
   std::vector<cudaEvent_t> ev;
+  std::vector<int32_t> solve_log;  // PCG iterations of every solve since the last reset
   long long prof_launch[PK_COUNT] = {0};
   double prof_ms[PK_COUNT] = {0};
   double prof_bytes[PK_COUNT] = {0};
@@ -294,6 +295,7 @@ struct TimeStep {
     }
     SSIM_CUDA(cudaStreamSynchronize(stream));
     has_reset = true;
+    solve_log.clear();
   }
 
   // time_step_solver_pd::reset_impl (projective_dynamics.hpp:53-93): (mass(rho) + laplace(dt^2 kappa)) (x) I3
@@ -451,6 +453,7 @@ struct TimeStep {
         }
         if (rel_res) *rel_res = hsc->rr0 > 0 ? std::sqrt(hsc->rr / hsc->rr0) : 0.0;
         if (hsc->status == 2) throw numerical_error("PCG produced a non-finite residual");
+        if (solve_log.size() < (1u << 20)) solve_log.push_back(hsc->iters);
         return hsc->iters;
       }
     }
@@ -499,6 +502,7 @@ struct TimeStep {
     }
     if (rel_res) *rel_res = hsc->rr0 > 0 ? std::sqrt(hsc->rr / hsc->rr0) : 0.0;
     if (hsc->status == 2) throw numerical_error("PCG produced a non-finite residual");
+    if (solve_log.size() < (1u << 20)) solve_log.push_back(hsc->iters);
     return hsc->iters;
   }
 
@@ -1239,6 +1243,15 @@ ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h) {
 ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st) {
   CHECK_H(h);
   if (st) *st = h->ts.stats;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_get_solve_log(const ssim_gb_timestep* h, int32_t* iters, int32_t capacity, int32_t* count) {
+  CHECK_H(h);
+  const auto& log = h->ts.solve_log;
+  if (count) *count = (int32_t)log.size();
+  if (iters && capacity > 0)
+    std::copy(log.begin(), log.begin() + std::min<size_t>(log.size(), (size_t)capacity), iters);
   return SSIM_GB_OK;
 }
 

@@ -182,6 +182,14 @@ class TimeStep:
         self._c(self._L.ssim_gb_get_step_stats(self._h, C.byref(s)))
         return s.as_dict()
 
+    def solve_log(self) -> list[int]:
+        """PCG iterations of every solve since the last reset."""
+        n = C.c_int32()
+        self._c(self._L.ssim_gb_get_solve_log(self._h, None, 0, C.byref(n)))
+        buf = np.zeros(max(1, n.value), dtype=np.int32)
+        self._c(self._L.ssim_gb_get_solve_log(self._h, iptr(buf), n.value, C.byref(n)))
+        return buf[: n.value].tolist()
+
     def check_convergence(self) -> bool:
         c = C.c_int32()
         self._c(self._L.ssim_gb_check_convergence(self._h, C.byref(c)))
