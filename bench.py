@@ -372,12 +372,13 @@ def main():
         p = prof["pcg_iteration"]
         avg_s = p["total_ms"] / p["launches"] / 1e3
         algo = spmv_algo + 7 * s_b * n
-        roofline = {"kernel": "pcg_persistent_kernel<float> (whole PCG solve in one cooperative launch; "
-                              "unit = one PCG iteration: symmetric SELL-32 SpMV + update, 2 grid barriers)",
+        roofline = {"kernel": "cgcg_persistent_kernel<float> (whole Chronopoulos-Gear PCG solve in one cooperative "
+                              "launch; unit = one PCG iteration: symmetric SELL-32 SpMV + dots, grid reduction, "
+                              "vector update, grid barrier)",
                     "bound": "hbm", "achieved": round(algo / avg_s / 1e9, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(algo / avg_s / 1e9 / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_iteration": algo, "avg_iteration_us": round(avg_s * 1e6, 2),
-                    "iterations_timed": p["launches"], "traffic": ncu_traffic(args.workload, "pcg_persistent"),
+                    "iterations_timed": p["launches"], "traffic": ncu_traffic(args.workload, "cgcg_persistent"),
                     "format_bytes_per_iteration": round(p["bytes_per_launch"]),
                     "format_frac": round(p["bytes_per_launch"] / avg_s / 1e9 / peak, 4)}
     elif prof and prof["pcg_spmv"]["launches"] > 0:

@@ -125,6 +125,14 @@ def _function():
 _FN = None
 
 
+def implicit_rollout_function():
+    """The autograd Function class behind ``rollout`` (created on first use: torch is imported lazily)."""
+    global _FN
+    if _FN is None:
+        _FN = _function()
+    return _FN
+
+
 def rollout(E_cells, v0, engine: RolloutEngine, num_steps: int, checkpoint_every: int = 8):
     """Final displacement u_N [V,3] (torch, cuda, float64), differentiable w.r.t. E_cells and v0."""
     global _FN

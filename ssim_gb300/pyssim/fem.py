@@ -106,3 +106,20 @@ class TetFiniteElementSolver_Cuda:
 
 class TetFiniteElementSolver_Host(TetFiniteElementSolver_Cuda):
     """Same interface as the reference's CPU solver class; computes on the GPU."""
+
+
+def ImplicitStep():
+    """The ``torch.autograd.Function`` class of a differentiable backward-Euler rollout (forward: N implicit
+    steps from per-element Young's moduli and initial velocities; backward: the hand-written adjoint with
+    checkpoint recomputation).  See ``rollout``."""
+    from .. import adjoint
+
+    return adjoint.implicit_rollout_function()
+
+
+def rollout(E_cells, v0, engine, num_steps: int, checkpoint_every: int = 8):
+    """Final displacement after ``num_steps`` implicit steps, differentiable w.r.t. E_cells [T] and v0 [V,3]
+    (torch CUDA float64 tensors); ``engine`` is an ``ssim_gb300.adjoint.RolloutEngine``."""
+    from .. import adjoint
+
+    return adjoint.rollout(E_cells, v0, engine, num_steps, checkpoint_every)
