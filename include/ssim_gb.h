@@ -53,7 +53,9 @@ typedef enum {
   SSIM_GB_STEPPER_PD = 2,     /* time_step_solver_pd (projective_dynamics.hpp:9-97) */
   SSIM_GB_STEPPER_NONE = 3,   /* time_step_solver_nothing (time_step.hpp:131-142) */
   SSIM_GB_STEPPER_FORWARD_EULER = 4, /* time_step_solver_forward_euler (time_step.hpp:717-736) */
-  SSIM_GB_STEPPER_H0 = 5      /* time_step_solver_h0 (projective_dynamics.hpp:100-150) */
+  SSIM_GB_STEPPER_H0 = 5,     /* time_step_solver_h0 (projective_dynamics.hpp:100-150) */
+  SSIM_GB_STEPPER_NCG = 6,    /* time_step_solver_ncg (nonlinear_cg.hpp:9-38) */
+  SSIM_GB_STEPPER_NCG_EXT = 7 /* time_step_solver_ncg_with_ext_prec (nonlinear_cg.hpp:40-97): x = L L^T g */
 } ssim_gb_stepper;
 
 typedef enum {
@@ -101,6 +103,10 @@ typedef struct {
   int32_t pcg_barrier_extra; /* test hook: arrivals a grid barrier waits for beyond the grid; 0 in normal use,
                                 > 0 makes every wait run out after pcg_spin_limit polls */
   int32_t pcg_max_blocks; /* cap on the persistent PCG grid (0: as many 256-thread blocks as are resident) */
+  int32_t ncg_max_iters;  /* nonlinear CG iteration cap: 1000 as the reference (nonlinear_cg.hpp:20) */
+  double ncg_step0;       /* first trial step of the first NCG iteration: the reference's learning rate 1e-2 */
+  double ncg_eta;         /* Dai-Kou truncation: beta >= ncg_eta * g.d / |d|^2 (0.5) */
+  int32_t ncg_expand;     /* line-search expansions toward the fitted parabola's minimiser (3) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
@@ -180,6 +186,11 @@ SSIM_GB_API ssim_gb_status ssim_gb_step_next(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_step(ssim_gb_timestep* h, double* elapsed_ms);
 SSIM_GB_API ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st);
+/* NCG preconditioner factor L of SSIM_GB_STEPPER_NCG_EXT (x = L L^T g; timestep_ncg::set_matrix,
+ * fem_cuda.cu:206): nnz values in the CSR order of ssim_gb_get_csr_pattern; NULL restores the identity,
+ * which reset() installs (fem_cuda.cu:174-204).  Unlike the reference wrapper, whose solver never
+ * receives the matrix (fem_cuda.cu:177-204 vs nonlinear_cg.hpp:73), the values set here are used. */
+SSIM_GB_API ssim_gb_status ssim_gb_set_ncg_matrix(ssim_gb_timestep* h, const double* values);
 /* PCG iteration counts of every solve since the last reset, oldest first: *count = number logged, the
  * first min(count, capacity) copied to iters (diagnostics; no reference counterpart) */
 SSIM_GB_API ssim_gb_status ssim_gb_get_solve_log(const ssim_gb_timestep* h, int32_t* iters, int32_t capacity,

@@ -272,6 +272,7 @@ struct orc_ts {
   Vec dminv, vol, defgrad, local_energy, local_force, local_K;
   // CSR (identical pattern for mass, system and PD matrices)
   std::vector<int32_t> row_ptr, col_idx;
+  Vec ncg_L;                  // NCG preconditioner factor on the CSR pattern (empty: identity)
   Vec mass_vals, massf_vals, sys_vals, pd_vals;
   std::vector<int32_t> hess_dst;            // [nt*144] CSR slot of each local entry
   std::vector<int32_t> hcon_ptr, hcon_src;  // per CSR slot, the local entries that add into it
@@ -713,6 +714,10 @@ void orc_default_params(orc_params* p) {
   p->lbfgs_armijo = 1e-4;
   p->max_lbfgs_iters = 1000;
   p->ls_energy_slack = 1e-14;
+  p->ncg_max_iters = 1000;
+  p->ncg_step0 = 1e-2;
+  p->ncg_eta = 0.5;
+  p->ncg_expand = 3;
 }
 
 orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double dt, double E, double nu,
@@ -1006,6 +1011,143 @@ static double lbfgs_core(orc_ts* s, const orc_params* p, orc_stats* st, int mode
   if (st) *st = loc;
   energy_and_gradients(*s, false);
   return nrm2(s->forces);
+}
+
+// ---------------------------------------------------------------- nonlinear CG
+// Reference: time_step_solver_ncg / _with_ext_prec (nonlinear_cg.hpp:9-97) run mathprim's ncg_optimizer
+// with the Dai-Kou strategy, a backtracking line search, learning rate 1e-2 and at most 1000 iterations;
+// the preconditioned variant applies x = L (L^T g) (nonlinear_cg.hpp:52-57).  mathprim is not in the
+// reference tree, so the iteration is restated from the published method and is parity-unpinned:
+//   direction: d0 = -H g0 (H = L L^T, identity by default); d_{k+1} = -H g_{k+1} + beta d_k with the
+//     Dai-Kou beta (Y.-H. Dai, C.-X. Kou, SIAM J. Optim. 23(1) 2013, tau_k = s^T y / |s|^2):
+//     beta = g^T H y / d^T y - (y^T H y) (g^T d) / (d^T y)^2, truncated to >= eta g^T d / |d|^2
+//     (g the new gradient, d the last direction, y = g_new - g_old); restart d = -H g when not descending;
+//   line search: Armijo (lbfgs_armijo) backtracking from alpha_init, a failed trial shrinks to the
+//     minimiser of the parabola through E, g^T d and the trial energy, clamped to [0.1, 0.5] alpha; after
+//     an accepted trial, up to ncg_expand moves to that parabola's minimiser when it lies beyond 1.5
+//     alpha (at most 10 alpha), kept while the energy decreases;
+//   alpha_init(0) = ncg_step0, alpha_init(k) = alpha(k-1) (g_{k-1}^T d_{k-1}) / (g_k^T d_k).
+static void ncg_apply(const orc_ts& s, bool prec, const Vec& g, Vec& z) {
+  const int n = s.n;
+  if (!prec || s.ncg_L.empty()) {
+    z = g;
+    return;
+  }
+  // t = L^T g (row i of L^T = column i of L: read through the transposed entry of the symmetric pattern)
+  Vec t(n, 0.0);
+  for (int r = 0; r < n; ++r) {
+    double acc = 0;
+    for (int k = s.row_ptr[r]; k < s.row_ptr[r + 1]; ++k) {
+      const int c = s.col_idx[k];
+      // L[c][r]: position of r in row c
+      const int* b = s.col_idx.data() + s.row_ptr[c];
+      const int* e = s.col_idx.data() + s.row_ptr[c + 1];
+      const int kt = (int)(std::lower_bound(b, e, r) - s.col_idx.data());
+      acc += s.ncg_L[kt] * g[c];
+    }
+    t[r] = acc;
+  }
+  z.assign(n, 0.0);
+  for (int r = 0; r < n; ++r) {
+    double acc = 0;
+    for (int k = s.row_ptr[r]; k < s.row_ptr[r + 1]; ++k) acc += s.ncg_L[k] * t[s.col_idx[k]];
+    z[r] = acc;
+  }
+}
+
+static double ncg_core(orc_ts* s, const orc_params* p, orc_stats* st, bool prec) {
+  orc_stats loc{};
+  const int n = s->n;
+  double E = energy_and_gradients(*s, false);
+  double Escale = s->energy_scale;
+  Vec g = s->forces, gprev = g, z(n), y(n), hy(n), d(n), xt(n);
+  const double g0 = nrm2(g);
+  loc.grad_norm0 = g0;
+  ncg_apply(*s, prec, g, z);
+  for (int k = 0; k < n; ++k) d[k] = -z[k];
+  double gd = dot(g, d);
+  double alpha_init = p->ncg_step0;
+  int it = 0;
+  auto trial = [&](double a) {
+    for (int k = 0; k < n; ++k) xt[k] = s->next[k] + a * d[k];
+    loc.ls_steps_total++;
+    return energy_only(*s, xt);
+  };
+  for (;; ++it) {
+    const double gn = nrm2(g);
+    loc.grad_norm = gn;
+    loc.energy = E;
+    if (stop_ok(*s, *p, gn, g0)) {
+      loc.converged = 1;
+      break;
+    }
+    if (it >= p->ncg_max_iters) break;
+    if (!(gd < 0)) {  // restart
+      for (int k = 0; k < n; ++k) d[k] = -z[k];
+      gd = dot(g, d);
+      if (!(gd < 0)) {
+        for (int k = 0; k < n; ++k) d[k] = -g[k];
+        gd = dot(g, d);
+      }
+      alpha_init = p->ncg_step0;
+    }
+    double a = alpha_init, Et = trial(a);
+    const double slack = p->ls_energy_slack * Escale;
+    auto armijo = [&](double aa, double ee) { return ee <= E + p->lbfgs_armijo * aa * gd + slack; };
+    for (int ls = 1; ls < p->max_ls_iters && !armijo(a, Et); ++ls) {
+      const double c2 = (Et - E - gd * a) / (a * a);
+      double an = c2 > 0 ? -gd / (2 * c2) : 0.5 * a;
+      if (!std::isfinite(an)) an = 0.5 * a;
+      a = std::min(std::max(an, 0.1 * a), 0.5 * a);
+      Et = trial(a);
+    }
+    for (int ex = 0; ex < p->ncg_expand && armijo(a, Et); ++ex) {
+      const double c2 = (Et - E - gd * a) / (a * a);
+      if (!(c2 > 0)) break;
+      const double astar = -gd / (2 * c2);
+      if (!(astar > 1.5 * a)) break;
+      const double an = std::min(astar, 10 * a);
+      const double En = trial(an);
+      if (!(En < Et) || !armijo(an, En)) break;
+      a = an;
+      Et = En;
+    }
+    for (int k = 0; k < n; ++k) s->next[k] += a * d[k];
+    loc.last_change = a * nrm2(d);
+    E = energy_and_gradients(*s, false);
+    Escale = s->energy_scale;
+    g = s->forces;
+    for (int k = 0; k < n; ++k) y[k] = g[k] - gprev[k];
+    gprev = g;
+    ncg_apply(*s, prec, g, z);
+    if (prec && !s->ncg_L.empty())
+      ncg_apply(*s, prec, y, hy);
+    else
+      hy = y;
+    const double dy = dot(d, y), zy = dot(z, y), yhy = dot(y, hy), gdn = dot(g, d), dd = dot(d, d);
+    double beta = 0;
+    if (dy > 1e-300) beta = zy / dy - yhy * gdn / (dy * dy);
+    if (dd > 0) beta = std::max(beta, p->ncg_eta * gdn / dd);
+    const double gd_old = gd;
+    for (int k = 0; k < n; ++k) d[k] = beta * d[k] - z[k];
+    gd = dot(g, d);
+    alpha_init = (gd < 0 && gd_old < 0) ? a * gd_old / gd : p->ncg_step0;
+  }
+  loc.newton_iters = it;
+  if (st) *st = loc;
+  energy_and_gradients(*s, false);
+  return nrm2(s->forces);
+}
+
+double orc_compute_step_ncg(orc_ts* s, const orc_params* p, orc_stats* st) { return ncg_core(s, p, st, false); }
+double orc_compute_step_ncg_prec(orc_ts* s, const orc_params* p, orc_stats* st) { return ncg_core(s, p, st, true); }
+
+void orc_set_ncg_matrix(orc_ts* s, const double* values) {
+  if (!values) {
+    s->ncg_L.clear();
+    return;
+  }
+  s->ncg_L.assign(values, values + s->col_idx.size());
 }
 
 double orc_compute_step_lbfgs(orc_ts* s, const orc_params* p, orc_stats* st) { return lbfgs_core(s, p, st, 0); }

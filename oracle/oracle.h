@@ -78,6 +78,10 @@ typedef struct {
   double lbfgs_armijo;   /* L-BFGS Armijo constant */
   int max_lbfgs_iters;
   double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack S_E, S_E = sum of |energy terms| */
+  int ncg_max_iters;      /* nonlinear CG: reference 1000 (nonlinear_cg.hpp:20) */
+  double ncg_step0;       /* first trial step of the first iteration: reference learning_rate 1e-2 (:21) */
+  double ncg_eta;         /* Dai-Kou truncation beta >= eta g.d / |d|^2 */
+  int ncg_expand;         /* line-search expansions toward the parabola's minimiser */
 } orc_params;
 
 typedef struct {
@@ -128,6 +132,12 @@ double orc_compute_step_lbfgs(orc_ts* ts, const orc_params* p, orc_stats* st);
 double orc_compute_step_pd(orc_ts* ts, const orc_params* p, orc_stats* st);
 double orc_compute_step_h0(orc_ts* ts, const orc_params* p, orc_stats* st);
 double orc_compute_step_forward_euler(orc_ts* ts, const orc_params* p, orc_stats* st);
+/* time_step_solver_ncg (nonlinear_cg.hpp:9-38) and _with_ext_prec (:40-97): nonlinear CG, the latter
+ * preconditioned by x = L L^T g with L on the system matrix's CSR pattern (identity until set) */
+double orc_compute_step_ncg(orc_ts* ts, const orc_params* p, orc_stats* st);
+double orc_compute_step_ncg_prec(orc_ts* ts, const orc_params* p, orc_stats* st);
+/* L's values in the CSR order of the system matrix (orc_get_csr); NULL restores the identity */
+void orc_set_ncg_matrix(orc_ts* ts, const double* values);
 void orc_step_next(orc_ts* ts);
 void orc_restore(orc_ts* ts);
 int orc_check_convergence(orc_ts* ts);

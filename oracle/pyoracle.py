@@ -51,6 +51,10 @@ class OrcParams(C.Structure):
         ("lbfgs_armijo", C.c_double),
         ("max_lbfgs_iters", C.c_int),
         ("ls_energy_slack", C.c_double),
+        ("ncg_max_iters", C.c_int),
+        ("ncg_step0", C.c_double),
+        ("ncg_eta", C.c_double),
+        ("ncg_expand", C.c_int),
     ]
 
 
@@ -132,6 +136,9 @@ def lib():
         "orc_compute_step_pd": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_compute_step_h0": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_compute_step_forward_euler": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
+        "orc_compute_step_ncg": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
+        "orc_compute_step_ncg_prec": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
+        "orc_set_ncg_matrix": (None, [vp, C.c_void_p]),
         "orc_step_next": (None, [vp]),
         "orc_restore": (None, [vp]),
         "orc_check_convergence": (C.c_int, [vp]),
@@ -354,9 +361,20 @@ class OracleTimeStep:
             "pd": self._L.orc_compute_step_pd,
             "h0": self._L.orc_compute_step_h0,
             "forward_euler": self._L.orc_compute_step_forward_euler,
+            "ncg": self._L.orc_compute_step_ncg,
+            "ncg_ext": self._L.orc_compute_step_ncg_prec,
         }[method]
         r = fn(self._h, C.byref(p), C.byref(st))
         return r, st.as_dict()
+
+    def set_ncg_matrix(self, values=None):
+        """Values of the NCG preconditioner factor L in the system matrix's CSR order (None: identity)."""
+        if values is None:
+            self._L.orc_set_ncg_matrix(self._h, None)
+            return
+        self._ncg_vals = _f64(values).reshape(-1)
+        assert self._ncg_vals.size == self.nnz
+        self._L.orc_set_ncg_matrix(self._h, self._ncg_vals.ctypes.data)
 
     def step_next(self):
         self._L.orc_step_next(self._h)

@@ -20,6 +20,7 @@ HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "ssim_gb.h")
  ERR_DEVICE_TIMEOUT) = range(8)
 FP64, MIXED = 0, 1
 STEPPER_NEWTON, STEPPER_LBFGS, STEPPER_PD, STEPPER_NONE = 0, 1, 2, 3
+STEPPER_FORWARD_EULER, STEPPER_H0, STEPPER_NCG, STEPPER_NCG_EXT = 4, 5, 6, 7
 FIELDS = {
     "deformation": 0,
     "prev_deform": 1,
@@ -57,6 +58,10 @@ class Params(C.Structure):
         ("pcg_spin_limit", C.c_int64),
         ("pcg_barrier_extra", C.c_int32),
         ("pcg_max_blocks", C.c_int32),
+        ("ncg_max_iters", C.c_int32),
+        ("ncg_step0", C.c_double),
+        ("ncg_eta", C.c_double),
+        ("ncg_expand", C.c_int32),
     ]
 
     def as_dict(self):
@@ -135,6 +140,7 @@ _SIGS = {
     "ssim_gb_restore": (C.c_int, [_H]),
     "ssim_gb_get_step_stats": (C.c_int, [_H, C.POINTER(StepStats)]),
     "ssim_gb_get_solve_log": (C.c_int, [_H, _I, C.c_int32, _I]),
+    "ssim_gb_set_ncg_matrix": (C.c_int, [_H, _D]),
     "ssim_gb_check_convergence": (C.c_int, [_H, _I]),
     "ssim_gb_threshold_abs": (C.c_int, [_H, _D]),
     "ssim_gb_update_energy_and_gradients": (C.c_int, [_H, C.c_int32, _D]),

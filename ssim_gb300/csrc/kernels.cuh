@@ -105,6 +105,10 @@ template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned int* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st);
+// y = A x, A a scalar CSR matrix over dofs, x / y 4-wide vertex vectors
+template <typename S>
+void launch_csr_dof_spmv(int n, const int* rp, const int* ci, const S* vals, const V4<S>* x, V4<S>* y,
+                         cudaStream_t st);
 template <typename S>
 void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                        int max_iters, const Reduce& red, cudaStream_t st);

@@ -724,6 +724,25 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
   if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
 }
 
+// ------------------------------------------------------------------ scalar CSR on 4-wide vectors
+// y = A x for a scalar CSR matrix over dofs (row / column i = vertex i / 3, component i % 3), x and y in the
+// solver's 4-wide vertex layout; one thread per row, entries in CSR order (the NCG preconditioner factor).
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    csr_dof_spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const S* __restrict__ vals,
+                        const V4<S>* __restrict__ x, V4<S>* __restrict__ y) {
+  const int r = blockIdx.x * SB + threadIdx.x;
+  if (r >= n) return;
+  const S* xs = reinterpret_cast<const S*>(x);
+  S acc = S(0);
+  const int k1 = rp[r + 1];
+  for (int k = rp[r]; k < k1; ++k) {
+    const int c = ci[k];
+    acc += vals[k] * xs[4 * (c / 3) + c % 3];
+  }
+  reinterpret_cast<S*>(y)[4 * (r / 3) + r % 3] = acc;
+}
+
 // ------------------------------------------------------------------ vectors
 template <typename S>
 __global__ void __launch_bounds__(SB)
@@ -1008,6 +1027,14 @@ bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv
 }
 
 template <typename S>
+void launch_csr_dof_spmv(int n, const int* rp, const int* ci, const S* vals, const V4<S>* x, V4<S>* y,
+                         cudaStream_t st) {
+  if (n <= 0) return;
+  csr_dof_spmv_kernel<S><<<div_up(n, SB), SB, 0, st>>>(n, rp, ci, vals, x, y);
+  after_launch("csr_dof_spmv");
+}
+
+template <typename S>
 void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                        int max_iters, const Reduce& red, cudaStream_t st) {
   pcg_update_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, p, q, dinv, x, r, z, max_iters, red);
@@ -1132,6 +1159,7 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
                                          V4<S>*, V4<S>*, V4<S>*, int, const Reduce&, unsigned int*, long long,   \
                                          int, int, int, cudaStream_t);                                            \
   template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
+  template void launch_csr_dof_spmv<S>(int, const int*, const int*, const S*, const V4<S>*, V4<S>*, cudaStream_t); \
   template void launch_axpy_update<S>(int, double, const V4<S>*, const double*, double*, float4*, cudaStream_t); \
   template void launch_to_vec4<S>(int, const double*, V4<S>*, bool, cudaStream_t);                               \
   template void launch_from_vec4<S>(int, const V4<S>*, double*, cudaStream_t);                                  \

@@ -59,8 +59,11 @@ struct Solver {
   std::vector<std::unique_ptr<DBuf<V4<S>>>> hs, hy;
   DBuf<S> pd_vals, slot_pd;
   DBuf<V4<S>> pd_dinv;
+  DBuf<S> ncg_L, ncg_Lt;  // NCG preconditioner factor and its transpose on the CSR pattern
+  long ncg_version = -1;
   void release() {
-    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd}) b->release();
+    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &ncg_L, &ncg_Lt}) b->release();
+    ncg_version = -1;
     for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &ld, &lq, &pd_dinv}) b->release();
     hs.clear();
     hy.clear();
@@ -123,6 +126,12 @@ struct TimeStep {
   bool profiling = false;
   std::vector<cudaEvent_t> ev;
   std::vector<int32_t> solve_log;  // PCG iterations of every solve since the last reset
+  // NCG preconditioner factor L (host copy; empty = identity), its CSR pattern on the device and the
+  // position of each entry's transpose
+  std::vector<double> ncg_vals;
+  long ncg_ver = 0;
+  DBuf<int32_t> ncg_rp, ncg_ci;
+  std::vector<int64_t> ncg_tperm;
   long long prof_launch[PK_COUNT] = {0};
   double prof_ms[PK_COUNT] = {0};
   double prof_bytes[PK_COUNT] = {0};
@@ -248,7 +257,7 @@ struct TimeStep {
     if (!(E >= 0)) throw invalid_argument("Young's modulus must be positive, got " + std::to_string(E));
     if (!(nu > 0 && nu < 0.5)) throw invalid_argument("Poisson's ratio must be in (0, 0.5), got " + std::to_string(nu));
     if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
-    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_H0) throw invalid_argument("unknown stepper");
+    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NCG_EXT) throw invalid_argument("unknown stepper");
     stepper = stepper_kind;
     for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
     // material: per element Lame parameters (basic_elast.hpp:10-20)
@@ -296,6 +305,8 @@ struct TimeStep {
     SSIM_CUDA(cudaStreamSynchronize(stream));
     has_reset = true;
     solve_log.clear();
+    ncg_vals.clear();  // timestep_ncg::reset installs the identity (fem_cuda.cu:174-204)
+    ++ncg_ver;
   }
 
   // time_step_solver_pd::reset_impl (projective_dynamics.hpp:53-93): (mass(rho) + laplace(dt^2 kappa)) (x) I3
@@ -748,6 +759,161 @@ struct TimeStep {
     st.newton_iters = it;
   }
 
+  // ------------------------------------------------------------------ nonlinear CG
+  void set_ncg_matrix(const double* values) {
+    if (!values) {
+      ncg_vals.clear();
+      ++ncg_ver;
+      return;
+    }
+    const size_t nnz = 9 * (size_t)topo.nnzb;
+    if (ncg_rp.n == 0) {
+      std::vector<int32_t> rp(n + 1), ci(nnz);
+      csr_pattern(topo, rp.data(), ci.data());
+      ncg_tperm.assign(nnz, 0);
+      for (int r = 0; r < n; ++r)
+        for (int k = rp[r]; k < rp[r + 1]; ++k) {
+          const int c = ci[k];
+          ncg_tperm[k] = std::lower_bound(ci.begin() + rp[c], ci.begin() + rp[c + 1], r) - ci.begin();
+        }
+      ncg_rp.upload(rp, stream);
+      ncg_ci.upload(ci, stream);
+    }
+    ncg_vals.assign(values, values + nnz);
+    ++ncg_ver;
+  }
+
+  template <typename S>
+  void ncg_sync(Solver<S>& s) {
+    if (s.ncg_version == ncg_ver || ncg_vals.empty()) return;
+    std::vector<S> L(ncg_vals.begin(), ncg_vals.end()), Lt(ncg_vals.size());
+    for (size_t k = 0; k < ncg_vals.size(); ++k) Lt[k] = (S)ncg_vals[ncg_tperm[k]];
+    s.ncg_L.upload(L, stream);
+    s.ncg_Lt.upload(Lt, stream);
+    s.ncg_version = ncg_ver;
+  }
+
+  // out = H in with H = L L^T (out = in without a factor); tmp is scratch
+  template <typename S>
+  void ncg_apply(Solver<S>& s, bool prec, const V4<S>* in, V4<S>* out, V4<S>* tmp) {
+    if (!prec || ncg_vals.empty()) {
+      if (out != in) launch_vaxpby<S>(nv, 0.0, out, 1.0, in, stream);
+      return;
+    }
+    launch_csr_dof_spmv<S>(n, ncg_rp.p, ncg_ci.p, s.ncg_Lt.p, in, tmp, stream);
+    launch_csr_dof_spmv<S>(n, ncg_rp.p, ncg_ci.p, s.ncg_L.p, tmp, out, stream);
+  }
+
+  // time_step_solver_ncg / _with_ext_prec (nonlinear_cg.hpp:9-97) over mathprim's ncg_optimizer (Dai-Kou,
+  // backtracking, learning rate 1e-2, 1000 iterations).  mathprim is not in the reference tree: the
+  // iteration is the published Dai-Kou method (Y.-H. Dai, C.-X. Kou, SIAM J. Optim. 23(1) 2013) with the
+  // line search described at the FP64 oracle's ncg_core, which this follows step for step.
+  template <typename S>
+  void ncg(ssim_gb_step_stats& st, bool prec) {
+    Solver<S>& s = solver<S>();
+    if (prec) ncg_sync<S>(s);
+    V4<S>* d = s.ld.p;   // direction
+    V4<S>* z = s.lq.p;   // H g
+    V4<S>* y = s.r.p;    // g - g_prev
+    V4<S>* hy = s.x.p;   // H y
+    V4<S>* gv = s.z.p;   // g, 4-wide
+    V4<S>* t = s.tmp.p;  // scratch of ncg_apply
+    double E = energy_grad();
+    double Escale = hsc->energy_scale;
+    double gn = std::sqrt(hsc->gnorm2);
+    const double g0 = gn;
+    st.grad_norm0 = g0;
+    start_instances();
+    SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    launch_to_vec4<S>(nv, forces.p, gv, false, stream);
+    ncg_apply<S>(s, prec, gv, z, t);
+    launch_vaxpby<S>(nv, 0.0, d, -1.0, z, stream);
+    auto dot_g = [&]() {  // g.d and |d|^2 of the current forces and direction
+      launch_dot_gd<S>(nv, forces.p, d, red(), stream);
+      sync_scalars();
+    };
+    dot_g();
+    double gd = hsc->gd, dn2 = hsc->dnorm2;
+    double alpha_init = params.ncg_step0;
+    auto trial = [&](double a) {
+      launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, d, a, dt * dt, rho, nullptr, false, true, red(), stream);
+      sync_scalars();
+      st.ls_steps_total++;
+      return hsc->trial_energy;
+    };
+    int it = 0;
+    for (;; ++it) {
+      st.grad_norm = gn;
+      st.energy = E;
+      if (stop_test(gn, g0)) {
+        st.converged = 1;
+        break;
+      }
+      if (it >= params.ncg_max_iters) break;
+      if (!(gd < 0)) {  // restart
+        launch_vaxpby<S>(nv, 0.0, d, -1.0, z, stream);
+        dot_g();
+        gd = hsc->gd;
+        dn2 = hsc->dnorm2;
+        if (!(gd < 0)) {
+          launch_to_vec4<S>(nv, forces.p, d, true, stream);
+          dot_g();
+          gd = hsc->gd;
+          dn2 = hsc->dnorm2;
+        }
+        alpha_init = params.ncg_step0;
+      }
+      const double slack = params.ls_energy_slack * Escale;
+      auto armijo = [&](double aa, double ee) { return ee <= E + params.lbfgs_armijo * aa * gd + slack; };
+      double a = alpha_init, Et = trial(a);
+      for (int ls = 1; ls < params.max_ls_iters && !armijo(a, Et); ++ls) {
+        const double c2 = (Et - E - gd * a) / (a * a);
+        double an = c2 > 0 ? -gd / (2 * c2) : 0.5 * a;
+        if (!std::isfinite(an)) an = 0.5 * a;
+        a = std::min(std::max(an, 0.1 * a), 0.5 * a);
+        Et = trial(a);
+      }
+      for (int ex = 0; ex < params.ncg_expand && armijo(a, Et); ++ex) {
+        const double c2 = (Et - E - gd * a) / (a * a);
+        if (!(c2 > 0)) break;
+        const double astar = -gd / (2 * c2);
+        if (!(astar > 1.5 * a)) break;
+        const double an = std::min(astar, 10 * a);
+        const double En = trial(an);
+        if (!(En < Et) || !armijo(an, En)) break;
+        a = an;
+        Et = En;
+      }
+      launch_axpy_update<S>(nv, a, d, dX.p, next.p, nullptr, stream);
+      st.last_change = a * std::sqrt(dn2);
+      E = energy_grad();
+      Escale = hsc->energy_scale;
+      gn = std::sqrt(hsc->gnorm2);
+      launch_vdiff<S>(nv, forces.p, gprev.p, y, stream);
+      SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+      launch_to_vec4<S>(nv, forces.p, gv, false, stream);
+      ncg_apply<S>(s, prec, gv, z, t);
+      const V4<S>* hyp = y;
+      if (prec && !ncg_vals.empty()) {
+        ncg_apply<S>(s, prec, y, hy, t);
+        hyp = hy;
+      }
+      const double dy = vdot<S>(d, y), zy = vdot<S>(z, y), yhy = vdot<S>(y, hyp);
+      dot_g();
+      const double gdn = hsc->gd, dd = hsc->dnorm2;
+      double beta = 0;
+      if (dy > 1e-300) beta = zy / dy - yhy * gdn / (dy * dy);
+      if (dd > 0) beta = std::max(beta, params.ncg_eta * gdn / dd);
+      const double gd_old = gd;
+      launch_vaxpby<S>(nv, beta, d, -1.0, z, stream);
+      dot_g();
+      gd = hsc->gd;
+      dn2 = hsc->dnorm2;
+      alpha_init = (gd < 0 && gd_old < 0) ? a * gd_old / gd : params.ncg_step0;
+    }
+    st.newton_iters = it;
+  }
+
   // compute_step (time_step.hpp:520-528): run the stepper, then |g| at the result
   double compute_step() {
     if (!has_reset) throw state_error("compute_step() before reset()");
@@ -768,6 +934,11 @@ struct TimeStep {
         lbfgs<float>(st, false, true);
       else
         lbfgs<double>(st, false, true);
+    } else if (stepper == SSIM_GB_STEPPER_NCG || stepper == SSIM_GB_STEPPER_NCG_EXT) {
+      if (mixed())
+        ncg<float>(st, stepper == SSIM_GB_STEPPER_NCG_EXT);
+      else
+        ncg<double>(st, stepper == SSIM_GB_STEPPER_NCG_EXT);
     } else if (stepper == SSIM_GB_STEPPER_FORWARD_EULER) {
       // time_step_solver_forward_euler (time_step.hpp:717-736): evaluate, next += dt^2 / 2 * forces; then
       // the re-evaluation of compute_step
@@ -968,6 +1139,10 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->pcg_spin_limit = 0;
   p->pcg_barrier_extra = 0;
   p->pcg_max_blocks = 0;
+  p->ncg_max_iters = 1000;
+  p->ncg_step0 = 1e-2;
+  p->ncg_eta = 0.5;
+  p->ncg_expand = 3;
 }
 
 ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
@@ -1070,7 +1245,8 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
   if (p->max_newton_iters < 0 || p->cg_max_iters < 0 || p->max_ls_iters < 1 || !(p->ls_shrink > 0 && p->ls_shrink < 1) ||
       !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 1 ||
       p->pcg_persistent < 0 || p->pcg_persistent > 3 || p->pcg_spin_limit < 0 || p->pcg_barrier_extra < 0 ||
-      p->pcg_max_blocks < 0 ||
+      p->pcg_max_blocks < 0 || p->ncg_max_iters < 0 || !(p->ncg_step0 > 0) || !(p->ncg_eta >= 0) ||
+      p->ncg_expand < 0 ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;
@@ -1244,6 +1420,13 @@ ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_st
   CHECK_H(h);
   if (st) *st = h->ts.stats;
   return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_set_ncg_matrix(ssim_gb_timestep* h, const double* values) {
+  CHECK_H(h);
+  API_TRY
+  h->ts.set_ncg_matrix(values);
+  API_CATCH(h)
 }
 
 ssim_gb_status ssim_gb_get_solve_log(const ssim_gb_timestep* h, int32_t* iters, int32_t capacity, int32_t* count) {

@@ -135,3 +135,17 @@ class tet_lbfgs(_TimeStepWrapper):
 
 class tet_lbfgs_pd(_TimeStepWrapper):
     _stepper = "pd"
+
+
+class tet_ncg_cuda_ext_ai(_TimeStepWrapper):
+    """timestep_ncg (fem_cuda.cu:171-207): nonlinear CG preconditioned by x = L L^T g, L on the system
+    matrix's CSR pattern; reset() installs L = I, set_matrix(values) sets its nonzeros (CSR order of
+    ``hessian()``)."""
+
+    _stepper = "ncg_ext"
+
+    def set_matrix(self, values):
+        v = np.asarray(values)
+        if v.dtype != np.float64 or v.ndim != 1:
+            raise TypeError("values must be a float64 vector")  # nb::arg().noconvert() in the reference
+        self.step_.set_ncg_matrix(v)

@@ -153,7 +153,8 @@ class TimeStep:
     # ---------------------------------------------------------------- loop
     def reset(self, stepper: int | str | None = None):
         if isinstance(stepper, str):
-            stepper = {"newton": 0, "lbfgs": 1, "pd": 2, "none": 3, "forward_euler": 4, "h0": 5}[stepper]
+            stepper = {"newton": 0, "lbfgs": 1, "pd": 2, "none": 3, "forward_euler": 4, "h0": 5, "ncg": 6,
+                       "ncg_ext": 7}[stepper]
         if stepper is not None:
             self._stepper = int(stepper)
         self._c(self._L.ssim_gb_reset(self._h, self._stepper))
@@ -181,6 +182,17 @@ class TimeStep:
         s = _lib.StepStats()
         self._c(self._L.ssim_gb_get_step_stats(self._h, C.byref(s)))
         return s.as_dict()
+
+    def set_ncg_matrix(self, values=None):
+        """Values of the NCG preconditioner factor L (x = L L^T g) in the CSR order of ``csr_pattern``;
+        None restores the identity."""
+        if values is None:
+            self._c(self._L.ssim_gb_set_ncg_matrix(self._h, None))
+            return
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if v.size != self.nnz:
+            raise ValueError(f"expected {self.nnz} values, got {v.size}")
+        self._c(self._L.ssim_gb_set_ncg_matrix(self._h, dptr(v)))
 
     def solve_log(self) -> list[int]:
         """PCG iterations of every solve since the last reset."""
