@@ -48,6 +48,8 @@ def make_scene(name):
         return scenes.cube10()
     if name == "bar":
         return scenes.bar()
+    if name == "batch":
+        return scenes.batch_cubes()
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -138,9 +140,13 @@ def run_gpu_arm(args, scene):
     result = {}
     launches0 = g.launch_count()
 
-    ts = scenes.build_timestep(scene, precision="mixed", params=params)
+    if scene.get("vertex_offsets") is not None:  # batched instances: one handle over the disjoint union
+        ts = scenes.build_batch_timestep(scene, precision="mixed", params=params)
+    else:
+        ts = scenes.build_timestep(scene, precision="mixed", params=params)
     ts.set_stream(stream.cuda_stream)
     zeros = np.zeros_like(scene["X"])
+    v0 = scene.get("velocity", zeros)
 
     import torch.distributed as tdist
 
@@ -151,9 +157,10 @@ def run_gpu_arm(args, scene):
     def timed_run(precision, steps, warmup, profile=False):
         # restart from rest: same initial state for every run
         ts.set_precision(precision)
-        ts.reset("newton")
-        for f in ("deformation", "prev_deform", "velocity"):
-            ts.set(f, zeros if scene.get("u0") is None or f == "velocity" else scene["u0"])
+        ts.reset(args.stepper)
+        for f in ("deformation", "prev_deform"):
+            ts.set(f, zeros if scene.get("u0") is None else scene["u0"])
+        ts.set("velocity", v0)
         for _ in range(warmup):
             ts.step()
         ts.profile(profile)
@@ -308,7 +315,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="beam1m")
+    ap.add_argument("--workload", default="beam1m", help="beam1m (default), beam_small, cube10, bar, batch")
+    ap.add_argument("--stepper", default="newton", choices=["newton", "lbfgs", "pd", "ncg", "ncg_ext"],
+                    help="stepper of the timed GPU runs (the CPU baseline is Newton)")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
@@ -412,7 +421,10 @@ def main():
             "data": "synthetic (seeded SplitMix64 material)",
             "config": {
                 "workload": scene["name"], "tets": T, "vertices": V, "dofs": 3 * V,
-                "solver": "Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(1e-2, |g|/|g0|)); mixed: Chronopoulos-Gear PCG in one cooperative launch per solve, FP64: two launches per PCG iteration",
+                "solver": ("Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(1e-2, "
+                           "|g|/|g0|)); mixed: Chronopoulos-Gear PCG in one cooperative launch per solve, FP64: two "
+                           "launches per PCG iteration") if args.stepper == "newton" else
+                          f"{args.stepper}, stop |g| <= 1e-6 |g0| (per instance for batches)",
                 "precision": "mixed: FP32 Hessian/assembly/PCG vectors, FP64 energy/gradient/state/dots",
                 "parallelism": "replicas" if world > 1 else "1 GPU",
                 "l2": "working set per step ~1 GB > L2 (no explicit flush)",

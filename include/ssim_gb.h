@@ -58,6 +58,12 @@ typedef enum {
   SSIM_GB_STEPPER_NCG_EXT = 7 /* time_step_solver_ncg_with_ext_prec (nonlinear_cg.hpp:40-97): x = L L^T g */
 } ssim_gb_stepper;
 
+/* The ElastModel template argument of basic_time_step */
+typedef enum {
+  SSIM_GB_MODEL_STABLE_NEOHOOKEAN = 0, /* elast::stable_neohookean (stable_neohookean.hpp:11-112) */
+  SSIM_GB_MODEL_LINEAR = 1             /* elast::linear (linear.hpp:7-70) */
+} ssim_gb_elastic_model;
+
 typedef enum {
   SSIM_GB_DEFORMATION = 0,
   SSIM_GB_PREV_DEFORM = 1,
@@ -186,6 +192,9 @@ SSIM_GB_API ssim_gb_status ssim_gb_step_next(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_step(ssim_gb_timestep* h, double* elapsed_ms);
 SSIM_GB_API ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st);
+/* elastic model (the reference picks it as basic_time_step's ElastModel template argument); takes effect
+ * immediately for every energy, gradient and Hessian evaluation */
+SSIM_GB_API ssim_gb_status ssim_gb_set_elastic_model(ssim_gb_timestep* h, int32_t model);
 /* NCG preconditioner factor L of SSIM_GB_STEPPER_NCG_EXT (x = L L^T g; timestep_ncg::set_matrix,
  * fem_cuda.cu:206): nnz values in the CSR order of ssim_gb_get_csr_pattern; NULL restores the identity,
  * which reset() installs (fem_cuda.cu:174-204).  Unlike the reference wrapper, whose solver never

@@ -220,11 +220,65 @@ inline void shape_grads(const double* Dm, double D[4][3]) {
   }
 }
 
+// ---------------------------------------------------------------- linear elasticity
+// elast::linear (linear.hpp:23-68): eps = (F + F^T)/2 - I (approx_green_strain, internal_physic.hpp:27-30),
+// Psi = mu |eps|^2 + lambda/2 tr(eps)^2, P = 2 mu eps + lambda tr(eps) I,
+// H = mu I + mu [(i,j),(j,i)] + lambda [(i,i),(j,j)] (row-major flat index i*3+j).
+inline double linear_energy(const double* F, double lambda, double mu) {
+  double n2 = 0, tr = 0;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      const double e = 0.5 * (F[r * 3 + c] + F[c * 3 + r]) - (r == c ? 1.0 : 0.0);
+      n2 += e * e;
+      if (r == c) tr += e;
+    }
+  return mu * n2 + 0.5 * lambda * tr * tr;
+}
+
+inline double linear_stress(const double* F, double lambda, double mu, double* P) {
+  double eps[9], tr = 0;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      eps[r * 3 + c] = 0.5 * (F[r * 3 + c] + F[c * 3 + r]) - (r == c ? 1.0 : 0.0);
+      if (r == c) tr += eps[r * 3 + c];
+    }
+  for (int k = 0; k < 9; ++k) P[k] = 2 * mu * eps[k] + (k % 4 == 0 ? lambda * tr : 0.0);
+  return linear_energy(F, lambda, mu);
+}
+
+inline void linear_hessian(double lambda, double mu, double* H) {
+  for (int k = 0; k < 81; ++k) H[k] = 0;
+  for (int k = 0; k < 9; ++k) H[k * 9 + k] = mu;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      H[(i * 3 + j) * 9 + (j * 3 + i)] += mu;
+      H[(i * 3 + i) * 9 + (j * 3 + j)] += lambda;
+    }
+}
+
+// the elastic model of a time step: 0 stable Neo-Hookean, 1 linear
+inline double model_energy(int model, const double* F, double l, double m) {
+  return model == 1 ? linear_energy(F, l, m) : snh_energy(F, l, m);
+}
+inline double model_stress(int model, const double* F, double l, double m, double* P) {
+  return model == 1 ? linear_stress(F, l, m, P) : snh_stress(F, l, m, P);
+}
+// the scale of the energy's round-off (the linear energy's terms are all non-negative)
+inline double model_energy_scale(int model, const double* F, double l, double m) {
+  return model == 1 ? linear_energy(F, l, m) : snh_energy_scale(F, l, m);
+}
+inline void model_hessian(int model, const double* F, double l, double m, double* H) {
+  if (model == 1)
+    linear_hessian(l, m, H);
+  else
+    snh_hessian(F, l, m, H);
+}
+
 // K = pfpx^T * H * pfpx (time_step.hpp:58); rows/cols vertex*3 + dof.
 void element_stiffness(const double* F, const double* Dminv, double lambda, double mu, bool make_spsd,
-                       double* K) {
+                       double* K, int model = 0) {
   double H[81], Hp[81];
-  snh_hessian(F, lambda, mu, H);
+  model_hessian(model, F, lambda, mu, H);
   const double* Hu = H;
   if (make_spsd) {
     project_spd(H, 1e-3, Hp);
@@ -273,6 +327,7 @@ struct orc_ts {
   // CSR (identical pattern for mass, system and PD matrices)
   std::vector<int32_t> row_ptr, col_idx;
   Vec ncg_L;                  // NCG preconditioner factor on the CSR pattern (empty: identity)
+  int model = 0;              // elastic model: 0 stable Neo-Hookean, 1 linear
   Vec mass_vals, massf_vals, sys_vals, pd_vals;
   std::vector<int32_t> hess_dst;            // [nt*144] CSR slot of each local entry
   std::vector<int32_t> hcon_ptr, hcon_src;  // per CSR slot, the local entries that add into it
@@ -406,8 +461,8 @@ double elastic_energy(orc_ts& s, double* scale) {
   double sum = 0, sc = 0;
 #pragma omp parallel for reduction(+ : sum, sc) schedule(static)
   for (int e = 0; e < s.nt; ++e) {
-    sum += snh_energy(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
-    sc += snh_energy_scale(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+    sum += model_energy(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+    sc += model_energy_scale(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
   }
   if (scale) *scale = sc * s.dt * s.dt;
   return sum * s.dt * s.dt;
@@ -422,7 +477,7 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < s.nt; ++e) {
     double P[9];
-    s.local_energy[e] = snh_stress(&s.defgrad[e * 9], s.lam(e), s.mu(e), P);
+    s.local_energy[e] = model_stress(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e), P);
     const double* Dm = &s.dminv[e * 9];
     double* lf = &s.local_force[e * 12];
     for (int j = 0; j < 3; ++j) {
@@ -456,7 +511,7 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
   double elast = 0, sc = 0;
   for (int e = 0; e < s.nt; ++e) {
     elast += s.local_energy[e] * s.vol[e];
-    sc += snh_energy_scale(&s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+    sc += model_energy_scale(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
   }
   s.energy_scale = inertia_energy + sc * s.dt * s.dt;
   return inertia_energy + elast * s.dt * s.dt;
@@ -473,7 +528,8 @@ void update_hessian(orc_ts& s, bool F_updated, bool make_spsd, bool filter) {
   if (!F_updated) update_def_grad(s, s.next);
 #pragma omp parallel for schedule(dynamic, 256)
   for (int e = 0; e < s.nt; ++e)
-    element_stiffness(&s.defgrad[e * 9], &s.dminv[e * 9], s.lam(e), s.mu(e), make_spsd, &s.local_K[(size_t)e * 144]);
+    element_stiffness(&s.defgrad[e * 9], &s.dminv[e * 9], s.lam(e), s.mu(e), make_spsd, &s.local_K[(size_t)e * 144],
+                      s.model);
   const double a = s.dt * s.dt;
   const int nnz = (int)s.col_idx.size();
 #pragma omp parallel for schedule(static)
@@ -1141,6 +1197,17 @@ static double ncg_core(orc_ts* s, const orc_params* p, orc_stats* st, bool prec)
 
 double orc_compute_step_ncg(orc_ts* s, const orc_params* p, orc_stats* st) { return ncg_core(s, p, st, false); }
 double orc_compute_step_ncg_prec(orc_ts* s, const orc_params* p, orc_stats* st) { return ncg_core(s, p, st, true); }
+
+void orc_set_model(orc_ts* s, int model) { s->model = model; }
+
+double orc_linear_stress(const double F[9], double lambda, double mu, double P[9]) {
+  return linear_stress(F, lambda, mu, P);
+}
+void orc_linear_hessian(double lambda, double mu, double H[81]) { linear_hessian(lambda, mu, H); }
+void orc_element_stiffness_model(const double F[9], const double Dminv[9], double lambda, double mu, int make_spsd,
+                                 int model, double K[144]) {
+  element_stiffness(F, Dminv, lambda, mu, make_spsd != 0, K, model);
+}
 
 void orc_set_ncg_matrix(orc_ts* s, const double* values) {
   if (!values) {

@@ -138,6 +138,12 @@ double orc_compute_step_ncg(orc_ts* ts, const orc_params* p, orc_stats* st);
 double orc_compute_step_ncg_prec(orc_ts* ts, const orc_params* p, orc_stats* st);
 /* L's values in the CSR order of the system matrix (orc_get_csr); NULL restores the identity */
 void orc_set_ncg_matrix(orc_ts* ts, const double* values);
+/* elastic model of the time step: 0 stable Neo-Hookean (stable_neohookean.hpp), 1 linear (linear.hpp) */
+void orc_set_model(orc_ts* ts, int model);
+double orc_linear_stress(const double F[9], double lambda, double mu, double P[9]);
+void orc_linear_hessian(double lambda, double mu, double H[81]);
+void orc_element_stiffness_model(const double F[9], const double Dminv[9], double lambda, double mu, int make_spsd,
+                                 int model, double K[144]);
 void orc_step_next(orc_ts* ts);
 void orc_restore(orc_ts* ts);
 int orc_check_convergence(orc_ts* ts);

@@ -139,6 +139,10 @@ def lib():
         "orc_compute_step_ncg": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_compute_step_ncg_prec": (C.c_double, [vp, C.POINTER(OrcParams), C.POINTER(OrcStats)]),
         "orc_set_ncg_matrix": (None, [vp, C.c_void_p]),
+        "orc_set_model": (None, [vp, C.c_int]),
+        "orc_linear_stress": (C.c_double, [dp, C.c_double, C.c_double, dp]),
+        "orc_linear_hessian": (None, [C.c_double, C.c_double, dp]),
+        "orc_element_stiffness_model": (None, [dp, dp, C.c_double, C.c_double, C.c_int, C.c_int, dp]),
         "orc_step_next": (None, [vp]),
         "orc_restore": (None, [vp]),
         "orc_check_convergence": (C.c_int, [vp]),
@@ -216,6 +220,18 @@ def snh_hessian(F, lam, mu):
     return H.reshape(9, 9)
 
 
+def linear_stress(F, lam, mu):
+    P = np.zeros(9)
+    e = lib().orc_linear_stress(_f64(F, (9,)), lam, mu, P)
+    return e, P.reshape(3, 3)
+
+
+def linear_hessian(lam, mu):
+    H = np.zeros(81)
+    lib().orc_linear_hessian(lam, mu, H)
+    return H.reshape(9, 9)
+
+
 def sym_eigen(A):
     A = _f64(A)
     n = A.shape[0]
@@ -238,9 +254,9 @@ def dminv(x0, x1, x2, x3):
     return D.reshape(3, 3), v.value
 
 
-def element_stiffness(F, Dminv, lam, mu, make_spsd=True):
+def element_stiffness(F, Dminv, lam, mu, make_spsd=True, model=0):
     K = np.zeros(144)
-    lib().orc_element_stiffness(_f64(F, (9,)), _f64(Dminv, (9,)), lam, mu, int(make_spsd), K)
+    lib().orc_element_stiffness_model(_f64(F, (9,)), _f64(Dminv, (9,)), lam, mu, int(make_spsd), int(model), K)
     return K.reshape(12, 12)
 
 
@@ -366,6 +382,10 @@ class OracleTimeStep:
         }[method]
         r = fn(self._h, C.byref(p), C.byref(st))
         return r, st.as_dict()
+
+    def set_model(self, model):
+        """Elastic model: "stable_neohookean" (0) or "linear" (1)."""
+        self._L.orc_set_model(self._h, {"stable_neohookean": 0, "linear": 1}.get(model, model))
 
     def set_ncg_matrix(self, values=None):
         """Values of the NCG preconditioner factor L in the system matrix's CSR order (None: identity)."""

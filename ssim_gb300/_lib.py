@@ -19,6 +19,7 @@ HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "ssim_gb.h")
 (OK, ERR_INVALID_ARGUMENT, ERR_NOT_CONVERGED, ERR_CUDA, ERR_NUMERICAL, ERR_STATE, ERR_OUT_OF_MEMORY,
  ERR_DEVICE_TIMEOUT) = range(8)
 FP64, MIXED = 0, 1
+MODELS = {"stable_neohookean": 0, "linear": 1}
 STEPPER_NEWTON, STEPPER_LBFGS, STEPPER_PD, STEPPER_NONE = 0, 1, 2, 3
 STEPPER_FORWARD_EULER, STEPPER_H0, STEPPER_NCG, STEPPER_NCG_EXT = 4, 5, 6, 7
 FIELDS = {
@@ -141,6 +142,7 @@ _SIGS = {
     "ssim_gb_get_step_stats": (C.c_int, [_H, C.POINTER(StepStats)]),
     "ssim_gb_get_solve_log": (C.c_int, [_H, _I, C.c_int32, _I]),
     "ssim_gb_set_ncg_matrix": (C.c_int, [_H, _D]),
+    "ssim_gb_set_elastic_model": (C.c_int, [_H, C.c_int32]),
     "ssim_gb_check_convergence": (C.c_int, [_H, _I]),
     "ssim_gb_threshold_abs": (C.c_int, [_H, _D]),
     "ssim_gb_update_energy_and_gradients": (C.c_int, [_H, C.c_int32, _D]),

@@ -136,6 +136,72 @@ __device__ __forceinline__ void block_sum_s(const S (&vals)[NV], double (&out)[N
   }
 }
 
+// Fixed-order tree sums of per-256-row partials (the PCG dots): partials are grouped 32 at a time (group g =
+// parts 32g..32g+31); a group is summed by one warp's shuffle tree, and the group sums by the same tree in
+// chunks of 32, chunks added in order.  The order depends only on the number of parts, so the distributed
+// version in the persistent PCG (each group summed by whichever block completes it) and the single-block
+// version below give identical bits.  Results in lane 0.
+template <int NV>
+__device__ __forceinline__ void warp_group_sum(const double* parts, int base, int count, double (&v)[NV]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = lane < count ? __ldcg(parts + (size_t)(base + lane) * NV + k) : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ void warp_top_sum(const double* gsums, int ngroups, double (&tot)[NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = 0.0;
+  for (int c0 = 0; c0 < ngroups; c0 += 32) {
+    double v[NV];
+    warp_group_sum<NV>(gsums, c0, min(32, ngroups - c0), v);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) tot[k] += v[k];
+  }
+}
+
+// grid_sum_last with the tree order above: the last block's warps sum the groups (group sums in gscratch,
+// ceil(grid / 32) * NV doubles), then warp 0 the group sums.  true in thread 0 of the last block.
+template <int NV, int BLOCK>
+__device__ __forceinline__ bool grid_sum_last_tree(const double (&blockval)[NV], double* partials, double* gscratch,
+                                                   unsigned int* counter, double (&tot)[NV]) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[blockIdx.x * NV + k] = blockval[k];
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  const int nparts = (int)gridDim.x, ngroups = (nparts + 31) / 32, warp = threadIdx.x >> 5;
+  for (int g = warp; g < ngroups; g += BLOCK / 32) {
+    double v[NV];
+    warp_group_sum<NV>(partials, 32 * g, min(32, nparts - 32 * g), v);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) gscratch[g * NV + k] = v[k];
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    warp_top_sum<NV>(gscratch, ngroups, tot);
+    if (threadIdx.x == 0) {
+      *counter = 0;  // ready for the next launch on this stream
+      __threadfence();
+      return true;
+    }
+  }
+  return false;
+}
+
 // returns true in exactly one thread (thread 0 of the last block), with tot[] = sum of all partials.
 // The last block reads the partials with every thread at once (L2-coherent loads) and combines them in a
 // fixed order, so the result depends only on the grid and block sizes.

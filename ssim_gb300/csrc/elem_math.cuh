@@ -97,6 +97,30 @@ __host__ __device__ __forceinline__ void snh_constants(S lam, S mu, S& alpha, S&
   psi0 = S(0.5) * (lam * (S(1) - alpha) * (S(1) - alpha) - mu * log(S(4)));
 }
 
+// Linear elasticity (linear.hpp:23-68) from the displacement gradient G = F - I: eps = (G + G^T) / 2
+// (approx_green_strain, internal_physic.hpp:27-30, without the cancellation of F + F^T - 2I),
+// Psi = mu |eps|^2 + lambda/2 tr(eps)^2, P = 2 mu eps + lambda tr(eps) I.  Every term is non-negative, so
+// the magnitude sum used for the line search's round-off slack is Psi itself.
+template <typename S, bool STRESS>
+__host__ __device__ __forceinline__ S linear_eval(const S* G, S lam, S mu, S* P, S& scale) {
+  S e[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) e[r * 3 + c] = S(0.5) * (G[r * 3 + c] + G[c * 3 + r]);
+  const S tr = e[0] + e[4] + e[8];
+  S n2 = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) n2 += e[k] * e[k];
+  if (STRESS) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) P[k] = S(2) * mu * e[k] + ((k % 4 == 0) ? lam * tr : S(0));
+  }
+  const S psi = mu * n2 + S(0.5) * lam * tr * tr;
+  scale = psi;
+  return psi;
+}
+
 // sum of the magnitudes of the terms of snh_energy: the scale of its absolute round-off (the terms are
 // O(mu) and cancel to O(mu strain^2) near rest); the line search compares energies only above it
 template <typename S>
@@ -225,6 +249,39 @@ __host__ __device__ __forceinline__ void rank1(S* K, S w, const S* g) {
 #pragma unroll
     for (int j = i; j < 12; ++j) K[kup(i, j)] += wi * g[j];
   }
+}
+
+// Element stiffness of the linear model, packed upper triangle (78) times scale.  Its 9x9 Hessian
+// mu (I + T) + lambda d d^T (T: the transpose permutation, d = vec I) has the eigenspaces symmetric-
+// deviatoric (2 mu, 5 modes), volumetric (2 mu + 3 lambda) and skew (0, 3 modes); with the make_spsd clamp
+// (time_step.hpp:50-56) applied to those eigenvalues, H = c_I I + c_T T + c_d d d^T with
+// c_I = (a_dev + a_skew)/2, c_T = (a_dev - a_skew)/2, c_d = (a_vol - a_dev)/3, and contracted with the shape
+// gradients g_v: K[(v,s),(w,t)] = c_I delta_st g_v.g_w + c_T g_v[t] g_w[s] + c_d g_v[s] g_w[t].
+template <typename S>
+__host__ __device__ __forceinline__ void linear_stiffness(const S D[4][3], S lam, S mu, bool spsd, S scale, S* K) {
+  S a_dev = S(2) * mu, a_vol = S(2) * mu + S(3) * lam, a_skew = S(0);
+  if (spsd) {
+    const S eps = S(1e-3);
+    a_dev = fmax(a_dev, eps);
+    a_vol = fmax(a_vol, eps);
+    a_skew = eps;
+  }
+  const S cI = S(0.5) * (a_dev + a_skew) * scale, cT = S(0.5) * (a_dev - a_skew) * scale,
+          cd = (a_vol - a_dev) / S(3) * scale;
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+#pragma unroll
+    for (int w = v; w < 4; ++w) {
+      const S gg = D[v][0] * D[w][0] + D[v][1] * D[w][1] + D[v][2] * D[w][2];
+#pragma unroll
+      for (int s = 0; s < 3; ++s)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const int i = v * 3 + s, j = w * 3 + t;
+          if (i > j) continue;
+          K[kup(i, j)] = (s == t ? cI * gg : S(0)) + cT * D[v][t] * D[w][s] + cd * D[v][s] * D[w][t];
+        }
+    }
 }
 
 // 12x12 element stiffness K = pfpx^T H+ pfpx (time_step.hpp:23-60) where H is the 9x9 SNH Hessian

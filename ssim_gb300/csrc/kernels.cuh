@@ -33,6 +33,7 @@ struct ElemFP64 {
   const double* mu;
   const double* alpha;  // 1 + 3/4 mu / lambda
   const double* psi0;   // stable Neo-Hookean energy at F = I
+  int model;            // 0 stable Neo-Hookean, 1 linear
 };
 
 struct ElemFP32 {
@@ -99,11 +100,11 @@ template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
                      V4<S>* q, bool first, const Reduce& red, cudaStream_t st);
 // the whole PCG loop (after launch_pcg_setup*) in one cooperative launch: variant 1 standard PCG (bitwise
-// the two-launch iterates), 2 Chronopoulos-Gear PCG; false if the device cannot launch it cooperatively
-// (the caller then runs the two-launch loop)
+// the two-launch iterates), 2 Chronopoulos-Gear PCG; gsync: 3 + ceil(ceil(nv / 256) / 32) zeroed words of
+// barrier state; false if the device cannot launch it cooperatively (the caller runs the two-launch loop)
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
-                           V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned int* gsync,
+                           V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st);
 // y = A x, A a scalar CSR matrix over dofs, x / y 4-wide vertex vectors
 template <typename S>

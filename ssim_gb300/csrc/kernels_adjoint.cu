@@ -9,7 +9,8 @@
 //   ubar   = -k/dt vbar' + xbar~,  vbar = dt xbar~          (k = 1 - damping)
 //   Ebar_e -= dt^2 V_e <Lambda_e Dm^-1, P_e> / E_e
 // The last line: the stable Neo-Hookean PK1 (stable_neohookean.hpp:38-62) is homogeneous of degree one in
-// (lambda, mu) jointly (alpha depends on mu / lambda only) and both scale with E, so dP/dE = P / E; the
+// (lambda, mu) jointly (alpha depends on mu / lambda only), and so is the linear model's (linear.hpp:37-52);
+// both Lame parameters scale with E, so dP/dE = P / E; the
 // element's forces contracted with the adjoint are <Lambda Dm^-1, P> with Lambda = [l1-l0, l2-l0, l3-l0].
 #include "elem_math.cuh"
 #include "kernels.cuh"
@@ -82,7 +83,14 @@ __global__ void __launch_bounds__(EB)
     }
   const double lam = el.lam[e], mu = el.mu[e];
   double P[9];
-  snh_stress<double>(F, lam, mu, P);
+  if (el.model == 1) {
+    double G[9], sc;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) G[k] = F[k] - ((k % 4 == 0) ? 1.0 : 0.0);
+    linear_eval<double, true>(G, lam, mu, P, sc);
+  } else {
+    snh_stress<double>(F, lam, mu, P);
+  }
   double wp = 0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) wp += W[k] * P[k];

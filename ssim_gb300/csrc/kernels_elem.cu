@@ -62,13 +62,14 @@ __global__ void __launch_bounds__(EB)
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int k = 0; k < 3; ++k) Du[r * 3 + k] = uu[k + 1][r] - uu[0][r];
-    double F[9];
+    double G[9], F[9];  // displacement gradient and F = I + G
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int cc = 0; cc < 3; ++cc)
-        F[r * 3 + cc] = (r == cc ? 1.0 : 0.0) + (Du[r * 3 + 0] * Dm[0 * 3 + cc] + Du[r * 3 + 1] * Dm[1 * 3 + cc] +
-                                                 Du[r * 3 + 2] * Dm[2 * 3 + cc]);
+      for (int cc = 0; cc < 3; ++cc) {
+        G[r * 3 + cc] = Du[r * 3 + 0] * Dm[0 * 3 + cc] + Du[r * 3 + 1] * Dm[1 * 3 + cc] + Du[r * 3 + 2] * Dm[2 * 3 + cc];
+        F[r * 3 + cc] = (r == cc ? 1.0 : 0.0) + G[r * 3 + cc];
+      }
     const double lam = el.lam[e], mu = el.mu[e], V = el.vol[e];
     const double m = rho * V * (1.0 / 20.0);
     double sd[3];
@@ -78,7 +79,8 @@ __global__ void __launch_bounds__(EB)
 #pragma unroll
     for (int i = 0; i < 4; ++i) q += dd[i][0] * dd[i][0] + dd[i][1] * dd[i][1] + dd[i][2] * dd[i][2];
     double P[9], sc;
-    const double psi = snh_eval<double, FORCES>(F, lam, mu, el.alpha[e], el.psi0[e], P, sc);
+    const double psi = el.model == 1 ? linear_eval<double, FORCES>(G, lam, mu, P, sc)
+                                     : snh_eval<double, FORCES>(F, lam, mu, el.alpha[e], el.psi0[e], P, sc);
     if (FORCES) {
       const double s = dt2 * V;
       double tot[3] = {0, 0, 0};
@@ -219,8 +221,12 @@ __global__ void __launch_bounds__(HB)
       D[0][j] = -(Dm[0 * 3 + j] + Dm[1 * 3 + j] + Dm[2 * 3 + j]);
     }
     S K[78];
-    element_stiffness<S>(F, D, ElemSel<S>::lam(e64, e32, e), ElemSel<S>::mu(e64, e32, e), spsd != 0,
-                         dt2 * ElemSel<S>::vol(e64, e32, e), K);
+    if (e64.model == 1)
+      linear_stiffness<S>(D, ElemSel<S>::lam(e64, e32, e), ElemSel<S>::mu(e64, e32, e), spsd != 0,
+                          dt2 * ElemSel<S>::vol(e64, e32, e), K);
+    else
+      element_stiffness<S>(F, D, ElemSel<S>::lam(e64, e32, e), ElemSel<S>::mu(e64, e32, e), spsd != 0,
+                           dt2 * ElemSel<S>::vol(e64, e32, e), K);
     S* st = stage + threadIdx.x * 90;
     int blk = 0;
 #pragma unroll

@@ -402,7 +402,8 @@ __global__ void __launch_bounds__(SB)
   double v1[1];
   block_sum_s<1, SB, S>(part, v1, shred);
   double tot[1];
-  if (grid_sum_last<1, SB>(v1, red.partials, red.counter, tot)) pcg_after_pq(red.sc, tot[0]);
+  if (grid_sum_last_tree<1, SB>(v1, red.partials, red.partials + 2 * (size_t)gridDim.x, red.counter, tot))
+    pcg_after_pq(red.sc, tot[0]);
 }
 
 template <typename S>
@@ -418,7 +419,8 @@ __global__ void __launch_bounds__(SB)
   double bs[2];
   block_sum_s<2, SB, S>(part, bs, shred);
   double tot[2];
-  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) pcg_after_rz(red.sc, tot[0], tot[1], max_iters);
+  if (grid_sum_last_tree<2, SB>(bs, red.partials, red.partials + 2 * (size_t)gridDim.x, red.counter, tot))
+    pcg_after_rz(red.sc, tot[0], tot[1], max_iters);
 }
 
 // ------------------------------------------------------------------ persistent PCG
@@ -431,87 +433,98 @@ __global__ void __launch_bounds__(SB)
 // loop are read with plain loads only after a barrier, whose acquire side orders them after the writers'
 // release (the cooperative-groups grid sync pattern); the scalars are read with L2 loads.
 struct GridSync {
-  unsigned int* count;  // arrivals in the current phase
-  unsigned int* gen;    // completed phases
-  unsigned int extra;   // arrivals beyond the grid (test hook; 0 in normal use)
+  unsigned long long* arrive;  // plain-barrier arrivals since the launch (never reset within it)
+  unsigned long long* top;     // arrivals of completed groups at the reducing barriers
+  unsigned long long* release; // reducing barriers completed (written by the one that completes each)
+  unsigned long long* group;   // [ngroups] arrivals of each group's virtual blocks
+  int ngroups;
+  unsigned int extra;  // arrivals beyond the grid / the groups (test hook; 0 in normal use)
   long long spin_limit;
 };
 
-__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
-  unsigned int v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-
-// Grid barrier; the last block to arrive runs last_fn() with all its threads before releasing the rest.
-// Returns false in every thread of a block whose wait gave up after spin_limit polls.
-template <typename F>
-__device__ __forceinline__ bool grid_barrier_last(const GridSync& gs, F&& last_fn) {
-  __shared__ int role;  // 0 released, 1 last arriver, 2 gave up
-  __shared__ unsigned int gen0;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    gen0 = ld_acquire_gpu(gs.gen);
-    __threadfence();
-    const bool last = atomicAdd(gs.count, 1u) == gridDim.x + gs.extra - 1;
-    if (last) __threadfence();  // acquire side of the other blocks' arrivals; the block follows via bar.sync
-    role = last ? 1 : 0;
-  }
-  __syncthreads();
-  if (role == 1) {
-    last_fn();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      atomicExch(gs.count, 0u);
-      __threadfence();
-      atomicAdd(gs.gen, 1u);
-    }
-    __syncthreads();
-    return true;
-  }
-  if (threadIdx.x == 0) {
-    long long n = 0;
-    int r = 0;
-    while (ld_acquire_gpu(gs.gen) == gen0) {
-      if (++n > gs.spin_limit) {
-        r = 2;
-        break;
-      }
-      __nanosleep(32);
-    }
-    __threadfence();
-    role = r;
-  }
-  __syncthreads();
-  return role != 2;
+__device__ __forceinline__ void st_release_gpu(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// grid_sum_last's final sum, run by one whole block: partials of nparts virtual blocks (stride NV)
-template <int NV>
-__device__ __forceinline__ void sum_partials(const double* partials, int nparts, double (*sh)[NV], double (&tot)[NV]) {
-  double acc[NV];
+// thread 0 polls *p until it reaches target (at most spin_limit polls); true if it did
+__device__ __forceinline__ bool wait_at_least(const unsigned long long* p, unsigned long long target,
+                                              long long spin_limit) {
+  long long n = 0;
+  while (ld_acquire_gpu(p) < target) {
+    if (++n > spin_limit) return false;
+    __nanosleep(32);
+  }
+  __threadfence();
+  return true;
+}
+
+// Barrier number k (0-based within the launch) without a reduction: the counter only grows, so nobody
+// resets or releases anything; each block waits until all (k + 1) * grid arrivals have happened.
+__device__ __forceinline__ bool plain_barrier(const GridSync& gs, unsigned long long k) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(gs.arrive, 1ull);
+    ok = wait_at_least(gs.arrive, (k + 1) * (unsigned long long)(gridDim.x + gs.extra), gs.spin_limit);
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Reducing barrier number kr: every block has written the partials of its virtual blocks (NV doubles each,
+// part[NV * vb]); warp 0 of each block marks them arrived in their groups of 32; the block completing a
+// group sums it (warp_group_sum) into gsum[g], and the block completing the last group sums the group
+// sums (warp_top_sum, the order of grid_sum_last_tree), runs epi(tot) in its lane 0 and releases everyone.
+// Returns false in every thread of a block whose wait gave up.
+template <int NV, typename EPI>
+__device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long long kr, const double* part,
+                                               double* gsum, int nvb, EPI&& epi) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int g = vb >> 5, gsize = min(32, nvb - 32 * g);
+      int last = 0;
+      if (lane == 0) {
+        __threadfence();
+        last = atomicAdd(gs.group + g, 1ull) == (kr + 1) * (unsigned long long)gsize - 1;
+        if (last) __threadfence();
+      }
+      last = __shfl_sync(0xffffffffu, last, 0);
+      __syncwarp();
+      if (!last) continue;
+      double v[NV];
+      warp_group_sum<NV>(part, 32 * g, gsize, v);
+      int top = 0;
+      if (lane == 0) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) acc[k] = 0;
-  // four partials per value in flight at once, added in the same order as one at a time
-  for (int b0 = threadIdx.x; b0 < nparts; b0 += 4 * SB) {
-    double v[4][NV];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int b = b0 + j * SB;
-#pragma unroll
-      for (int k = 0; k < NV; ++k) v[j][k] = b < nparts ? __ldcg(partials + b * NV + k) : 0.0;
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (b0 + j * SB < nparts) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) acc[k] += v[j][k];
+        for (int k = 0; k < NV; ++k) gsum[g * NV + k] = v[k];
+        __threadfence();
+        top = atomicAdd(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
+        if (top) __threadfence();
+      }
+      top = __shfl_sync(0xffffffffu, top, 0);
+      __syncwarp();
+      if (!top) continue;
+      double tot[NV];
+      warp_top_sum<NV>(gsum, gs.ngroups, tot);
+      if (lane == 0) {
+        epi(tot);
+        __threadfence();
+        st_release_gpu(gs.release, kr + 1);
       }
     }
   }
-  block_sum<NV, SB>(acc, sh);
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = acc[k];  // valid in thread 0
+  if (threadIdx.x == 0) ok = wait_at_least(gs.release, kr + 1, gs.spin_limit);
+  __syncthreads();
+  return ok != 0;
 }
 
 // Chronopoulos-Gear PCG (Chronopoulos & Gear, J. Comput. Appl. Math. 25, 1989): the same iterates as
@@ -615,6 +628,7 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
   if (s_done) return;
   const int nvb = (A.nv + SB - 1) / SB;
   double* part = red.partials;
+  double* gsum = red.partials + 3 * (size_t)nvb;
   bool ok = true;
   for (int k = 0;; ++k) {
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
@@ -629,11 +643,8 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
       }
       __syncthreads();
     }
-    ok = grid_barrier_last(gs, [&] {
-      double tot[3];
-      sum_partials<3>(part, nvb, shred, tot);
-      if (threadIdx.x == 0) cgcg_after(sc, tot[0], tot[1], tot[2], max_iters);
-    });
+    ok = reduce_barrier<3>(gs, (unsigned long long)k, part, gsum, nvb,
+                           [&](const double (&t)[3]) { cgcg_after(sc, t[0], t[1], t[2], max_iters); });
     if (!ok) break;
     if (threadIdx.x == 0) {
       s_done = __ldcg(&sc->done);
@@ -645,7 +656,7 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
     const S alpha = (S)s_alpha, beta = (S)s_beta;
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x)
       cgcg_update_row<S>(A.nv, k == 0, alpha, beta, dinv, z, q, p0, p1, x, r, vb * SB + threadIdx.x);
-    ok = grid_barrier_last(gs, [] {});
+    ok = plain_barrier(gs, (unsigned long long)k);
     if (!ok) break;
   }
   // a barrier wait gave up: flag it (the host clears the flag before the launch) and leave
@@ -671,6 +682,7 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
   const int nvb = (A.nv + SB - 1) / SB;
   double* part_pq = red.partials;
   double* part_rz = red.partials + 2 * (size_t)nvb;
+  double* gsum = red.partials + 4 * (size_t)nvb;
   bool ok = true;
   for (int k = 0;; ++k) {
     V4<S>* pold = (k & 1) ? p1 : p0;
@@ -683,11 +695,7 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
       if (threadIdx.x == 0) part_pq[vb] = v1[0];
       __syncthreads();
     }
-    ok = grid_barrier_last(gs, [&] {
-      double tot[1];
-      sum_partials<1>(part_pq, nvb, reinterpret_cast<double(*)[1]>(shred), tot);
-      if (threadIdx.x == 0) pcg_after_pq(sc, tot[0]);
-    });
+    ok = reduce_barrier<1>(gs, 2ull * k, part_pq, gsum, nvb, [&](const double (&t)[1]) { pcg_after_pq(sc, t[0]); });
     if (!ok) break;
     if (threadIdx.x == 0) {
       s_done = __ldcg(&sc->done);
@@ -707,11 +715,8 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
       }
       __syncthreads();
     }
-    ok = grid_barrier_last(gs, [&] {
-      double tot[2];
-      sum_partials<2>(part_rz, nvb, shred, tot);
-      if (threadIdx.x == 0) pcg_after_rz(sc, tot[0], tot[1], max_iters);
-    });
+    ok = reduce_barrier<2>(gs, 2ull * k + 1, part_rz, gsum, nvb,
+                           [&](const double (&t)[2]) { pcg_after_rz(sc, t[0], t[1], max_iters); });
     if (!ok) break;
     if (threadIdx.x == 0) {
       s_done = __ldcg(&sc->done);
@@ -1001,7 +1006,7 @@ void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V
 
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
-                           V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned int* gsync,
+                           V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st) {
   int dev = 0, coop = 0, nsm = 0, per_sm = 0;
   SSIM_CUDA(cudaGetDevice(&dev));
@@ -1014,9 +1019,11 @@ bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv
   int grid = std::min(div_up(A.nv, SB), per_sm * nsm);
   if (max_blocks > 0) grid = std::min(grid, max_blocks);
   if (grid < 1) return true;
-  SSIM_CUDA(cudaMemsetAsync(gsync, 0, 2 * sizeof(unsigned int), st));
+  const int ngroups = (div_up(A.nv, SB) + 31) / 32;
+  SSIM_CUDA(cudaMemsetAsync(gsync, 0, (3 + (size_t)ngroups) * sizeof(unsigned long long), st));
   SSIM_CUDA(cudaMemsetAsync(&red.sc->wait_failed, 0, sizeof(int32_t), st));
-  GridSync gs{gsync, gsync + 1, (unsigned int)extra, spin_limit > 0 ? spin_limit : (1LL << 25)};
+  GridSync gs{gsync, gsync + 1, gsync + 2, gsync + 3, ngroups, (unsigned int)extra,
+              spin_limit > 0 ? spin_limit : (1LL << 25)};
   SellMatrix a = A;
   Reduce rd = red;
   void* args[] = {(void*)&a,  (void*)&vals, (void*)&dinv, (void*)&x,         (void*)&r,  (void*)&z,
@@ -1156,7 +1163,8 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
   template void launch_pcg_update<S>(int, const V4<S>*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, int, \
                                      const Reduce&, cudaStream_t);                                                \
   template bool launch_pcg_persistent<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*,       \
-                                         V4<S>*, V4<S>*, V4<S>*, int, const Reduce&, unsigned int*, long long,   \
+                                         V4<S>*, V4<S>*, V4<S>*, int, const Reduce&, unsigned long long*,        \
+                                         long long,                                                               \
                                          int, int, int, cudaStream_t);                                            \
   template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
   template void launch_csr_dof_spmv<S>(int, const int*, const int*, const S*, const V4<S>*, V4<S>*, cudaStream_t); \

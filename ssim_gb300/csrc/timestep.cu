@@ -110,7 +110,7 @@ struct TimeStep {
   Solver<double> sd;
   DBuf<double> partials;
   DBuf<unsigned int> counter;
-  DBuf<unsigned int> gsync;  // grid-barrier state of the persistent PCG (count, generation)
+  DBuf<unsigned long long> gsync;  // grid-barrier state of the persistent PCG (counters, release, groups)
   DBuf<DevScalars> sc;
   DevScalars* hsc = nullptr;  // pinned
   DBuf<double> gprev, dscal;   // previous gradient (L-BFGS), device scalars of vdot
@@ -125,6 +125,7 @@ struct TimeStep {
   // ---- profiling
   bool profiling = false;
   std::vector<cudaEvent_t> ev;
+  int elastic_model = SSIM_GB_MODEL_STABLE_NEOHOOKEAN;  // ElastModel of basic_time_step
   std::vector<int32_t> solve_log;  // PCG iterations of every solve since the last reset
   // NCG preconditioner factor L (host copy; empty = identity), its CSR pattern on the device and the
   // position of each entry's transpose
@@ -145,7 +146,9 @@ struct TimeStep {
 
   bool mixed() const { return precision == SSIM_GB_MIXED; }
   Reduce red() { return Reduce{partials.p, counter.p, sc.p}; }
-  ElemFP64 e64() const { return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p, snh_alpha.p, snh_psi0.p}; }
+  ElemFP64 e64() const {
+    return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p, snh_alpha.p, snh_psi0.p, elastic_model};
+  }
   ElemFP32 e32() const { return ElemFP32{nt, dcells.p, fdminv.p, fvol.p, flam.p, fmu.p}; }
   SellMatrix A() const {
     return SellMatrix{nv, topo.nslots, sl_off.p, sl_col.p, slot_row.p, lo_off.p, lo_src.p, lo_col.p};
@@ -198,7 +201,7 @@ struct TimeStep {
     sc.zero(stream);
     counter.alloc(1);
     counter.zero(stream);
-    gsync.alloc(2);
+    gsync.alloc(3 + (size_t)(div_up(nv, 256) + 31) / 32);
     gsync.zero(stream);
     const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(3 * nv, topo.nslots), 256)) + 1;
     partials.alloc(maxgrid * 4);
@@ -1419,6 +1422,14 @@ ssim_gb_status ssim_gb_restore(ssim_gb_timestep* h) {
 ssim_gb_status ssim_gb_get_step_stats(const ssim_gb_timestep* h, ssim_gb_step_stats* st) {
   CHECK_H(h);
   if (st) *st = h->ts.stats;
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_set_elastic_model(ssim_gb_timestep* h, int32_t model) {
+  CHECK_H(h);
+  if (model != SSIM_GB_MODEL_STABLE_NEOHOOKEAN && model != SSIM_GB_MODEL_LINEAR)
+    return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "unknown elastic model");
+  h->ts.elastic_model = model;
   return SSIM_GB_OK;
 }
 

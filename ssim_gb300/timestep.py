@@ -183,6 +183,10 @@ class TimeStep:
         self._c(self._L.ssim_gb_get_step_stats(self._h, C.byref(s)))
         return s.as_dict()
 
+    def set_elastic_model(self, model: str | int):
+        """"stable_neohookean" (default) or "linear": the reference's ElastModel template argument."""
+        self._c(self._L.ssim_gb_set_elastic_model(self._h, _lib.MODELS.get(model, model)))
+
     def set_ncg_matrix(self, values=None):
         """Values of the NCG preconditioner factor L (x = L L^T g) in the CSR order of ``csr_pattern``;
         None restores the identity."""

@@ -56,6 +56,54 @@ def test_snh_hessian_fd(oracle):
     assert np.allclose(H, H.T, rtol=0, atol=1e-9 * np.abs(H).max())
 
 
+def test_linear_known_answer_and_fd(oracle):
+    """tests/fem_intro/main.cpp:13-83 (elast.linear3): E=1e6, nu=0.4; energy and PK1 vanish at F = I (1e-7);
+    central FD of the energy vs PK1 and of PK1 vs the Hessian at the same F, delta 1e-3, tol 1e-3 (the
+    reference compares H(i*3+j, k*3+l) with the FD of P(l, k); the model is symmetric in F and F^T)."""
+    lam, mu = oracle.lame(1e6, 0.4)
+    e, P = oracle.linear_stress(np.eye(3), lam, mu)
+    assert abs(e) < 1e-7 and np.abs(P).max() < 1e-7
+    d = 1e-3
+    _, P = oracle.linear_stress(F_FD, lam, mu)
+    H = oracle.linear_hessian(lam, mu)
+    for i in range(3):
+        for j in range(3):
+            Fp, Fm = F_FD.copy(), F_FD.copy()
+            Fp[i, j] += d
+            Fm[i, j] -= d
+            ep, Pp = oracle.linear_stress(Fp, lam, mu)
+            em, Pm = oracle.linear_stress(Fm, lam, mu)
+            assert abs(P[i, j] - (ep - em) / (2 * d)) < 1e-3 * max(1.0, abs(P[i, j]))
+            for k in range(3):
+                for l in range(3):
+                    fd = (Pp[l, k] - Pm[l, k]) / (2 * d)
+                    assert abs(H[i * 3 + j, k * 3 + l] - fd) < 1e-3 * max(1.0, abs(fd))
+
+
+def test_linear_projected_stiffness(oracle):
+    """The make_spsd clamp (time_step.hpp:50-56) lifts the linear model's three rotation (skew) modes from 0
+    to 1e-3 and leaves the 2 mu / 2 mu + 3 lambda modes: the element stiffness differs from the
+    unprojected one exactly by 1e-3 times the pfpx contraction of the skew projector."""
+    lam, mu = oracle.lame(1e5, 0.3)
+    Dm, _ = oracle.dminv([0, 0, 0], [1, 0.1, 0], [0.2, 1, 0], [0, 0.1, 1.1])
+    K0 = oracle.element_stiffness(np.eye(3), Dm, lam, mu, make_spsd=False, model=1)
+    K1 = oracle.element_stiffness(np.eye(3), Dm, lam, mu, make_spsd=True, model=1)
+    T = np.zeros((9, 9))
+    for i in range(3):
+        for j in range(3):
+            T[i * 3 + j, j * 3 + i] = 1
+    Pskew = 0.5 * (np.eye(9) - T)
+    D = np.zeros((9, 12))  # pfpx: dF(r,c)/dx(v,s) = delta_rs grad N_v[c]
+    g = np.zeros((4, 3))
+    g[1:] = np.asarray(Dm)
+    g[0] = -g[1:].sum(0)
+    for r in range(3):
+        for c in range(3):
+            for v in range(4):
+                D[r * 3 + c, v * 3 + r] = g[v, c]
+    assert np.allclose(K1 - K0, 1e-3 * D.T @ Pskew @ D, rtol=0, atol=1e-9 * np.abs(K0).max())
+
+
 def test_deform_rest_identity_and_volume(oracle):
     """tests/fem_intro/main.cpp:311-333: F == I at rest, sum of rest volumes == 1 on unit_box()."""
     X, cells = oracle.unit_box(2, 2, 2)
