@@ -207,6 +207,9 @@ def run_gpu_arm(args, scene):
         s.step_.set_material(scene["E_cells"], None)
     s.add_gravity(scene["gravity"])
     s.reset()
+    if scene.get("u0") is not None:  # the scene's initial state, as the device-timed runs start from
+        for f in ("deformation", "prev_deform"):
+            s.step_.set(f, scene["u0"])
     targ_np = pin_targ.numpy()
     for _ in range(args.warmup):
         s.mark_dirichlet_batched(fixed, targ_np)

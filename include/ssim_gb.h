@@ -113,6 +113,9 @@ typedef struct {
   double ncg_step0;       /* first trial step of the first NCG iteration: the reference's learning rate 1e-2 */
   double ncg_eta;         /* Dai-Kou truncation: beta >= ncg_eta * g.d / |d|^2 (0.5) */
   int32_t ncg_expand;     /* line-search expansions toward the fitted parabola's minimiser (3) */
+  double stop_floor;      /* stop_mode 1 also stops when |g| <= stop_floor * sum|M| / 3 (the reference's absolute
+                             rule with rtol = stop_floor; default 1e-12), so a step starting at rest, whose
+                             gradient is round-off, does not chase a fraction of it */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

@@ -318,7 +318,7 @@ struct orc_ts {
   int nv = 0, nt = 0, n = 0;
   Vec X;                     // [nv*3] rest positions
   std::vector<int32_t> cells;  // [nt*4]
-  double dt, E, nu, rho, damping = 0.0, rtol = 1e-2, abs_tol = 1e-2;
+  double dt, E, nu, rho, damping = 0.0, rtol = 1e-2, abs_tol = 1e-2, mass_third = 0.0;
   Vec E_elem, nu_elem;       // optional per-element material
   int pd_diff_mode = 0;
   std::vector<int8_t> dof_type;  // [nv*3]
@@ -652,7 +652,8 @@ void element_laplace(const double* Xv[4], double alpha, double L[16]) {
 
 bool stop_ok(const orc_ts& s, const orc_params& p, double gn, double g0) {
   if (p.stop_mode == 0) return gn < s.abs_tol;
-  return gn <= p.rel_tol * g0;
+  // the absolute rule at rtol = stop_floor as a floor (a step from rest has a round-off gradient)
+  return gn <= p.rel_tol * g0 || gn <= p.stop_floor * s.mass_third;
 }
 
 }  // namespace
@@ -774,6 +775,7 @@ void orc_default_params(orc_params* p) {
   p->ncg_step0 = 1e-2;
   p->ncg_eta = 0.5;
   p->ncg_expand = 3;
+  p->stop_floor = 1e-12;
 }
 
 orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double dt, double E, double nu,
@@ -888,6 +890,7 @@ void orc_reset(orc_ts* s) {
   double asum = 0;
   for (double v : s->mass_vals) asum += std::fabs(v);
   s->abs_tol = asum / 3.0 * s->rtol;
+  s->mass_third = asum / 3.0;
   s->has_reset = true;
   s->pd_ready = false;
 }

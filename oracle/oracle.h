@@ -82,6 +82,7 @@ typedef struct {
   double ncg_step0;       /* first trial step of the first iteration: reference learning_rate 1e-2 (:21) */
   double ncg_eta;         /* Dai-Kou truncation beta >= eta g.d / |d|^2 */
   int ncg_expand;         /* line-search expansions toward the parabola's minimiser */
+  double stop_floor;      /* stop_mode 1 also stops at |g| <= stop_floor * sum|M| / 3 */
 } orc_params;
 
 typedef struct {

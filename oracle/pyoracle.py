@@ -55,6 +55,7 @@ class OrcParams(C.Structure):
         ("ncg_step0", C.c_double),
         ("ncg_eta", C.c_double),
         ("ncg_expand", C.c_int),
+        ("stop_floor", C.c_double),
     ]
 
 

@@ -63,6 +63,7 @@ class Params(C.Structure):
         ("ncg_step0", C.c_double),
         ("ncg_eta", C.c_double),
         ("ncg_expand", C.c_int32),
+        ("stop_floor", C.c_double),
     ]
 
     def as_dict(self):

@@ -78,6 +78,9 @@ struct TimeStep {
   // ---- configuration (time_step.hpp:683-708)
   int nv = 0, nt = 0, n = 0;
   double dt = 1e-3, E = 1e6, nu = 0.33, rho = 1e3, damping = 0.0, rtol = 1e-2, abs_tol = 1e-2;
+  double mass_third = 0;  // sum |M_ij| / 3, the reference threshold's scale (abs_tol = rtol * mass_third)
+  DBuf<int32_t> mark_verts;  // scratch of the mark_* calls (grown, never shrunk)
+  DBuf<double> mark_targ;
   int precision = SSIM_GB_FP64;
   int stepper = SSIM_GB_STEPPER_NONE;
   ssim_gb_params params{};
@@ -121,6 +124,21 @@ struct TimeStep {
   DBuf<int32_t> inst_off;
   DBuf<double> inst_g2;
   std::vector<double> inst_g2_h, inst_g0_h;
+  std::vector<double> inst_mass_third;  // sum |M_ij| / 3 of each instance (its stop floor's scale)
+
+  // per-instance sums of |mass| (the instances are disjoint, so every block belongs to one instance)
+  void instance_masses() {
+    inst_mass_third.assign(std::max(1, ninst), 0.0);
+    if (ninst <= 1) return;
+    std::vector<double> smass;
+    slot_masses(topo, detJ, rho, smass);
+    for (int q = 0; q < topo.nslots; ++q) {
+      const int u = topo.slot_row[q];
+      if (u < 0) continue;
+      const int i = (int)(std::upper_bound(inst_off_h.begin(), inst_off_h.end(), u) - inst_off_h.begin()) - 1;
+      inst_mass_third[i] += (topo.sl_col[q] == u ? 1.0 : 2.0) * std::fabs(smass[q]);
+    }
+  }
   double* hscal = nullptr;     // pinned mirror of dscal
   // ---- profiling
   bool profiling = false;
@@ -288,6 +306,8 @@ struct TimeStep {
     for (int q = 0; q < topo.nslots; ++q)
       if (topo.slot_row[q] >= 0) asum += (topo.sl_col[q] == topo.slot_row[q] ? 3.0 : 6.0) * std::fabs(smass[q]);
     abs_tol = asum / 3.0 * rtol;
+    mass_third = asum / 3.0;
+    instance_masses();
     if (mixed()) {
       std::vector<float> sm(smass.begin(), smass.end());
       sf.slot_mass.upload(sm, stream);
@@ -535,10 +555,13 @@ struct TimeStep {
   // or, for a batch, the relative rule on every instance
   bool stop_test(double gn, double g0) {
     if (params.stop_mode == 0) return gn < abs_tol;
-    if (ninst <= 1) return gn <= params.rel_tol * g0;
+    // relative rule, with the reference's absolute rule at rtol = stop_floor as a floor (per instance for a
+    // batch): a step that starts at rest has a round-off gradient whose fraction cannot be reached
+    if (ninst <= 1) return gn <= params.rel_tol * g0 || gn <= params.stop_floor * mass_third;
     instance_norms();
     for (int i = 0; i < ninst; ++i)
-      if (std::sqrt(inst_g2_h[i]) > params.rel_tol * inst_g0_h[i]) return false;
+      if (std::sqrt(inst_g2_h[i]) > std::max(params.rel_tol * inst_g0_h[i], params.stop_floor * inst_mass_third[i]))
+        return false;
     return true;
   }
 
@@ -1146,6 +1169,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->ncg_step0 = 1e-2;
   p->ncg_eta = 0.5;
   p->ncg_expand = 3;
+  p->stop_floor = 1e-12;
 }
 
 ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
@@ -1249,7 +1273,7 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
       !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 1 ||
       p->pcg_persistent < 0 || p->pcg_persistent > 3 || p->pcg_spin_limit < 0 || p->pcg_barrier_extra < 0 ||
       p->pcg_max_blocks < 0 || p->ncg_max_iters < 0 || !(p->ncg_step0 > 0) || !(p->ncg_eta >= 0) ||
-      p->ncg_expand < 0 ||
+      p->ncg_expand < 0 || !(p->stop_floor >= 0) ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;
@@ -1292,11 +1316,11 @@ ssim_gb_status ssim_gb_mark_dirichlet_batched(ssim_gb_timestep* h, const int32_t
   for (int i = 0; i < n; ++i)
     if (verts[i] < 0 || verts[i] >= t.nv) throw ssim_gb::invalid_argument("vertex index out of range");
   if (n == 0) return SSIM_GB_OK;
-  ssim_gb::DBuf<int32_t> dv;
-  ssim_gb::DBuf<double> dt_;
-  dv.upload(verts, n, t.stream);
-  dt_.upload(targ, 3 * (size_t)n, t.stream);
-  ssim_gb::launch_mark_dofs(n, dv.p, dt_.p, 1, t.dof_type.p, t.dbc_values.p, t.stream);
+  if (t.mark_verts.n < (size_t)n) t.mark_verts.alloc(n);
+  if (t.mark_targ.n < 3 * (size_t)n) t.mark_targ.alloc(3 * (size_t)n);
+  SSIM_CUDA(cudaMemcpyAsync(t.mark_verts.p, verts, sizeof(int32_t) * n, cudaMemcpyHostToDevice, t.stream));
+  SSIM_CUDA(cudaMemcpyAsync(t.mark_targ.p, targ, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, t.stream));
+  ssim_gb::launch_mark_dofs(n, t.mark_verts.p, t.mark_targ.p, 1, t.dof_type.p, t.dbc_values.p, t.stream);
   ssim_gb::launch_build_mask(t.nv, t.dof_type.p, t.mask.p, t.stream);
   SSIM_CUDA(cudaStreamSynchronize(t.stream));
   API_CATCH(h)
@@ -1310,9 +1334,9 @@ ssim_gb_status ssim_gb_mark_general_batched(ssim_gb_timestep* h, const int32_t* 
   for (int i = 0; i < n; ++i)
     if (verts[i] < 0 || verts[i] >= t.nv) throw ssim_gb::invalid_argument("vertex index out of range");
   if (n == 0) return SSIM_GB_OK;
-  ssim_gb::DBuf<int32_t> dv;
-  dv.upload(verts, n, t.stream);
-  ssim_gb::launch_mark_dofs(n, dv.p, nullptr, 0, t.dof_type.p, t.dbc_values.p, t.stream);
+  if (t.mark_verts.n < (size_t)n) t.mark_verts.alloc(n);
+  SSIM_CUDA(cudaMemcpyAsync(t.mark_verts.p, verts, sizeof(int32_t) * n, cudaMemcpyHostToDevice, t.stream));
+  ssim_gb::launch_mark_dofs(n, t.mark_verts.p, nullptr, 0, t.dof_type.p, t.dbc_values.p, t.stream);
   ssim_gb::launch_build_mask(t.nv, t.dof_type.p, t.mask.p, t.stream);
   SSIM_CUDA(cudaStreamSynchronize(t.stream));
   API_CATCH(h)
@@ -1615,6 +1639,7 @@ ssim_gb_status ssim_gb_set_instances(ssim_gb_timestep* h, const int32_t* vertex_
   t.inst_g2.alloc(std::max(1, num_instances));
   t.inst_g2_h.assign(std::max(1, num_instances), 0.0);
   t.inst_g0_h.assign(std::max(1, num_instances), 0.0);
+  t.instance_masses();
   SSIM_CUDA(cudaStreamSynchronize(t.stream));
   API_CATCH(h)
 }

@@ -20,7 +20,8 @@ OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle_small.npz
 SETTINGS = dict(dt=1e-2, E=1e5, nu=0.45, rho=1000.0, gravity=(0.0, 0.0, -9.8))
 # twelve Newton iterations with near-exact inner solves: quadratic convergence reaches round-off well before the
 # last one, so two correct implementations agree to round-off whatever their stopping decisions
-NEWTON = dict(stop_mode=1, rel_tol=1e-14, cg_rtol=1e-13, cg_max_iters=20000, max_newton_iters=12)
+# a fixed 12 tight Newton iterations per step (no early stop: stop_floor 0)
+NEWTON = dict(stop_mode=1, rel_tol=1e-14, cg_rtol=1e-13, cg_max_iters=20000, max_newton_iters=12, stop_floor=0.0)
 
 
 def inputs():

@@ -20,7 +20,7 @@ def _setup():
     X, T = mesh.kuhn_box((4, 4, 4))
     fixed = np.where(X[:, 2] == 0.0)[0]
     params = g.default_params(stop_mode=1, rel_tol=1e-14, cg_rtol=1e-13, cg_max_iters=20000, max_newton_iters=25,
-                              precond=2)
+                              precond=2, stop_floor=0.0)
     eng = adjoint.RolloutEngine(X, T, fixed, dt=1e-2, nu=0.45, rho=1000.0, params=params, adjoint_rtol=1e-13)
     E = torch.tensor(10.0 ** mesh.uniform(5, T.shape[0], 4.0, 6.0), dtype=torch.float64, device="cuda")
     v0 = torch.tensor(0.5 * mesh.normal(6, X.size).reshape(X.shape), dtype=torch.float64, device="cuda")

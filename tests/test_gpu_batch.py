@@ -17,10 +17,12 @@ def test_batch_matches_instances_fp64():
     from oracle import pyoracle
 
     batch = scenes.batch_cubes(n=5, kmin=2, kmax=4, seed=14)
-    params = g.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000, precond=2)
+    params = g.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000, precond=2,
+                              stop_floor=0.0)
     ts = scenes.build_batch_timestep(batch, precision="fp64", params=params)
     ots = [scenes.batch_instance_oracle(batch, i) for i in range(5)]
-    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000, precond=2)
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000, precond=2,
+                                 stop_floor=0.0)
     for _ in range(3):
         ts.step()
         assert ts.stats()["converged"] == 1
