@@ -98,7 +98,8 @@ typedef struct {
   int32_t max_lbfgs_iters;
   int32_t cg_check_every; /* PCG iterations launched between host convergence checks */
   double ls_energy_slack; /* Armijo accepts E_t <= E + c a g.d + slack * sum|energy terms| (round-off) */
-  int32_t pd_kappa_mode;  /* PD matrix diffusivity: 0 as ssim builds it (time_step.hpp:356), 1 from Lame */
+  int32_t pd_kappa_mode;  /* PD matrix diffusivity: 0 as ssim builds it (time_step.hpp:356), 1 from the Lame
+                             parameters, 2 from each element's own Lame parameters (per-element materials) */
   int32_t pcg_persistent; /* 0: two launches per PCG iteration, host checks every cg_check_every iterations;
                              1: the same PCG in one cooperative launch per solve (grid barriers, no host
                              round trips; bitwise the iterates of 0); 2: Chronopoulos-Gear PCG in one
@@ -116,6 +117,11 @@ typedef struct {
   double stop_floor;      /* stop_mode 1 also stops when |g| <= stop_floor * sum|M| / 3 (the reference's absolute
                              rule with rtol = stop_floor; default 1e-12), so a step starting at rest, whose
                              gradient is round-off, does not chase a fraction of it */
+  int32_t mixed_elem32;   /* mixed precision, Newton: 1 (default) evaluates energy and forces with FP32 element
+                             arithmetic while the residual is above elem32_switch times the target, then in
+                             FP64 (the stopping test always sees an FP64 residual); 0 keeps every evaluation FP64 */
+  double ls_energy_slack32; /* Armijo round-off slack of the FP32 evaluations, times their term-magnitude sum */
+  double elem32_switch;   /* residual / target below which the FP32 phase ends (100) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

@@ -1242,11 +1242,12 @@ double orc_compute_step_forward_euler(orc_ts* s, const orc_params*, orc_stats* s
 // PD matrix (projective_dynamics.hpp:53-93): (mass(rho) + laplace(dt^2 * kappa)) (x) I3 with the DBC
 // identity filter.  kappa = approximated_diffusivity (stable_neohookean.hpp:106-111) of
 // uniform_elasticity() (time_step.hpp:356), which constructs the model as ElastModel{E, nu}: the
-// model's (lambda, mu) slots then hold (E, nu).  Mode 1 uses the Lame parameters instead.
+// model's (lambda, mu) slots then hold (E, nu).  Mode 1 uses the Lame parameters instead, mode 2 each
+// element's own Lame parameters (an extension for per-element materials).
 void orc_pd_matrix_values(orc_ts* s, double* out) {
   double lam_slot = s->E, mu_slot = s->nu;
   if (s->pd_diff_mode == 1) orc_lame(s->E, s->nu, &lam_slot, &mu_slot);
-  const double kappa = (lam_slot + 5.0 / 6.0 * mu_slot) + 2.0 * (4.0 / 3.0 * mu_slot);
+  const double kappa_u = (lam_slot + 5.0 / 6.0 * mu_slot) + 2.0 * (4.0 / 3.0 * mu_slot);
   const int nnz = (int)s->col_idx.size();
   Vec vals(nnz, 0.0);
   for (int e = 0; e < s->nt; ++e) {
@@ -1254,6 +1255,8 @@ void orc_pd_matrix_values(orc_ts* s, double* out) {
     const double* Xv[4] = {&s->X[c[0] * 3], &s->X[c[1] * 3], &s->X[c[2] * 3], &s->X[c[3] * 3]};
     double M[16], L[16];
     element_mass(Xv, s->rho, M);
+    const double kappa =
+        s->pd_diff_mode == 2 ? (s->lam(e) + 5.0 / 6.0 * s->mu(e)) + 2.0 * (4.0 / 3.0 * s->mu(e)) : kappa_u;
     element_laplace(Xv, s->dt * s->dt * kappa, L);
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 4; ++j)

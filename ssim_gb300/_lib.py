@@ -64,6 +64,9 @@ class Params(C.Structure):
         ("ncg_eta", C.c_double),
         ("ncg_expand", C.c_int32),
         ("stop_floor", C.c_double),
+        ("mixed_elem32", C.c_int32),
+        ("ls_energy_slack32", C.c_double),
+        ("elem32_switch", C.c_double),
     ]
 
     def as_dict(self):

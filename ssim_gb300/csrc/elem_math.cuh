@@ -90,6 +90,45 @@ __host__ __device__ __forceinline__ S snh_eval(const S* F, S lam, S mu, S alpha,
   return S(0.5) * (t1 + t2 - t3) - psi0;
 }
 
+// The stable Neo-Hookean energy and PK1 written in the displacement gradient G = F - I so that no O(mu) or
+// O(lambda) terms cancel (for FP32 evaluation of small strains): with s = Ic - 3 = 2 tr G + |G|^2,
+// J - 1 = tr G + (principal 2x2 minors of G) + det G, c1 = 1 - alpha = -3/4 mu / lambda:
+//   Psi - Psi(I) = 1/2 [ mu (s - log1p(s / 4)) + lambda (J - 1)(J - 1 + 2 c1) ]
+//   P = lambda (J - 1) cof F + 3/4 mu (G + G^T - tr G I - cof G) + mu s / (4 (4 + s)) F,
+// using cof(I + G) = I + tr G I - G^T + cof G.  Algebraically the same functions as snh_eval (the
+// reference's stable_neohookean.hpp:23-62); scale returns the magnitude sum of the terms above.
+template <typename S, bool STRESS>
+__host__ __device__ __forceinline__ S snh_eval_small(const S* G, S lam, S mu, S* P, S& scale) {
+  const S trG = G[0] + G[4] + G[8];
+  S n2 = 0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) n2 += G[i] * G[i];
+  const S s = S(2) * trG + n2;
+  S cG[9];
+  cofactor(G, cG);
+  const S m2 = cG[0] + cG[4] + cG[8];  // sum of the principal 2x2 minors
+  const S dG = G[0] * cG[0] + G[1] * cG[1] + G[2] * cG[2];
+  const S Jm1 = trG + m2 + dG;
+  const S c1 = S(-0.75) * mu / lam;
+  const S lg = log1p(S(0.25) * s);
+  if (STRESS) {
+    const S lj = lam * Jm1, q = mu * s / (S(4) * (S(4) + s)), h = S(0.75) * mu;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int k = r * 3 + c;
+        const S id = r == c ? S(1) : S(0);
+        const S cofF = id + (r == c ? trG : S(0)) - G[c * 3 + r] + cG[k];
+        const S D = G[k] + G[c * 3 + r] - (r == c ? trG : S(0)) - cG[k];
+        P[k] = lj * cofF + h * D + q * (id + G[k]);
+      }
+  }
+  const S t1 = mu * (s - lg), t2 = lam * Jm1 * (Jm1 + S(2) * c1);
+  scale = S(0.5) * (mu * (fabs(s) + fabs(lg)) + lam * fabs(Jm1) * (fabs(Jm1) + S(2) * fabs(c1)));
+  return S(0.5) * (t1 + t2);
+}
+
 // per-element constants of snh_eval
 template <typename S>
 __host__ __device__ __forceinline__ void snh_constants(S lam, S mu, S& alpha, S& psi0) {

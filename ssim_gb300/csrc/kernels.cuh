@@ -73,6 +73,11 @@ void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* 
                              const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
                              bool trial, const Reduce& red, cudaStream_t st);
 // g[v] = sum over incident (e, i) of lf[e][i], Dirichlet dofs zeroed; |g|^2 into sc->gnorm2
+// the same pass with FP32 element arithmetic (small-strain forms), FP64 differences and sums
+template <typename SD>
+void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const double* u, const double* xt,
+                               const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
+                               bool trial, const Reduce& red, cudaStream_t st);
 void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
                           double* g, const Reduce& red, cudaStream_t st);
 

@@ -123,6 +123,105 @@ __global__ void __launch_bounds__(EB)
   }
 }
 
+// The same pass with the element arithmetic in FP32 (the mixed Newton's inner iterations): differences
+// of displacements and inertia targets are formed in FP64 and rounded once, the energy and stress use
+// the small-strain forms (snh_eval_small / linear_eval), so results carry FP32 rounding relative to the
+// strain, not to lambda or mu; the element energies and term scales are summed in FP64.
+template <typename SD, bool FORCES, bool TRIAL>
+__global__ void __launch_bounds__(EB)
+    elem_energy_grad32_kernel(ElemFP64 el, ElemFP32 ef, const double* __restrict__ u, const double* __restrict__ xt,
+                              const V4<SD>* __restrict__ d, double alpha, float dt2, float rho,
+                              double* __restrict__ lf, Reduce red) {
+  __shared__ double stage[FORCES ? EB * 12 : 1];
+  __shared__ double shred[EB / 32][2];
+  const int e0 = blockIdx.x * EB;
+  const int e = e0 + threadIdx.x;
+  double energy = 0, escale = 0;
+  float lfv[12];
+  if (e < el.nt) {
+    const int4 c = el.cells[e];
+    const int vid[4] = {c.x, c.y, c.z, c.w};
+    double uu[4][3];
+    float dd[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      V4<SD> dv;
+      if (TRIAL) dv = d[vid[i]];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double uk = u[vid[i] * 3 + k];
+        if (TRIAL) uk += alpha * (double)comp<SD>(dv, k);
+        uu[i][k] = uk;
+        dd[i][k] = (float)(uk - xt[vid[i] * 3 + k]);
+      }
+    }
+    float Dm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Dm[k] = ef.dminv[(size_t)k * el.nt + e];
+    float Du[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) Du[r * 3 + k] = (float)(uu[k + 1][r] - uu[0][r]);
+    float G[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        G[r * 3 + cc] = Du[r * 3 + 0] * Dm[0 * 3 + cc] + Du[r * 3 + 1] * Dm[1 * 3 + cc] + Du[r * 3 + 2] * Dm[2 * 3 + cc];
+    const float lam = ef.lam[e], mu = ef.mu[e], V = ef.vol[e];
+    const float m = rho * V * (1.0f / 20.0f);
+    float sd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sd[k] = dd[0][k] + dd[1][k] + dd[2][k] + dd[3][k];
+    float q = sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q += dd[i][0] * dd[i][0] + dd[i][1] * dd[i][1] + dd[i][2] * dd[i][2];
+    float P[9], sc;
+    const float psi = el.model == 1 ? linear_eval<float, FORCES>(G, lam, mu, P, sc)
+                                    : snh_eval_small<float, FORCES>(G, lam, mu, P, sc);
+    if (FORCES) {
+      const float sV = dt2 * V;
+      float tot[3] = {0, 0, 0};
+#pragma unroll
+      for (int i = 1; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float h = P[j * 3 + 0] * Dm[(i - 1) * 3 + 0] + P[j * 3 + 1] * Dm[(i - 1) * 3 + 1] +
+                          P[j * 3 + 2] * Dm[(i - 1) * 3 + 2];
+          tot[j] += h;
+          lfv[i * 3 + j] = sV * h + m * (dd[i][j] + sd[j]);
+        }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) lfv[j] = -sV * tot[j] + m * (dd[0][j] + sd[j]);
+    }
+    energy = (double)(dt2 * V * psi) + (double)(0.5f * m * q);
+    escale = (double)(dt2 * V * sc) + (double)(0.5f * m * q);
+  }
+  if (FORCES) {
+    if (e < el.nt) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) stage[threadIdx.x * 12 + k] = (double)lfv[k];
+    }
+    __syncthreads();
+    const int nvalid = min(EB, el.nt - e0);
+    double* dst = lf + (size_t)e0 * 12;
+    for (int i = threadIdx.x; i < nvalid * 12; i += EB) dst[i] = stage[i];
+  }
+  double v2[2] = {energy, escale};
+  block_sum<2, EB>(v2, shred);
+  double tot[2];
+  if (grid_sum_last<2, EB>(v2, red.partials, red.counter, tot)) {
+    if (TRIAL) {
+      red.sc->trial_energy = tot[0];
+      red.sc->trial_energy_scale = tot[1];
+    } else {
+      red.sc->energy = tot[0];
+      red.sc->energy_scale = tot[1];
+    }
+  }
+}
+
 constexpr int GB = 256;
 
 __global__ void __launch_bounds__(GB)
@@ -274,6 +373,30 @@ template void launch_elem_energy_grad<float>(const ElemFP64&, const double*, con
 template void launch_elem_energy_grad<double>(const ElemFP64&, const double*, const double*, const double*,
                                               const double4_32a*, double, double, double, double*, bool, bool,
                                               const Reduce&, cudaStream_t);
+
+template <typename SD>
+void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const double* u, const double* xt,
+                               const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
+                               bool trial, const Reduce& red, cudaStream_t st) {
+  if (el.nt <= 0) return;
+  const int grid = div_up(el.nt, EB);
+  const float f_dt2 = (float)dt2, f_rho = (float)rho;
+  if (trial && with_forces)
+    elem_energy_grad32_kernel<SD, true, true><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+  else if (trial)
+    elem_energy_grad32_kernel<SD, false, true><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+  else if (with_forces)
+    elem_energy_grad32_kernel<SD, true, false><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+  else
+    elem_energy_grad32_kernel<SD, false, false><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+  after_launch("elem_energy_grad32");
+}
+template void launch_elem_energy_grad32<float>(const ElemFP64&, const ElemFP32&, const double*, const double*,
+                                               const float4*, double, double, double, double*, bool, bool,
+                                               const Reduce&, cudaStream_t);
+template void launch_elem_energy_grad32<double>(const ElemFP64&, const ElemFP32&, const double*, const double*,
+                                                const double4_32a*, double, double, double, double*, bool, bool,
+                                                const Reduce&, cudaStream_t);
 
 void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
                           double* g, const Reduce& red, cudaStream_t st) {

@@ -168,6 +168,7 @@ struct TimeStep {
     return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p, snh_alpha.p, snh_psi0.p, elastic_model};
   }
   ElemFP32 e32() const { return ElemFP32{nt, dcells.p, fdminv.p, fvol.p, flam.p, fmu.p}; }
+  ElemFP32 e32s() const { return e32(); }
   SellMatrix A() const {
     return SellMatrix{nv, topo.nslots, sl_off.p, sl_col.p, slot_row.p, lo_off.p, lo_src.p, lo_col.p};
   }
@@ -336,7 +337,7 @@ struct TimeStep {
   // with the Dirichlet identity filter, assembled once into the symmetric block store.  kappa is
   // approximated_diffusivity (stable_neohookean.hpp:106-111) of uniform_elasticity() (time_step.hpp:356),
   // which builds the model as ElastModel{E, nu}, i.e. with (E, nu) in its (lambda, mu) slots; mode 1 uses the
-  // Lame parameters instead.
+  // Lame parameters instead, mode 2 each element's own Lame parameters (per-element materials).
   template <typename S>
   void pd_setup(Solver<S>& s) {
     double lam_slot = E, mu_slot = nu;
@@ -345,8 +346,17 @@ struct TimeStep {
       lam_slot = E * nu / ((1 + nu) * (1 - 2 * nu));
     }
     const double kappa = (lam_slot + 5.0 / 6.0 * mu_slot) + 2.0 * (4.0 / 3.0 * mu_slot);
-    std::vector<double> pd;
-    slot_pd_values(topo, cells.data(), X.data(), detJ, rho, dt * dt * kappa, pd);
+    std::vector<double> pd, alpha_e;
+    if (params.pd_kappa_mode == 2) {
+      alpha_e.resize(nt);
+      for (int e = 0; e < nt; ++e) {
+        const double Ee = E_elem.empty() ? E : E_elem[e], ne = nu_elem.empty() ? nu : nu_elem[e];
+        const double m = Ee / (2 * (1 + ne)), l = Ee * ne / ((1 + ne) * (1 - 2 * ne));
+        alpha_e[e] = dt * dt * ((l + 5.0 / 6.0 * m) + 2.0 * (4.0 / 3.0 * m));
+      }
+    }
+    slot_pd_values(topo, cells.data(), X.data(), detJ, rho, dt * dt * kappa, pd,
+                   params.pd_kappa_mode == 2 ? &alpha_e : nullptr);
     std::vector<S> pds(pd.begin(), pd.end());
     s.slot_pd.upload(pds, stream);
     s.pd_vals.alloc(9 * (size_t)topo.nslots);
@@ -399,6 +409,20 @@ struct TimeStep {
     else
       launch_elem_energy_grad<double>(e64(), dX.p, next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
                                       red(), stream);
+    if (profiling) prof_end(e0, e1, PK_GRAD, 0);
+    launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+    sync_scalars();
+    if (!std::isfinite(hsc->energy) || !std::isfinite(hsc->gnorm2))
+      throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
+    return hsc->energy;
+  }
+
+  // energy and forces with FP32 element arithmetic (mixed Newton's inner iterations), FP64 gather and sums
+  double energy_grad32() {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (profiling) prof_begin(e0, e1);
+    launch_elem_energy_grad32<float>(e64(), e32s(), next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
+                                     red(), stream);
     if (profiling) prof_end(e0, e1, PK_GRAD, 0);
     launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
     sync_scalars();
@@ -729,16 +753,36 @@ struct TimeStep {
   template <typename S>
   void newton(ssim_gb_step_stats& st) {
     Solver<S>& s = solver<S>();
-    double E0 = energy_grad();
+    // mixed precision: the inner iterations evaluate energy and forces with FP32 element arithmetic (the
+    // small-strain forms); the stopping test is then confirmed with an FP64 evaluation, and if the FP64
+    // residual is above the target (or the FP32 residual stalls) the remaining iterations run in FP64
+    bool e32 = mixed() && params.mixed_elem32 != 0;
+    double E0 = e32 ? energy_grad32() : energy_grad();
     double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
     st.grad_norm0 = g0;
     start_instances();
+    double gn_prev = gn;
+    int stall = 0;
+    auto to_fp64 = [&]() {
+      e32 = false;
+      E0 = energy_grad();
+      Escale = hsc->energy_scale;
+      gn = std::sqrt(hsc->gnorm2);
+    };
     int it = 0;
     for (;; ++it) {
       st.grad_norm = gn;
       st.energy = E0;
+      // the FP32 phase ends once the residual is within elem32_switch times the target (FP32 rounding of
+      // the O(|g0|) inertia and elastic forces is close to a 1e-6 target), or when it stalls
+      const double tgt = params.stop_mode == 0 ? abs_tol : params.rel_tol * g0;
+      if (e32 && (gn <= params.elem32_switch * tgt || stall >= 2)) {
+        to_fp64();
+        st.grad_norm = gn;
+        st.energy = E0;
+      }
       if (stop_test(gn, g0)) {
         st.converged = 1;
         break;
@@ -762,14 +806,19 @@ struct TimeStep {
       // pass, so the accepted trial's forces are the next gradient (no separate evaluation)
       double alpha = 1.0;
       double Et = 0, Et_scale = 0;
+      const double slack = (e32 ? params.ls_energy_slack32 : params.ls_energy_slack) * Escale;
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
-        launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
-                                   red(), stream);
+        if (e32)
+          launch_elem_energy_grad32<S>(e64(), e32s(), next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
+                                       red(), stream);
+        else
+          launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
+                                     red(), stream);
         sync_scalars();
         st.ls_steps_total++;
         Et = hsc->trial_energy;
         Et_scale = hsc->trial_energy_scale;
-        if (Et <= E0 + params.armijo * alpha * gd + params.ls_energy_slack * Escale) break;
+        if (Et <= E0 + params.armijo * alpha * gd + slack) break;
         if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
       launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
@@ -781,6 +830,8 @@ struct TimeStep {
       E0 = Et;
       Escale = Et_scale;
       gn = std::sqrt(hsc->gnorm2);
+      stall = gn > 0.5 * gn_prev ? stall + 1 : 0;
+      gn_prev = gn;
     }
     st.newton_iters = it;
   }
@@ -1170,6 +1221,9 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->ncg_eta = 0.5;
   p->ncg_expand = 3;
   p->stop_floor = 1e-12;
+  p->mixed_elem32 = 1;
+  p->ls_energy_slack32 = 1e-6;
+  p->elem32_switch = 100.0;
 }
 
 ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
@@ -1270,10 +1324,11 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
   CHECK_H(h);
   if (!p) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null params");
   if (p->max_newton_iters < 0 || p->cg_max_iters < 0 || p->max_ls_iters < 1 || !(p->ls_shrink > 0 && p->ls_shrink < 1) ||
-      !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 1 ||
+      !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 2 ||
       p->pcg_persistent < 0 || p->pcg_persistent > 3 || p->pcg_spin_limit < 0 || p->pcg_barrier_extra < 0 ||
       p->pcg_max_blocks < 0 || p->ncg_max_iters < 0 || !(p->ncg_step0 > 0) || !(p->ncg_eta >= 0) ||
-      p->ncg_expand < 0 || !(p->stop_floor >= 0) ||
+      p->ncg_expand < 0 || !(p->stop_floor >= 0) || p->mixed_elem32 < 0 || p->mixed_elem32 > 1 ||
+      !(p->ls_energy_slack32 >= 0) || !(p->elem32_switch >= 1) ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;

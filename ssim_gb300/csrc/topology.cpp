@@ -195,7 +195,7 @@ void slot_masses(const Topology& t, const std::vector<double>& detJ, double rho,
 }
 
 void slot_pd_values(const Topology& t, const int32_t* cells, const double* X, const std::vector<double>& detJ,
-                    double rho, double alpha, std::vector<double>& out) {
+                    double rho, double alpha, std::vector<double>& out, const std::vector<double>* alpha_e) {
   // per element: grad phi_i from the inverse Jacobian (bilinears.hpp:158-167 summed over k = l)
   std::vector<double> lap(10 * (size_t)t.nt);
   for (int e = 0; e < t.nt; ++e) {
@@ -223,7 +223,8 @@ void slot_pd_values(const Topology& t, const int32_t* cells, const double* X, co
     for (int b = 0; b < 10; ++b) {
       const int v = kBlkV[b], w = kBlkW[b];
       lap[10 * (size_t)e + b] =
-          (detJ[e] / 6.0 * (g[v][0] * g[w][0] + g[v][1] * g[w][1] + g[v][2] * g[w][2])) * alpha;
+          (detJ[e] / 6.0 * (g[v][0] * g[w][0] + g[v][1] * g[w][1] + g[v][2] * g[w][2])) *
+          (alpha_e ? (*alpha_e)[e] : alpha);
     }
   }
   out.assign(t.nslots, 0.0);

@@ -49,7 +49,9 @@ void csr_pattern(const Topology& t, int32_t* row_ptr, int32_t* col_idx);
 void slot_masses(const Topology& t, const std::vector<double>& detJ, double rho, std::vector<double>& out);
 
 // PD matrix scalar per upper slot: mass(rho) + laplace(alpha) element integrals (projective_dynamics.hpp:62-82)
+// alpha_e (optional): per-element Laplacian weights replacing the uniform alpha
 void slot_pd_values(const Topology& t, const int32_t* cells, const double* X, const std::vector<double>& detJ,
-                    double rho, double alpha, std::vector<double>& out);
+                    double rho, double alpha, std::vector<double>& out,
+                    const std::vector<double>* alpha_e = nullptr);
 
 }  // namespace ssim_gb
