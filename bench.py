@@ -33,7 +33,7 @@ def newton_params(g):
     """Solver settings shared by the mixed and FP64 GPU paths and the CPU baseline."""
     return g.default_params(
         stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=1e-2, cg_max_iters=5000,
-        max_newton_iters=100, cg_check_every=16, precond=2,
+        max_newton_iters=100, cg_check_every=16, precond=2, max_lbfgs_iters=20000,
     )
 
 
@@ -50,6 +50,10 @@ def make_scene(name):
         return scenes.bar()
     if name == "batch":
         return scenes.batch_cubes()
+    if name == "cloth512":
+        return scenes.cloth()
+    if name == "cloth_small":
+        return scenes.cloth(128)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -127,6 +131,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class _SpringFacade:
+    """The calls the e2e loop makes, on a spring-system TimeStep (the libssim facade is tets only)."""
+
+    def __init__(self, ts):
+        self.step_ = ts
+
+    def mark_dirichlet_batched(self, verts, targets):
+        self.step_.mark_dirichlet_batched(verts, np.ascontiguousarray(np.asarray(targets).T))
+
+    def step(self):
+        self.step_.step()
+
+    def deformation(self):
+        return self.step_.get("deformation")
+
+
 def run_gpu_arm(args, scene):
     import torch
 
@@ -201,12 +221,15 @@ def run_gpu_arm(args, scene):
 
     fixed = np.asarray(scene["fixed"], dtype=np.int32)
     pin_targ = torch.zeros((3, fixed.size), dtype=torch.float64).pin_memory()
-    s = fem.tet_newton_cuda(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"],
-                            precision="mixed", params=params)
-    if scene.get("E_cells") is not None:
-        s.step_.set_material(scene["E_cells"], None)
-    s.add_gravity(scene["gravity"])
-    s.reset()
+    if scene.get("springs"):  # no reference-facing spring API: the TimeStep handle itself
+        s = _SpringFacade(scenes.build_timestep(scene, precision="mixed", stepper=args.stepper, params=params))
+    else:
+        s = fem.tet_newton_cuda(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"],
+                                precision="mixed", params=params)
+        if scene.get("E_cells") is not None:
+            s.step_.set_material(scene["E_cells"], None)
+        s.add_gravity(scene["gravity"])
+        s.reset()
     if scene.get("u0") is not None:  # the scene's initial state, as the device-timed runs start from
         for f in ("deformation", "prev_deform"):
             s.step_.set(f, scene["u0"])
@@ -270,9 +293,9 @@ def run_adjoint(precision, n=32, steps=40, checkpoint_every=8):
             "grad_finite": bool(torch.isfinite(E.grad).all().item() and torch.isfinite(v0.grad).all().item())}
 
 
-def cpu_baseline_inproc(scene, max_seconds, max_steps):
-    """The FP64 oracle on this host's cores: whole Newton steps of the same workload from rest, as many as
-    fit in ``max_seconds`` (at least one, at most ``max_steps``)."""
+def cpu_baseline_inproc(scene, max_seconds, max_steps, method="newton"):
+    """The FP64 oracle on this host's cores: whole steps (``method``: newton, lbfgs or pd) of the same
+    workload from rest, as many as fit in ``max_seconds`` (at least one, at most ``max_steps``)."""
     from oracle import pyoracle
     from ssim_gb300 import scenes
 
@@ -281,27 +304,28 @@ def cpu_baseline_inproc(scene, max_seconds, max_steps):
     gp = newton_params(g)
     op = pyoracle.default_params(stop_mode=1, rel_tol=gp.rel_tol, cg_forcing=1, cg_rtol=gp.cg_rtol,
                                  cg_eta_min=gp.cg_eta_min, cg_max_iters=gp.cg_max_iters,
-                                 max_newton_iters=gp.max_newton_iters, precond=gp.precond)
+                                 max_newton_iters=gp.max_newton_iters, precond=gp.precond,
+                                 max_lbfgs_iters=gp.max_lbfgs_iters)
     ot = scenes.build_oracle(scene)
     t0 = time.perf_counter()
     steps = 0
     while True:
         ot.prepare_step()
-        ot.compute_step("newton", op)
+        ot.compute_step(method, op)
         ot.step_next()
         steps += 1
         if steps >= max_steps or time.perf_counter() - t0 >= max_seconds:
             break
     dt = time.perf_counter() - t0
     return {"value": steps / dt, "unit": "steps/s", "cores": pyoracle.num_threads(), "kind": "port",
-            "sample": f"{steps} backward-Euler Newton step(s) of the same workload from rest, FP64 oracle "
+            "sample": f"{steps} backward-Euler {method} step(s) of the same workload from rest, FP64 oracle "
                       f"(C++/OpenMP restatement of the reference path), {dt:.1f} s, no warm-up (CPU)"}
 
 
-def cpu_baseline(workload, max_seconds, max_steps):
+def cpu_baseline(workload, max_seconds, max_steps, stepper="newton"):
     """Runs the CPU baseline in a fresh process so its OpenMP pool does not share the process with torch."""
     cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
-           "--cpu-seconds", str(max_seconds), "--steps", str(max_steps), "--warmup", "0"]
+           "--cpu-seconds", str(max_seconds), "--steps", str(max_steps), "--warmup", "0", "--stepper", stepper]
     env = dict(os.environ)
     for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
         env.pop(k, None)
@@ -318,7 +342,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="beam1m", help="beam1m (default), beam_small, cube10, bar, batch")
+    ap.add_argument("--workload", default="beam1m",
+                    help="beam1m (default), beam_small, cube10, bar, batch, cloth512, cloth_small")
     ap.add_argument("--stepper", default="newton", choices=["newton", "lbfgs", "pd", "ncg", "ncg_ext"],
                     help="stepper of the timed GPU runs (the CPU baseline is Newton)")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
@@ -340,15 +365,18 @@ def main():
 
     scene = make_scene(args.workload)
     T, V = scene["cells"].shape[0], scene["X"].shape[0]
+    cells_key = "springs" if scene.get("springs") else "tets"
 
     if args.impl == "reference":
         if rank == 0:
-            cb = cpu_baseline_inproc(scene, args.cpu_seconds, max(1, args.steps))
+            method = args.stepper if args.stepper in ("newton", "lbfgs", "pd") else "newton"
+            cb = cpu_baseline_inproc(scene, args.cpu_seconds, max(1, args.steps), method)
             line = {
                 "metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-                "config": {"workload": scene["name"], "tets": T, "vertices": V, "solver": "Newton + block-Jacobi PCG, stop 1e-6 rel"},
+                "config": {"workload": scene["name"], cells_key: T, "vertices": V,
+                           "solver": f"{method} (Newton: block-Jacobi PCG), stop 1e-6 rel"},
                 "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             }
@@ -408,7 +436,8 @@ def main():
     if rank == 0:
         cb = None
         if not args.no_cpu_baseline:
-            cb = cpu_baseline(args.workload, args.cpu_seconds, args.steps)
+            cb = cpu_baseline(args.workload, args.cpu_seconds, args.steps,
+                              args.stepper if args.stepper in ("newton", "lbfgs", "pd") else "newton")
         line = {
             "metric": METRIC,
             "value": round(value, 4),
@@ -423,7 +452,7 @@ def main():
             "dtype": "f32+f64",
             "data": "synthetic (seeded SplitMix64 material)",
             "config": {
-                "workload": scene["name"], "tets": T, "vertices": V, "dofs": 3 * V,
+                "workload": scene["name"], cells_key: T, "vertices": V, "dofs": 3 * V,
                 "solver": ("Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(1e-2, "
                            "|g|/|g0|)); mixed: Chronopoulos-Gear PCG in one cooperative launch per solve, FP64: two "
                            "launches per PCG iteration") if args.stepper == "newton" else
@@ -438,7 +467,7 @@ def main():
             "newton_iters": [s["newton_iters"] for s in st],
             "cg_iters": [s["cg_iters_total"] for s in st],
             "rel_residual": [s["grad_norm"] / s["grad_norm0"] if s["grad_norm0"] > 0 else 0.0 for s in st],
-            "tets_per_s": round(T * value, 1),
+            f"{cells_key}_per_s": round(T * value, 1),
             "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
             "adjoint": r.get("adjoint"),
             "e2e": {"value": round(steps_total / e2e_s, 4), "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],

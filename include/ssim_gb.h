@@ -158,6 +158,14 @@ SSIM_GB_API ssim_gb_status ssim_gb_mesh_csr_pattern(const int32_t* cells, int32_
 SSIM_GB_API ssim_gb_status ssim_gb_create(const double* vertices, int32_t num_vertices, const int32_t* cells,
                               int32_t num_cells, double time_step, double youngs, double poisson,
                               double density, ssim_gb_timestep** out);
+/* A mass-spring system (cloth) stepped by the same object: springs [num_springs][2] vertex pairs with rest
+ * lengths from the vertices, stiffness k, vertex masses (vertex_mass[num_vertices], or `mass` for every
+ * vertex when NULL), energy 1/2 |x - x~|^2_M + dt^2 sum k/2 (|x_i - x_j| - L)^2 with the lumped mass.  No
+ * reference counterpart (the reference has no spring model); Newton, L-BFGS, PD (mass + dt^2 k spring
+ * Laplacian), NCG and forward Euler apply, the adjoint does not. */
+SSIM_GB_API ssim_gb_status ssim_gb_create_springs(const double* vertices, int32_t num_vertices, const int32_t* springs,
+                                                  int32_t num_springs, double stiffness, const double* vertex_mass,
+                                                  double mass, double time_step, ssim_gb_timestep** out);
 SSIM_GB_API ssim_gb_status ssim_gb_destroy(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_sizes(const ssim_gb_timestep* h, int32_t* num_vertices, int32_t* num_cells,
                              int32_t* num_dofs, int64_t* nnz);

@@ -328,6 +328,9 @@ struct orc_ts {
   std::vector<int32_t> row_ptr, col_idx;
   Vec ncg_L;                  // NCG preconditioner factor on the CSR pattern (empty: identity)
   int model = 0;              // elastic model: 0 stable Neo-Hookean, 1 linear
+  int cv = 4;                 // vertices per cell: 4 (tets) or 2 (springs)
+  bool springs = false;       // mass-spring system: cells are springs, lumped vertex masses
+  Vec sp_rest, sp_k, vmass;
   Vec mass_vals, massf_vals, sys_vals, pd_vals;
   std::vector<int32_t> hess_dst;            // [nt*144] CSR slot of each local entry
   std::vector<int32_t> hcon_ptr, hcon_src;  // per CSR slot, the local entries that add into it
@@ -355,10 +358,11 @@ namespace {
 // of (3*cell[i]+a, 3*cell[j]+b), rows ascending, columns strictly ascending, full storage.  The
 // enumeration order of the CSR is the offset map of global_composer.hpp:94-100.
 void build_pattern(orc_ts& s) {
+  const int cv = s.cv, L = 3 * cv, LL = L * L;
   std::vector<std::vector<int32_t>> nb(s.nv);
   for (int e = 0; e < s.nt; ++e)
-    for (int i = 0; i < 4; ++i)
-      for (int j = 0; j < 4; ++j) nb[s.cells[e * 4 + i]].push_back(s.cells[e * 4 + j]);
+    for (int i = 0; i < cv; ++i)
+      for (int j = 0; j < cv; ++j) nb[s.cells[e * cv + i]].push_back(s.cells[e * cv + j]);
   for (auto& v : nb) {
     std::sort(v.begin(), v.end());
     v.erase(std::unique(v.begin(), v.end()), v.end());
@@ -375,16 +379,16 @@ void build_pattern(orc_ts& s) {
         for (int b = 0; b < 3; ++b) s.col_idx[o++] = 3 * w + b;
     }
   // element-local -> CSR slot map (global_composer.hpp:103-119)
-  s.hess_dst.resize((size_t)s.nt * 144);
+  s.hess_dst.resize((size_t)s.nt * LL);
   for (int e = 0; e < s.nt; ++e)
-    for (int i = 0; i < 4; ++i) {
-      const int u = s.cells[e * 4 + i];
-      for (int j = 0; j < 4; ++j) {
-        const int w = s.cells[e * 4 + j];
+    for (int i = 0; i < cv; ++i) {
+      const int u = s.cells[e * cv + i];
+      for (int j = 0; j < cv; ++j) {
+        const int w = s.cells[e * cv + j];
         const int k = (int)(std::lower_bound(nb[u].begin(), nb[u].end(), w) - nb[u].begin());
         for (int a = 0; a < 3; ++a)
           for (int b = 0; b < 3; ++b)
-            s.hess_dst[(size_t)e * 144 + (i * 3 + a) * 12 + j * 3 + b] = s.row_ptr[3 * u + a] + 3 * k + b;
+            s.hess_dst[(size_t)e * LL + (i * 3 + a) * L + j * 3 + b] = s.row_ptr[3 * u + a] + 3 * k + b;
       }
     }
   // invert: per slot, its contributing local entries (in element order)
@@ -399,12 +403,12 @@ void build_pattern(orc_ts& s) {
   }
   // force gather (global_composer.hpp:36-66)
   s.fcon_ptr.assign(s.nv + 1, 0);
-  for (int t = 0; t < s.nt * 4; ++t) s.fcon_ptr[s.cells[t] + 1]++;
+  for (int t = 0; t < s.nt * cv; ++t) s.fcon_ptr[s.cells[t] + 1]++;
   for (int i = 0; i < s.nv; ++i) s.fcon_ptr[i + 1] += s.fcon_ptr[i];
-  s.fcon_src.resize((size_t)s.nt * 4);
+  s.fcon_src.resize((size_t)s.nt * cv);
   {
     std::vector<int32_t> fill(s.fcon_ptr.begin(), s.fcon_ptr.end() - 1);
-    for (int t = 0; t < s.nt * 4; ++t) s.fcon_src[fill[s.cells[t]]++] = t;
+    for (int t = 0; t < s.nt * cv; ++t) s.fcon_src[fill[s.cells[t]]++] = t;
   }
 }
 
@@ -429,6 +433,7 @@ void spmv(const orc_ts& s, const Vec& vals, const double* x, double* y) {
 
 // deformation_gradient::def_grad_task (def_grad.hpp:93-132): F = Ds * Dminv, x = X + u
 void update_def_grad(orc_ts& s, const Vec& u) {
+  if (s.springs) return;
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < s.nt; ++e) {
     const int32_t* c = &s.cells[e * 4];
@@ -457,6 +462,31 @@ double inertia_term(const orc_ts& s, const Vec& u, Vec* f_out) {
   return e;
 }
 
+// mass-spring elastic part: sum_s k/2 (|x_i - x_j| - L)^2 (times dt^2), edge vectors from differences
+// (X_i - X_j) + (u_i - u_j); local forces k (l - L) / l (x_i - x_j) and its negative when lf != null;
+// scale = dt^2 sum k/2 (l^2 + L^2)
+double spring_energy(const orc_ts& s, const Vec& u, Vec* lf, double* scale) {
+  double sum = 0, sc = 0;
+  for (int e = 0; e < s.nt; ++e) {
+    const int i = s.cells[2 * e], j = s.cells[2 * e + 1];
+    double d[3];
+    for (int q = 0; q < 3; ++q) d[q] = (s.X[3 * i + q] - s.X[3 * j + q]) + (u[3 * i + q] - u[3 * j + q]);
+    const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double L = s.sp_rest[e], k = s.sp_k[e], dl = l - L;
+    sum += 0.5 * k * dl * dl;
+    sc += 0.5 * k * (l * l + L * L);
+    if (lf) {
+      const double c = l > 0 ? k * dl / l : 0.0;
+      for (int q = 0; q < 3; ++q) {
+        (*lf)[6 * (size_t)e + q] = c * d[q];
+        (*lf)[6 * (size_t)e + 3 + q] = -c * d[q];
+      }
+    }
+  }
+  if (scale) *scale = sc * s.dt * s.dt;
+  return sum * s.dt * s.dt;
+}
+
 double elastic_energy(orc_ts& s, double* scale) {
   double sum = 0, sc = 0;
 #pragma omp parallel for reduction(+ : sum, sc) schedule(static)
@@ -469,6 +499,24 @@ double elastic_energy(orc_ts& s, double* scale) {
 }
 
 double energy_and_gradients(orc_ts& s, bool F_updated) {
+  if (s.springs) {
+    Vec f;
+    const double ei = inertia_term(s, s.next, &f);
+    double sc = 0;
+    const double ee = spring_energy(s, s.next, &s.local_force, &sc);
+    const double a = s.dt * s.dt;
+    for (int v = 0; v < s.nv; ++v) {
+      double acc[3] = {0, 0, 0};
+      for (int k = s.fcon_ptr[v]; k < s.fcon_ptr[v + 1]; ++k)
+        for (int d = 0; d < 3; ++d) acc[d] += s.local_force[(size_t)s.fcon_src[k] * 3 + d];
+      for (int d = 0; d < 3; ++d) f[v * 3 + d] += a * acc[d];
+    }
+    for (int i = 0; i < s.n; ++i)
+      if (s.dbc(i)) f[i] = 0;
+    s.forces = std::move(f);
+    s.energy_scale = ei + sc;
+    return ei + ee;
+  }
   if (!F_updated) update_def_grad(s, s.next);
   Vec f;
   const double inertia_energy = inertia_term(s, s.next, &f);
@@ -518,6 +566,7 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
 }
 
 double energy_only(orc_ts& s, const Vec& u) {
+  if (s.springs) return inertia_term(s, u, nullptr) + spring_energy(s, u, nullptr, nullptr);
   update_def_grad(s, u);
   const double ei = inertia_term(s, u, nullptr);
   return ei + elastic_energy(s, nullptr);
@@ -525,6 +574,38 @@ double energy_only(orc_ts& s, const Vec& u) {
 
 // update_hessian (time_step.hpp:626-658)
 void update_hessian(orc_ts& s, bool F_updated, bool make_spsd, bool filter) {
+  if (s.springs) {
+    // spring blocks [K, -K; -K, K], K = k [n n^T + c (I - n n^T)], c = 1 - L / l (>= 0 when make_spsd)
+    for (int e = 0; e < s.nt; ++e) {
+      const int i = s.cells[2 * e], j = s.cells[2 * e + 1];
+      double d[3];
+      for (int q = 0; q < 3; ++q) d[q] = (s.X[3 * i + q] - s.X[3 * j + q]) + (s.next[3 * i + q] - s.next[3 * j + q]);
+      const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      double c = l > 0 ? 1.0 - s.sp_rest[e] / l : 0.0;
+      if (make_spsd) c = std::max(c, 0.0);
+      double nn[3] = {0, 0, 0};
+      if (l > 0)
+        for (int q = 0; q < 3; ++q) nn[q] = d[q] / l;
+      double* K = &s.local_K[(size_t)e * 36];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          const double v = s.sp_k[e] * ((1.0 - c) * nn[a] * nn[b] + (a == b ? c : 0.0));
+          K[a * 6 + b] = v;
+          K[(3 + a) * 6 + 3 + b] = v;
+          K[a * 6 + 3 + b] = -v;
+          K[(3 + a) * 6 + b] = -v;
+        }
+    }
+    const double a = s.dt * s.dt;
+    const int nnz = (int)s.col_idx.size();
+    for (int k = 0; k < nnz; ++k) {
+      double acc = 0;
+      for (int q = s.hcon_ptr[k]; q < s.hcon_ptr[k + 1]; ++q) acc += s.local_K[s.hcon_src[q]];
+      s.sys_vals[k] = s.mass_vals[k] + a * acc;
+    }
+    if (filter) filter_dbc_matrix(s, s.sys_vals);
+    return;
+  }
   if (!F_updated) update_def_grad(s, s.next);
 #pragma omp parallel for schedule(dynamic, 256)
   for (int e = 0; e < s.nt; ++e)
@@ -798,6 +879,40 @@ orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double
   return s;
 }
 
+orc_ts* orc_create_springs(const double* X, int nv, const int32_t* springs, int ns, double k, const double* vmass,
+                           double m, double dt) {
+  orc_ts* s = new orc_ts;
+  s->springs = true;
+  s->cv = 2;
+  s->nv = nv;
+  s->nt = ns;
+  s->n = nv * 3;
+  s->X.assign(X, X + (size_t)nv * 3);
+  s->cells.assign(springs, springs + (size_t)ns * 2);
+  s->dt = dt;
+  s->E = 1.0;
+  s->nu = 0.25;
+  s->rho = 0.0;
+  s->sp_rest.assign(ns, 0.0);
+  for (int e = 0; e < ns; ++e) {
+    const int i = springs[2 * e], j = springs[2 * e + 1];
+    double l2 = 0;
+    for (int q = 0; q < 3; ++q) l2 += (X[3 * i + q] - X[3 * j + q]) * (X[3 * i + q] - X[3 * j + q]);
+    s->sp_rest[e] = std::sqrt(l2);
+  }
+  s->sp_k.assign(ns, k);
+  if (vmass)
+    s->vmass.assign(vmass, vmass + nv);
+  else
+    s->vmass.assign(nv, m);
+  s->dof_type.assign(s->n, 0);
+  for (Vec* v : {&s->dbc_values, &s->deformation, &s->prev_deform, &s->inertia, &s->next, &s->velocity,
+                 &s->ext_accel, &s->forces})
+    v->assign(s->n, 0.0);
+  orc_reset(s);
+  return s;
+}
+
 void orc_destroy(orc_ts* s) { delete s; }
 int orc_num_vertices(const orc_ts* s) { return s->nv; }
 int orc_num_cells(const orc_ts* s) { return s->nt; }
@@ -858,6 +973,27 @@ int orc_add_ext_force_dof(orc_ts* s, int dof, double a) {
 
 // reset (time_step.hpp:363-494)
 void orc_reset(orc_ts* s) {
+  if (s->springs) {
+    s->local_force.assign((size_t)s->nt * 6, 0);
+    s->local_K.assign((size_t)s->nt * 36, 0);
+    for (Vec* v : {&s->inertia, &s->next, &s->forces}) v->assign(s->n, 0.0);
+    build_pattern(*s);
+    const int nnz = (int)s->col_idx.size();
+    s->mass_vals.assign(nnz, 0.0);  // lumped: m_v on the dof diagonals
+    for (int r = 0; r < s->n; ++r)
+      for (int k = s->row_ptr[r]; k < s->row_ptr[r + 1]; ++k)
+        if (s->col_idx[k] == r) s->mass_vals[k] = s->vmass[r / 3];
+    s->massf_vals = s->mass_vals;
+    filter_dbc_matrix(*s, s->massf_vals);
+    s->sys_vals = s->mass_vals;
+    double asum = 0;
+    for (double v : s->mass_vals) asum += std::fabs(v);
+    s->abs_tol = asum / 3.0 * s->rtol;
+    s->mass_third = asum / 3.0;
+    s->has_reset = true;
+    s->pd_ready = false;
+    return;
+  }
   s->dminv.assign((size_t)s->nt * 9, 0);
   s->vol.assign(s->nt, 0);
   s->defgrad.assign((size_t)s->nt * 9, 0);
@@ -1245,6 +1381,22 @@ double orc_compute_step_forward_euler(orc_ts* s, const orc_params*, orc_stats* s
 // model's (lambda, mu) slots then hold (E, nu).  Mode 1 uses the Lame parameters instead, mode 2 each
 // element's own Lame parameters (an extension for per-element materials).
 void orc_pd_matrix_values(orc_ts* s, double* out) {
+  if (s->springs) {
+    // mass-spring projective dynamics (Liu et al. 2013): M + dt^2 sum_s k_s (A_s^T A_s) (x) I3
+    Vec vals = s->mass_vals;
+    for (int e = 0; e < s->nt; ++e) {
+      const double w = s->dt * s->dt * s->sp_k[e];
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+          for (int a = 0; a < 3; ++a)
+            vals[s->hess_dst[(size_t)e * 36 + (i * 3 + a) * 6 + j * 3 + a]] += (i == j ? w : -w);
+    }
+    filter_dbc_matrix(*s, vals);
+    s->pd_vals = vals;
+    s->pd_ready = true;
+    if (out) std::copy(vals.begin(), vals.end(), out);
+    return;
+  }
   double lam_slot = s->E, mu_slot = s->nu;
   if (s->pd_diff_mode == 1) orc_lame(s->E, s->nu, &lam_slot, &mu_slot);
   const double kappa_u = (lam_slot + 5.0 / 6.0 * mu_slot) + 2.0 * (4.0 / 3.0 * mu_slot);

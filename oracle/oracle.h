@@ -100,6 +100,10 @@ void orc_default_params(orc_params* p);
 
 orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double dt, double E, double nu,
                    double rho);
+/* a mass-spring system (no reference counterpart): springs [ns][2], rest lengths from X, stiffness k, vertex
+ * masses vmass[nv] (or m each), lumped mass, energy 1/2|x - x~|_M^2 + dt^2 sum k/2 (|x_i - x_j| - L)^2 */
+orc_ts* orc_create_springs(const double* X, int nv, const int32_t* springs, int ns, double k, const double* vmass,
+                           double m, double dt);
 void orc_destroy(orc_ts* ts);
 int orc_num_vertices(const orc_ts* ts);
 int orc_num_cells(const orc_ts* ts);

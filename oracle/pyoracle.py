@@ -111,6 +111,10 @@ def lib():
         "orc_element_stiffness": (None, [dp, dp, C.c_double, C.c_double, C.c_int, dp]),
         "orc_default_params": (None, [C.POINTER(OrcParams)]),
         "orc_create": (vp, [dp, C.c_int, ip, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "orc_create_springs": (
+            vp,
+            [dp, C.c_int, ip, C.c_int, C.c_double, C.c_void_p, C.c_double, C.c_double],
+        ),
         "orc_destroy": (None, [vp]),
         "orc_num_vertices": (C.c_int, [vp]),
         "orc_num_cells": (C.c_int, [vp]),
@@ -289,6 +293,29 @@ class OracleTimeStep:
         self._h = L.orc_create(X.reshape(-1), self.nv, cells.reshape(-1), self.nt, time_step, youngs, poisson, density)
         self.X, self.cells = X, cells
 
+    @classmethod
+    def springs(cls, X, springs, stiffness, vertex_mass=None, mass=None, time_step=1e-2):
+        """A mass-spring system (no reference counterpart): rest lengths from X, lumped vertex masses
+        (vertex_mass[nv], or `mass` each), energy 1/2|x - x~|_M^2 + dt^2 sum k/2 (|x_i - x_j| - L)^2."""
+        L = lib()
+        self = cls.__new__(cls)
+        self._L = L
+        X = _f64(X).reshape(-1, 3)
+        sp = np.ascontiguousarray(springs, dtype=np.int32).reshape(-1, 2)
+        self.nv, self.nt = X.shape[0], sp.shape[0]
+        self.n = 3 * self.nv
+        vm = None if vertex_mass is None else _f64(vertex_mass).reshape(-1)
+        if vm is not None and vm.size != self.nv:
+            raise ValueError("vertex_mass must have one entry per vertex")
+        m = float(mass) if mass is not None else 0.0
+        self._vm = vm
+        self._h = L.orc_create_springs(
+            X.reshape(-1), self.nv, sp.reshape(-1), self.nt, float(stiffness),
+            None if vm is None else vm.ctypes.data, m, float(time_step),
+        )
+        self.X, self.cells = X, sp
+        return self
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -439,9 +466,10 @@ class OracleTimeStep:
         return out.reshape(-1, 3, 3)
 
     def local_stiffness(self):
-        out = np.zeros(self.nt * 144)
+        L = 3 * self.cells.shape[1]
+        out = np.zeros(self.nt * L * L)
         self._L.orc_get_local_stiffness(self._h, out)
-        return out.reshape(-1, 12, 12)
+        return out.reshape(-1, L, L)
 
     def csr_pattern(self):
         rp = np.zeros(self.n + 1, dtype=np.int32)

@@ -118,6 +118,10 @@ _SIGS = {
         C.c_int,
         [_D, C.c_int32, _I, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.POINTER(_H)],
     ),
+    "ssim_gb_create_springs": (
+        C.c_int,
+        [_D, C.c_int32, _I, C.c_int32, C.c_double, _D, C.c_double, C.c_double, C.POINTER(_H)],
+    ),
     "ssim_gb_destroy": (C.c_int, [_H]),
     "ssim_gb_sizes": (C.c_int, [_H, _I, _I, _I, C.POINTER(C.c_int64)]),
     "ssim_gb_set_stream": (C.c_int, [_H, C.c_void_p]),

@@ -45,6 +45,15 @@ struct ElemFP32 {
   const float* mu;
 };
 
+// springs (2-vertex cells) of a mass-spring system
+struct SpringData {
+  int ns;
+  const int2* ends;     // [ns] (i, j)
+  const double* X;      // [V][3] rest positions
+  const double* rest;   // [ns] rest lengths
+  const double* k;      // [ns] stiffness
+};
+
 struct Reduce {
   double* partials;       // [grid * 4] scratch
   unsigned int* counter;  // zero-initialised, restored by the last block
@@ -78,6 +87,18 @@ template <typename SD>
 void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const double* u, const double* xt,
                                const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
                                bool trial, const Reduce& red, cudaStream_t st);
+// mass-spring energy (+ spring forces into lf[s][2][3]) at u (+ alpha d), plus the lumped inertia energy
+template <typename SD>
+void launch_spring_energy_grad(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
+                               const V4<SD>* d, double alpha, double dt2, double* lf, bool with_forces, bool trial,
+                               const Reduce& red, cudaStream_t st);
+// g = spring forces gathered per vertex + m (u - x~), Dirichlet dofs zeroed; |g|^2 into the scalars
+void launch_spring_gather(int nv, const int* vptr, const int* vinc, const double* lf, const double* m,
+                          const double* u, const double* xt, const uint8_t* mask, double* g, const Reduce& red,
+                          cudaStream_t st);
+// spring Hessian blocks Kbuf[s][3][9] (scaled by dt^2), the compressed transverse part dropped when spsd
+template <typename S>
+void launch_spring_hessian(const SpringData& sp, const double* u, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
 void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
                           double* g, const Reduce& red, cudaStream_t st);
 

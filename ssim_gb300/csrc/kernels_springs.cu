@@ -1,0 +1,230 @@
+// kernels_springs.cu -- mass-spring systems (cloth) through the same time-step machinery as the tets:
+// energy 1/2 |x - x~|^2_M + dt^2 sum_s k_s / 2 (|x_i - x_j| - L_s)^2 with a lumped (diagonal) mass.  There
+// is no spring model in the reference; this is the classic mass-spring energy the projective-dynamics
+// literature uses (Liu et al., "Fast Simulation of Mass-Spring Systems", SIGGRAPH Asia 2013).
+//
+// Springs are 2-vertex cells: the vertex gather, the block pattern, the atomic-free assembly and the
+// PCG are the tet ones; the spring forces go to lf[s][2][3], the Hessian blocks to Kbuf[s][3][9] (upper
+// vertex blocks (0,0), (0,1), (1,1)).
+#include "kernels.cuh"
+
+namespace ssim_gb {
+namespace {
+
+constexpr int PB = 256;
+
+template <typename S>
+__device__ __forceinline__ S comp4(const V4<S>& v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : v.z);
+}
+
+// edge vector x_i - x_j = (X_i - X_j) + (u_i - u_j) (+ alpha (d_i - d_j)), from differences so a short
+// spring keeps its digits
+template <typename SD, bool TRIAL>
+__device__ __forceinline__ void edge_vec(const SpringData& sp, const double* __restrict__ u, const V4<SD>* d,
+                                         double alpha, int s, int& i, int& j, double (&e)[3]) {
+  const int2 c = sp.ends[s];
+  i = c.x;
+  j = c.y;
+  V4<SD> di, dj;
+  if (TRIAL) {
+    di = d[i];
+    dj = d[j];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double v = (sp.X[3 * i + k] - sp.X[3 * j + k]) + (u[3 * i + k] - u[3 * j + k]);
+    if (TRIAL) v += alpha * ((double)comp4<SD>(di, k) - (double)comp4<SD>(dj, k));
+    e[k] = v;
+  }
+}
+
+template <typename SD, bool FORCES, bool TRIAL>
+__global__ void __launch_bounds__(PB)
+    spring_energy_grad_kernel(SpringData sp, const double* __restrict__ u, const V4<SD>* __restrict__ d,
+                              double alpha, double dt2, double* __restrict__ lf, Reduce red) {
+  __shared__ double shred[PB / 32][2];
+  const int s = blockIdx.x * PB + threadIdx.x;
+  double energy = 0, escale = 0;
+  if (s < sp.ns) {
+    int i, j;
+    double e[3];
+    edge_vec<SD, TRIAL>(sp, u, d, alpha, s, i, j, e);
+    const double l = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    const double L = sp.rest[s], k = sp.k[s];
+    const double dl = l - L;
+    energy = 0.5 * dt2 * k * dl * dl;
+    escale = 0.5 * dt2 * k * (l * l + L * L);  // magnitude of the terms whose difference dl is
+    if (FORCES) {
+      const double c = l > 0 ? dt2 * k * dl / l : 0.0;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        lf[(size_t)s * 6 + q] = c * e[q];
+        lf[(size_t)s * 6 + 3 + q] = -c * e[q];
+      }
+    }
+  }
+  double v2[2] = {energy, escale};
+  block_sum<2, PB>(v2, shred);
+  double tot[2];
+  if (grid_sum_last<2, PB>(v2, red.partials, red.counter, tot)) {
+    if (TRIAL) {
+      red.sc->trial_energy = tot[0];
+      red.sc->trial_energy_scale = tot[1];
+    } else {
+      red.sc->energy = tot[0];
+      red.sc->energy_scale = tot[1];
+    }
+  }
+}
+
+// lumped inertia 1/2 sum_v m_v |u_v (+ alpha d_v) - x~_v|^2, added to the (trial) energy and its scale
+template <typename SD, bool TRIAL>
+__global__ void __launch_bounds__(PB)
+    lumped_inertia_energy_kernel(int nv, const double* __restrict__ m, const double* __restrict__ u,
+                                 const double* __restrict__ xt, const V4<SD>* __restrict__ d, double alpha,
+                                 Reduce red) {
+  __shared__ double shred[PB / 32][1];
+  const int v = blockIdx.x * PB + threadIdx.x;
+  double part = 0;
+  if (v < nv) {
+    V4<SD> dv;
+    if (TRIAL) dv = d[v];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double w = u[3 * v + k] - xt[3 * v + k];
+      if (TRIAL) w += alpha * (double)comp4<SD>(dv, k);
+      part += w * w;
+    }
+    part *= 0.5 * m[v];
+  }
+  double v1[1] = {part};
+  block_sum<1, PB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1, PB>(v1, red.partials, red.counter, tot)) {
+    if (TRIAL) {
+      red.sc->trial_energy += tot[0];
+      red.sc->trial_energy_scale += tot[0];
+    } else {
+      red.sc->energy += tot[0];
+      red.sc->energy_scale += tot[0];
+    }
+  }
+}
+
+// g_v = sum of the incident spring forces + m_v (u_v - x~_v), Dirichlet dofs zeroed; |g|^2
+__global__ void __launch_bounds__(PB)
+    spring_gather_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
+                         const double* __restrict__ lf, const double* __restrict__ m, const double* __restrict__ u,
+                         const double* __restrict__ xt, const uint8_t* __restrict__ mask, double* __restrict__ g,
+                         Reduce red) {
+  __shared__ double shred[PB / 32][1];
+  const int v = blockIdx.x * PB + threadIdx.x;
+  double part = 0;
+  if (v < nv) {
+    double a[3] = {0, 0, 0};
+    const int k1 = vptr[v + 1];
+    for (int k = vptr[v]; k < k1; ++k) {
+      const double* s = lf + (size_t)vinc[k] * 3;
+      a[0] += s[0];
+      a[1] += s[1];
+      a[2] += s[2];
+    }
+    const uint8_t mk = mask[v];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      a[q] += m[v] * (u[3 * v + q] - xt[3 * v + q]);
+      if ((mk >> q) & 1) a[q] = 0;
+      g[3 * v + q] = a[q];
+      part += a[q] * a[q];
+    }
+  }
+  double v1[1] = {part};
+  block_sum<1, PB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1, PB>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+}
+
+// Hessian blocks of a spring: K = dt^2 k [n n^T + c (I - n n^T)], c = 1 - L / l, with c clamped to >= 0
+// when make_spsd (the compressed spring's negative transverse stiffness removed, the standard projection of
+// a spring Hessian); upper vertex blocks (0,0) = K, (0,1) = -K, (1,1) = K.
+template <typename S>
+__global__ void __launch_bounds__(PB)
+    spring_hessian_kernel(SpringData sp, const double* __restrict__ u, double dt2, int spsd, S* __restrict__ Kbuf) {
+  const int s = blockIdx.x * PB + threadIdx.x;
+  if (s >= sp.ns) return;
+  int i, j;
+  double e[3];
+  edge_vec<S, false>(sp, u, nullptr, 0.0, s, i, j, e);
+  const double l = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+  const double L = sp.rest[s], k = sp.k[s];
+  double c = l > 0 ? 1.0 - L / l : 0.0;
+  if (spsd) c = fmax(c, 0.0);
+  double n[3] = {0, 0, 0};
+  if (l > 0)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) n[q] = e[q] / l;
+  S K[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      K[a * 3 + b] = (S)(dt2 * k * ((1.0 - c) * n[a] * n[b] + (a == b ? c : 0.0)));
+  S* o = Kbuf + (size_t)s * 27;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    o[q] = K[q];
+    o[9 + q] = -K[q];
+    o[18 + q] = K[q];
+  }
+}
+
+}  // namespace
+
+template <typename SD>
+void launch_spring_energy_grad(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
+                               const V4<SD>* d, double alpha, double dt2, double* lf, bool with_forces, bool trial,
+                               const Reduce& red, cudaStream_t st) {
+  if (sp.ns > 0) {
+    const int grid = div_up(sp.ns, PB);
+    if (trial && with_forces)
+      spring_energy_grad_kernel<SD, true, true><<<grid, PB, 0, st>>>(sp, u, d, alpha, dt2, lf, red);
+    else if (trial)
+      spring_energy_grad_kernel<SD, false, true><<<grid, PB, 0, st>>>(sp, u, d, alpha, dt2, lf, red);
+    else if (with_forces)
+      spring_energy_grad_kernel<SD, true, false><<<grid, PB, 0, st>>>(sp, u, d, alpha, dt2, lf, red);
+    else
+      spring_energy_grad_kernel<SD, false, false><<<grid, PB, 0, st>>>(sp, u, d, alpha, dt2, lf, red);
+    after_launch("spring_energy_grad");
+  }
+  if (trial)
+    lumped_inertia_energy_kernel<SD, true><<<div_up(nv, PB), PB, 0, st>>>(nv, m, u, xt, d, alpha, red);
+  else
+    lumped_inertia_energy_kernel<SD, false><<<div_up(nv, PB), PB, 0, st>>>(nv, m, u, xt, d, alpha, red);
+  after_launch("lumped_inertia_energy");
+}
+
+void launch_spring_gather(int nv, const int* vptr, const int* vinc, const double* lf, const double* m,
+                          const double* u, const double* xt, const uint8_t* mask, double* g, const Reduce& red,
+                          cudaStream_t st) {
+  spring_gather_kernel<<<div_up(nv, PB), PB, 0, st>>>(nv, vptr, vinc, lf, m, u, xt, mask, g, red);
+  after_launch("spring_gather");
+}
+
+template <typename S>
+void launch_spring_hessian(const SpringData& sp, const double* u, double dt2, bool spsd, S* Kbuf, cudaStream_t st) {
+  if (sp.ns <= 0) return;
+  spring_hessian_kernel<S><<<div_up(sp.ns, PB), PB, 0, st>>>(sp, u, dt2, spsd ? 1 : 0, Kbuf);
+  after_launch("spring_hessian");
+}
+
+template void launch_spring_energy_grad<float>(const SpringData&, const double*, const double*, const double*, int,
+                                               const float4*, double, double, double*, bool, bool, const Reduce&,
+                                               cudaStream_t);
+template void launch_spring_energy_grad<double>(const SpringData&, const double*, const double*, const double*, int,
+                                                const double4_32a*, double, double, double*, bool, bool,
+                                                const Reduce&, cudaStream_t);
+template void launch_spring_hessian<float>(const SpringData&, const double*, double, bool, float*, cudaStream_t);
+template void launch_spring_hessian<double>(const SpringData&, const double*, double, bool, double*, cudaStream_t);
+
+}  // namespace ssim_gb

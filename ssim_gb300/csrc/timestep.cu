@@ -131,7 +131,7 @@ struct TimeStep {
     inst_mass_third.assign(std::max(1, ninst), 0.0);
     if (ninst <= 1) return;
     std::vector<double> smass;
-    slot_masses(topo, detJ, rho, smass);
+    slot_mass_values(smass);
     for (int q = 0; q < topo.nslots; ++q) {
       const int u = topo.slot_row[q];
       if (u < 0) continue;
@@ -144,6 +144,40 @@ struct TimeStep {
   bool profiling = false;
   std::vector<cudaEvent_t> ev;
   int elastic_model = SSIM_GB_MODEL_STABLE_NEOHOOKEAN;  // ElastModel of basic_time_step
+  // mass-spring system instead of tets (cells are the springs' vertex pairs)
+  bool springs = false;
+  DBuf<int2> sp_ends;
+  DBuf<double> sp_rest, sp_k, vmass;
+  std::vector<double> vmass_h, sp_k_h;
+  SpringData spd() const { return SpringData{nt, sp_ends.p, dX.p, sp_rest.p, sp_k.p}; }
+
+  // element / spring pass at u = next (+ alpha d): energy (+ local forces into lf) into the trial scalars
+  template <typename S>
+  void launch_trial(const V4<S>* d, double alpha, bool forces) {
+    if (springs)
+      launch_spring_energy_grad<S>(spd(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt, forces ? lf.p : nullptr,
+                                   forces, true, red(), stream);
+    else
+      launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr,
+                                 forces, true, red(), stream);
+  }
+  // forces at next from lf (gathered), Dirichlet dofs zeroed, |g|^2
+  void gather_forces() {
+    if (springs)
+      launch_spring_gather(nv, vptr.p, vinc.p, lf.p, vmass.p, next.p, inertia.p, mask.p, forces.p, red(), stream);
+    else
+      launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+  }
+  // mass per upper slot: consistent (tets) or lumped on the diagonal (springs)
+  void slot_mass_values(std::vector<double>& smass) {
+    if (!springs) {
+      slot_masses(topo, detJ, rho, smass);
+      return;
+    }
+    smass.assign(topo.nslots, 0.0);
+    for (int q = 0; q < topo.nslots; ++q)
+      if (topo.slot_row[q] >= 0 && topo.slot_row[q] == topo.sl_col[q]) smass[q] = vmass_h[topo.slot_row[q]];
+  }
   std::vector<int32_t> solve_log;  // PCG iterations of every solve since the last reset
   // NCG preconditioner factor L (host copy; empty = identity), its CSR pattern on the device and the
   // position of each entry's transpose
@@ -181,67 +215,13 @@ struct TimeStep {
   // ------------------------------------------------------------------ construction
   void create(const double* Xh, int nv_, const int32_t* cells_h, int nt_, double dt_, double E_, double nu_,
               double rho_) {
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-      cudaGetLastError();
-      throw cuda_error("no CUDA device available (this library has no CPU path)");
-    }
-    if (!Xh || !cells_h) throw invalid_argument("null mesh pointer");
-    nv = nv_;
-    nt = nt_;
-    n = 3 * nv;
-    dt = dt_;
     E = E_;
     nu = nu_;
     rho = rho_;
-    X.assign(Xh, Xh + (size_t)n);
-    cells.assign(cells_h, cells_h + 4 * (size_t)nt);
-    build_topology(nv, nt, cells.data(), topo);  // validates indices
-    topo_ready = true;
-    ssim_gb_default_params(&params);
-    SSIM_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
-    stream = own_stream;
-    SSIM_CUDA(cudaMallocHost((void**)&hsc, sizeof(DevScalars)));
-    SSIM_CUDA(cudaMallocHost((void**)&hscal, 8 * sizeof(double)));
-    dscal.alloc(8);
-    gprev.alloc(n);
-    // state buffers (zero_if_not_valid, time_step.hpp:396-413)
-    for (DBuf<double>* b : {&deformation, &prev_deform, &inertia, &next, &velocity, &ext_accel, &forces,
-                            &dbc_values, &work}) {
-      b->alloc(n);
-      b->zero(stream);
-    }
-    dof_type.alloc(n);
-    dof_type.zero(stream);
-    mask.alloc(nv);
-    mask.zero(stream);
-    xf.alloc(nv);
-    sc.alloc(1);
-    sc.zero(stream);
-    counter.alloc(1);
-    counter.zero(stream);
-    gsync.alloc(3 + (size_t)(div_up(nv, 256) + 31) / 32);
-    gsync.zero(stream);
-    const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(3 * nv, topo.nslots), 256)) + 1;
-    partials.alloc(maxgrid * 4);
-    dX.upload(X, stream);
+    init_common(Xh, nv_, cells_h, nt_, 4, dt_);
     std::vector<int4> c4(nt);
     std::memcpy(c4.data(), cells.data(), sizeof(int4) * nt);
     dcells.upload(c4, stream);
-    vptr.upload(topo.vptr, stream);
-    vinc.upload(topo.vinc, stream);
-    sl_off.upload(topo.sl_off, stream);
-    sl_col.upload(topo.sl_col, stream);
-    slot_row.upload(topo.slot_row, stream);
-    cptr.upload(topo.cptr, stream);
-    csrc.upload(topo.csrc, stream);
-    bptr.upload(topo.bptr, stream);
-    slot_k.upload(topo.slot_k, stream);
-    slot_kt.upload(topo.slot_kt, stream);
-    lo_off.upload(topo.lo_off, stream);
-    lo_src.upload(topo.lo_src, stream);
-    lo_col.upload(topo.lo_col, stream);
-    lf.alloc(12 * (size_t)nt);
     // rest shape (dminv_task def_grad.hpp:56-91, rest_vol_task rest_vol.hpp:34-54)
     std::vector<double> dm(9 * (size_t)nt);
     detJ.assign(nt, 0);
@@ -274,15 +254,104 @@ struct TimeStep {
     reset(SSIM_GB_STEPPER_NONE);  // the constructor calls reset() (time_step.hpp:260-265)
   }
 
-  // ------------------------------------------------------------------ reset (time_step.hpp:363-494)
-  void reset(int stepper_kind) {
-    if (!(E >= 0)) throw invalid_argument("Young's modulus must be positive, got " + std::to_string(E));
-    if (!(nu > 0 && nu < 0.5)) throw invalid_argument("Poisson's ratio must be in (0, 0.5), got " + std::to_string(nu));
-    if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
-    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NCG_EXT) throw invalid_argument("unknown stepper");
-    stepper = stepper_kind;
-    for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
-    // material: per element Lame parameters (basic_elast.hpp:10-20)
+  // a mass-spring system: springs [ns][2] vertex pairs with rest lengths from X, stiffness k, vertex masses
+  // (mass_h[nv], or m for every vertex); gravity and Dirichlet vertices as for tets
+  void create_springs(const double* Xh, int nv_, const int32_t* ends_h, int ns_, double k, const double* mass_h,
+                      double m, double dt_) {
+    if (ns_ <= 0) throw invalid_argument("a spring system needs at least one spring");
+    if (!(k > 0)) throw invalid_argument("spring stiffness must be positive");
+    if (!mass_h && !(m > 0)) throw invalid_argument("vertex mass must be positive");
+    springs = true;
+    E = 1.0;  // unused by springs; keeps reset's material checks satisfied
+    nu = 0.25;
+    rho = 0.0;
+    init_common(Xh, nv_, ends_h, ns_, 2, dt_);
+    std::vector<double> rest(nt);
+    std::vector<int2> e2(nt);
+    for (int e = 0; e < nt; ++e) {
+      const int i = cells[2 * e], j = cells[2 * e + 1];
+      if (i == j) throw invalid_argument("a spring joins a vertex to itself");
+      double l2 = 0;
+      for (int q = 0; q < 3; ++q) l2 += (X[3 * i + q] - X[3 * j + q]) * (X[3 * i + q] - X[3 * j + q]);
+      if (!(l2 > 0)) throw invalid_argument("a spring has zero rest length");
+      rest[e] = std::sqrt(l2);
+      e2[e] = make_int2(i, j);
+    }
+    sp_k_h.assign(nt, k);
+    if (mass_h) {
+      vmass_h.assign(mass_h, mass_h + nv);
+      for (double mv : vmass_h)
+        if (!(mv > 0)) throw invalid_argument("vertex masses must be positive");
+    } else {
+      vmass_h.assign(nv, m);
+    }
+    sp_ends.upload(e2, stream);
+    sp_rest.upload(rest, stream);
+    sp_k.upload(sp_k_h, stream);
+    vmass.upload(vmass_h, stream);
+    reset(SSIM_GB_STEPPER_NONE);
+  }
+
+  void init_common(const double* Xh, int nv_, const int32_t* cells_h, int nt_, int cv, double dt_) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      throw cuda_error("no CUDA device available (this library has no CPU path)");
+    }
+    if (!Xh || !cells_h) throw invalid_argument("null mesh pointer");
+    nv = nv_;
+    nt = nt_;
+    n = 3 * nv;
+    dt = dt_;
+    X.assign(Xh, Xh + (size_t)n);
+    cells.assign(cells_h, cells_h + (size_t)cv * nt);
+    build_topology(nv, nt, cells.data(), topo, cv);  // validates indices
+    topo_ready = true;
+    ssim_gb_default_params(&params);
+    SSIM_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+    stream = own_stream;
+    SSIM_CUDA(cudaMallocHost((void**)&hsc, sizeof(DevScalars)));
+    SSIM_CUDA(cudaMallocHost((void**)&hscal, 8 * sizeof(double)));
+    dscal.alloc(8);
+    gprev.alloc(n);
+    // state buffers (zero_if_not_valid, time_step.hpp:396-413)
+    for (DBuf<double>* b : {&deformation, &prev_deform, &inertia, &next, &velocity, &ext_accel, &forces,
+                            &dbc_values, &work}) {
+      b->alloc(n);
+      b->zero(stream);
+    }
+    dof_type.alloc(n);
+    dof_type.zero(stream);
+    mask.alloc(nv);
+    mask.zero(stream);
+    xf.alloc(nv);
+    sc.alloc(1);
+    sc.zero(stream);
+    counter.alloc(1);
+    counter.zero(stream);
+    gsync.alloc(3 + (size_t)(div_up(nv, 256) + 31) / 32);
+    gsync.zero(stream);
+    const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(3 * nv, topo.nslots), 256)) + 1;
+    partials.alloc(maxgrid * 4);
+    dX.upload(X, stream);
+    vptr.upload(topo.vptr, stream);
+    vinc.upload(topo.vinc, stream);
+    sl_off.upload(topo.sl_off, stream);
+    sl_col.upload(topo.sl_col, stream);
+    slot_row.upload(topo.slot_row, stream);
+    cptr.upload(topo.cptr, stream);
+    csrc.upload(topo.csrc, stream);
+    bptr.upload(topo.bptr, stream);
+    slot_k.upload(topo.slot_k, stream);
+    slot_kt.upload(topo.slot_kt, stream);
+    lo_off.upload(topo.lo_off, stream);
+    lo_src.upload(topo.lo_src, stream);
+    lo_col.upload(topo.lo_col, stream);
+    lf.alloc((size_t)3 * cv * nt);
+  }
+
+  // material: per element Lame parameters (basic_elast.hpp:10-20) and the stable Neo-Hookean constants
+  void upload_material() {
     std::vector<double> l(nt), m(nt);
     for (int e = 0; e < nt; ++e) {
       const double Ee = E_elem.empty() ? E : E_elem[e];
@@ -299,10 +368,21 @@ struct TimeStep {
     std::vector<float> lf32(l.begin(), l.end()), mf32(m.begin(), m.end());
     flam.upload(lf32, stream);
     fmu.upload(mf32, stream);
+  }
+
+  // ------------------------------------------------------------------ reset (time_step.hpp:363-494)
+  void reset(int stepper_kind) {
+    if (!(E >= 0)) throw invalid_argument("Young's modulus must be positive, got " + std::to_string(E));
+    if (!(nu > 0 && nu < 0.5)) throw invalid_argument("Poisson's ratio must be in (0, 0.5), got " + std::to_string(nu));
+    if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
+    if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NCG_EXT) throw invalid_argument("unknown stepper");
+    stepper = stepper_kind;
+    for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
+    if (!springs) upload_material();
     // consistent mass per slot (time_step.hpp:437-461) and the threshold (time_step.hpp:490-491):
     // rtol * asum(mass CSR values) / 3; each slot's scalar appears on the 3 diagonal dofs of its block
     std::vector<double> smass;
-    slot_masses(topo, detJ, rho, smass);
+    slot_mass_values(smass);
     double asum = 0;  // the full CSR holds every off-diagonal block twice (the store keeps the upper one)
     for (int q = 0; q < topo.nslots; ++q)
       if (topo.slot_row[q] >= 0) asum += (topo.sl_col[q] == topo.slot_row[q] ? 3.0 : 6.0) * std::fabs(smass[q]);
@@ -340,6 +420,25 @@ struct TimeStep {
   // Lame parameters instead, mode 2 each element's own Lame parameters (per-element materials).
   template <typename S>
   void pd_setup(Solver<S>& s) {
+    if (springs) {
+      // mass-spring projective dynamics (Liu et al. 2013): (M + dt^2 sum_s k_s A_s^T A_s) (x) I3, A_s the
+      // edge difference, with the Dirichlet identity filter
+      std::vector<double> pd;
+      slot_mass_values(pd);
+      for (int e = 0; e < nt; ++e) {
+        const int i = cells[2 * e], j = cells[2 * e + 1];
+        const double w = dt * dt * sp_k_h[e];
+        pd[upper_slot(topo, i, i)] += w;
+        pd[upper_slot(topo, j, j)] += w;
+        if (i != j) pd[upper_slot(topo, std::min(i, j), std::max(i, j))] -= w;
+      }
+      std::vector<S> pds(pd.begin(), pd.end());
+      s.slot_pd.upload(pds, stream);
+      s.pd_vals.alloc(9 * (size_t)topo.nslots);
+      s.pd_dinv.alloc(3 * (size_t)nv);
+      launch_assemble<S>(A(), cptr.p, csrc.p, nullptr, s.slot_pd.p, mask.p, true, s.pd_vals.p, s.pd_dinv.p, 2, stream);
+      return;
+    }
     double lam_slot = E, mu_slot = nu;
     if (params.pd_kappa_mode == 1) {
       mu_slot = E / (2 * (1 + nu));
@@ -366,7 +465,7 @@ struct TimeStep {
 
   template <typename S>
   void alloc_solver(Solver<S>& s) {
-    s.K.alloc(90 * (size_t)nt);
+    s.K.alloc((size_t)9 * (topo.cv * (topo.cv + 1) / 2) * nt);
     s.vals.alloc(9 * (size_t)topo.nslots);
     s.vals.zero(stream);
     s.mvals.release();
@@ -403,14 +502,17 @@ struct TimeStep {
   double energy_grad() {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
-    if (mixed())
+    if (springs)
+      launch_spring_energy_grad<double>(spd(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt, lf.p, true,
+                                        false, red(), stream);
+    else if (mixed())
       launch_elem_energy_grad<float>(e64(), dX.p, next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
                                      red(), stream);
     else
       launch_elem_energy_grad<double>(e64(), dX.p, next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
                                       red(), stream);
     if (profiling) prof_end(e0, e1, PK_GRAD, 0);
-    launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+    gather_forces();
     sync_scalars();
     if (!std::isfinite(hsc->energy) || !std::isfinite(hsc->gnorm2))
       throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
@@ -434,7 +536,13 @@ struct TimeStep {
   double energy_at(const double* u_dev) {
     // value only: trial kernel with alpha = 0 against an arbitrary displacement
     if (mixed()) sf.tmp.zero(stream); else sd.tmp.zero(stream);
-    if (mixed())
+    if (springs && mixed())
+      launch_spring_energy_grad<float>(spd(), u_dev, inertia.p, vmass.p, nv, sf.tmp.p, 0.0, dt * dt, nullptr, false,
+                                       true, red(), stream);
+    else if (springs)
+      launch_spring_energy_grad<double>(spd(), u_dev, inertia.p, vmass.p, nv, sd.tmp.p, 0.0, dt * dt, nullptr, false,
+                                        true, red(), stream);
+    else if (mixed())
       launch_elem_energy_grad<float>(e64(), dX.p, u_dev, inertia.p, sf.tmp.p, 0.0, dt * dt, rho, nullptr, false,
                                      true, red(), stream);
     else
@@ -453,7 +561,10 @@ struct TimeStep {
     Solver<S>& s = solver<S>();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
-    launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream);
+    if (springs)
+      launch_spring_hessian<S>(spd(), next.p, dt * dt, spsd, s.K.p, stream);
+    else
+      launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream);
     if (profiling) prof_end(e0, e1, PK_HESS, 0);
     if (profiling) prof_begin(e0, e1);
     launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
@@ -676,8 +787,7 @@ struct TimeStep {
       const double Escale = E0_scale;
       double alpha = 1.0;
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
-        launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.ld.p, alpha, dt * dt, rho, nullptr, false, true,
-                                   red(), stream);
+        launch_trial<S>(s.ld.p, alpha, false);
         sync_scalars();
         st.ls_steps_total++;
         if (hsc->trial_energy <= E0 + params.lbfgs_armijo * alpha * gd + params.ls_energy_slack * Escale) break;
@@ -756,7 +866,7 @@ struct TimeStep {
     // mixed precision: the inner iterations evaluate energy and forces with FP32 element arithmetic (the
     // small-strain forms); the stopping test is then confirmed with an FP64 evaluation, and if the FP64
     // residual is above the target (or the FP32 residual stalls) the remaining iterations run in FP64
-    bool e32 = mixed() && params.mixed_elem32 != 0;
+    bool e32 = mixed() && params.mixed_elem32 != 0 && !springs;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);
@@ -812,8 +922,7 @@ struct TimeStep {
           launch_elem_energy_grad32<S>(e64(), e32s(), next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
                                        red(), stream);
         else
-          launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
-                                     red(), stream);
+          launch_trial<S>(s.x.p, alpha, true);
         sync_scalars();
         st.ls_steps_total++;
         Et = hsc->trial_energy;
@@ -822,7 +931,7 @@ struct TimeStep {
         if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
       launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
-      launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+      gather_forces();
       sync_scalars();
       if (!std::isfinite(Et) || !std::isfinite(hsc->gnorm2))
         throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
@@ -913,7 +1022,7 @@ struct TimeStep {
     double gd = hsc->gd, dn2 = hsc->dnorm2;
     double alpha_init = params.ncg_step0;
     auto trial = [&](double a) {
-      launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, d, a, dt * dt, rho, nullptr, false, true, red(), stream);
+      launch_trial<S>(d, a, false);
       sync_scalars();
       st.ls_steps_total++;
       return hsc->trial_energy;
@@ -1270,6 +1379,27 @@ ssim_gb_status ssim_gb_create(const double* vertices, int32_t num_vertices, cons
   return SSIM_GB_OK;
 }
 
+ssim_gb_status ssim_gb_create_springs(const double* vertices, int32_t num_vertices, const int32_t* springs,
+                                      int32_t num_springs, double stiffness, const double* vertex_mass,
+                                      double mass, double time_step, ssim_gb_timestep** out) {
+  if (!out) return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  std::unique_ptr<ssim_gb_timestep> h(new ssim_gb_timestep());
+  try {
+    h->ts.create_springs(vertices, num_vertices, springs, num_springs, stiffness, vertex_mass, mass, time_step);
+  } catch (const std::invalid_argument& e) {
+    return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, e.what());
+  } catch (const ssim_gb::cuda_error& e) {
+    return fail(nullptr, SSIM_GB_ERR_CUDA, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(nullptr, SSIM_GB_ERR_OUT_OF_MEMORY, "out of memory");
+  } catch (const std::exception& e) {
+    return fail(nullptr, SSIM_GB_ERR_CUDA, e.what());
+  }
+  *out = h.release();
+  return SSIM_GB_OK;
+}
+
 ssim_gb_status ssim_gb_destroy(ssim_gb_timestep* h) {
   if (!h) return SSIM_GB_OK;
   if (h->ts.stream) cudaStreamSynchronize(h->ts.stream);
@@ -1344,6 +1474,7 @@ ssim_gb_status ssim_gb_get_params(const ssim_gb_timestep* h, ssim_gb_params* p) 
 ssim_gb_status ssim_gb_set_material(ssim_gb_timestep* h, const double* Ee, const double* ne) {
   CHECK_H(h);
   TimeStep& t = h->ts;
+  if (t.springs) return fail(h, SSIM_GB_ERR_STATE, "a spring system has no elastic material");
   if (Ee) {
     for (int e = 0; e < t.nt; ++e)
       if (!(Ee[e] > 0)) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "Young's modulus must be positive.");
@@ -1630,6 +1761,7 @@ ssim_gb_status ssim_gb_get_matrix_values(ssim_gb_timestep* h, int32_t which, dou
 ssim_gb_status ssim_gb_get_rest_volume(const ssim_gb_timestep* h, double* out) {
   CHECK_H(h);
   if (!out) return fail(const_cast<ssim_gb_timestep*>(h), SSIM_GB_ERR_INVALID_ARGUMENT, "null output");
+  if (h->ts.springs) return fail(const_cast<ssim_gb_timestep*>(h), SSIM_GB_ERR_STATE, "a spring system has no cells");
   std::copy(h->ts.vol_h.begin(), h->ts.vol_h.end(), out);
   return SSIM_GB_OK;
 }
@@ -1640,6 +1772,7 @@ ssim_gb_status ssim_gb_get_dminv(const ssim_gb_timestep* hc, double* out) {
   API_TRY
   TimeStep& t = h->ts;
   if (!out) throw ssim_gb::invalid_argument("null output");
+  if (t.springs) throw ssim_gb::state_error("a spring system has no cells");
   std::vector<double> soa(9 * (size_t)t.nt);
   SSIM_CUDA(cudaMemcpyAsync(soa.data(), t.dminv.p, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost, t.stream));
   SSIM_CUDA(cudaStreamSynchronize(t.stream));
@@ -1720,6 +1853,7 @@ ssim_gb_status ssim_gb_adjoint_step(ssim_gb_timestep* h, double* ubar, double* v
   if (!ubar || !vbar || !ebar) throw ssim_gb::invalid_argument("null adjoint buffer");
   if (!(rtol > 0) || max_iters <= 0) throw ssim_gb::invalid_argument("invalid adjoint solve tolerance");
   if (!t.has_reset) throw ssim_gb::state_error("adjoint_step() before reset()");
+  if (t.springs) throw ssim_gb::state_error("the adjoint is built for the tet models");
   int proj = 0;
   const int it = t.mixed() ? t.adjoint_step<float>(ubar, vbar, ebar, rtol, max_iters, &proj)
                            : t.adjoint_step<double>(ubar, vbar, ebar, rtol, max_iters, &proj);

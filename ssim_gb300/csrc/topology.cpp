@@ -22,26 +22,29 @@ int find_pos(const Topology& t, int u, int w) {
 }
 }  // namespace
 
-void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
+void build_topology(int nv, int nt, const int32_t* cells, Topology& t, int cv) {
   if (nv <= 0 || nt <= 0) throw invalid_argument("mesh must have at least one vertex and one cell");
-  for (long long i = 0; i < 4LL * nt; ++i)
+  if (cv != 4 && cv != 2) throw invalid_argument("cells must have 4 (tets) or 2 (springs) vertices");
+  for (long long i = 0; i < (long long)cv * nt; ++i)
     if (cells[i] < 0 || cells[i] >= nv)
       throw invalid_argument("cell index out of range at cells[" + std::to_string(i) + "] = " +
                              std::to_string(cells[i]));
-  if (10LL * nt >= (1LL << 31)) throw invalid_argument("too many cells for 32-bit assembly codes");
+  const int nb = cv * (cv + 1) / 2;  // upper vertex blocks per cell
+  if ((long long)nb * nt >= (1LL << 31)) throw invalid_argument("too many cells for 32-bit assembly codes");
   t.nv = nv;
   t.nt = nt;
-  // neighbour lists (two-pass CSR of the 4x4 vertex pairs of every tet, then sort + unique per row)
+  t.cv = cv;
+  // neighbour lists (two-pass CSR of the cv x cv vertex pairs of every cell, then sort + unique per row)
   std::vector<int32_t> cnt(nv + 1, 0);
-  for (long long i = 0; i < 4LL * nt; ++i) cnt[cells[i] + 1] += 4;
+  for (long long i = 0; i < (long long)cv * nt; ++i) cnt[cells[i] + 1] += cv;
   for (int v = 0; v < nv; ++v) cnt[v + 1] += cnt[v];
   std::vector<int32_t> raw(cnt[nv]);
   {
     std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
     for (int e = 0; e < nt; ++e)
-      for (int i = 0; i < 4; ++i) {
-        const int u = cells[4 * e + i];
-        for (int j = 0; j < 4; ++j) raw[fill[u]++] = cells[4 * e + j];
+      for (int i = 0; i < cv; ++i) {
+        const int u = cells[cv * e + i];
+        for (int j = 0; j < cv; ++j) raw[fill[u]++] = cells[cv * e + j];
       }
   }
   t.bptr.assign(nv + 1, 0);
@@ -135,13 +138,13 @@ void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
   std::vector<int32_t> ccnt(t.nslots + 1, 0);
   auto visit = [&](auto&& fn) {
     for (int e = 0; e < nt; ++e)
-      for (int v = 0; v < 4; ++v)
-        for (int w = 0; w < 4; ++w) {
-          const int gu = cells[4 * e + v], gw = cells[4 * e + w];
+      for (int v = 0; v < cv; ++v)
+        for (int w = 0; w < cv; ++w) {
+          const int gu = cells[cv * e + v], gw = cells[cv * e + w];
           if (gu > gw) continue;
           const int q = slot_of(gu, find_pos(t, gu, gw) - lo_deg[gu]);
           const int lo = std::min(v, w), hi = std::max(v, w);
-          int32_t code = (int32_t)(10 * e + upper_block_id(lo, hi));
+          int32_t code = (int32_t)(nb * e + (lo * cv - (lo * (lo - 1)) / 2 + (hi - lo)));
           if (v > w) code = (int32_t)((uint32_t)code | 0x80000000u);
           fn(q, code);
         }
@@ -156,13 +159,18 @@ void build_topology(int nv, int nt, const int32_t* cells, Topology& t) {
   }
   // vertex incidence (global_composer.hpp:36-66)
   t.vptr.assign(nv + 1, 0);
-  for (long long i = 0; i < 4LL * nt; ++i) t.vptr[cells[i] + 1]++;
+  for (long long i = 0; i < (long long)cv * nt; ++i) t.vptr[cells[i] + 1]++;
   for (int v = 0; v < nv; ++v) t.vptr[v + 1] += t.vptr[v];
-  t.vinc.assign(4LL * nt, 0);
+  t.vinc.assign((long long)cv * nt, 0);
   {
     std::vector<int32_t> fill(t.vptr.begin(), t.vptr.end() - 1);
-    for (long long i = 0; i < 4LL * nt; ++i) t.vinc[fill[cells[i]]++] = (int32_t)i;
+    for (long long i = 0; i < (long long)cv * nt; ++i) t.vinc[fill[cells[i]]++] = (int32_t)i;
   }
+}
+
+int upper_slot(const Topology& t, int u, int w) {
+  const int lo = find_pos(t, u, u);
+  return t.sl_off[u >> 5] + 32 * (find_pos(t, u, w) - lo) + (u & 31);
 }
 
 void csr_pattern(const Topology& t, int32_t* row_ptr, int32_t* col_idx) {

@@ -8,6 +8,7 @@ namespace ssim_gb {
 
 struct Topology {
   int nv = 0, nt = 0;
+  int cv = 4;  // vertices per cell: 4 (tets) or 2 (springs)
   // block CSR of the full pattern: block row u holds its sorted neighbour vertices (self included).  The
   // scalar CSR of the reference (global_composer.hpp:68-100) follows: row 3u+a has columns
   // {3w+b : w in bcol[u], b<3}, so row_ptr[3u+a] = 9*bptr[u] + 3*deg(u)*a.
@@ -28,18 +29,22 @@ struct Topology {
   std::vector<int32_t> lo_off;  // [nslices+1]
   std::vector<int32_t> lo_src;  // [nlslots] upper slot holding block (w, u), zero_slot for padding
   std::vector<int32_t> lo_col;  // [nlslots] w (own row for padding)
-  // assembly lists: per upper slot, codes (e*10 + local upper block id) | (bit 31 if that element block
-  // enters transposed)
+  // assembly lists: per upper slot, codes (e*nb + local upper block id) | (bit 31 if that element block
+  // enters transposed), nb = cv (cv + 1) / 2 upper vertex blocks per cell (10 for tets, 3 for springs)
   std::vector<int32_t> cptr, csrc;
-  // vertex incidence for the force gather: per vertex, the (e*4 + i) with cells[e][i] == vertex
+  // vertex incidence for the force gather: per vertex, the (e*cv + i) with cells[e][i] == vertex
   std::vector<int32_t> vptr, vinc;
 };
 
-// validates the cell indices (throws ssim_gb::invalid_argument) and builds everything above
-void build_topology(int nv, int nt, const int32_t* cells, Topology& t);
+// validates the cell indices (throws ssim_gb::invalid_argument) and builds everything above; cells are
+// [nt][cv] with cv = 4 (tets) or 2 (springs)
+void build_topology(int nv, int nt, const int32_t* cells, Topology& t, int cv = 4);
 
 // the upper-triangular block id of the local vertex pair (v <= w) used by the element Hessian kernel
 inline int upper_block_id(int v, int w) { return v * 4 - (v * (v - 1)) / 2 + (w - v); }
+
+// SELL slot of the upper block (u, w), u <= w, w a neighbour of u
+int upper_slot(const Topology& t, int u, int w);
 
 // scalar CSR pattern (row_ptr [3nv+1], col_idx [9*nnzb])
 void csr_pattern(const Topology& t, int32_t* row_ptr, int32_t* col_idx);

@@ -97,11 +97,57 @@ def beam(nx=100, ny=50, nz=34, h=0.02, seed=3):
     )
 
 
+def cloth_springs(n):
+    """Spring list of an n x n vertex grid (vertex (i, j) = i * n + j): structural (grid edges,
+    2 n (n-1)), shear (both quad diagonals, 2 (n-1)^2) and bend (every second vertex along the rows and
+    columns, 2 n (n-2)) springs, in that order."""
+    idx = np.arange(n * n, dtype=np.int32).reshape(n, n)
+    parts = [
+        (idx[:, :-1], idx[:, 1:]),  # structural, along j
+        (idx[:-1, :], idx[1:, :]),  # structural, along i
+        (idx[:-1, :-1], idx[1:, 1:]),  # shear
+        (idx[:-1, 1:], idx[1:, :-1]),  # shear
+        (idx[:, :-2], idx[:, 2:]),  # bend, along j
+        (idx[:-2, :], idx[2:, :]),  # bend, along i
+    ]
+    return np.concatenate([np.stack([a.reshape(-1), b.reshape(-1)], axis=1) for a, b in parts]).astype(np.int32)
+
+
+def cloth(n=512, h=0.01, k=1e3, areal_density=0.5, dt=1e-2, steps=10):
+    """Mass-spring cloth: n x n vertex grid in the z = 0 plane with spacing h (512^2 vertices, h = 1 cm:
+    a 5.11 m square sheet), structural + shear + bend springs (1,567,746 for n = 512) of stiffness k = 1e3
+    N/m, rest lengths from the grid, lumped vertex masses areal_density x h^2 (0.5 kg/m^2, a heavy fabric),
+    the four corners pinned, gravity -9.8 e_z, dt = 1e-2 s, 10 steps."""
+    g = np.arange(n, dtype=np.float64) * h
+    X = np.zeros((n * n, 3))
+    X[:, 0] = np.repeat(g, n)
+    X[:, 1] = np.tile(g, n)
+    S = cloth_springs(n)
+    return dict(
+        name=f"cloth_{n}x{n}_{S.shape[0]}springs",
+        X=X,
+        cells=S,
+        springs=True,
+        k=k,
+        vertex_mass=np.full(n * n, areal_density * h * h),
+        dt=dt,
+        fixed=np.array([0, n - 1, n * (n - 1), n * n - 1]),
+        gravity=(0.0, 0.0, -9.8),
+        steps=steps,
+        u0=None,
+        E_cells=None,
+    )
+
+
 def build_timestep(scene, precision="fp64", stepper="newton", params=None, rtol=None):
     """A GPU TimeStep set up for ``scene`` (material, Dirichlet face, gravity, initial state)."""
     from .timestep import TimeStep
 
-    ts = TimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
+    if scene.get("springs"):
+        ts = TimeStep.springs(scene["X"], scene["cells"], scene["k"], vertex_mass=scene["vertex_mass"],
+                              time_step=scene["dt"])
+    else:
+        ts = TimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
     ts.set_precision(precision)
     if scene.get("E_cells") is not None:
         ts.set_material(scene["E_cells"], None)
@@ -124,7 +170,12 @@ def build_oracle(scene, rtol=None):
     """The same scene on the FP64 CPU oracle (test infrastructure)."""
     from oracle import pyoracle
 
-    ts = pyoracle.OracleTimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
+    if scene.get("springs"):
+        ts = pyoracle.OracleTimeStep.springs(scene["X"], scene["cells"], scene["k"],
+                                             vertex_mass=scene["vertex_mass"], time_step=scene["dt"])
+    else:
+        ts = pyoracle.OracleTimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"],
+                                     scene["rho"])
     if scene.get("E_cells") is not None:
         ts.set_material(scene["E_cells"], None)
     if len(scene["fixed"]):

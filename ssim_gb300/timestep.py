@@ -41,6 +41,36 @@ class TimeStep:
             self.set_precision(precision)
             self.reset()
 
+    @classmethod
+    def springs(cls, vertices, springs, stiffness, vertex_mass=None, mass=None, time_step=1e-2, precision="fp64"):
+        """A mass-spring system (ssim_gb_create_springs): springs [S, 2] vertex pairs (rest lengths from the
+        vertices), uniform stiffness, vertex masses [V] (or one mass for all)."""
+        self = cls.__new__(cls)
+        L = _lib.lib()
+        self._L = L
+        X = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+        Sp = np.ascontiguousarray(springs, dtype=np.int32).reshape(-1, 2)
+        self.num_vertices, self.num_cells = X.shape[0], Sp.shape[0]
+        self.n = 3 * self.num_vertices
+        m = None
+        if vertex_mass is not None:
+            m = np.ascontiguousarray(vertex_mass, dtype=np.float64).reshape(-1)
+            if m.size != X.shape[0]:
+                raise ValueError("vertex_mass must have one entry per vertex")
+        h = C.c_void_p()
+        check(
+            L.ssim_gb_create_springs(dptr(X), X.shape[0], iptr(Sp), Sp.shape[0], stiffness,
+                                     dptr(m) if m is not None else None, mass if mass is not None else 0.0,
+                                     time_step, C.byref(h))
+        )
+        self._h = h
+        self._X, self._cells = X, Sp
+        self._stepper = _lib.STEPPER_NONE
+        if precision != "fp64":
+            self.set_precision(precision)
+            self.reset()
+        return self
+
     def close(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:
