@@ -55,6 +55,7 @@ struct DevScalars {
   double trial_energy_scale;
   double gd;              // g . d
   double dnorm2;          // |d|^2
+  double pair_sy, pair_yy;  // s . y and y . y of the L-BFGS pair formed at the last trial point
   // PCG
   double rz, rz_old, pq, rr, rr0, tol2;
   double alpha, beta;  // rz / pq and rz / rz_old, formed once by the reducing block

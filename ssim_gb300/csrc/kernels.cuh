@@ -24,6 +24,17 @@ namespace ssim_gb {
 template <typename S>
 using V4 = typename vec4<S>::type;
 
+// a 4-wide vector with w = 0
+template <typename S>
+__device__ __forceinline__ V4<S> mk4(S a, S b, S c) {
+  V4<S> r;
+  r.x = a;
+  r.y = b;
+  r.z = c;
+  r.w = S(0);
+  return r;
+}
+
 struct ElemFP64 {
   int nt;
   const int4* cells;
@@ -52,6 +63,8 @@ struct SpringData {
   const double* X;      // [V][3] rest positions
   const double* rest;   // [ns] rest lengths
   const double* k;      // [ns] stiffness
+  const float4* e0;     // [ns] FP32 rest edge X_i - X_j and rest length (the FP32 spring pass)
+  const float* k32;     // [ns] FP32 stiffness
 };
 
 struct Reduce {
@@ -93,9 +106,21 @@ void launch_spring_energy_grad(const SpringData& sp, const double* u, const doub
                                const V4<SD>* d, double alpha, double dt2, double* lf, bool with_forces, bool trial,
                                const Reduce& red, cudaStream_t st);
 // g = spring forces gathered per vertex + m (u - x~), Dirichlet dofs zeroed; |g|^2 into the scalars
+template <typename SD>
 void launch_spring_gather(int nv, const int* vptr, const int* vinc, const double* lf, const double* m,
-                          const double* u, const double* xt, const uint8_t* mask, double* g, const Reduce& red,
-                          cudaStream_t st);
+                          const double* u, const V4<SD>* d, double alpha, const double* xt, const uint8_t* mask,
+                          double* g, const Reduce& red, cudaStream_t st);
+// FP32 spring pass (strain-relative: l - L = (2 E0.D + D.D) / (l + L) with D = the displacement difference
+// formed in FP64): energy (+ the spring force vector f_s into lf32[s] when with_forces), FP64 sums
+template <typename SD>
+void launch_spring_energy_grad32(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
+                                 const V4<SD>* d, double alpha, double dt2, float4* lf32, bool with_forces,
+                                 bool trial, const Reduce& red, cudaStream_t st);
+// g from the FP32 spring forces (vertex i of a spring receives +f_s, vertex j -f_s) + m (u (+ alpha d) - x~)
+template <typename SD>
+void launch_spring_gather32(int nv, const int* vptr, const int* vinc, const float4* lf32, const double* m,
+                            const double* u, const V4<SD>* d, double alpha, const double* xt, const uint8_t* mask,
+                            double* g, const Reduce& red, cudaStream_t st);
 // spring Hessian blocks Kbuf[s][3][9] (scaled by dt^2), the compressed transverse part dropped when spsd
 template <typename S>
 void launch_spring_hessian(const SpringData& sp, const double* u, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
@@ -170,6 +195,40 @@ void launch_vaxpby(int nv, double alpha, V4<S>* y, double beta, const V4<S>* x, 
 // y = (S)(a - b) for FP64 [3V] a, b
 template <typename S>
 void launch_vdiff(int nv, const double* a, const double* b, V4<S>* y, cudaStream_t st);
+
+// L-BFGS in compact form (history of at most kLbfgsMaxCompact pairs): the pairs in age order (oldest first)
+// and their storage slots
+constexpr int kLbfgsMaxCompact = 8;
+template <typename S>
+struct LbfgsHist {
+  int n;
+  const V4<S>* s[kLbfgsMaxCompact];
+  const V4<S>* y[kLbfgsMaxCompact];
+  int slot[kLbfgsMaxCompact];
+};
+// S^T g, Y^T g and the newest column of S^T Y, Y^T Y in one pass; tab = [S^T Y (M x M by slot) | Y^T Y |
+// coefficients p (M), -gamma q (M), gamma]; partials: lbfgs_multidot_partials(nv) doubles
+template <typename S>
+void launch_lbfgs_multidot(int nv, const double* g, const LbfgsHist<S>& h, double* partials, double* tab,
+                           unsigned int* counter, cudaStream_t st);
+template <typename S>
+void launch_lbfgs_combine(int nv, const double* g, const LbfgsHist<S>& h, const double* coef, double gamma_host,
+                          V4<S>* d, const Reduce& red, cudaStream_t st);
+int lbfgs_multidot_partials(int nv);
+// L-BFGS two-loop recursion with device-resident coefficients (kernels_lbfgs.cu)
+template <typename S>
+void launch_lbfgs_pass(int nv, const V4<S>* vin, const double* g, V4<S>* vout, const V4<S>* w, const double* cA,
+                       const double* cB, double csign, const double* scale_ptr, double scale, const V4<S>* a,
+                       double rho, double* out, const Reduce& red, cudaStream_t st);
+template <typename S>
+void launch_lbfgs_final(int nv, const V4<S>* z, const V4<S>* w, const double* cA, const double* cB, const double* g,
+                        V4<S>* d, const Reduce& red, cudaStream_t st);
+template <typename S>
+void launch_lbfgs_pair(int nv, double alpha, const V4<S>* d, const double* gnew, const double* gold, V4<S>* sv,
+                       V4<S>* yv, const Reduce& red, cudaStream_t st);
+template <typename S>
+void launch_lbfgs_accept(int nv, double alpha, const V4<S>* d, double* u, const double* gnew, double* gold,
+                         cudaStream_t st);
 // per-instance |g|^2 over contiguous vertex ranges voff[i]..voff[i+1] (one block per instance, fixed order)
 void launch_instance_norms(int ninst, const int* voff, const double* g, double* out, cudaStream_t st);
 // PCG setup from an S right-hand side (the PD stepper's inner solve)

@@ -8,15 +8,6 @@ namespace {
 
 constexpr int SB = 256;  // block of the slot / row / dof kernels (a multiple of the 32-row slice)
 
-template <typename S>
-__device__ __forceinline__ V4<S> mk4(S a, S b, S c) {
-  V4<S> r;
-  r.x = a;
-  r.y = b;
-  r.z = c;
-  r.w = S(0);
-  return r;
-}
 
 __device__ __forceinline__ size_t sell_base(int q) { return (size_t)9 * (size_t)(q & ~31) + (size_t)(q & 31); }
 

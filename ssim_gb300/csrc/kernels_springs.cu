@@ -78,6 +78,102 @@ __global__ void __launch_bounds__(PB)
   }
 }
 
+// FP32 spring pass.  The displacement difference D = (u_i - u_j) (+ alpha (d_i - d_j)) is formed in FP64 and
+// rounded once; with E0 the rest edge, e = E0 + D and l^2 - L^2 = 2 E0.D + D.D, so l - L = (l^2 - L^2) / (l + L)
+// carries FP32 rounding relative to the stretch itself rather than to the length (a direct FP32 |e| - L
+// would lose the stretch of a stiff spring to cancellation).  Forces f_s = dt^2 k (l - L) / l e go to
+// lf32[s] (vertex i gets +f_s, vertex j -f_s).
+template <typename SD, bool FORCES, bool TRIAL>
+__global__ void __launch_bounds__(PB)
+    spring_energy_grad32_kernel(SpringData sp, const double* __restrict__ u, const V4<SD>* __restrict__ d,
+                                double alpha, float dt2, float4* __restrict__ lf32, Reduce red) {
+  __shared__ double shred[PB / 32][2];
+  const int s = blockIdx.x * PB + threadIdx.x;
+  float part[2] = {0.f, 0.f};
+  if (s < sp.ns) {
+    const int2 c = sp.ends[s];
+    const float4 e0 = sp.e0[s];
+    float D[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) D[q] = (float)(u[3 * c.x + q] - u[3 * c.y + q]);
+    if (TRIAL) {
+      const V4<SD> di = d[c.x], dj = d[c.y];
+      const float a = (float)alpha;
+      D[0] += a * (float)(di.x - dj.x);
+      D[1] += a * (float)(di.y - dj.y);
+      D[2] += a * (float)(di.z - dj.z);
+    }
+    const float ex = e0.x + D[0], ey = e0.y + D[1], ez = e0.z + D[2];
+    const float L = e0.w, l2 = ex * ex + ey * ey + ez * ez;
+    const float l = sqrtf(l2);
+    const float dl2 = 2.f * (e0.x * D[0] + e0.y * D[1] + e0.z * D[2]) + (D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
+    const float dl = dl2 / (l + L);
+    const float kk = dt2 * sp.k32[s];
+    part[0] = 0.5f * kk * dl * dl;
+    part[1] = 0.5f * kk * (l2 + L * L);
+    if (FORCES) {
+      const float cf = l > 0.f ? kk * dl / l : 0.f;
+      lf32[s] = make_float4(cf * ex, cf * ey, cf * ez, 0.f);
+    }
+  }
+  double v2[2];
+  block_sum_s<2, PB, float>(part, v2, shred);
+  double tot[2];
+  if (grid_sum_last<2, PB>(v2, red.partials, red.counter, tot)) {
+    if (TRIAL) {
+      red.sc->trial_energy = tot[0];
+      red.sc->trial_energy_scale = tot[1];
+    } else {
+      red.sc->energy = tot[0];
+      red.sc->energy_scale = tot[1];
+    }
+  }
+}
+
+// g_v from the FP32 spring forces (summed in FP32 over the incident springs) + m_v (u_v (+ alpha d_v) - x~_v)
+// in FP64, Dirichlet dofs zeroed; |g|^2
+template <typename SD>
+__global__ void __launch_bounds__(PB)
+    spring_gather32_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
+                           const float4* __restrict__ lf32, const double* __restrict__ m, const double* __restrict__ u,
+                           const V4<SD>* __restrict__ d, double alpha, const double* __restrict__ xt,
+                           const uint8_t* __restrict__ mask, double* __restrict__ g, Reduce red) {
+  __shared__ double shred[PB / 32][1];
+  const int v = blockIdx.x * PB + threadIdx.x;
+  double part = 0;
+  if (v < nv) {
+    float a[3] = {0.f, 0.f, 0.f};
+    const int k1 = vptr[v + 1];
+    for (int k = vptr[v]; k < k1; ++k) {
+      const int code = vinc[k];
+      const float4 f = lf32[code >> 1];
+      const float sg = (code & 1) ? -1.f : 1.f;
+      a[0] += sg * f.x;
+      a[1] += sg * f.y;
+      a[2] += sg * f.z;
+    }
+    double dv[3] = {0, 0, 0};
+    if (d != nullptr) {
+      const V4<SD> t = d[v];
+      dv[0] = alpha * (double)t.x;
+      dv[1] = alpha * (double)t.y;
+      dv[2] = alpha * (double)t.z;
+    }
+    const uint8_t mk = mask[v];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double gq = (double)a[q] + m[v] * ((u[3 * v + q] - xt[3 * v + q]) + dv[q]);
+      if ((mk >> q) & 1) gq = 0;
+      g[3 * v + q] = gq;
+      part += gq * gq;
+    }
+  }
+  double v1[1] = {part};
+  block_sum<1, PB>(v1, shred);
+  double tot[1];
+  if (grid_sum_last<1, PB>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+}
+
 // lumped inertia 1/2 sum_v m_v |u_v (+ alpha d_v) - x~_v|^2, added to the (trial) energy and its scale
 template <typename SD, bool TRIAL>
 __global__ void __launch_bounds__(PB)
@@ -112,12 +208,14 @@ __global__ void __launch_bounds__(PB)
   }
 }
 
-// g_v = sum of the incident spring forces + m_v (u_v - x~_v), Dirichlet dofs zeroed; |g|^2
+// g_v = sum of the incident spring forces + m_v (u_v (+ alpha d_v) - x~_v), Dirichlet dofs zeroed; |g|^2.
+// With d the springs' forces must be those of the same trial point u + alpha d.
+template <typename SD>
 __global__ void __launch_bounds__(PB)
     spring_gather_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
                          const double* __restrict__ lf, const double* __restrict__ m, const double* __restrict__ u,
-                         const double* __restrict__ xt, const uint8_t* __restrict__ mask, double* __restrict__ g,
-                         Reduce red) {
+                         const V4<SD>* __restrict__ d, double alpha, const double* __restrict__ xt,
+                         const uint8_t* __restrict__ mask, double* __restrict__ g, Reduce red) {
   __shared__ double shred[PB / 32][1];
   const int v = blockIdx.x * PB + threadIdx.x;
   double part = 0;
@@ -131,9 +229,16 @@ __global__ void __launch_bounds__(PB)
       a[2] += s[2];
     }
     const uint8_t mk = mask[v];
+    double dv[3] = {0, 0, 0};
+    if (d != nullptr) {
+      const V4<SD> t = d[v];
+      dv[0] = alpha * (double)t.x;
+      dv[1] = alpha * (double)t.y;
+      dv[2] = alpha * (double)t.z;
+    }
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-      a[q] += m[v] * (u[3 * v + q] - xt[3 * v + q]);
+      a[q] += m[v] * ((u[3 * v + q] - xt[3 * v + q]) + dv[q]);
       if ((mk >> q) & 1) a[q] = 0;
       g[3 * v + q] = a[q];
       part += a[q] * a[q];
@@ -204,11 +309,44 @@ void launch_spring_energy_grad(const SpringData& sp, const double* u, const doub
   after_launch("lumped_inertia_energy");
 }
 
+template <typename SD>
 void launch_spring_gather(int nv, const int* vptr, const int* vinc, const double* lf, const double* m,
-                          const double* u, const double* xt, const uint8_t* mask, double* g, const Reduce& red,
-                          cudaStream_t st) {
-  spring_gather_kernel<<<div_up(nv, PB), PB, 0, st>>>(nv, vptr, vinc, lf, m, u, xt, mask, g, red);
+                          const double* u, const V4<SD>* d, double alpha, const double* xt, const uint8_t* mask,
+                          double* g, const Reduce& red, cudaStream_t st) {
+  spring_gather_kernel<SD><<<div_up(nv, PB), PB, 0, st>>>(nv, vptr, vinc, lf, m, u, d, alpha, xt, mask, g, red);
   after_launch("spring_gather");
+}
+
+template <typename SD>
+void launch_spring_energy_grad32(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
+                                 const V4<SD>* d, double alpha, double dt2, float4* lf32, bool with_forces,
+                                 bool trial, const Reduce& red, cudaStream_t st) {
+  if (sp.ns > 0) {
+    const int grid = div_up(sp.ns, PB);
+    const float f2 = (float)dt2;
+    if (trial && with_forces)
+      spring_energy_grad32_kernel<SD, true, true><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+    else if (trial)
+      spring_energy_grad32_kernel<SD, false, true><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+    else if (with_forces)
+      spring_energy_grad32_kernel<SD, true, false><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+    else
+      spring_energy_grad32_kernel<SD, false, false><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+    after_launch("spring_energy_grad32");
+  }
+  if (trial)
+    lumped_inertia_energy_kernel<SD, true><<<div_up(nv, PB), PB, 0, st>>>(nv, m, u, xt, d, alpha, red);
+  else
+    lumped_inertia_energy_kernel<SD, false><<<div_up(nv, PB), PB, 0, st>>>(nv, m, u, xt, d, alpha, red);
+  after_launch("lumped_inertia_energy");
+}
+
+template <typename SD>
+void launch_spring_gather32(int nv, const int* vptr, const int* vinc, const float4* lf32, const double* m,
+                            const double* u, const V4<SD>* d, double alpha, const double* xt, const uint8_t* mask,
+                            double* g, const Reduce& red, cudaStream_t st) {
+  spring_gather32_kernel<SD><<<div_up(nv, PB), PB, 0, st>>>(nv, vptr, vinc, lf32, m, u, d, alpha, xt, mask, g, red);
+  after_launch("spring_gather32");
 }
 
 template <typename S>
@@ -224,6 +362,18 @@ template void launch_spring_energy_grad<float>(const SpringData&, const double*,
 template void launch_spring_energy_grad<double>(const SpringData&, const double*, const double*, const double*, int,
                                                 const double4_32a*, double, double, double*, bool, bool,
                                                 const Reduce&, cudaStream_t);
+template void launch_spring_gather<float>(int, const int*, const int*, const double*, const double*, const double*,
+                                          const float4*, double, const double*, const uint8_t*, double*,
+                                          const Reduce&, cudaStream_t);
+template void launch_spring_gather<double>(int, const int*, const int*, const double*, const double*, const double*,
+                                           const double4_32a*, double, const double*, const uint8_t*, double*,
+                                           const Reduce&, cudaStream_t);
+template void launch_spring_energy_grad32<float>(const SpringData&, const double*, const double*, const double*,
+                                                 int, const float4*, double, double, float4*, bool, bool,
+                                                 const Reduce&, cudaStream_t);
+template void launch_spring_gather32<float>(int, const int*, const int*, const float4*, const double*,
+                                            const double*, const float4*, double, const double*, const uint8_t*,
+                                            double*, const Reduce&, cudaStream_t);
 template void launch_spring_hessian<float>(const SpringData&, const double*, double, bool, float*, cudaStream_t);
 template void launch_spring_hessian<double>(const SpringData&, const double*, double, bool, double*, cudaStream_t);
 

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -148,23 +149,44 @@ struct TimeStep {
   bool springs = false;
   DBuf<int2> sp_ends;
   DBuf<double> sp_rest, sp_k, vmass;
+  DBuf<float4> sp_e0, sp_lf32;
+  DBuf<float> sp_k32;
   std::vector<double> vmass_h, sp_k_h;
-  SpringData spd() const { return SpringData{nt, sp_ends.p, dX.p, sp_rest.p, sp_k.p}; }
+  SpringData spd() const { return SpringData{nt, sp_ends.p, dX.p, sp_rest.p, sp_k.p, sp_e0.p, sp_k32.p}; }
 
-  // element / spring pass at u = next (+ alpha d): energy (+ local forces into lf) into the trial scalars
+  // element / spring pass at u = next (+ alpha d): energy (+ local forces into lf) into the trial scalars;
+  // fp32: the FP32 element / spring arithmetic of the mixed path's early iterations
   template <typename S>
-  void launch_trial(const V4<S>* d, double alpha, bool forces) {
-    if (springs)
+  void launch_trial(const V4<S>* d, double alpha, bool forces, bool fp32 = false) {
+    if (springs && fp32) {
+      if constexpr (std::is_same<S, float>::value)
+        launch_spring_energy_grad32<float>(spd(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt,
+                                           forces ? sp_lf32.p : nullptr, forces, true, red(), stream);
+      else
+        throw state_error("the FP32 spring pass takes FP32 directions");
+    } else if (springs)
       launch_spring_energy_grad<S>(spd(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt, forces ? lf.p : nullptr,
+                                   forces, true, red(), stream);
+    else if (fp32)
+      launch_elem_energy_grad32<S>(e64(), e32s(), next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr,
                                    forces, true, red(), stream);
     else
       launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr,
                                  forces, true, red(), stream);
   }
-  // forces at next from lf (gathered), Dirichlet dofs zeroed, |g|^2
-  void gather_forces() {
-    if (springs)
-      launch_spring_gather(nv, vptr.p, vinc.p, lf.p, vmass.p, next.p, inertia.p, mask.p, forces.p, red(), stream);
+  // forces at next (+ alpha d: the point of the last trial pass) from the last pass's local forces,
+  // Dirichlet dofs zeroed, |g|^2
+  template <typename S = double>
+  void gather_forces(const V4<S>* d = nullptr, double alpha = 0.0, bool fp32 = false) {
+    if (springs && fp32) {
+      if constexpr (std::is_same<S, float>::value)
+        launch_spring_gather32<float>(nv, vptr.p, vinc.p, sp_lf32.p, vmass.p, next.p, d, alpha, inertia.p, mask.p,
+                                      forces.p, red(), stream);
+      else
+        throw state_error("the FP32 spring pass takes FP32 directions");
+    } else if (springs)
+      launch_spring_gather<S>(nv, vptr.p, vinc.p, lf.p, vmass.p, next.p, d, alpha, inertia.p, mask.p, forces.p, red(),
+                              stream);
     else
       launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
   }
@@ -179,6 +201,8 @@ struct TimeStep {
       if (topo.slot_row[q] >= 0 && topo.slot_row[q] == topo.sl_col[q]) smass[q] = vmass_h[topo.slot_row[q]];
   }
   std::vector<int32_t> solve_log;  // PCG iterations of every solve since the last reset
+  DBuf<double> lbc;                // L-BFGS two-loop coefficients a_i, b_i
+  DBuf<double> lbtab, lbpart;      // compact L-BFGS: S^T Y / Y^T Y tables + coefficients; multidot partials
   // NCG preconditioner factor L (host copy; empty = identity), its CSR pattern on the device and the
   // position of each entry's transpose
   std::vector<double> ncg_vals;
@@ -289,6 +313,16 @@ struct TimeStep {
     sp_rest.upload(rest, stream);
     sp_k.upload(sp_k_h, stream);
     vmass.upload(vmass_h, stream);
+    std::vector<float4> e0(nt);
+    for (int e = 0; e < nt; ++e) {
+      const int i = cells[2 * e], j = cells[2 * e + 1];
+      e0[e] = make_float4((float)(X[3 * i] - X[3 * j]), (float)(X[3 * i + 1] - X[3 * j + 1]),
+                          (float)(X[3 * i + 2] - X[3 * j + 2]), (float)rest[e]);
+    }
+    sp_e0.upload(e0, stream);
+    std::vector<float> k32(sp_k_h.begin(), sp_k_h.end());
+    sp_k32.upload(k32, stream);
+    sp_lf32.alloc(nt);
     reset(SSIM_GB_STEPPER_NONE);
   }
 
@@ -523,10 +557,14 @@ struct TimeStep {
   double energy_grad32() {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
-    launch_elem_energy_grad32<float>(e64(), e32s(), next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
-                                     red(), stream);
+    if (springs)
+      launch_spring_energy_grad32<float>(spd(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt, sp_lf32.p, true,
+                                         false, red(), stream);
+    else
+      launch_elem_energy_grad32<float>(e64(), e32s(), next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true,
+                                       false, red(), stream);
     if (profiling) prof_end(e0, e1, PK_GRAD, 0);
-    launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
+    gather_forces<float>(nullptr, 0.0, true);
     sync_scalars();
     if (!std::isfinite(hsc->energy) || !std::isfinite(hsc->gnorm2))
       throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
@@ -729,9 +767,29 @@ struct TimeStep {
       pd = true;
     }
     const int m = std::max(1, std::min(params.lbfgs_history, (int)s.hs.size()));
-    std::vector<double> rho_h(m, 0.0), al(m, 0.0);
+    // The two-loop coefficients a_i (lbc[i]) and b_i (lbc[m + i]) stay on the device; rho_i and the initial
+    // scaling are known on the host from the pair's s.y and y.y, read with the trial point's energy.  One
+    // host round trip per line-search trial: the trial pass also forms the forces at the trial point and
+    // the curvature pair against the current gradient (kept in gprev), so an accepted trial needs no
+    // further evaluation.
+    lbc.alloc(2 * (size_t)m);
+    double* al = lbc.p;
+    double* bb = lbc.p + m;
+    // without a PD/H0 solve and with at most kLbfgsMaxCompact pairs the direction comes from the compact
+    // form of the same matrix: two passes instead of 2m dependent ones
+    const bool compact = !pd && m <= kLbfgsMaxCompact;
+    constexpr int MC = kLbfgsMaxCompact;
+    if (compact) {
+      lbtab.alloc(2 * MC * MC + 2 * MC + 1);
+      lbpart.alloc((size_t)lbfgs_multidot_partials(nv));
+    }
+    std::vector<double> rho_h(m, 0.0);
+    double gamma = 0.0;     // s.y / y.y of the newest pair
     int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
-    double E0 = energy_grad();
+    // mixed precision: FP32 element / spring arithmetic until the residual is within elem32_switch times
+    // the target or a line search runs out, FP64 after that and for the stopping test
+    bool e32 = mixed() && params.mixed_elem32 != 0, e32_stall = false;
+    double E0 = e32 ? energy_grad32() : energy_grad();
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
     st.grad_norm0 = g0;
@@ -739,8 +797,20 @@ struct TimeStep {
     SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
     const double pd_tol = mixed() ? std::max(params.cg_rtol, 1e-6) : params.cg_rtol;
     double E0_scale = hsc->energy_scale;
+    auto to_fp64 = [&]() {
+      e32 = false;
+      E0 = energy_grad();
+      E0_scale = hsc->energy_scale;
+      gn = std::sqrt(hsc->gnorm2);
+      SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    };
+    V4<S>* q = s.lq.p;
+    V4<S>* d = s.ld.p;
+    auto slot = [&](int j) { return (head - hsize + j + m) % m; };  // j-th oldest entry
     int it = 0;
     for (;; ++it) {
+      const double tgt = params.stop_mode == 0 ? abs_tol : params.rel_tol * g0;
+      if (e32 && (gn <= params.elem32_switch * tgt || e32_stall)) to_fp64();
       st.grad_norm = gn;
       st.energy = E0;
       if (stop_test(gn, g0)) {
@@ -748,66 +818,108 @@ struct TimeStep {
         break;
       }
       if (it >= params.max_lbfgs_iters) break;
-      launch_to_vec4<S>(nv, forces.p, s.lq.p, false, stream);  // q = g
-      for (int j = hsize - 1; j >= 0; --j) {
-        const int i = (head - hsize + j + m) % m;
-        al[i] = rho_h[i] * vdot<S>(s.hs[i]->p, s.lq.p);
-        launch_vaxpby<S>(nv, 1.0, s.lq.p, -al[i], s.hy[i]->p, stream);
-      }
-      if (pd) {
-        double rr = 0;
-        st.cg_iters_total += pcg_on<S>(s.pd_vals.p, s.pd_dinv.p, s.lq.p, pd_tol, params.cg_max_iters, &rr);
-        launch_vaxpby<S>(nv, 0.0, s.ld.p, 1.0, s.x.p, stream);  // z = A^-1 q
-      } else {
-        double gamma = 1.0 / std::max(gn, 1e-300);
-        if (hsize > 0) {
-          const int i = (head - 1 + m) % m;
-          gamma = vdot<S>(s.hs[i]->p, s.hy[i]->p) / vdot<S>(s.hy[i]->p, s.hy[i]->p);
+      if (compact) {
+        LbfgsHist<S> hist{};
+        hist.n = hsize;
+        for (int j = 0; j < hsize; ++j) {
+          hist.s[j] = s.hs[slot(j)]->p;
+          hist.y[j] = s.hy[slot(j)]->p;
+          hist.slot[j] = slot(j);
         }
-        launch_vaxpby<S>(nv, 0.0, s.ld.p, gamma, s.lq.p, stream);
+        if (hsize > 0) launch_lbfgs_multidot<S>(nv, gprev.p, hist, lbpart.p, lbtab.p, counter.p, stream);
+        launch_lbfgs_combine<S>(nv, gprev.p, hist, lbtab.p + 2 * MC * MC, 1.0 / std::max(gn, 1e-300), d, red(),
+                                stream);
+      } else {
+        // first loop, newest pair first: a_i = rho_i s_i.q, q -= a_i y_i (q starts as g, read from gprev,
+        // which holds the current gradient)
+        for (int j = hsize - 1; j >= 0; --j) {
+          const int i = slot(j), inext = j + 1 < hsize ? slot(j + 1) : -1;
+          launch_lbfgs_pass<S>(nv, j == hsize - 1 ? nullptr : q, gprev.p, q, inext >= 0 ? s.hy[inext]->p : nullptr,
+                               inext >= 0 ? al + inext : nullptr, nullptr, -1.0, nullptr, 1.0, s.hs[i]->p, rho_h[i],
+                               al + i, red(), stream);
+        }
+        // z = H0 q (q -= a_0 y_0 folded in), then b_0 = rho_0 y_0.z
+        V4<S>* z = pd ? s.x.p : d;
+        const int i0 = hsize > 0 ? slot(0) : -1;
+        if (pd) {
+          launch_lbfgs_pass<S>(nv, hsize > 0 ? q : nullptr, gprev.p, q, i0 >= 0 ? s.hy[i0]->p : nullptr,
+                               i0 >= 0 ? al + i0 : nullptr, nullptr, -1.0, nullptr, 1.0, nullptr, 0.0, nullptr, red(),
+                               stream);
+          double rr = 0;
+          st.cg_iters_total += pcg_on<S>(s.pd_vals.p, s.pd_dinv.p, q, pd_tol, params.cg_max_iters, &rr);
+          if (i0 >= 0)
+            launch_lbfgs_pass<S>(nv, z, nullptr, z, nullptr, nullptr, nullptr, 0.0, nullptr, 1.0, s.hy[i0]->p,
+                                 rho_h[i0], bb + i0, red(), stream);
+        } else {
+          const double h0 = hsize > 0 ? gamma : 1.0 / std::max(gn, 1e-300);
+          launch_lbfgs_pass<S>(nv, hsize > 0 ? q : nullptr, gprev.p, z, i0 >= 0 ? s.hy[i0]->p : nullptr,
+                               i0 >= 0 ? al + i0 : nullptr, nullptr, -1.0, nullptr, h0,
+                               i0 >= 0 ? s.hy[i0]->p : nullptr, i0 >= 0 ? rho_h[i0] : 0.0,
+                               i0 >= 0 ? bb + i0 : nullptr, red(), stream);
+        }
+        // second loop, oldest pair first: z += (a_{j-1} - b_{j-1}) s_{j-1}, b_j = rho_j y_j.z
+        for (int j = 1; j < hsize; ++j) {
+          const int i = slot(j), ip = slot(j - 1);
+          launch_lbfgs_pass<S>(nv, z, nullptr, z, s.hs[ip]->p, al + ip, bb + ip, 1.0, nullptr, 1.0, s.hy[i]->p,
+                               rho_h[i], bb + i, red(), stream);
+        }
+        // d = -(z + (a - b) s) of the newest pair; g.d and |d|^2
+        const int il = hsize > 0 ? slot(hsize - 1) : -1;
+        launch_lbfgs_final<S>(nv, z, il >= 0 ? s.hs[il]->p : nullptr, il >= 0 ? al + il : nullptr,
+                              il >= 0 ? bb + il : nullptr, gprev.p, d, red(), stream);
       }
-      for (int j = 0; j < hsize; ++j) {
-        const int i = (head - hsize + j + m) % m;
-        const double bb = rho_h[i] * vdot<S>(s.hy[i]->p, s.ld.p);
-        launch_vaxpby<S>(nv, 1.0, s.ld.p, al[i] - bb, s.hs[i]->p, stream);
-      }
-      launch_vaxpby<S>(nv, -1.0, s.ld.p, 0.0, s.ld.p, stream);  // d = -z
-      launch_dot_gd<S>(nv, forces.p, s.ld.p, red(), stream);
-      sync_scalars();
-      double gd = hsc->gd;
-      if (!(gd < 0)) {  // not a descent direction: drop the history, normalised steepest descent
-        hsize = 0;
-        launch_to_vec4<S>(nv, forces.p, s.ld.p, false, stream);
-        launch_vaxpby<S>(nv, -1.0 / std::max(gn, 1e-300), s.ld.p, 0.0, s.ld.p, stream);
-        launch_dot_gd<S>(nv, forces.p, s.ld.p, red(), stream);
-        sync_scalars();
-        gd = hsc->gd;
-      }
-      const double dn = std::sqrt(hsc->dnorm2);
-      const double Escale = E0_scale;
-      double alpha = 1.0;
-      for (int ls = 0; ls < params.max_ls_iters; ++ls) {
-        launch_trial<S>(s.ld.p, alpha, false);
+      // backtracking line search; each trial forms energy, forces and the curvature pair at u + alpha d
+      const double Escale = (e32 ? params.ls_energy_slack32 : params.ls_energy_slack) * E0_scale;
+      double alpha = 1.0, gd = 0.0, dn = 0.0;
+      bool have_gd = false, accepted = false;
+      auto trial = [&](double a) {
+        launch_trial<S>(d, a, true, e32);
+        gather_forces<S>(d, a, e32);
+        launch_lbfgs_pair<S>(nv, a, d, forces.p, gprev.p, s.hs[head]->p, s.hy[head]->p, red(), stream);
         sync_scalars();
         st.ls_steps_total++;
-        if (hsc->trial_energy <= E0 + params.lbfgs_armijo * alpha * gd + params.ls_energy_slack * Escale) break;
+      };
+      for (int ls = 0; ls < params.max_ls_iters; ++ls) {
+        trial(alpha);
+        if (!have_gd) {
+          gd = hsc->gd;
+          have_gd = true;
+          if (!(gd < 0)) {  // not a descent direction: drop the history, normalised steepest descent
+            hsize = 0;
+            st.ls_steps_total--;
+            launch_lbfgs_pass<S>(nv, nullptr, gprev.p, q, nullptr, nullptr, nullptr, 0.0, nullptr,
+                                 1.0 / std::max(gn, 1e-300), nullptr, 0.0, nullptr, red(), stream);
+            launch_lbfgs_final<S>(nv, q, nullptr, nullptr, nullptr, gprev.p, d, red(), stream);
+            trial(alpha);
+            gd = hsc->gd;
+          }
+          dn = std::sqrt(hsc->dnorm2);
+        }
+        if (hsc->trial_energy <= E0 + params.lbfgs_armijo * alpha * gd + Escale) {
+          accepted = true;
+          break;
+        }
         alpha *= params.ls_shrink;
       }
-      launch_axpy_update<S>(nv, alpha, s.ld.p, dX.p, next.p, nullptr, stream);
+      if (!accepted) {  // the search ran out: the step is taken at the last shrunk alpha
+        trial(alpha);
+        e32_stall = e32;
+      }
+      launch_lbfgs_accept<S>(nv, alpha, d, next.p, forces.p, gprev.p, stream);
       st.last_change = alpha * dn;
-      E0 = energy_grad();
-      E0_scale = hsc->energy_scale;
+      E0 = hsc->trial_energy;
+      E0_scale = hsc->trial_energy_scale;
       gn = std::sqrt(hsc->gnorm2);
-      // s = alpha d, y = g_new - g_old
-      const int slot = head;
-      launch_vaxpby<S>(nv, 0.0, s.hs[slot]->p, alpha, s.ld.p, stream);
-      launch_vdiff<S>(nv, forces.p, gprev.p, s.hy[slot]->p, stream);
-      SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
-      const double sy = vdot<S>(s.hs[slot]->p, s.hy[slot]->p);
+      if (!std::isfinite(E0) || !std::isfinite(gn))
+        throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
+      const double sy = hsc->pair_sy, yy = hsc->pair_yy;
       if (sy > 1e-300) {
-        rho_h[slot] = 1.0 / sy;
+        rho_h[head] = 1.0 / sy;
+        gamma = sy / yy;
         head = (head + 1) % m;
         hsize = std::min(hsize + 1, m);
+      } else if (hsize == m) {
+        hsize = m - 1;  // the pair was formed in the oldest entry's storage: that entry is gone
       }
     }
     st.newton_iters = it;
@@ -866,7 +978,7 @@ struct TimeStep {
     // mixed precision: the inner iterations evaluate energy and forces with FP32 element arithmetic (the
     // small-strain forms); the stopping test is then confirmed with an FP64 evaluation, and if the FP64
     // residual is above the target (or the FP32 residual stalls) the remaining iterations run in FP64
-    bool e32 = mixed() && params.mixed_elem32 != 0 && !springs;
+    bool e32 = mixed() && params.mixed_elem32 != 0;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);
@@ -918,11 +1030,7 @@ struct TimeStep {
       double Et = 0, Et_scale = 0;
       const double slack = (e32 ? params.ls_energy_slack32 : params.ls_energy_slack) * Escale;
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
-        if (e32)
-          launch_elem_energy_grad32<S>(e64(), e32s(), next.p, inertia.p, s.x.p, alpha, dt * dt, rho, lf.p, true, true,
-                                       red(), stream);
-        else
-          launch_trial<S>(s.x.p, alpha, true);
+        launch_trial<S>(s.x.p, alpha, true, e32);
         sync_scalars();
         st.ls_steps_total++;
         Et = hsc->trial_energy;
@@ -931,7 +1039,7 @@ struct TimeStep {
         if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
       launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
-      gather_forces();
+      gather_forces<S>(nullptr, 0.0, e32);
       sync_scalars();
       if (!std::isfinite(Et) || !std::isfinite(hsc->gnorm2))
         throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");

@@ -294,6 +294,28 @@ def test_lbfgs_and_pd_fp64(method):
     assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6
 
 
+@pytest.mark.parametrize("history", [3, 12])
+def test_lbfgs_history_compact_and_two_loop(history):
+    """L-BFGS with up to 8 pairs takes its direction from the compact form of the L-BFGS matrix, with more
+    from the two-loop recursion; both are the oracle's two-loop direction, and land on its state."""
+    from oracle import pyoracle
+
+    scene = scenes.cube10()
+    params = g.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, lbfgs_history=history)
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, lbfgs_history=history)
+    ts = scenes.build_timestep(scene, precision="fp64", stepper="lbfgs", params=params)
+    ot = scenes.build_oracle(scene)
+    for _ in range(2):
+        ts.step()
+        st = ts.stats()
+        ot.prepare_step()
+        _, sto = ot.compute_step("lbfgs", op)
+        ot.step_next()
+        assert st["converged"] == 1 and sto["converged"] == 1
+        assert abs(st["newton_iters"] - sto["newton_iters"]) <= max(5, 0.1 * sto["newton_iters"])
+    assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6
+
+
 def test_pd_matrix_matches_oracle():
     """The PD stepper's matrix (mass + dt^2 kappa Laplacian, DBC identity) through a PCG solve: the PD
     preconditioner applied to a vector equals the oracle's solve with its PD matrix."""
