@@ -297,6 +297,151 @@ void element_stiffness(const double* F, const double* Dminv, double lambda, doub
         }
 }
 
+// ---------------------------------------------------------------- 2D (triangles in the plane)
+// stable_neohookean<2> (stable_neohookean.hpp:23-104): delta = the positive root of
+// (2t+1) d^2 + (2t+2) d - 2t = 0, t = mu/lambda; alpha = (1 - 1/(2 + delta)) mu/lambda + 1;
+// Psi = (mu (Ic - 2) + lambda (J - alpha)^2 - mu log(Ic + delta))/2 - (lambda (1-alpha)^2 - mu log(2 + delta))/2;
+// P = lambda (J - alpha) dJ/dF + mu (1 - 1/(Ic + delta)) F with dJ/dF = [[F11, -F10], [-F01, F00]];
+// H = mu (1 - 1/(Ic+delta)) I + 2 mu/(Ic+delta)^2 f f^T + lambda g g^T + lambda (J - alpha) d2J/dF2
+// (internal_physic.hpp:33-54 partial_determinant / add_HJ); F row-major, flat index r*2+c.
+inline double snh2_delta(double lambda, double mu) {
+  const double t = mu / lambda, a = 2 * t + 1, b = 2 * t + 2, c = -2 * t;
+  return (-b + std::sqrt(b * b - 4 * a * c)) / (2 * a);
+}
+inline double snh2_alpha(double lambda, double mu) {
+  return (1 - 1 / (2 + snh2_delta(lambda, mu))) * mu / lambda + 1;
+}
+inline double snh2_energy(const double* F, double lambda, double mu) {
+  const double del = snh2_delta(lambda, mu), alpha = snh2_alpha(lambda, mu);
+  const double Ic = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const double Jm = F[0] * F[3] - F[1] * F[2] - alpha;
+  const double zero = 0.5 * (lambda * (1 - alpha) * (1 - alpha) - mu * std::log(2 + del));
+  return 0.5 * (mu * (Ic - 2) + lambda * Jm * Jm - mu * std::log(Ic + del)) - zero;
+}
+inline double snh2_energy_scale(const double* F, double lambda, double mu) {
+  const double del = snh2_delta(lambda, mu), alpha = snh2_alpha(lambda, mu);
+  const double Ic = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const double Jm = F[0] * F[3] - F[1] * F[2] - alpha;
+  const double zero = 0.5 * (lambda * (1 - alpha) * (1 - alpha) - mu * std::log(2 + del));
+  return 0.5 * (mu * std::fabs(Ic - 2) + lambda * Jm * Jm + mu * std::fabs(std::log(Ic + del))) + std::fabs(zero);
+}
+inline double snh2_stress(const double* F, double lambda, double mu, double* P) {
+  const double del = snh2_delta(lambda, mu), alpha = snh2_alpha(lambda, mu);
+  const double Ic = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const double Jm = F[0] * F[3] - F[1] * F[2] - alpha;
+  const double dJ[4] = {F[3], -F[2], -F[1], F[0]};
+  const double c = mu * (1.0 - 1.0 / (Ic + del));
+  for (int k = 0; k < 4; ++k) P[k] = lambda * Jm * dJ[k] + c * F[k];
+  return snh2_energy(F, lambda, mu);
+}
+inline void snh2_hessian(const double* F, double lambda, double mu, double* H) {
+  const double del = snh2_delta(lambda, mu), alpha = snh2_alpha(lambda, mu);
+  const double Ic = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const double J = F[0] * F[3] - F[1] * F[2];
+  const double g[4] = {F[3], -F[2], -F[1], F[0]};
+  const double a = mu * (1.0 - 1.0 / (Ic + del)), b = mu * 2.0 / ((Ic + del) * (Ic + del));
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) H[i * 4 + j] = (i == j ? a : 0.0) + b * F[i] * F[j] + lambda * g[i] * g[j];
+  const double sc = lambda * (J - alpha);
+  H[0 * 4 + 3] += sc;
+  H[3 * 4 + 0] += sc;
+  H[1 * 4 + 2] -= sc;
+  H[2 * 4 + 1] -= sc;
+}
+// elast::linear<2> (linear.hpp:23-68) with the 2x2 approx_green_strain
+inline double linear2_energy(const double* F, double lambda, double mu) {
+  const double e00 = F[0] - 1, e11 = F[3] - 1, e01 = 0.5 * (F[1] + F[2]);
+  const double tr = e00 + e11;
+  return mu * (e00 * e00 + e11 * e11 + 2 * e01 * e01) + 0.5 * lambda * tr * tr;
+}
+inline double linear2_stress(const double* F, double lambda, double mu, double* P) {
+  const double e00 = F[0] - 1, e11 = F[3] - 1, e01 = 0.5 * (F[1] + F[2]);
+  const double tr = e00 + e11;
+  P[0] = 2 * mu * e00 + lambda * tr;
+  P[1] = 2 * mu * e01;
+  P[2] = 2 * mu * e01;
+  P[3] = 2 * mu * e11 + lambda * tr;
+  return linear2_energy(F, lambda, mu);
+}
+inline void linear2_hessian(double lambda, double mu, double* H) {
+  for (int k = 0; k < 16; ++k) H[k] = 0;
+  for (int k = 0; k < 4; ++k) H[k * 4 + k] = mu;
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      H[(i * 2 + j) * 4 + (j * 2 + i)] += mu;
+      H[(i * 2 + i) * 4 + (j * 2 + j)] += lambda;
+    }
+}
+inline double model2_energy(int model, const double* F, double l, double m) {
+  return model == 1 ? linear2_energy(F, l, m) : snh2_energy(F, l, m);
+}
+inline double model2_stress(int model, const double* F, double l, double m, double* P) {
+  return model == 1 ? linear2_stress(F, l, m, P) : snh2_stress(F, l, m, P);
+}
+inline double model2_energy_scale(int model, const double* F, double l, double m) {
+  return model == 1 ? linear2_energy(F, l, m) : snh2_energy_scale(F, l, m);
+}
+inline void model2_hessian(int model, const double* F, double l, double m, double* H) {
+  if (model == 1)
+    linear2_hessian(l, m, H);
+  else
+    snh2_hessian(F, l, m, H);
+}
+// the 6x6 triangle stiffness pfpx^T H pfpx (compute_pfpx_2, internal_physic.hpp:79-104), embedded in 3 dofs
+// per vertex (z rows and columns zero): K[(v*3+a)*9 + w*3+b]
+void element_stiffness_2d(const double* F, const double* Dm, double lambda, double mu, bool make_spsd, double* K,
+                          int model) {
+  double H[16], w[4], V[16];
+  model2_hessian(model, F, lambda, mu, H);
+  if (make_spsd) {
+    sym_eigen(4, H, w, V);
+    for (int i = 0; i < 4; ++i) w[i] = std::max(w[i], 1e-3);
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        double t = 0;
+        for (int k = 0; k < 4; ++k) t += V[i * 4 + k] * w[k] * V[j * 4 + k];
+        H[i * 4 + j] = t;
+      }
+  }
+  double D[3][2];
+  for (int j = 0; j < 2; ++j) {
+    D[1][j] = Dm[0 * 2 + j];
+    D[2][j] = Dm[1 * 2 + j];
+    D[0][j] = -(Dm[0 * 2 + j] + Dm[1 * 2 + j]);
+  }
+  for (int k = 0; k < 81; ++k) K[k] = 0;
+  for (int v = 0; v < 3; ++v)
+    for (int a = 0; a < 2; ++a)
+      for (int wv = 0; wv < 3; ++wv)
+        for (int b = 0; b < 2; ++b) {
+          double t = 0;
+          for (int j = 0; j < 2; ++j)
+            for (int l = 0; l < 2; ++l) t += D[v][j] * H[(a * 2 + j) * 4 + b * 2 + l] * D[wv][l];
+          K[(v * 3 + a) * 9 + wv * 3 + b] = t;
+        }
+}
+// p1_element_2d (bilinears.hpp:45-96): |det J| = 2 area; mass |det J| {1/12, 1/24} rho; Laplacian
+// alpha area grad phi_i . grad phi_j
+void element_mass_2d(const double* Xv[3], double rho, double M[9]) {
+  const double J[4] = {Xv[1][0] - Xv[0][0], Xv[2][0] - Xv[0][0], Xv[1][1] - Xv[0][1], Xv[2][1] - Xv[0][1]};
+  const double detJ = std::fabs(J[0] * J[3] - J[1] * J[2]);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) M[i * 3 + j] = (detJ * (i == j ? 1.0 / 12 : 1.0 / 24)) * rho;
+}
+void element_laplace_2d(const double* Xv[3], double alpha, double L[9]) {
+  const double J[4] = {Xv[1][0] - Xv[0][0], Xv[2][0] - Xv[0][0], Xv[1][1] - Xv[0][1], Xv[2][1] - Xv[0][1]};
+  const double det = J[0] * J[3] - J[1] * J[2];
+  const double iJ[4] = {J[3] / det, -J[1] / det, -J[2] / det, J[0] / det};
+  double g[3][2];
+  for (int k = 0; k < 2; ++k) {
+    g[1][k] = iJ[0 * 2 + k];
+    g[2][k] = iJ[1 * 2 + k];
+    g[0][k] = -(g[1][k] + g[2][k]);
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) L[i * 3 + j] = alpha * std::fabs(det) / 2.0 * (g[i][0] * g[j][0] + g[i][1] * g[j][1]);
+}
+
 // ---------------------------------------------------------------------------
 // BLAS-1 helpers
 // ---------------------------------------------------------------------------
@@ -328,8 +473,9 @@ struct orc_ts {
   std::vector<int32_t> row_ptr, col_idx;
   Vec ncg_L;                  // NCG preconditioner factor on the CSR pattern (empty: identity)
   int model = 0;              // elastic model: 0 stable Neo-Hookean, 1 linear
-  int cv = 4;                 // vertices per cell: 4 (tets) or 2 (springs)
+  int cv = 4;                 // vertices per cell: 4 (tets), 3 (triangles in the plane) or 2 (springs)
   bool springs = false;       // mass-spring system: cells are springs, lumped vertex masses
+  bool tri2d = false;         // 2D triangles: x, y dofs (the z dof of every vertex carries no force)
   Vec sp_rest, sp_k, vmass;
   Vec mass_vals, massf_vals, sys_vals, pd_vals;
   std::vector<int32_t> hess_dst;            // [nt*144] CSR slot of each local entry
@@ -434,6 +580,22 @@ void spmv(const orc_ts& s, const Vec& vals, const double* x, double* y) {
 // deformation_gradient::def_grad_task (def_grad.hpp:93-132): F = Ds * Dminv, x = X + u
 void update_def_grad(orc_ts& s, const Vec& u) {
   if (s.springs) return;
+  if (s.tri2d) {
+    for (int e = 0; e < s.nt; ++e) {
+      const int32_t* c = &s.cells[e * 3];
+      double x[3][2];
+      for (int i = 0; i < 3; ++i)
+        for (int d = 0; d < 2; ++d) x[i][d] = s.X[c[i] * 3 + d] + u[c[i] * 3 + d];
+      double Ds[4];
+      for (int r = 0; r < 2; ++r)
+        for (int k = 0; k < 2; ++k) Ds[r * 2 + k] = x[k + 1][r] - x[0][r];
+      const double* Dm = &s.dminv[e * 9];
+      double* F = &s.defgrad[e * 9];
+      for (int r = 0; r < 2; ++r)
+        for (int cc = 0; cc < 2; ++cc) F[r * 2 + cc] = Ds[r * 2 + 0] * Dm[0 * 2 + cc] + Ds[r * 2 + 1] * Dm[1 * 2 + cc];
+    }
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < s.nt; ++e) {
     const int32_t* c = &s.cells[e * 4];
@@ -489,6 +651,14 @@ double spring_energy(const orc_ts& s, const Vec& u, Vec* lf, double* scale) {
 
 double elastic_energy(orc_ts& s, double* scale) {
   double sum = 0, sc = 0;
+  if (s.tri2d) {
+    for (int e = 0; e < s.nt; ++e) {
+      sum += model2_energy(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+      sc += model2_energy_scale(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+    }
+    if (scale) *scale = sc * s.dt * s.dt;
+    return sum * s.dt * s.dt;
+  }
 #pragma omp parallel for reduction(+ : sum, sc) schedule(static)
   for (int e = 0; e < s.nt; ++e) {
     sum += model_energy(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
@@ -522,6 +692,24 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
   const double inertia_energy = inertia_term(s, s.next, &f);
   // PK1 per element (time_step.hpp:603) and the local-force conversion
   // stress_element_to_vertex (time_step.hpp:62-90): rows 1..3 = (P Dminv^T) columns, row 0 = -sum
+  if (s.tri2d) {
+    for (int e = 0; e < s.nt; ++e) {
+      double P[4];
+      s.local_energy[e] = model2_stress(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e), P);
+      const double* Dm = &s.dminv[e * 9];
+      double* lf = &s.local_force[e * 9];
+      for (int j = 0; j < 3; ++j) lf[0 * 3 + j] = lf[1 * 3 + j] = lf[2 * 3 + j] = 0;
+      for (int j = 0; j < 2; ++j) {
+        double tot = 0;
+        for (int i = 1; i < 3; ++i) {
+          const double v = P[j * 2 + 0] * Dm[(i - 1) * 2 + 0] + P[j * 2 + 1] * Dm[(i - 1) * 2 + 1];
+          lf[i * 3 + j] = v;
+          tot += v;
+        }
+        lf[0 * 3 + j] = -tot;
+      }
+    }
+  } else
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < s.nt; ++e) {
     double P[9];
@@ -547,7 +735,7 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
     double acc[3] = {0, 0, 0};
     for (int k = s.fcon_ptr[v]; k < s.fcon_ptr[v + 1]; ++k) {
       const int t = s.fcon_src[k];
-      const int e = t / 4;
+      const int e = t / s.cv;
       for (int d = 0; d < 3; ++d) acc[d] += s.vol[e] * s.local_force[t * 3 + d];
     }
     for (int d = 0; d < 3; ++d) f[v * 3 + d] += a * acc[d];
@@ -559,7 +747,9 @@ double energy_and_gradients(orc_ts& s, bool F_updated) {
   double elast = 0, sc = 0;
   for (int e = 0; e < s.nt; ++e) {
     elast += s.local_energy[e] * s.vol[e];
-    sc += model_energy_scale(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e)) * s.vol[e];
+    sc += (s.tri2d ? model2_energy_scale(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e))
+                   : model_energy_scale(s.model, &s.defgrad[e * 9], s.lam(e), s.mu(e))) *
+          s.vol[e];
   }
   s.energy_scale = inertia_energy + sc * s.dt * s.dt;
   return inertia_energy + elast * s.dt * s.dt;
@@ -607,10 +797,17 @@ void update_hessian(orc_ts& s, bool F_updated, bool make_spsd, bool filter) {
     return;
   }
   if (!F_updated) update_def_grad(s, s.next);
+  const int LL = 9 * s.cv * s.cv;
+  if (s.tri2d) {
+    for (int e = 0; e < s.nt; ++e)
+      element_stiffness_2d(&s.defgrad[e * 9], &s.dminv[e * 9], s.lam(e), s.mu(e), make_spsd,
+                           &s.local_K[(size_t)e * LL], s.model);
+  } else {
 #pragma omp parallel for schedule(dynamic, 256)
-  for (int e = 0; e < s.nt; ++e)
-    element_stiffness(&s.defgrad[e * 9], &s.dminv[e * 9], s.lam(e), s.mu(e), make_spsd, &s.local_K[(size_t)e * 144],
-                      s.model);
+    for (int e = 0; e < s.nt; ++e)
+      element_stiffness(&s.defgrad[e * 9], &s.dminv[e * 9], s.lam(e), s.mu(e), make_spsd,
+                        &s.local_K[(size_t)e * 144], s.model);
+  }
   const double a = s.dt * s.dt;
   const int nnz = (int)s.col_idx.size();
 #pragma omp parallel for schedule(static)
@@ -618,7 +815,7 @@ void update_hessian(orc_ts& s, bool F_updated, bool make_spsd, bool filter) {
     double acc = 0;
     for (int q = s.hcon_ptr[k]; q < s.hcon_ptr[k + 1]; ++q) {
       const int t = s.hcon_src[q];
-      acc += s.vol[t / 144] * s.local_K[t];
+      acc += s.vol[t / LL] * s.local_K[t];
     }
     s.sys_vals[k] = s.mass_vals[k] + a * acc;
   }
@@ -811,6 +1008,19 @@ void orc_lame(double E, double nu, double* lambda, double* mu) {
   *lambda = E * nu / ((1 + nu) * (1 - 2 * nu));
 }
 double orc_snh_energy(const double F[9], double lambda, double mu) { return snh_energy(F, lambda, mu); }
+double orc_snh2_energy(const double F[4], double lambda, double mu) { return snh2_energy(F, lambda, mu); }
+double orc_snh2_stress(const double F[4], double lambda, double mu, double P[4]) {
+  return snh2_stress(F, lambda, mu, P);
+}
+void orc_snh2_hessian(const double F[4], double lambda, double mu, double H[16]) { snh2_hessian(F, lambda, mu, H); }
+double orc_linear2_stress(const double F[4], double lambda, double mu, double P[4]) {
+  return linear2_stress(F, lambda, mu, P);
+}
+void orc_linear2_hessian(double lambda, double mu, double H[16]) { linear2_hessian(lambda, mu, H); }
+void orc_element_stiffness_2d(const double F[4], const double Dminv[4], double lambda, double mu, int make_spsd,
+                              int model, double K[81]) {
+  element_stiffness_2d(F, Dminv, lambda, mu, make_spsd != 0, K, model);
+}
 double orc_snh_stress(const double F[9], double lambda, double mu, double P[9]) {
   return snh_stress(F, lambda, mu, P);
 }
@@ -876,6 +1086,32 @@ orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double
                  &s->ext_accel, &s->forces})
     v->assign(s->n, 0.0);
   orc_reset(s);  // the constructor calls reset() (time_step.hpp:260-265)
+  return s;
+}
+
+orc_ts* orc_create_2d(const double* X2, int nv, const int32_t* tris, int nt, double dt, double E, double nu,
+                      double rho) {
+  orc_ts* s = new orc_ts;
+  s->tri2d = true;
+  s->cv = 3;
+  s->nv = nv;
+  s->nt = nt;
+  s->n = nv * 3;
+  s->X.assign((size_t)nv * 3, 0.0);
+  for (int v = 0; v < nv; ++v) {
+    s->X[3 * v] = X2[2 * v];
+    s->X[3 * v + 1] = X2[2 * v + 1];
+  }
+  s->cells.assign(tris, tris + (size_t)nt * 3);
+  s->dt = dt;
+  s->E = E;
+  s->nu = nu;
+  s->rho = rho;
+  s->dof_type.assign(s->n, 0);
+  for (Vec* v : {&s->dbc_values, &s->deformation, &s->prev_deform, &s->inertia, &s->next, &s->velocity,
+                 &s->ext_accel, &s->forces})
+    v->assign(s->n, 0.0);
+  orc_reset(s);
   return s;
 }
 
@@ -987,6 +1223,51 @@ void orc_reset(orc_ts* s) {
     filter_dbc_matrix(*s, s->massf_vals);
     s->sys_vals = s->mass_vals;
     double asum = 0;
+    for (double v : s->mass_vals) asum += std::fabs(v);
+    s->abs_tol = asum / 3.0 * s->rtol;
+    s->mass_third = asum / 3.0;
+    s->has_reset = true;
+    s->pd_ready = false;
+    return;
+  }
+  if (s->tri2d) {
+    // rest shape (def_grad.hpp:56-91, rest_vol.hpp:34-54 with PhysicalDim 2): Dm^-1 (row-major 2x2 in the
+    // first 4 of 9 slots), area |det Dm| / 2; consistent mass from p1_element_2d
+    s->dminv.assign((size_t)s->nt * 9, 0);
+    s->vol.assign(s->nt, 0);
+    s->defgrad.assign((size_t)s->nt * 9, 0);
+    s->local_energy.assign(s->nt, 0);
+    s->local_force.assign((size_t)s->nt * 9, 0);
+    s->local_K.assign((size_t)s->nt * 81, 0);
+    for (Vec* v : {&s->inertia, &s->next, &s->forces}) v->assign(s->n, 0.0);
+    for (int e = 0; e < s->nt; ++e) {
+      const int32_t* c = &s->cells[e * 3];
+      const double D[4] = {s->X[c[1] * 3] - s->X[c[0] * 3], s->X[c[2] * 3] - s->X[c[0] * 3],
+                           s->X[c[1] * 3 + 1] - s->X[c[0] * 3 + 1], s->X[c[2] * 3 + 1] - s->X[c[0] * 3 + 1]};
+      const double det = D[0] * D[3] - D[1] * D[2];
+      double* Dm = &s->dminv[e * 9];
+      Dm[0] = D[3] / det;
+      Dm[1] = -D[1] / det;
+      Dm[2] = -D[2] / det;
+      Dm[3] = D[0] / det;
+      s->vol[e] = std::fabs(det / 2);
+    }
+    build_pattern(*s);
+    const int nnz = (int)s->col_idx.size();
+    s->mass_vals.assign(nnz, 0.0);
+    for (int e = 0; e < s->nt; ++e) {
+      const int32_t* c = &s->cells[e * 3];
+      const double* Xv[3] = {&s->X[c[0] * 3], &s->X[c[1] * 3], &s->X[c[2] * 3]};
+      double M[9];
+      element_mass_2d(Xv, s->rho, M);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int a = 0; a < 3; ++a) s->mass_vals[s->hess_dst[(size_t)e * 81 + (i * 3 + a) * 9 + j * 3 + a]] += M[i * 3 + j];
+    }
+    s->massf_vals = s->mass_vals;
+    filter_dbc_matrix(*s, s->massf_vals);
+    s->sys_vals = s->mass_vals;
+    double asum = 0;  // asum(mass) / dofs_per_node (time_step.hpp:490): the z copies add 1/3 of it
     for (double v : s->mass_vals) asum += std::fabs(v);
     s->abs_tol = asum / 3.0 * s->rtol;
     s->mass_third = asum / 3.0;
@@ -1402,6 +1683,21 @@ void orc_pd_matrix_values(orc_ts* s, double* out) {
   const double kappa_u = (lam_slot + 5.0 / 6.0 * mu_slot) + 2.0 * (4.0 / 3.0 * mu_slot);
   const int nnz = (int)s->col_idx.size();
   Vec vals(nnz, 0.0);
+  if (s->tri2d) {
+    for (int e = 0; e < s->nt; ++e) {
+      const int32_t* c = &s->cells[e * 3];
+      const double* Xv[3] = {&s->X[c[0] * 3], &s->X[c[1] * 3], &s->X[c[2] * 3]};
+      double M[9], L[9];
+      element_mass_2d(Xv, s->rho, M);
+      const double kappa =
+          s->pd_diff_mode == 2 ? (s->lam(e) + 5.0 / 6.0 * s->mu(e)) + 2.0 * (4.0 / 3.0 * s->mu(e)) : kappa_u;
+      element_laplace_2d(Xv, s->dt * s->dt * kappa, L);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int a = 0; a < 3; ++a)
+            vals[s->hess_dst[(size_t)e * 81 + (i * 3 + a) * 9 + j * 3 + a]] += M[i * 3 + j] + L[i * 3 + j];
+    }
+  } else
   for (int e = 0; e < s->nt; ++e) {
     const int32_t* c = &s->cells[e * 4];
     const double* Xv[4] = {&s->X[c[0] * 3], &s->X[c[1] * 3], &s->X[c[2] * 3], &s->X[c[3] * 3]};

@@ -100,6 +100,19 @@ void orc_default_params(orc_params* p);
 
 orc_ts* orc_create(const double* X, int nv, const int32_t* cells, int nt, double dt, double E, double nu,
                    double rho);
+/* 2D triangles in the plane (basic_time_step<Scalar, Device, 2, 3, ...>): X2 [nv][2], tris [nt][3]; the
+ * state vectors keep 3 entries per vertex with z identically zero */
+orc_ts* orc_create_2d(const double* X2, int nv, const int32_t* tris, int nt, double dt, double E, double nu,
+                      double rho);
+/* 2D element models on a row-major 2x2 F (Hessian flat index r*2+c) */
+double orc_snh2_energy(const double F[4], double lambda, double mu);
+double orc_snh2_stress(const double F[4], double lambda, double mu, double P[4]);
+void orc_snh2_hessian(const double F[4], double lambda, double mu, double H[16]);
+double orc_linear2_stress(const double F[4], double lambda, double mu, double P[4]);
+void orc_linear2_hessian(double lambda, double mu, double H[16]);
+/* 6x6 triangle stiffness embedded in 9x9 (3 dofs per vertex), Dm^-1 row-major 2x2 */
+void orc_element_stiffness_2d(const double F[4], const double Dminv[4], double lambda, double mu, int make_spsd,
+                              int model, double K[81]);
 /* a mass-spring system (no reference counterpart): springs [ns][2], rest lengths from X, stiffness k, vertex
  * masses vmass[nv] (or m each), lumped mass, energy 1/2|x - x~|_M^2 + dt^2 sum k/2 (|x_i - x_j| - L)^2 */
 orc_ts* orc_create_springs(const double* X, int nv, const int32_t* springs, int ns, double k, const double* vmass,

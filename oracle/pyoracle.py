@@ -111,6 +111,13 @@ def lib():
         "orc_element_stiffness": (None, [dp, dp, C.c_double, C.c_double, C.c_int, dp]),
         "orc_default_params": (None, [C.POINTER(OrcParams)]),
         "orc_create": (vp, [dp, C.c_int, ip, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "orc_create_2d": (vp, [dp, C.c_int, ip, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "orc_snh2_energy": (C.c_double, [dp, C.c_double, C.c_double]),
+        "orc_snh2_stress": (C.c_double, [dp, C.c_double, C.c_double, dp]),
+        "orc_snh2_hessian": (None, [dp, C.c_double, C.c_double, dp]),
+        "orc_linear2_stress": (C.c_double, [dp, C.c_double, C.c_double, dp]),
+        "orc_linear2_hessian": (None, [C.c_double, C.c_double, dp]),
+        "orc_element_stiffness_2d": (None, [dp, dp, C.c_double, C.c_double, C.c_int, C.c_int, dp]),
         "orc_create_springs": (
             vp,
             [dp, C.c_int, ip, C.c_int, C.c_double, C.c_void_p, C.c_double, C.c_double],
@@ -225,6 +232,41 @@ def snh_hessian(F, lam, mu):
     return H.reshape(9, 9)
 
 
+def snh2_energy(F, lam, mu):
+    return lib().orc_snh2_energy(_f64(F).reshape(-1), lam, mu)
+
+
+def snh2_stress(F, lam, mu):
+    P = np.zeros(4)
+    e = lib().orc_snh2_stress(_f64(F).reshape(-1), lam, mu, P)
+    return e, P.reshape(2, 2)
+
+
+def snh2_hessian(F, lam, mu):
+    H = np.zeros(16)
+    lib().orc_snh2_hessian(_f64(F).reshape(-1), lam, mu, H)
+    return H.reshape(4, 4)
+
+
+def linear2_stress(F, lam, mu):
+    P = np.zeros(4)
+    e = lib().orc_linear2_stress(_f64(F).reshape(-1), lam, mu, P)
+    return e, P.reshape(2, 2)
+
+
+def linear2_hessian(lam, mu):
+    H = np.zeros(16)
+    lib().orc_linear2_hessian(lam, mu, H)
+    return H.reshape(4, 4)
+
+
+def element_stiffness_2d(F, Dminv, lam, mu, make_spsd=True, model=0):
+    K = np.zeros(81)
+    lib().orc_element_stiffness_2d(_f64(F).reshape(-1), _f64(Dminv).reshape(-1), lam, mu, int(make_spsd),
+                                   int(model), K)
+    return K.reshape(9, 9)
+
+
 def linear_stress(F, lam, mu):
     P = np.zeros(9)
     e = lib().orc_linear_stress(_f64(F, (9,)), lam, mu, P)
@@ -292,6 +334,23 @@ class OracleTimeStep:
         self.n = 3 * self.nv
         self._h = L.orc_create(X.reshape(-1), self.nv, cells.reshape(-1), self.nt, time_step, youngs, poisson, density)
         self.X, self.cells = X, cells
+
+    @classmethod
+    def tri2d(cls, X2, tris, time_step=1e-3, youngs=1e6, poisson=0.33, density=1e3):
+        """2D triangles in the plane (basic_time_step with PhysicalDim 2, TopologyDim 3): X2 [V, 2],
+        tris [T, 3]; state vectors are [V, 3] with z identically zero."""
+        L = lib()
+        self = cls.__new__(cls)
+        self._L = L
+        X2 = _f64(X2).reshape(-1, 2)
+        T = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+        self.nv, self.nt = X2.shape[0], T.shape[0]
+        self.n = 3 * self.nv
+        self._h = L.orc_create_2d(X2.reshape(-1), self.nv, T.reshape(-1), self.nt, time_step, youngs, poisson,
+                                  density)
+        self.X = np.concatenate([X2, np.zeros((self.nv, 1))], axis=1)
+        self.cells = T
+        return self
 
     @classmethod
     def springs(cls, X, springs, stiffness, vertex_mass=None, mass=None, time_step=1e-2):

@@ -77,6 +77,18 @@ def unit_box(nx: int = 2, ny: int = 2, nz: int = 2):
     return X, tets.reshape(-1, 4).astype(np.int32)
 
 
+def unit_square(nx: int = 2, ny: int = 2):
+    """Triangles of the unit square: an nx x ny vertex grid (vertex (i, j) = i * ny + j at (i/(nx-1),
+    j/(ny-1))), each cell cut along its (i, j)-(i+1, j+1) diagonal into two counter-clockwise triangles."""
+    xs = np.linspace(0.0, 1.0, nx)
+    ys = np.linspace(0.0, 1.0, ny)
+    X = np.stack(np.meshgrid(xs, ys, indexing="ij"), axis=-1).reshape(-1, 2)
+    idx = np.arange(nx * ny, dtype=np.int32).reshape(nx, ny)
+    a, b, c, d = idx[:-1, :-1], idx[1:, :-1], idx[1:, 1:], idx[:-1, 1:]
+    T = np.concatenate([np.stack([a, b, c], -1).reshape(-1, 3), np.stack([a, c, d], -1).reshape(-1, 3)])
+    return X, T.astype(np.int32)
+
+
 def tetra():
     """ssim::mesh::tetra (common_shapes.hpp:134-145)."""
     X = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
