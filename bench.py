@@ -52,6 +52,8 @@ def make_scene(name):
         return scenes.batch_cubes()
     if name == "cloth512":
         return scenes.cloth()
+    if name == "sheet2d":
+        return scenes.sheet2d(1001, 501)
     if name == "cloth_small":
         return scenes.cloth(128)
     raise SystemExit(f"unknown workload {name}")
@@ -131,8 +133,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-class _SpringFacade:
-    """The calls the e2e loop makes, on a spring-system TimeStep (the libssim facade is tets only)."""
+class _HandleFacade:
+    """The calls the e2e loop makes, on a TimeStep handle (for the systems and steppers the libssim facade
+    does not cover)."""
 
     def __init__(self, ts):
         self.step_ = ts
@@ -221,8 +224,9 @@ def run_gpu_arm(args, scene):
 
     fixed = np.asarray(scene["fixed"], dtype=np.int32)
     pin_targ = torch.zeros((3, fixed.size), dtype=torch.float64).pin_memory()
-    if scene.get("springs"):  # no reference-facing spring API: the TimeStep handle itself
-        s = _SpringFacade(scenes.build_timestep(scene, precision="mixed", stepper=args.stepper, params=params))
+    if scene.get("springs") or scene.get("tri2d") or args.stepper != "newton":
+        # springs and triangles have no libssim facade, and tet_newton_cuda is Newton: the TimeStep handle
+        s = _HandleFacade(scenes.build_timestep(scene, precision="mixed", stepper=args.stepper, params=params))
     else:
         s = fem.tet_newton_cuda(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"],
                                 precision="mixed", params=params)
@@ -343,7 +347,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam1m",
-                    help="beam1m (default), beam_small, cube10, bar, batch, cloth512, cloth_small")
+                    help="beam1m (default), beam_small, cube10, bar, batch, cloth512, cloth_small, sheet2d")
     ap.add_argument("--stepper", default="newton", choices=["newton", "lbfgs", "pd", "ncg", "ncg_ext"],
                     help="stepper of the timed GPU runs (the CPU baseline is Newton)")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
@@ -365,7 +369,7 @@ def main():
 
     scene = make_scene(args.workload)
     T, V = scene["cells"].shape[0], scene["X"].shape[0]
-    cells_key = "springs" if scene.get("springs") else "tets"
+    cells_key = "springs" if scene.get("springs") else ("triangles" if scene.get("tri2d") else "tets")
 
     if args.impl == "reference":
         if rank == 0:

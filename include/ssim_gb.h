@@ -166,6 +166,22 @@ SSIM_GB_API ssim_gb_status ssim_gb_create(const double* vertices, int32_t num_ve
 SSIM_GB_API ssim_gb_status ssim_gb_create_springs(const double* vertices, int32_t num_vertices, const int32_t* springs,
                                                   int32_t num_springs, double stiffness, const double* vertex_mass,
                                                   double mass, double time_step, ssim_gb_timestep** out);
+/* 2D triangles in the plane: basic_time_step<Scalar, Device, 2, 3, ElastModel, ...> (time_step.hpp:168-715
+ * with PhysicalDim 2, TopologyDim 3; rest shape def_grad.hpp:56-91 and rest_vol.hpp:34-54 in 2D, consistent
+ * mass p1_element_2d bilinears.hpp:45-96, stable_neohookean<2> / linear<2>).  vertices [V][2], triangles
+ * [T][3].  The handle keeps 3 dofs per vertex: fields are [V,3] with z identically zero, the system matrix
+ * carries the mass alone on the z dofs; ssim_gb_get_csr_2d gives the reference's 2-dof CSR.  The adjoint
+ * and the FP32 element phase of the mixed steppers are tets only. */
+SSIM_GB_API ssim_gb_status ssim_gb_create_2d(const double* vertices, int32_t num_vertices, const int32_t* triangles,
+                                             int32_t num_triangles, double time_step, double youngs, double poisson,
+                                             double density, ssim_gb_timestep** out);
+/* physical dimension of a handle: 3 (tets, springs) or 2 (triangles) */
+SSIM_GB_API ssim_gb_status ssim_gb_get_dim(const ssim_gb_timestep* h, int32_t* dim);
+/* the reference's 2-dof CSR of a 2D handle's matrix `which` (SSIM_GB_SYSTEM, _MASS, _MASS_FILTERED):
+ * row 2u+a holds columns {2w+b : w in N(u) sorted, b < 2}; row_ptr [2V+1], col_idx and values [nnz2] with
+ * nnz2 = 4/9 of ssim_gb_sizes' nnz; any of the three outputs may be NULL */
+SSIM_GB_API ssim_gb_status ssim_gb_get_csr_2d(ssim_gb_timestep* h, int32_t which, int32_t* row_ptr, int32_t* col_idx,
+                                              double* values);
 SSIM_GB_API ssim_gb_status ssim_gb_destroy(ssim_gb_timestep* h);
 SSIM_GB_API ssim_gb_status ssim_gb_sizes(const ssim_gb_timestep* h, int32_t* num_vertices, int32_t* num_cells,
                              int32_t* num_dofs, int64_t* nnz);
@@ -240,7 +256,7 @@ SSIM_GB_API ssim_gb_status ssim_gb_field_device_ptr(ssim_gb_timestep* h, int32_t
 SSIM_GB_API ssim_gb_status ssim_gb_get_csr_pattern(const ssim_gb_timestep* h, int32_t* row_ptr, int32_t* col_idx);
 SSIM_GB_API ssim_gb_status ssim_gb_get_matrix_values(ssim_gb_timestep* h, int32_t which, double* values /* [nnz] */);
 SSIM_GB_API ssim_gb_status ssim_gb_get_rest_volume(const ssim_gb_timestep* h, double* out /* [T] */);
-SSIM_GB_API ssim_gb_status ssim_gb_get_dminv(const ssim_gb_timestep* h, double* out /* [T,3,3] */);
+SSIM_GB_API ssim_gb_status ssim_gb_get_dminv(const ssim_gb_timestep* h, double* out /* [T,3,3]; 2D: [T,2,2] */);
 /* y = A x with the current system matrix (or mass) in the handle's precision, host buffers [V,3] */
 SSIM_GB_API ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, const double* x, double* y);
 /* PCG on the current system matrix: x [V,3] in/out (initial guess zero if x_is_guess == 0) */

@@ -118,6 +118,12 @@ _SIGS = {
         C.c_int,
         [_D, C.c_int32, _I, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.POINTER(_H)],
     ),
+    "ssim_gb_create_2d": (
+        C.c_int,
+        [_D, C.c_int32, _I, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.POINTER(_H)],
+    ),
+    "ssim_gb_get_dim": (C.c_int, [_H, C.POINTER(C.c_int32)]),
+    "ssim_gb_get_csr_2d": (C.c_int, [_H, C.c_int32, _I, _I, _D]),
     "ssim_gb_create_springs": (
         C.c_int,
         [_D, C.c_int32, _I, C.c_int32, C.c_double, _D, C.c_double, C.c_double, C.POINTER(_H)],

@@ -45,6 +45,7 @@ struct ElemFP64 {
   const double* alpha;  // 1 + 3/4 mu / lambda
   const double* psi0;   // stable Neo-Hookean energy at F = I
   int model;            // 0 stable Neo-Hookean, 1 linear
+  const double* delta;  // triangles: the 2D stable Neo-Hookean log offset per element (tets: 1, unused)
 };
 
 struct ElemFP32 {
@@ -126,6 +127,16 @@ template <typename S>
 void launch_spring_hessian(const SpringData& sp, const double* u, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
 void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
                           double* g, const Reduce& red, cudaStream_t st);
+
+// ---------------- 2D triangles (kernels_tri.cu) ----------------
+// cells int4 (x, y, z = the triangle), dminv rows 0..3 = the row-major 2x2 Dm^-1, vol = area; local forces
+// lf[t][3][3] (z = 0), element blocks Kbuf[t][6][9] (the 6 upper 3x3 vertex blocks, z rows/columns 0)
+template <typename SD>
+void launch_tri_energy_grad(const ElemFP64& el, const double* u, const double* xt, const V4<SD>* d, double alpha,
+                            double dt2, double rho, double* lf, bool with_forces, bool trial, const Reduce& red,
+                            cudaStream_t st);
+template <typename S>
+void launch_tri_hessian(const ElemFP64& el, const double* u, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
 
 // ---------------- element Hessian ----------------
 template <typename S>

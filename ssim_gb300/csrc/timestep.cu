@@ -99,7 +99,7 @@ struct TimeStep {
   // ---- device: mesh, element constants
   DBuf<double> dX;
   DBuf<int4> dcells;
-  DBuf<double> dminv, vol, lam, mu, snh_alpha, snh_psi0;
+  DBuf<double> dminv, vol, lam, mu, snh_alpha, snh_psi0, snh_delta;
   DBuf<float> fdminv, fvol, flam, fmu;
   // ---- device: state [n] (time_step.hpp:668-679)
   DBuf<double> deformation, prev_deform, inertia, next, velocity, ext_accel, forces, dbc_values, work;
@@ -147,6 +147,8 @@ struct TimeStep {
   int elastic_model = SSIM_GB_MODEL_STABLE_NEOHOOKEAN;  // ElastModel of basic_time_step
   // mass-spring system instead of tets (cells are the springs' vertex pairs)
   bool springs = false;
+  // 2D triangles in the plane (cells are triangles; the z dof of every vertex carries no force)
+  bool tri2d = false;
   DBuf<int2> sp_ends;
   DBuf<double> sp_rest, sp_k, vmass;
   DBuf<float4> sp_e0, sp_lf32;
@@ -167,6 +169,9 @@ struct TimeStep {
     } else if (springs)
       launch_spring_energy_grad<S>(spd(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt, forces ? lf.p : nullptr,
                                    forces, true, red(), stream);
+    else if (tri2d)
+      launch_tri_energy_grad<S>(e64(), next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr, forces,
+                                true, red(), stream);
     else if (fp32)
       launch_elem_energy_grad32<S>(e64(), e32s(), next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr,
                                    forces, true, red(), stream);
@@ -192,6 +197,10 @@ struct TimeStep {
   }
   // mass per upper slot: consistent (tets) or lumped on the diagonal (springs)
   void slot_mass_values(std::vector<double>& smass) {
+    if (tri2d) {
+      slot_masses_2d(topo, detJ, rho, smass);
+      return;
+    }
     if (!springs) {
       slot_masses(topo, detJ, rho, smass);
       return;
@@ -223,7 +232,7 @@ struct TimeStep {
   bool mixed() const { return precision == SSIM_GB_MIXED; }
   Reduce red() { return Reduce{partials.p, counter.p, sc.p}; }
   ElemFP64 e64() const {
-    return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p, snh_alpha.p, snh_psi0.p, elastic_model};
+    return ElemFP64{nt, dcells.p, dminv.p, vol.p, lam.p, mu.p, snh_alpha.p, snh_psi0.p, elastic_model, snh_delta.p};
   }
   ElemFP32 e32() const { return ElemFP32{nt, dcells.p, fdminv.p, fvol.p, flam.p, fmu.p}; }
   ElemFP32 e32s() const { return e32(); }
@@ -326,6 +335,49 @@ struct TimeStep {
     reset(SSIM_GB_STEPPER_NONE);
   }
 
+  // 2D triangles: vertices [nv][2] (embedded at z = 0), triangles [nt][3] (basic_time_step with
+  // PhysicalDim 2, TopologyDim 3); Dm^-1 row-major 2x2 in dminv rows 0..3, vol = area, detJ = 2 area
+  void create_2d(const double* X2, int nv_, const int32_t* tris, int nt_, double dt_, double E_, double nu_,
+                 double rho_) {
+    if (!X2) throw invalid_argument("null mesh pointer");
+    if (nv_ <= 0) throw invalid_argument("mesh must have at least one vertex and one cell");
+    E = E_;
+    nu = nu_;
+    rho = rho_;
+    tri2d = true;
+    std::vector<double> X3(3 * (size_t)nv_, 0.0);
+    for (int v = 0; v < nv_; ++v) {
+      X3[3 * (size_t)v] = X2[2 * (size_t)v];
+      X3[3 * (size_t)v + 1] = X2[2 * (size_t)v + 1];
+    }
+    init_common(X3.data(), nv_, tris, nt_, 3, dt_);
+    std::vector<int4> c4(nt);
+    for (int e = 0; e < nt; ++e) c4[e] = make_int4(cells[3 * e], cells[3 * e + 1], cells[3 * e + 2], cells[3 * e]);
+    dcells.upload(c4, stream);
+    std::vector<double> dm(9 * (size_t)nt, 0.0);
+    detJ.assign(nt, 0);
+    vol_h.assign(nt, 0);
+    for (int e = 0; e < nt; ++e) {
+      const double* x0 = &X[3 * (size_t)cells[3 * e]];
+      const double* x1 = &X[3 * (size_t)cells[3 * e + 1]];
+      const double* x2 = &X[3 * (size_t)cells[3 * e + 2]];
+      const double D[4] = {x1[0] - x0[0], x2[0] - x0[0], x1[1] - x0[1], x2[1] - x0[1]};
+      const double det = D[0] * D[3] - D[1] * D[2];
+      if (!(det != 0)) throw invalid_argument("degenerate triangle " + std::to_string(e));
+      const double B[4] = {D[3] / det, -D[1] / det, -D[2] / det, D[0] / det};
+      for (int k = 0; k < 4; ++k) dm[(size_t)k * nt + e] = B[k];
+      detJ[e] = std::fabs(det);
+      vol_h[e] = std::fabs(det / 2);
+    }
+    dminv.upload(dm, stream);
+    vol.upload(vol_h, stream);
+    std::vector<float> f(dm.begin(), dm.end());
+    fdminv.upload(f, stream);
+    std::vector<float> fv(vol_h.begin(), vol_h.end());
+    fvol.upload(fv, stream);
+    reset(SSIM_GB_STEPPER_NONE);
+  }
+
   void init_common(const double* Xh, int nv_, const int32_t* cells_h, int nt_, int cv, double dt_) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -396,7 +448,20 @@ struct TimeStep {
     lam.upload(l, stream);
     mu.upload(m, stream);
     std::vector<double> al(nt), p0(nt);
-    for (int e = 0; e < nt; ++e) snh_constants<double>(l[e], m[e], al[e], p0[e]);
+    if (tri2d) {
+      // stable_neohookean<2> (stable_neohookean.hpp:30-35, 93-100): delta the positive root of
+      // (2t+1) d^2 + (2t+2) d - 2t = 0 with t = mu / lambda, alpha = (1 - 1/(2 + delta)) mu/lambda + 1
+      std::vector<double> dl(nt);
+      for (int e = 0; e < nt; ++e) {
+        const double t = m[e] / l[e], a = 2 * t + 1, b = 2 * t + 2, c = -2 * t;
+        dl[e] = (-b + std::sqrt(b * b - 4 * a * c)) / (2 * a);
+        al[e] = (1 - 1 / (2 + dl[e])) * m[e] / l[e] + 1;
+        p0[e] = 0.5 * (l[e] * (1 - al[e]) * (1 - al[e]) - m[e] * std::log(2 + dl[e]));
+      }
+      snh_delta.upload(dl, stream);
+    } else {
+      for (int e = 0; e < nt; ++e) snh_constants<double>(l[e], m[e], al[e], p0[e]);
+    }
     snh_alpha.upload(al, stream);
     snh_psi0.upload(p0, stream);
     std::vector<float> lf32(l.begin(), l.end()), mf32(m.begin(), m.end());
@@ -488,8 +553,12 @@ struct TimeStep {
         alpha_e[e] = dt * dt * ((l + 5.0 / 6.0 * m) + 2.0 * (4.0 / 3.0 * m));
       }
     }
-    slot_pd_values(topo, cells.data(), X.data(), detJ, rho, dt * dt * kappa, pd,
-                   params.pd_kappa_mode == 2 ? &alpha_e : nullptr);
+    if (tri2d)
+      slot_pd_values_2d(topo, cells.data(), X.data(), detJ, rho, dt * dt * kappa, pd,
+                        params.pd_kappa_mode == 2 ? &alpha_e : nullptr);
+    else
+      slot_pd_values(topo, cells.data(), X.data(), detJ, rho, dt * dt * kappa, pd,
+                     params.pd_kappa_mode == 2 ? &alpha_e : nullptr);
     std::vector<S> pds(pd.begin(), pd.end());
     s.slot_pd.upload(pds, stream);
     s.pd_vals.alloc(9 * (size_t)topo.nslots);
@@ -539,6 +608,9 @@ struct TimeStep {
     if (springs)
       launch_spring_energy_grad<double>(spd(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt, lf.p, true,
                                         false, red(), stream);
+    else if (tri2d)
+      launch_tri_energy_grad<double>(e64(), next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false, red(),
+                                     stream);
     else if (mixed())
       launch_elem_energy_grad<float>(e64(), dX.p, next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true, false,
                                      red(), stream);
@@ -580,6 +652,12 @@ struct TimeStep {
     else if (springs)
       launch_spring_energy_grad<double>(spd(), u_dev, inertia.p, vmass.p, nv, sd.tmp.p, 0.0, dt * dt, nullptr, false,
                                         true, red(), stream);
+    else if (tri2d && mixed())
+      launch_tri_energy_grad<float>(e64(), u_dev, inertia.p, sf.tmp.p, 0.0, dt * dt, rho, nullptr, false, true, red(),
+                                    stream);
+    else if (tri2d)
+      launch_tri_energy_grad<double>(e64(), u_dev, inertia.p, sd.tmp.p, 0.0, dt * dt, rho, nullptr, false, true,
+                                     red(), stream);
     else if (mixed())
       launch_elem_energy_grad<float>(e64(), dX.p, u_dev, inertia.p, sf.tmp.p, 0.0, dt * dt, rho, nullptr, false,
                                      true, red(), stream);
@@ -601,6 +679,8 @@ struct TimeStep {
     if (profiling) prof_begin(e0, e1);
     if (springs)
       launch_spring_hessian<S>(spd(), next.p, dt * dt, spsd, s.K.p, stream);
+    else if (tri2d)
+      launch_tri_hessian<S>(e64(), next.p, dt * dt, spsd, s.K.p, stream);
     else
       launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream);
     if (profiling) prof_end(e0, e1, PK_HESS, 0);
@@ -788,7 +868,7 @@ struct TimeStep {
     int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
     // mixed precision: FP32 element / spring arithmetic until the residual is within elem32_switch times
     // the target or a line search runs out, FP64 after that and for the stopping test
-    bool e32 = mixed() && params.mixed_elem32 != 0, e32_stall = false;
+    bool e32 = mixed() && params.mixed_elem32 != 0 && !tri2d, e32_stall = false;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
@@ -978,7 +1058,7 @@ struct TimeStep {
     // mixed precision: the inner iterations evaluate energy and forces with FP32 element arithmetic (the
     // small-strain forms); the stopping test is then confirmed with an FP64 evaluation, and if the FP64
     // residual is above the target (or the FP32 residual stalls) the remaining iterations run in FP64
-    bool e32 = mixed() && params.mixed_elem32 != 0;
+    bool e32 = mixed() && params.mixed_elem32 != 0 && !tri2d;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);
@@ -1515,6 +1595,34 @@ ssim_gb_status ssim_gb_destroy(ssim_gb_timestep* h) {
   return SSIM_GB_OK;
 }
 
+ssim_gb_status ssim_gb_create_2d(const double* vertices, int32_t num_vertices, const int32_t* triangles,
+                                 int32_t num_triangles, double time_step, double youngs, double poisson,
+                                 double density, ssim_gb_timestep** out) {
+  if (!out) return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  std::unique_ptr<ssim_gb_timestep> h(new ssim_gb_timestep());
+  try {
+    h->ts.create_2d(vertices, num_vertices, triangles, num_triangles, time_step, youngs, poisson, density);
+  } catch (const std::invalid_argument& e) {
+    return fail(nullptr, SSIM_GB_ERR_INVALID_ARGUMENT, e.what());
+  } catch (const ssim_gb::cuda_error& e) {
+    return fail(nullptr, SSIM_GB_ERR_CUDA, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(nullptr, SSIM_GB_ERR_OUT_OF_MEMORY, "out of memory");
+  } catch (const std::exception& e) {
+    return fail(nullptr, SSIM_GB_ERR_CUDA, e.what());
+  }
+  *out = h.release();
+  return SSIM_GB_OK;
+}
+
+ssim_gb_status ssim_gb_get_dim(const ssim_gb_timestep* h, int32_t* dim) {
+  CHECK_H(h);
+  if (!dim) return fail(const_cast<ssim_gb_timestep*>(h), SSIM_GB_ERR_INVALID_ARGUMENT, "null output");
+  *dim = h->ts.tri2d ? 2 : 3;
+  return SSIM_GB_OK;
+}
+
 ssim_gb_status ssim_gb_sizes(const ssim_gb_timestep* h, int32_t* nv, int32_t* nt, int32_t* ndofs, int64_t* nnz) {
   CHECK_H(h);
   if (nv) *nv = h->ts.nv;
@@ -1866,6 +1974,40 @@ ssim_gb_status ssim_gb_get_matrix_values(ssim_gb_timestep* h, int32_t which, dou
   API_CATCH(h)
 }
 
+ssim_gb_status ssim_gb_get_csr_2d(ssim_gb_timestep* h, int32_t which, int32_t* row_ptr, int32_t* col_idx,
+                                  double* values) {
+  CHECK_H(h);
+  API_TRY
+  TimeStep& t = h->ts;
+  if (!t.tri2d) throw ssim_gb::state_error("the 2-dof CSR is for 2D handles");
+  if (which < 0 || which > 2) throw ssim_gb::invalid_argument("invalid matrix");
+  const ssim_gb::Topology& tp = t.topo;
+  // 3-dof row 3u+a starts at 9 bptr[u] + 3 deg(u) a; 2-dof row 2u+a at 4 bptr[u] + 2 deg(u) a
+  std::vector<double> v3;
+  if (values) {
+    if (!t.has_reset) throw ssim_gb::state_error("matrix values before reset()");
+    v3.resize(9 * (size_t)tp.nnzb);
+    if (t.mixed())
+      export_values<float>(t, which, v3.data());
+    else
+      export_values<double>(t, which, v3.data());
+  }
+  for (int u = 0; u < t.nv; ++u) {
+    const int deg = tp.bptr[u + 1] - tp.bptr[u];
+    for (int a = 0; a < 2; ++a) {
+      const long long r2 = 4LL * tp.bptr[u] + 2LL * deg * a, r3 = 9LL * tp.bptr[u] + 3LL * deg * a;
+      if (row_ptr) row_ptr[2 * u + a] = (int32_t)r2;
+      for (int k = 0; k < deg; ++k)
+        for (int b = 0; b < 2; ++b) {
+          if (col_idx) col_idx[r2 + 2 * k + b] = 2 * tp.bcol[tp.bptr[u] + k] + b;
+          if (values) values[r2 + 2 * k + b] = v3[r3 + 3 * k + b];
+        }
+    }
+  }
+  if (row_ptr) row_ptr[2 * t.nv] = (int32_t)(4 * tp.nnzb);
+  API_CATCH(h)
+}
+
 ssim_gb_status ssim_gb_get_rest_volume(const ssim_gb_timestep* h, double* out) {
   CHECK_H(h);
   if (!out) return fail(const_cast<ssim_gb_timestep*>(h), SSIM_GB_ERR_INVALID_ARGUMENT, "null output");
@@ -1884,8 +2026,9 @@ ssim_gb_status ssim_gb_get_dminv(const ssim_gb_timestep* hc, double* out) {
   std::vector<double> soa(9 * (size_t)t.nt);
   SSIM_CUDA(cudaMemcpyAsync(soa.data(), t.dminv.p, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost, t.stream));
   SSIM_CUDA(cudaStreamSynchronize(t.stream));
+  const int per = t.tri2d ? 4 : 9;
   for (int e = 0; e < t.nt; ++e)
-    for (int k = 0; k < 9; ++k) out[9 * (size_t)e + k] = soa[(size_t)k * t.nt + e];
+    for (int k = 0; k < per; ++k) out[per * (size_t)e + k] = soa[(size_t)k * t.nt + e];
   API_CATCH(h)
 }
 
@@ -1961,7 +2104,7 @@ ssim_gb_status ssim_gb_adjoint_step(ssim_gb_timestep* h, double* ubar, double* v
   if (!ubar || !vbar || !ebar) throw ssim_gb::invalid_argument("null adjoint buffer");
   if (!(rtol > 0) || max_iters <= 0) throw ssim_gb::invalid_argument("invalid adjoint solve tolerance");
   if (!t.has_reset) throw ssim_gb::state_error("adjoint_step() before reset()");
-  if (t.springs) throw ssim_gb::state_error("the adjoint is built for the tet models");
+  if (t.springs || t.tri2d) throw ssim_gb::state_error("the adjoint is built for the tet models");
   int proj = 0;
   const int it = t.mixed() ? t.adjoint_step<float>(ubar, vbar, ebar, rtol, max_iters, &proj)
                            : t.adjoint_step<double>(ubar, vbar, ebar, rtol, max_iters, &proj);

@@ -14,6 +14,9 @@ namespace {
 // local upper block id -> (v, w)
 constexpr int kBlkV[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3};
 constexpr int kBlkW[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+// the same for triangles (3 vertices, 6 upper blocks)
+constexpr int kTriV[6] = {0, 0, 0, 1, 1, 2};
+constexpr int kTriW[6] = {0, 1, 2, 1, 2, 2};
 
 int find_pos(const Topology& t, int u, int w) {
   const int32_t* nb = t.bcol.data() + t.bptr[u];
@@ -24,7 +27,8 @@ int find_pos(const Topology& t, int u, int w) {
 
 void build_topology(int nv, int nt, const int32_t* cells, Topology& t, int cv) {
   if (nv <= 0 || nt <= 0) throw invalid_argument("mesh must have at least one vertex and one cell");
-  if (cv != 4 && cv != 2) throw invalid_argument("cells must have 4 (tets) or 2 (springs) vertices");
+  if (cv != 4 && cv != 3 && cv != 2)
+    throw invalid_argument("cells must have 4 (tets), 3 (triangles) or 2 (springs) vertices");
   for (long long i = 0; i < (long long)cv * nt; ++i)
     if (cells[i] < 0 || cells[i] >= nv)
       throw invalid_argument("cell index out of range at cells[" + std::to_string(i) + "] = " +
@@ -244,6 +248,54 @@ void slot_pd_values(const Topology& t, const int32_t* cells, const double* X, co
       const int e = eb / 10, blk = eb % 10;
       const bool diag = kBlkV[blk] == kBlkW[blk];
       m += (detJ[e] * (diag ? 1.0 / 60 : 1.0 / 120)) * rho + lap[eb];
+    }
+    out[q] = m;
+  }
+}
+
+void slot_masses_2d(const Topology& t, const std::vector<double>& detJ, double rho, std::vector<double>& out) {
+  out.assign(t.nslots, 0.0);
+  for (int q = 0; q < t.nslots; ++q) {
+    double m = 0;
+    for (int c = t.cptr[q]; c < t.cptr[q + 1]; ++c) {
+      const int eb = (int)((uint32_t)t.csrc[c] & 0x7fffffffu);
+      const int e = eb / 6, blk = eb % 6;
+      m += (detJ[e] * (kTriV[blk] == kTriW[blk] ? 1.0 / 12 : 1.0 / 24)) * rho;  // p12_element_f_f
+    }
+    out[q] = m;
+  }
+}
+
+void slot_pd_values_2d(const Topology& t, const int32_t* cells, const double* X, const std::vector<double>& detJ,
+                       double rho, double alpha, std::vector<double>& out, const std::vector<double>* alpha_e) {
+  // per triangle: grad phi_i from the inverse 2x2 Jacobian; integral = |det J| / 2 * grad phi_v . grad phi_w
+  std::vector<double> lap(6 * (size_t)t.nt);
+  for (int e = 0; e < t.nt; ++e) {
+    const double* x0 = X + 3 * (size_t)cells[3 * e];
+    const double* x1 = X + 3 * (size_t)cells[3 * e + 1];
+    const double* x2 = X + 3 * (size_t)cells[3 * e + 2];
+    const double J[4] = {x1[0] - x0[0], x2[0] - x0[0], x1[1] - x0[1], x2[1] - x0[1]};
+    const double d = J[0] * J[3] - J[1] * J[2];
+    const double B[4] = {J[3] / d, -J[1] / d, -J[2] / d, J[0] / d};
+    double g[3][2];
+    for (int k = 0; k < 2; ++k) {
+      g[1][k] = B[0 * 2 + k];
+      g[2][k] = B[1 * 2 + k];
+      g[0][k] = -(g[1][k] + g[2][k]);
+    }
+    for (int b = 0; b < 6; ++b) {
+      const int v = kTriV[b], w = kTriW[b];
+      lap[6 * (size_t)e + b] =
+          (detJ[e] / 2.0 * (g[v][0] * g[w][0] + g[v][1] * g[w][1])) * (alpha_e ? (*alpha_e)[e] : alpha);
+    }
+  }
+  out.assign(t.nslots, 0.0);
+  for (int q = 0; q < t.nslots; ++q) {
+    double m = 0;
+    for (int c = t.cptr[q]; c < t.cptr[q + 1]; ++c) {
+      const int eb = (int)((uint32_t)t.csrc[c] & 0x7fffffffu);
+      const int e = eb / 6, blk = eb % 6;
+      m += (detJ[e] * (kTriV[blk] == kTriW[blk] ? 1.0 / 12 : 1.0 / 24)) * rho + lap[eb];
     }
     out[q] = m;
   }

@@ -8,7 +8,7 @@ namespace ssim_gb {
 
 struct Topology {
   int nv = 0, nt = 0;
-  int cv = 4;  // vertices per cell: 4 (tets) or 2 (springs)
+  int cv = 4;  // vertices per cell: 4 (tets), 3 (triangles) or 2 (springs)
   // block CSR of the full pattern: block row u holds its sorted neighbour vertices (self included).  The
   // scalar CSR of the reference (global_composer.hpp:68-100) follows: row 3u+a has columns
   // {3w+b : w in bcol[u], b<3}, so row_ptr[3u+a] = 9*bptr[u] + 3*deg(u)*a.
@@ -37,7 +37,7 @@ struct Topology {
 };
 
 // validates the cell indices (throws ssim_gb::invalid_argument) and builds everything above; cells are
-// [nt][cv] with cv = 4 (tets) or 2 (springs)
+// [nt][cv] with cv = 4 (tets), 3 (triangles) or 2 (springs)
 void build_topology(int nv, int nt, const int32_t* cells, Topology& t, int cv = 4);
 
 // the upper-triangular block id of the local vertex pair (v <= w) used by the element Hessian kernel
@@ -58,5 +58,12 @@ void slot_masses(const Topology& t, const std::vector<double>& detJ, double rho,
 void slot_pd_values(const Topology& t, const int32_t* cells, const double* X, const std::vector<double>& detJ,
                     double rho, double alpha, std::vector<double>& out,
                     const std::vector<double>* alpha_e = nullptr);
+
+// the 2D (triangle) versions: p12_element_f_f masses |det J| {1/12, 1/24} rho and the 2D Laplacian
+// (bilinears.hpp:45-96); detJ = |det Dm| = twice the area
+void slot_masses_2d(const Topology& t, const std::vector<double>& detJ, double rho, std::vector<double>& out);
+void slot_pd_values_2d(const Topology& t, const int32_t* cells, const double* X, const std::vector<double>& detJ,
+                       double rho, double alpha, std::vector<double>& out,
+                       const std::vector<double>* alpha_e = nullptr);
 
 }  // namespace ssim_gb

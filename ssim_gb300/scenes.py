@@ -139,6 +139,33 @@ def cloth(n=512, h=0.01, k=1e3, areal_density=0.5, dt=1e-2, steps=10):
     )
 
 
+def sheet2d(nx=41, ny=21, E=1e5, nu=0.4, rho=100.0, seed=7):
+    """2D sheet: unit_square(nx, ny) scaled to [0, 2] x [0, 1] with interior vertices jittered by
+    U(-0.1h, 0.1h) (SplitMix64 seed 7), x = 0 edge fixed, gravity -9.8 e_y, dt = 1e-2, 10 steps."""
+    X2, T = mesh.unit_square(nx, ny)
+    X2 = X2 * np.array([2.0, 1.0])
+    h = 1.0 / (ny - 1)
+    inner = (X2[:, 0] > 0) & (X2[:, 0] < 2.0) & (X2[:, 1] > 0) & (X2[:, 1] < 1.0)
+    jit = (mesh.uniform(seed, 2 * X2.shape[0], -0.1 * h, 0.1 * h)).reshape(-1, 2)
+    X2 = X2 + jit * inner[:, None]
+    return dict(
+        name=f"sheet2d_{nx}x{ny}_{T.shape[0]}tris",
+        X=np.concatenate([X2, np.zeros((X2.shape[0], 1))], axis=1),
+        X2=X2,
+        cells=T,
+        tri2d=True,
+        dt=1e-2,
+        E=E,
+        nu=nu,
+        rho=rho,
+        fixed=np.where(X2[:, 0] == 0.0)[0],
+        gravity=(0.0, -9.8, 0.0),
+        steps=10,
+        u0=None,
+        E_cells=None,
+    )
+
+
 def build_timestep(scene, precision="fp64", stepper="newton", params=None, rtol=None):
     """A GPU TimeStep set up for ``scene`` (material, Dirichlet face, gravity, initial state)."""
     from .timestep import TimeStep
@@ -146,6 +173,8 @@ def build_timestep(scene, precision="fp64", stepper="newton", params=None, rtol=
     if scene.get("springs"):
         ts = TimeStep.springs(scene["X"], scene["cells"], scene["k"], vertex_mass=scene["vertex_mass"],
                               time_step=scene["dt"])
+    elif scene.get("tri2d"):
+        ts = TimeStep.tri2d(scene["X2"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
     else:
         ts = TimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
     ts.set_precision(precision)
@@ -173,6 +202,9 @@ def build_oracle(scene, rtol=None):
     if scene.get("springs"):
         ts = pyoracle.OracleTimeStep.springs(scene["X"], scene["cells"], scene["k"],
                                              vertex_mass=scene["vertex_mass"], time_step=scene["dt"])
+    elif scene.get("tri2d"):
+        ts = pyoracle.OracleTimeStep.tri2d(scene["X2"], scene["cells"], scene["dt"], scene["E"], scene["nu"],
+                                           scene["rho"])
     else:
         ts = pyoracle.OracleTimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"],
                                      scene["rho"])

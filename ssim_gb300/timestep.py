@@ -42,6 +42,44 @@ class TimeStep:
             self.reset()
 
     @classmethod
+    def tri2d(cls, vertices, triangles, time_step, youngs, poisson, density, precision="fp64"):
+        """2D triangles in the plane (ssim_gb_create_2d): vertices [V, 2], triangles [T, 3].  Fields stay
+        [V, 3] with z identically zero; csr_2d() gives the reference's 2-dof matrices."""
+        self = cls.__new__(cls)
+        L = _lib.lib()
+        self._L = L
+        X2 = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 2)
+        T = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+        self.num_vertices, self.num_cells = X2.shape[0], T.shape[0]
+        self.n = 3 * self.num_vertices
+        h = C.c_void_p()
+        check(L.ssim_gb_create_2d(dptr(X2), X2.shape[0], iptr(T), T.shape[0], time_step, youngs, poisson, density,
+                                  C.byref(h)))
+        self._h = h
+        self._X = np.concatenate([X2, np.zeros((X2.shape[0], 1))], axis=1)
+        self._cells = T
+        self._stepper = _lib.STEPPER_NONE
+        if precision != "fp64":
+            self.set_precision(precision)
+            self.reset()
+        return self
+
+    @property
+    def dim(self) -> int:
+        d = C.c_int32()
+        self._c(self._L.ssim_gb_get_dim(self._h, C.byref(d)))
+        return d.value
+
+    def csr_2d(self, which="sysmatrix"):
+        """(row_ptr [2V+1], col_idx, values) of a 2D handle's matrix in the reference's 2-dof layout."""
+        nnz2 = self.nnz * 4 // 9
+        rp = np.zeros(2 * self.num_vertices + 1, dtype=np.int32)
+        ci = np.zeros(nnz2, dtype=np.int32)
+        v = np.zeros(nnz2)
+        self._c(self._L.ssim_gb_get_csr_2d(self._h, _lib.MATRICES[which], iptr(rp), iptr(ci), dptr(v)))
+        return rp, ci, v
+
+    @classmethod
     def springs(cls, vertices, springs, stiffness, vertex_mass=None, mass=None, time_step=1e-2, precision="fp64"):
         """A mass-spring system (ssim_gb_create_springs): springs [S, 2] vertex pairs (rest lengths from the
         vertices), uniform stiffness, vertex masses [V] (or one mass for all)."""
@@ -323,9 +361,10 @@ class TimeStep:
         return out
 
     def dminv(self) -> np.ndarray:
-        out = np.zeros(self.num_cells * 9)
+        d = self.dim
+        out = np.zeros(self.num_cells * d * d)
         self._c(self._L.ssim_gb_get_dminv(self._h, dptr(out)))
-        return out.reshape(-1, 3, 3)
+        return out.reshape(-1, d, d)
 
     def spmv(self, x, which="sysmatrix") -> np.ndarray:
         xv = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
