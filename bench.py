@@ -278,8 +278,11 @@ def run_adjoint(precision, n=32, steps=40, checkpoint_every=8):
     v0 = torch.tensor(sc["v0"], dtype=torch.float64, device="cuda", requires_grad=True)
     Xt = torch.tensor(sc["X"], dtype=torch.float64, device="cuda")
     target = torch.tensor(sc["target"], dtype=torch.float64, device="cuda")
-    # one untimed short rollout (allocations, first-use costs)
-    adjoint.rollout(E, v0, eng, 2, checkpoint_every)
+    # one untimed short rollout with its loss and backward pass (allocations and first-use costs: the first
+    # torch kernel launch of a process loads torch's kernel modules, seconds on a fresh box)
+    u = adjoint.rollout(E, v0, eng, 2, checkpoint_every)
+    ((Xt + u - target) ** 2).sum().backward()
+    E.grad, v0.grad = None, None
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     u = adjoint.rollout(E, v0, eng, steps, checkpoint_every)
