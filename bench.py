@@ -160,6 +160,7 @@ def run_gpu_arm(args, scene):
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
     params = newton_params(g)
+    params.pd_kappa_mode = args.pd_kappa
     result = {}
     launches0 = g.launch_count()
 
@@ -353,6 +354,8 @@ def main():
                     help="beam1m (default), beam_small, cube10, bar, batch, cloth512, cloth_small, sheet2d")
     ap.add_argument("--stepper", default="newton", choices=["newton", "lbfgs", "pd", "ncg", "ncg_ext"],
                     help="stepper of the timed GPU runs (the CPU baseline is Newton)")
+    ap.add_argument("--pd-kappa", type=int, default=0, choices=[0, 1, 2],
+                    help="PD diffusivity: 0 the reference's (E, nu) slots, 1 Lame, 2 per element")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")

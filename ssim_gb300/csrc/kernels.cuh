@@ -160,14 +160,19 @@ void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S
                       double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st);
 template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
-                     V4<S>* q, bool first, const Reduce& red, cudaStream_t st);
+                     V4<S>* q, bool first, const Reduce& red, cudaStream_t st, bool kron = false);
 // the whole PCG loop (after launch_pcg_setup*) in one cooperative launch: variant 1 standard PCG (bitwise
 // the two-launch iterates), 2 Chronopoulos-Gear PCG; gsync: 3 + ceil(ceil(nv / 256) / 32) zeroed words of
 // barrier state; false if the device cannot launch it cooperatively (the caller runs the two-launch loop)
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
-                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st);
+                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st,
+                           bool kron = false);
+// kron: vals holds one value per slot (the matrix is (scalar) (x) I3); launch_kron_extract makes that form
+// from a 9-value store and sets *not_kron when some block is not a multiple of I3
+template <typename S>
+void launch_kron_extract(const SellMatrix& A, const S* vals, S* svals, int* not_kron, cudaStream_t st);
 // y = A x, A a scalar CSR matrix over dofs, x / y 4-wide vertex vectors
 template <typename S>
 void launch_csr_dof_spmv(int n, const int* rp, const int* ci, const S* vals, const V4<S>* x, V4<S>* y,

@@ -128,9 +128,26 @@ __device__ __forceinline__ V4<S> load_x(const V4<S>* x0, const V4<S>* x1, S beta
 // y_u = sum over the upper slots of A_uw x_w + sum over the lower slots of (A_wu)^T x_w, accumulated slot
 // by slot in chunks of two (indices first, then the two slots' x gathers and 18 values, then the FMAs);
 // lower padding entries point at an all-zero slot, so no branch stops the loads from being hoisted.
-template <typename S, int U>
+// KRON: a matrix (scalar) (x) I3 stored with one value per block (the 3x3 block is v I3); vb then walks
+// one value per slot (stride 32 per slot row of the slice)
+template <typename S, int U, bool KRON = false>
 __device__ __forceinline__ void upper_chunk(const S* __restrict__ vb, const int (&c)[U], const V4<S>* x0,
                                             const V4<S>* x1, S beta, int k, S& a0, S& a1, S& a2) {
+  if (KRON) {
+    S v[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) v[j] = vb[(size_t)(k + j) * 32];
+    V4<S> xv[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      a0 += v[j] * xv[j].x;
+      a1 += v[j] * xv[j].y;
+      a2 += v[j] * xv[j].z;
+    }
+    return;
+  }
   S v[U][9];
 #pragma unroll
   for (int j = 0; j < U; ++j)
@@ -147,9 +164,24 @@ __device__ __forceinline__ void upper_chunk(const S* __restrict__ vb, const int 
   }
 }
 
-template <typename S, int U>
+template <typename S, int U, bool KRON = false>
 __device__ __forceinline__ void lower_chunk(const S* __restrict__ vals, const int (&q)[U], const int (&c)[U],
                                             const V4<S>* x0, const V4<S>* x1, S beta, S& a0, S& a1, S& a2) {
+  if (KRON) {  // v I3 is its own transpose
+    S v[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) v[j] = vals[q[j]];
+    V4<S> xv[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      a0 += v[j] * xv[j].x;
+      a1 += v[j] * xv[j].y;
+      a2 += v[j] * xv[j].z;
+    }
+    return;
+  }
   S v[U][9];
 #pragma unroll
   for (int j = 0; j < U; ++j) {
@@ -182,7 +214,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
-template <typename S, bool STAGED>
+template <typename S, bool STAGED, bool KRON = false>
 __device__ __forceinline__ void row_product_t(const SellMatrix& A, const S* __restrict__ vals, int u, const V4<S>* x0,
                                               const V4<S>* x1, S beta, int (*sidx)[32], S& a0, S& a1, S& a2) {
   const int lane = u & 31, s = u >> 5;
@@ -204,24 +236,24 @@ __device__ __forceinline__ void row_product_t(const SellMatrix& A, const S* __re
   auto lsrc = [&](int k) { return (STAGED && k < ST_LO) ? sidx[ST_UP + 2 * k][lane] : sb[k * 32]; };
   auto lcol = [&](int k) { return (STAGED && k < ST_LO) ? sidx[ST_UP + 2 * k + 1][lane] : lcb[k * 32]; };
   a0 = a1 = a2 = S(0);
-  const S* vb = vals + (size_t)9 * ub + lane;
+  const S* vb = vals + (size_t)(KRON ? 1 : 9) * ub + lane;
   int k = 0;
   for (; k + 2 <= Wu; k += 2) {
     const int c[2] = {ucol(k), ucol(k + 1)};
-    upper_chunk<S, 2>(vb, c, x0, x1, beta, k, a0, a1, a2);
+    upper_chunk<S, 2, KRON>(vb, c, x0, x1, beta, k, a0, a1, a2);
   }
   if (k < Wu) {
     const int c[1] = {ucol(k)};
-    upper_chunk<S, 1>(vb, c, x0, x1, beta, k, a0, a1, a2);
+    upper_chunk<S, 1, KRON>(vb, c, x0, x1, beta, k, a0, a1, a2);
   }
   k = 0;
   for (; k + 2 <= Wl; k += 2) {
     const int qq[2] = {lsrc(k), lsrc(k + 1)}, c[2] = {lcol(k), lcol(k + 1)};
-    lower_chunk<S, 2>(vals, qq, c, x0, x1, beta, a0, a1, a2);
+    lower_chunk<S, 2, KRON>(vals, qq, c, x0, x1, beta, a0, a1, a2);
   }
   if (k < Wl) {
     const int qq[1] = {lsrc(k)}, c[1] = {lcol(k)};
-    lower_chunk<S, 1>(vals, qq, c, x0, x1, beta, a0, a1, a2);
+    lower_chunk<S, 1, KRON>(vals, qq, c, x0, x1, beta, a0, a1, a2);
   }
 }
 
@@ -317,13 +349,13 @@ __global__ void __launch_bounds__(SB)
 
 // One row of the fused PCG SpMV: p_new = z + beta p_old (formed on the fly for the gathered columns),
 // q = A p_new; returns the row's share of p_new . q.
-template <typename S>
+template <typename S, bool KRON = false>
 __device__ __forceinline__ S pcg_spmv_row(const SellMatrix& A, const S* __restrict__ vals, const V4<S>* z,
                                           const V4<S>* p_old, V4<S>* p_new, V4<S>* q, S beta, int u,
                                           int (*sidx)[32]) {
   if (u >= A.nv) return S(0);
   S a0, a1, a2;
-  row_product_t<S, true>(A, vals, u, z, p_old, beta, sidx, a0, a1, a2);
+  row_product_t<S, true, KRON>(A, vals, u, z, p_old, beta, sidx, a0, a1, a2);
   const V4<S> zu = z[u], pu = p_old[u];
   const V4<S> pn = mk4<S>(zu.x + beta * pu.x, zu.y + beta * pu.y, zu.z + beta * pu.z);
   p_new[u] = pn;
@@ -379,7 +411,7 @@ __device__ __forceinline__ void pcg_after_rz(DevScalars* sc, double rz, double r
   }
 }
 
-template <typename S>
+template <typename S, bool KRON>
 __global__ void __launch_bounds__(SB)
     pcg_spmv_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ z,
                     const V4<S>* __restrict__ p_old, V4<S>* __restrict__ p_new, V4<S>* __restrict__ q, int first,
@@ -388,8 +420,8 @@ __global__ void __launch_bounds__(SB)
   __shared__ double shred[SB / 32][1];
   __shared__ int sidx[SB / 32][ST_K][32];
   const S beta = first ? S(0) : (S)red.sc->beta;
-  S part[1] = {pcg_spmv_row<S>(A, vals, z, p_old, p_new, q, beta, blockIdx.x * SB + threadIdx.x,
-                               sidx[threadIdx.x >> 5])};
+  S part[1] = {pcg_spmv_row<S, KRON>(A, vals, z, p_old, p_new, q, beta, blockIdx.x * SB + threadIdx.x,
+                                     sidx[threadIdx.x >> 5])};
   double v1[1];
   block_sum_s<1, SB, S>(part, v1, shred);
   double tot[1];
@@ -526,13 +558,13 @@ __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long
 //   phase B:  p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = M r   (per vertex)
 // The SpMV gathers one vector (u) instead of forming z + beta p for every neighbour; the barrier after
 // phase B only orders u's writes before the next gathers.  Vectors: u = z, w = q, p = p0, s = p1.
-template <typename S>
+template <typename S, bool KRON = false>
 __device__ __forceinline__ void cgcg_spmv_row(const SellMatrix& A, const S* __restrict__ vals, const V4<S>* z,
                                               const V4<S>* r, V4<S>* q, int u, int (*sidx)[32], S (&part)[3]) {
   part[0] = part[1] = part[2] = S(0);
   if (u >= A.nv) return;
   S a0, a1, a2;
-  row_product_t<S, true>(A, vals, u, z, nullptr, S(0), sidx, a0, a1, a2);
+  row_product_t<S, true, KRON>(A, vals, u, z, nullptr, S(0), sidx, a0, a1, a2);
   q[u] = mk4<S>(a0, a1, a2);
   const V4<S> uu = z[u], ru = r[u];
   part[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
@@ -604,7 +636,7 @@ __device__ __forceinline__ void cgcg_after(DevScalars* sc, double g, double d, d
   sc->iters += 1;
 }
 
-template <typename S>
+template <typename S, bool KRON>
 __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
     cgcg_persistent_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ dinv, V4<S>* x,
                            V4<S>* r, V4<S>* z, V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, Reduce red,
@@ -624,7 +656,7 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
   for (int k = 0;; ++k) {
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       S pr[3];
-      cgcg_spmv_row<S>(A, vals, z, r, q, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5], pr);
+      cgcg_spmv_row<S, KRON>(A, vals, z, r, q, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5], pr);
       double bs[3];
       block_sum_s<3, SB, S>(pr, bs, shred);
       if (threadIdx.x == 0) {
@@ -657,7 +689,7 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
 // Standard PCG in one launch: the two-launch loop's phases (SpMV forming p = z + beta p_old, then the
 // update) separated by reducing grid barriers; the last block runs the same reductions and epilogues as
 // the two-launch kernels, so the iterates are bitwise theirs.
-template <typename S>
+template <typename S, bool KRON>
 __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
     pcg_persistent_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ dinv, V4<S>* x,
                           V4<S>* r, V4<S>* z, V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, Reduce red,
@@ -680,7 +712,8 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
     V4<S>* pnew = (k & 1) ? p0 : p1;
     const S beta = k == 0 ? S(0) : (S)s_coef;
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-      S part[1] = {pcg_spmv_row<S>(A, vals, z, pold, pnew, q, beta, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5])};
+      S part[1] = {pcg_spmv_row<S, KRON>(A, vals, z, pold, pnew, q, beta, vb * SB + threadIdx.x,
+                                         sidx[threadIdx.x >> 5])};
       double v1[1];
       block_sum_s<1, SB, S>(part, v1, reinterpret_cast<double(*)[1]>(shred));
       if (threadIdx.x == 0) part_pq[vb] = v1[0];
@@ -955,7 +988,31 @@ __global__ void from_vec4_kernel(int nv, const V4<S>* __restrict__ in, double* _
 
 }  // namespace
 
+// one value per slot for a matrix whose blocks are all multiples of I3 (the projective-dynamics matrix
+// (M + dt^2 kappa L) (x) I3, Dirichlet rows included): the SpMV then reads 4 bytes per block instead of 36
+template <typename S>
+__global__ void __launch_bounds__(SB)
+    kron_extract_kernel(int nslots, const S* __restrict__ vals, S* __restrict__ svals, int* not_kron) {
+  const int q = blockIdx.x * SB + threadIdx.x;
+  if (q >= nslots) return;
+  const size_t b = sell_base(q);
+  S v[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) v[c] = vals[b + 32 * c];
+  svals[q] = v[0];
+  if (v[1] != S(0) || v[2] != S(0) || v[3] != S(0) || v[5] != S(0) || v[6] != S(0) || v[7] != S(0) ||
+      v[4] != v[0] || v[8] != v[0])
+    atomicOr(not_kron, 1);
+}
+
 // ------------------------------------------------------------------ launchers
+template <typename S>
+void launch_kron_extract(const SellMatrix& A, const S* vals, S* svals, int* not_kron, cudaStream_t st) {
+  if (A.nslots <= 0) return;
+  kron_extract_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A.nslots, vals, svals, not_kron);
+  after_launch("kron_extract");
+}
+
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
                      const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st) {
@@ -990,21 +1047,27 @@ void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S
 
 template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
-                     V4<S>* q, bool first, const Reduce& red, cudaStream_t st) {
-  pcg_spmv_kernel<S><<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, z, p_old, p_new, q, first ? 1 : 0, red);
+                     V4<S>* q, bool first, const Reduce& red, cudaStream_t st, bool kron) {
+  if (kron)
+    pcg_spmv_kernel<S, true><<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, z, p_old, p_new, q, first ? 1 : 0, red);
+  else
+    pcg_spmv_kernel<S, false><<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, z, p_old, p_new, q, first ? 1 : 0, red);
   after_launch("pcg_spmv");
 }
 
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
-                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st) {
+                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st, bool kron) {
   int dev = 0, coop = 0, nsm = 0, per_sm = 0;
   SSIM_CUDA(cudaGetDevice(&dev));
   SSIM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return false;
   SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const void* fn = variant == 2 ? (const void*)cgcg_persistent_kernel<S> : (const void*)pcg_persistent_kernel<S>;
+  const void* fn = variant == 2 ? (kron ? (const void*)cgcg_persistent_kernel<S, true>
+                                        : (const void*)cgcg_persistent_kernel<S, false>)
+                                 : (kron ? (const void*)pcg_persistent_kernel<S, true>
+                                         : (const void*)pcg_persistent_kernel<S, false>);
   SSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SB, 0));
   if (per_sm < 1) return false;
   int grid = std::min(div_up(A.nv, SB), per_sm * nsm);
@@ -1145,18 +1208,19 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
   template void launch_assemble<S>(const SellMatrix&, const int*, const int*, const S*, const S*, const uint8_t*, \
                                    bool, S*, V4<S>*, int, cudaStream_t);                                          \
   template void launch_spmv<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, cudaStream_t);                 \
+  template void launch_kron_extract<S>(const SellMatrix&, const S*, S*, int*, cudaStream_t);                     \
   template void launch_export_csr<S>(const SellMatrix&, const int*, const int*, const int*, const S*, double*,   \
                                      cudaStream_t);                                                               \
   template void launch_pcg_setup<S>(int, const double*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, V4<S>*, double,   \
                                     int, bool, const Reduce&, cudaStream_t);                                      \
   template void launch_pcg_spmv<S>(const SellMatrix&, const S*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*,     \
-                                   bool, const Reduce&, cudaStream_t);                                            \
+                                   bool, const Reduce&, cudaStream_t, bool);                                      \
   template void launch_pcg_update<S>(int, const V4<S>*, const V4<S>*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*, int, \
                                      const Reduce&, cudaStream_t);                                                \
   template bool launch_pcg_persistent<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*,       \
                                          V4<S>*, V4<S>*, V4<S>*, int, const Reduce&, unsigned long long*,        \
                                          long long,                                                               \
-                                         int, int, int, cudaStream_t);                                            \
+                                         int, int, int, cudaStream_t, bool);                                      \
   template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
   template void launch_csr_dof_spmv<S>(int, const int*, const int*, const S*, const V4<S>*, V4<S>*, cudaStream_t); \
   template void launch_axpy_update<S>(int, double, const V4<S>*, const double*, double*, float4*, cudaStream_t); \

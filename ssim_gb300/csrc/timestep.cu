@@ -59,11 +59,14 @@ struct Solver {
   DBuf<V4<S>> ld, lq;
   std::vector<std::unique_ptr<DBuf<V4<S>>>> hs, hy;
   DBuf<S> pd_vals, slot_pd;
+  DBuf<S> pd_svals;      // the PD matrix as (scalar) (x) I3: one value per slot, when its blocks allow
+  bool pd_kron = false;
   DBuf<V4<S>> pd_dinv;
   DBuf<S> ncg_L, ncg_Lt;  // NCG preconditioner factor and its transpose on the CSR pattern
   long ncg_version = -1;
   void release() {
-    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &ncg_L, &ncg_Lt}) b->release();
+    for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &pd_svals, &ncg_L, &ncg_Lt}) b->release();
+    pd_kron = false;
     ncg_version = -1;
     for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &ld, &lq, &pd_dinv}) b->release();
     hs.clear();
@@ -536,6 +539,7 @@ struct TimeStep {
       s.pd_vals.alloc(9 * (size_t)topo.nslots);
       s.pd_dinv.alloc(3 * (size_t)nv);
       launch_assemble<S>(A(), cptr.p, csrc.p, nullptr, s.slot_pd.p, mask.p, true, s.pd_vals.p, s.pd_dinv.p, 2, stream);
+      pd_kron_form<S>(s);
       return;
     }
     double lam_slot = E, mu_slot = nu;
@@ -564,6 +568,18 @@ struct TimeStep {
     s.pd_vals.alloc(9 * (size_t)topo.nslots);
     s.pd_dinv.alloc(3 * (size_t)nv);
     launch_assemble<S>(A(), cptr.p, csrc.p, nullptr, s.slot_pd.p, mask.p, true, s.pd_vals.p, s.pd_dinv.p, 2, stream);
+    pd_kron_form<S>(s);
+  }
+
+  // the PD matrix is (M + dt^2 kappa L) (x) I3 with the Dirichlet identity on whole vertices; when every
+  // block is a multiple of I3 (no vertex is only partly fixed) the PCG reads it with one value per block
+  template <typename S>
+  void pd_kron_form(Solver<S>& s) {
+    s.pd_svals.alloc(std::max(topo.nslots, 1));
+    SSIM_CUDA(cudaMemsetAsync(&sc.p->status, 0, sizeof(int32_t), stream));
+    launch_kron_extract<S>(A(), s.pd_vals.p, s.pd_svals.p, &sc.p->status, stream);
+    sync_scalars();
+    s.pd_kron = hsc->status == 0;
   }
 
   template <typename S>
@@ -710,14 +726,16 @@ struct TimeStep {
 
   // PCG on another matrix of the same block pattern (the PD matrix) with an S right-hand side
   template <typename S>
-  int pcg_on(const S* vals, const V4<S>* dinv, const V4<S>* b, double eta, int max_iters, double* rel_res) {
+  int pcg_on(const S* vals, const V4<S>* dinv, const V4<S>* b, double eta, int max_iters, double* rel_res,
+             bool kron = false) {
     Solver<S>& s = solver<S>();
     launch_pcg_setup_v<S>(nv, b, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, red(), stream);
-    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false);
+    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false, kron);
   }
 
   template <typename S>
-  int pcg_loop(const S* vals, const V4<S>* dinv, int max_iters, double* rel_res, bool profile_spmv) {
+  int pcg_loop(const S* vals, const V4<S>* dinv, int max_iters, double* rel_res, bool profile_spmv,
+               bool kron = false) {
     Solver<S>& s = solver<S>();
     int variant = params.pcg_persistent;
     if (variant == 3) variant = sizeof(S) == 4 ? 2 : 0;
@@ -726,7 +744,7 @@ struct TimeStep {
       if (prof) SSIM_CUDA(cudaEventRecord(ev[0], stream));
       const bool ran = launch_pcg_persistent<S>(A(), vals, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters,
                                                 red(), gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra,
-                                                params.pcg_max_blocks, variant, stream);
+                                                params.pcg_max_blocks, variant, stream, kron);
       if (ran) {
         if (prof) SSIM_CUDA(cudaEventRecord(ev[1], stream));
         sync_scalars();
@@ -755,7 +773,7 @@ struct TimeStep {
         V4<S>* pold = (k & 1) ? s.p1.p : s.p0.p;
         V4<S>* pnew = (k & 1) ? s.p0.p : s.p1.p;
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c], stream));
-        launch_pcg_spmv<S>(A(), vals, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream);
+        launch_pcg_spmv<S>(A(), vals, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream, kron);
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c + 1], stream));
         launch_pcg_update<S>(nv, pnew, s.q.p, dinv, s.x.p, s.r.p, s.z.p, max_iters, red(), stream);
       }
@@ -844,6 +862,7 @@ struct TimeStep {
                                 stream));
       SSIM_CUDA(cudaMemcpyAsync(s.pd_dinv.p, s.dinv.p, sizeof(V4<S>) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice,
                                 stream));
+      s.pd_kron = false;  // the projected Hessian is not a multiple of I3 per block
       pd = true;
     }
     const int m = std::max(1, std::min(params.lbfgs_history, (int)s.hs.size()));
@@ -926,7 +945,8 @@ struct TimeStep {
                                i0 >= 0 ? al + i0 : nullptr, nullptr, -1.0, nullptr, 1.0, nullptr, 0.0, nullptr, red(),
                                stream);
           double rr = 0;
-          st.cg_iters_total += pcg_on<S>(s.pd_vals.p, s.pd_dinv.p, q, pd_tol, params.cg_max_iters, &rr);
+          st.cg_iters_total += pcg_on<S>(s.pd_kron ? s.pd_svals.p : s.pd_vals.p, s.pd_dinv.p, q, pd_tol,
+                                       params.cg_max_iters, &rr, s.pd_kron);
           if (i0 >= 0)
             launch_lbfgs_pass<S>(nv, z, nullptr, z, nullptr, nullptr, nullptr, 0.0, nullptr, 1.0, s.hy[i0]->p,
                                  rho_h[i0], bb + i0, red(), stream);

@@ -316,6 +316,36 @@ def test_lbfgs_history_compact_and_two_loop(history):
     assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6
 
 
+def test_pd_partly_fixed_vertices_fall_back_to_blocks():
+    """The PD matrix is read as (scalar) (x) I3 when every block allows; a vertex fixed in z only breaks that
+    and the solve falls back to the 3x3 blocks.  Both forms land on the oracle's PD trajectory."""
+    from oracle import pyoracle
+
+    scene = scenes.cube10()
+    params = g.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-11, max_lbfgs_iters=20000, precond=2,
+                              stop_floor=0.0)
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, stop_floor=0.0)
+    for partial in (False, True):
+        ts = scenes.build_timestep(scene, precision="fp64", stepper="none", params=params)
+        ot = scenes.build_oracle(scene)
+        if partial:  # the bottom face may slide in x and y
+            X = scene["X"]
+            t = ts.dof_type().copy()
+            t[np.where(X[:, 2] == 0.0)[0], 2] = 1
+            ts.set_dof_type(t)
+            ot.set_dof_type(t)
+        ts.reset("pd")
+        ot.reset()
+        for _ in range(2):
+            ts.step()
+            st = ts.stats()
+            ot.prepare_step()
+            _, sto = ot.compute_step("pd", op)
+            ot.step_next()
+            assert st["converged"] == 1 and sto["converged"] == 1
+        assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6, partial
+
+
 def test_pd_matrix_matches_oracle():
     """The PD stepper's matrix (mass + dt^2 kappa Laplacian, DBC identity) through a PCG solve: the PD
     preconditioner applied to a vector equals the oracle's solve with its PD matrix."""
