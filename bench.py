@@ -225,12 +225,14 @@ def run_gpu_arm(args, scene):
 
     fixed = np.asarray(scene["fixed"], dtype=np.int32)
     pin_targ = torch.zeros((3, fixed.size), dtype=torch.float64).pin_memory()
-    if scene.get("springs") or scene.get("tri2d") or args.stepper != "newton":
-        # springs and triangles have no libssim facade, and tet_newton_cuda is Newton: the TimeStep handle
+    facades = {"newton": fem.tet_newton_cuda, "lbfgs": fem.tet_lbfgs_cuda, "pd": fem.tet_lbfgs_pd,
+               "ncg_ext": fem.tet_ncg_cuda_ext_ai}
+    if scene.get("springs") or scene.get("tri2d") or args.stepper not in facades:
+        # springs, triangles and the plain NCG have no libssim facade: the TimeStep handle itself
         s = _HandleFacade(scenes.build_timestep(scene, precision="mixed", stepper=args.stepper, params=params))
     else:
-        s = fem.tet_newton_cuda(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"],
-                                precision="mixed", params=params)
+        s = facades[args.stepper](scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"],
+                                  precision="mixed", params=params)
         if scene.get("E_cells") is not None:
             s.step_.set_material(scene["E_cells"], None)
         s.add_gravity(scene["gravity"])
