@@ -57,6 +57,14 @@ struct ElemFP32 {
   const float* mu;
 };
 
+// per-vertex FP32 split of the state for the FP32 element / spring passes: uh + ul = u (to ~2^-48),
+// w = u - x~ rounded once
+struct Split32 {
+  const float4* uh;
+  const float4* ul;
+  const float4* w;
+};
+
 // springs (2-vertex cells) of a mass-spring system
 struct SpringData {
   int ns;
@@ -96,11 +104,14 @@ void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* 
                              const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
                              bool trial, const Reduce& red, cudaStream_t st);
 // g[v] = sum over incident (e, i) of lf[e][i], Dirichlet dofs zeroed; |g|^2 into sc->gnorm2
-// the same pass with FP32 element arithmetic (small-strain forms), FP64 differences and sums
-template <typename SD>
-void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const double* u, const double* xt,
-                               const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
-                               bool trial, const Reduce& red, cudaStream_t st);
+// the mixed steppers' FP32 element pass: per-vertex FP32 split of u (hi + lo) and of w = u - x~ (made by
+// launch_split32 once per base point), FP32 element arithmetic, forces to lf32[t][4][3]
+void launch_split32(int nv, const double* u, const double* xt, float4* uh, float4* ul, float4* w, cudaStream_t st);
+void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
+                               double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
+                               const Reduce& red, cudaStream_t st);
+void launch_vertex_gather32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
+                            double* g, const Reduce& red, cudaStream_t st);
 // mass-spring energy (+ spring forces into lf[s][2][3]) at u (+ alpha d), plus the lumped inertia energy
 template <typename SD>
 void launch_spring_energy_grad(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
@@ -114,9 +125,9 @@ void launch_spring_gather(int nv, const int* vptr, const int* vinc, const double
 // FP32 spring pass (strain-relative: l - L = (2 E0.D + D.D) / (l + L) with D = the displacement difference
 // formed in FP64): energy (+ the spring force vector f_s into lf32[s] when with_forces), FP64 sums
 template <typename SD>
-void launch_spring_energy_grad32(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
-                                 const V4<SD>* d, double alpha, double dt2, float4* lf32, bool with_forces,
-                                 bool trial, const Reduce& red, cudaStream_t st);
+void launch_spring_energy_grad32(const SpringData& sp, const Split32& s3, const double* u, const double* xt,
+                                 const double* m, int nv, const V4<SD>* d, double alpha, double dt2, float4* lf32,
+                                 bool with_forces, bool trial, const Reduce& red, cudaStream_t st);
 // g from the FP32 spring forces (vertex i of a spring receives +f_s, vertex j -f_s) + m (u (+ alpha d) - x~)
 template <typename SD>
 void launch_spring_gather32(int nv, const int* vptr, const int* vinc, const float4* lf32, const double* m,

@@ -123,46 +123,74 @@ __global__ void __launch_bounds__(EB)
   }
 }
 
-// The same pass with the element arithmetic in FP32 (the mixed Newton's inner iterations): differences
-// of displacements and inertia targets are formed in FP64 and rounded once, the energy and stress use
-// the small-strain forms (snh_eval_small / linear_eval), so results carry FP32 rounding relative to the
-// strain, not to lambda or mu; the element energies and term scales are summed in FP64.
-template <typename SD, bool FORCES, bool TRIAL>
+// The same pass with the element arithmetic in FP32 (the mixed steppers' early iterations).  Per vertex,
+// u is split into FP32 (hi, lo) with hi + lo = u to ~2^-48 and the inertia offset w = u - x~ is rounded
+// once (split32_kernel, once per base point), so the element forms its displacement differences
+// (hi_j - hi_i) + (lo_j - lo_i) (+ alpha (d_j - d_i)) in FP32 with rounding relative to the difference:
+// no FP64 arithmetic per element (GB300's FP64 pipe bound the earlier version).  Energy and stress use
+// the small-strain forms (snh_eval_small / linear_eval); energies are summed in FP32 within a warp and in
+// FP64 across warps and blocks; forces go to lf32[t][4][3] (FP32).
+__global__ void __launch_bounds__(256)
+    split32_kernel(int nv, const double* __restrict__ u, const double* __restrict__ xt, float4* __restrict__ uh,
+                   float4* __restrict__ ul, float4* __restrict__ w) {
+  const int v = blockIdx.x * 256 + threadIdx.x;
+  if (v >= nv) return;
+  float h[3], l[3], o[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double x = u[3 * v + k];
+    h[k] = (float)x;
+    l[k] = (float)(x - (double)h[k]);
+    o[k] = xt != nullptr ? (float)(x - xt[3 * v + k]) : 0.f;
+  }
+  uh[v] = make_float4(h[0], h[1], h[2], 0.f);
+  ul[v] = make_float4(l[0], l[1], l[2], 0.f);
+  if (w != nullptr) w[v] = make_float4(o[0], o[1], o[2], 0.f);
+}
+
+template <bool FORCES, bool TRIAL>
 __global__ void __launch_bounds__(EB)
-    elem_energy_grad32_kernel(ElemFP64 el, ElemFP32 ef, const double* __restrict__ u, const double* __restrict__ xt,
-                              const V4<SD>* __restrict__ d, double alpha, float dt2, float rho,
-                              double* __restrict__ lf, Reduce red) {
-  __shared__ double stage[FORCES ? EB * 12 : 1];
+    elem_energy_grad32_kernel(ElemFP64 el, ElemFP32 ef, Split32 sp, const float4* __restrict__ d, float alpha,
+                              float dt2, float rho, float* __restrict__ lf32, Reduce red) {
+  __shared__ float stage[FORCES ? EB * 12 : 1];
   __shared__ double shred[EB / 32][2];
   const int e0 = blockIdx.x * EB;
   const int e = e0 + threadIdx.x;
-  double energy = 0, escale = 0;
+  float part[2] = {0.f, 0.f};
   float lfv[12];
   if (e < el.nt) {
     const int4 c = el.cells[e];
     const int vid[4] = {c.x, c.y, c.z, c.w};
-    double uu[4][3];
+    float4 hv[4], lv[4], dv[4];
     float dd[4][3];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      V4<SD> dv;
-      if (TRIAL) dv = d[vid[i]];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        double uk = u[vid[i] * 3 + k];
-        if (TRIAL) uk += alpha * (double)comp<SD>(dv, k);
-        uu[i][k] = uk;
-        dd[i][k] = (float)(uk - xt[vid[i] * 3 + k]);
-      }
+      hv[i] = sp.uh[vid[i]];
+      lv[i] = sp.ul[vid[i]];
+      const float4 wv = sp.w[vid[i]];
+      if (TRIAL) dv[i] = d[vid[i]];
+      dd[i][0] = TRIAL ? wv.x + alpha * dv[i].x : wv.x;
+      dd[i][1] = TRIAL ? wv.y + alpha * dv[i].y : wv.y;
+      dd[i][2] = TRIAL ? wv.z + alpha * dv[i].z : wv.z;
     }
     float Dm[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) Dm[k] = ef.dminv[(size_t)k * el.nt + e];
     float Du[9];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) Du[r * 3 + k] = (float)(uu[k + 1][r] - uu[0][r]);
+    for (int k = 0; k < 3; ++k) {
+      float a0 = (hv[k + 1].x - hv[0].x) + (lv[k + 1].x - lv[0].x);
+      float a1 = (hv[k + 1].y - hv[0].y) + (lv[k + 1].y - lv[0].y);
+      float a2 = (hv[k + 1].z - hv[0].z) + (lv[k + 1].z - lv[0].z);
+      if (TRIAL) {
+        a0 += alpha * (dv[k + 1].x - dv[0].x);
+        a1 += alpha * (dv[k + 1].y - dv[0].y);
+        a2 += alpha * (dv[k + 1].z - dv[0].z);
+      }
+      Du[0 * 3 + k] = a0;
+      Du[1 * 3 + k] = a1;
+      Du[2 * 3 + k] = a2;
+    }
     float G[9];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -195,21 +223,21 @@ __global__ void __launch_bounds__(EB)
 #pragma unroll
       for (int j = 0; j < 3; ++j) lfv[j] = -sV * tot[j] + m * (dd[0][j] + sd[j]);
     }
-    energy = (double)(dt2 * V * psi) + (double)(0.5f * m * q);
-    escale = (double)(dt2 * V * sc) + (double)(0.5f * m * q);
+    part[0] = dt2 * V * psi + 0.5f * m * q;
+    part[1] = dt2 * V * sc + 0.5f * m * q;
   }
   if (FORCES) {
     if (e < el.nt) {
 #pragma unroll
-      for (int k = 0; k < 12; ++k) stage[threadIdx.x * 12 + k] = (double)lfv[k];
+      for (int k = 0; k < 12; ++k) stage[threadIdx.x * 12 + k] = lfv[k];
     }
     __syncthreads();
     const int nvalid = min(EB, el.nt - e0);
-    double* dst = lf + (size_t)e0 * 12;
+    float* dst = lf32 + (size_t)e0 * 12;
     for (int i = threadIdx.x; i < nvalid * 12; i += EB) dst[i] = stage[i];
   }
-  double v2[2] = {energy, escale};
-  block_sum<2, EB>(v2, shred);
+  double v2[2];
+  block_sum_s<2, EB, float>(part, v2, shred);
   double tot[2];
   if (grid_sum_last<2, EB>(v2, red.partials, red.counter, tot)) {
     if (TRIAL) {
@@ -220,6 +248,38 @@ __global__ void __launch_bounds__(EB)
       red.sc->energy_scale = tot[1];
     }
   }
+}
+
+// forces from FP32 local forces lf32[(e, i)][3], summed per vertex in FP32, Dirichlet dofs zeroed; |g|^2
+__global__ void __launch_bounds__(256)
+    vertex_gather32_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
+                           const float* __restrict__ lf32, const uint8_t* __restrict__ mask, double* __restrict__ g,
+                           Reduce red) {
+  __shared__ double shred[256 / 32][1];
+  const int v = blockIdx.x * 256 + threadIdx.x;
+  float part[1] = {0.f};
+  if (v < nv) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    const int k1 = vptr[v + 1];
+    for (int k = vptr[v]; k < k1; ++k) {
+      const float* s = lf32 + (size_t)vinc[k] * 3;
+      a0 += s[0];
+      a1 += s[1];
+      a2 += s[2];
+    }
+    const uint8_t mk = mask[v];
+    if (mk & 1) a0 = 0.f;
+    if (mk & 2) a1 = 0.f;
+    if (mk & 4) a2 = 0.f;
+    g[3 * v] = a0;
+    g[3 * v + 1] = a1;
+    g[3 * v + 2] = a2;
+    part[0] = a0 * a0 + a1 * a1 + a2 * a2;
+  }
+  double v1[1];
+  block_sum_s<1, 256, float>(part, v1, shred);
+  double tot[1];
+  if (grid_sum_last<1, 256>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
 }
 
 constexpr int GB = 256;
@@ -374,29 +434,35 @@ template void launch_elem_energy_grad<double>(const ElemFP64&, const double*, co
                                               const double4_32a*, double, double, double, double*, bool, bool,
                                               const Reduce&, cudaStream_t);
 
-template <typename SD>
-void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const double* u, const double* xt,
-                               const V4<SD>* d, double alpha, double dt2, double rho, double* lf, bool with_forces,
-                               bool trial, const Reduce& red, cudaStream_t st) {
+void launch_split32(int nv, const double* u, const double* xt, float4* uh, float4* ul, float4* w, cudaStream_t st) {
+  if (nv <= 0) return;
+  split32_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, u, xt, uh, ul, w);
+  after_launch("split32");
+}
+
+void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
+                               double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
+                               const Reduce& red, cudaStream_t st) {
   if (el.nt <= 0) return;
   const int grid = div_up(el.nt, EB);
-  const float f_dt2 = (float)dt2, f_rho = (float)rho;
+  const float f_dt2 = (float)dt2, f_rho = (float)rho, a = (float)alpha;
   if (trial && with_forces)
-    elem_energy_grad32_kernel<SD, true, true><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+    elem_energy_grad32_kernel<true, true><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
   else if (trial)
-    elem_energy_grad32_kernel<SD, false, true><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+    elem_energy_grad32_kernel<false, true><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
   else if (with_forces)
-    elem_energy_grad32_kernel<SD, true, false><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+    elem_energy_grad32_kernel<true, false><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
   else
-    elem_energy_grad32_kernel<SD, false, false><<<grid, EB, 0, st>>>(el, ef, u, xt, d, alpha, f_dt2, f_rho, lf, red);
+    elem_energy_grad32_kernel<false, false><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
   after_launch("elem_energy_grad32");
 }
-template void launch_elem_energy_grad32<float>(const ElemFP64&, const ElemFP32&, const double*, const double*,
-                                               const float4*, double, double, double, double*, bool, bool,
-                                               const Reduce&, cudaStream_t);
-template void launch_elem_energy_grad32<double>(const ElemFP64&, const ElemFP32&, const double*, const double*,
-                                                const double4_32a*, double, double, double, double*, bool, bool,
-                                                const Reduce&, cudaStream_t);
+
+void launch_vertex_gather32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
+                            double* g, const Reduce& red, cudaStream_t st) {
+  if (nv <= 0) return;
+  vertex_gather32_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, vptr, vinc, lf32, mask, g, red);
+  after_launch("vertex_gather32");
+}
 
 void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
                           double* g, const Reduce& red, cudaStream_t st) {

@@ -78,24 +78,24 @@ __global__ void __launch_bounds__(PB)
   }
 }
 
-// FP32 spring pass.  The displacement difference D = (u_i - u_j) (+ alpha (d_i - d_j)) is formed in FP64 and
-// rounded once; with E0 the rest edge, e = E0 + D and l^2 - L^2 = 2 E0.D + D.D, so l - L = (l^2 - L^2) / (l + L)
+// FP32 spring pass.  The displacement difference D = (u_i - u_j) (+ alpha (d_i - d_j)) is formed in FP32
+// from the per-vertex split u = hi + lo as (hi_i - hi_j) + (lo_i - lo_j), rounding relative to D itself;
+// with E0 the rest edge, e = E0 + D and l^2 - L^2 = 2 E0.D + D.D, so l - L = (l^2 - L^2) / (l + L)
 // carries FP32 rounding relative to the stretch itself rather than to the length (a direct FP32 |e| - L
 // would lose the stretch of a stiff spring to cancellation).  Forces f_s = dt^2 k (l - L) / l e go to
 // lf32[s] (vertex i gets +f_s, vertex j -f_s).
 template <typename SD, bool FORCES, bool TRIAL>
 __global__ void __launch_bounds__(PB)
-    spring_energy_grad32_kernel(SpringData sp, const double* __restrict__ u, const V4<SD>* __restrict__ d,
-                                double alpha, float dt2, float4* __restrict__ lf32, Reduce red) {
+    spring_energy_grad32_kernel(SpringData sp, Split32 s3, const V4<SD>* __restrict__ d, double alpha, float dt2,
+                                float4* __restrict__ lf32, Reduce red) {
   __shared__ double shred[PB / 32][2];
   const int s = blockIdx.x * PB + threadIdx.x;
   float part[2] = {0.f, 0.f};
   if (s < sp.ns) {
     const int2 c = sp.ends[s];
     const float4 e0 = sp.e0[s];
-    float D[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) D[q] = (float)(u[3 * c.x + q] - u[3 * c.y + q]);
+    const float4 hi = s3.uh[c.x], hj = s3.uh[c.y], li = s3.ul[c.x], lj = s3.ul[c.y];
+    float D[3] = {(hi.x - hj.x) + (li.x - lj.x), (hi.y - hj.y) + (li.y - lj.y), (hi.z - hj.z) + (li.z - lj.z)};
     if (TRIAL) {
       const V4<SD> di = d[c.x], dj = d[c.y];
       const float a = (float)alpha;
@@ -318,20 +318,20 @@ void launch_spring_gather(int nv, const int* vptr, const int* vinc, const double
 }
 
 template <typename SD>
-void launch_spring_energy_grad32(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
-                                 const V4<SD>* d, double alpha, double dt2, float4* lf32, bool with_forces,
-                                 bool trial, const Reduce& red, cudaStream_t st) {
+void launch_spring_energy_grad32(const SpringData& sp, const Split32& s3, const double* u, const double* xt,
+                                 const double* m, int nv, const V4<SD>* d, double alpha, double dt2, float4* lf32,
+                                 bool with_forces, bool trial, const Reduce& red, cudaStream_t st) {
   if (sp.ns > 0) {
     const int grid = div_up(sp.ns, PB);
     const float f2 = (float)dt2;
     if (trial && with_forces)
-      spring_energy_grad32_kernel<SD, true, true><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+      spring_energy_grad32_kernel<SD, true, true><<<grid, PB, 0, st>>>(sp, s3, d, alpha, f2, lf32, red);
     else if (trial)
-      spring_energy_grad32_kernel<SD, false, true><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+      spring_energy_grad32_kernel<SD, false, true><<<grid, PB, 0, st>>>(sp, s3, d, alpha, f2, lf32, red);
     else if (with_forces)
-      spring_energy_grad32_kernel<SD, true, false><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+      spring_energy_grad32_kernel<SD, true, false><<<grid, PB, 0, st>>>(sp, s3, d, alpha, f2, lf32, red);
     else
-      spring_energy_grad32_kernel<SD, false, false><<<grid, PB, 0, st>>>(sp, u, d, alpha, f2, lf32, red);
+      spring_energy_grad32_kernel<SD, false, false><<<grid, PB, 0, st>>>(sp, s3, d, alpha, f2, lf32, red);
     after_launch("spring_energy_grad32");
   }
   if (trial)
@@ -368,9 +368,9 @@ template void launch_spring_gather<float>(int, const int*, const int*, const dou
 template void launch_spring_gather<double>(int, const int*, const int*, const double*, const double*, const double*,
                                            const double4_32a*, double, const double*, const uint8_t*, double*,
                                            const Reduce&, cudaStream_t);
-template void launch_spring_energy_grad32<float>(const SpringData&, const double*, const double*, const double*,
-                                                 int, const float4*, double, double, float4*, bool, bool,
-                                                 const Reduce&, cudaStream_t);
+template void launch_spring_energy_grad32<float>(const SpringData&, const Split32&, const double*, const double*,
+                                                 const double*, int, const float4*, double, double, float4*, bool,
+                                                 bool, const Reduce&, cudaStream_t);
 template void launch_spring_gather32<float>(int, const int*, const int*, const float4*, const double*,
                                             const double*, const float4*, double, const double*, const uint8_t*,
                                             double*, const Reduce&, cudaStream_t);

@@ -158,26 +158,41 @@ struct TimeStep {
   DBuf<float> sp_k32;
   std::vector<double> vmass_h, sp_k_h;
   SpringData spd() const { return SpringData{nt, sp_ends.p, dX.p, sp_rest.p, sp_k.p, sp_e0.p, sp_k32.p}; }
+  // the FP32 passes' per-vertex split of next (hi + lo) and of next - x~; split32() refreshes it for the
+  // current next (once per base point: every trial of a line search shares it), lf32t holds the tets'
+  // FP32 local forces
+  DBuf<float4> uh32, ul32, w32;
+  DBuf<float> lf32t;
+  Split32 s32() const { return Split32{uh32.p, ul32.p, w32.p}; }
+  void split32() {
+    uh32.alloc(nv);
+    ul32.alloc(nv);
+    w32.alloc(nv);
+    if (!springs && !tri2d) lf32t.alloc(12 * (size_t)nt);
+    launch_split32(nv, next.p, inertia.p, uh32.p, ul32.p, w32.p, stream);
+  }
 
   // element / spring pass at u = next (+ alpha d): energy (+ local forces into lf) into the trial scalars;
   // fp32: the FP32 element / spring arithmetic of the mixed path's early iterations
   template <typename S>
   void launch_trial(const V4<S>* d, double alpha, bool forces, bool fp32 = false) {
-    if (springs && fp32) {
-      if constexpr (std::is_same<S, float>::value)
-        launch_spring_energy_grad32<float>(spd(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt,
-                                           forces ? sp_lf32.p : nullptr, forces, true, red(), stream);
-      else
-        throw state_error("the FP32 spring pass takes FP32 directions");
+    if (fp32 && !tri2d) {
+      if constexpr (std::is_same<S, float>::value) {
+        if (springs)
+          launch_spring_energy_grad32<float>(spd(), s32(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt,
+                                             forces ? sp_lf32.p : nullptr, forces, true, red(), stream);
+        else
+          launch_elem_energy_grad32(e64(), e32s(), s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
+                                    forces, true, red(), stream);
+      } else {
+        throw state_error("the FP32 element pass takes FP32 directions");
+      }
     } else if (springs)
       launch_spring_energy_grad<S>(spd(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt, forces ? lf.p : nullptr,
                                    forces, true, red(), stream);
     else if (tri2d)
       launch_tri_energy_grad<S>(e64(), next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr, forces,
                                 true, red(), stream);
-    else if (fp32)
-      launch_elem_energy_grad32<S>(e64(), e32s(), next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr,
-                                   forces, true, red(), stream);
     else
       launch_elem_energy_grad<S>(e64(), dX.p, next.p, inertia.p, d, alpha, dt * dt, rho, forces ? lf.p : nullptr,
                                  forces, true, red(), stream);
@@ -195,6 +210,8 @@ struct TimeStep {
     } else if (springs)
       launch_spring_gather<S>(nv, vptr.p, vinc.p, lf.p, vmass.p, next.p, d, alpha, inertia.p, mask.p, forces.p, red(),
                               stream);
+    else if (fp32 && !tri2d)
+      launch_vertex_gather32(nv, vptr.p, vinc.p, lf32t.p, mask.p, forces.p, red(), stream);
     else
       launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
   }
@@ -645,12 +662,13 @@ struct TimeStep {
   double energy_grad32() {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
+    split32();
     if (springs)
-      launch_spring_energy_grad32<float>(spd(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt, sp_lf32.p, true,
-                                         false, red(), stream);
+      launch_spring_energy_grad32<float>(spd(), s32(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt,
+                                         sp_lf32.p, true, false, red(), stream);
     else
-      launch_elem_energy_grad32<float>(e64(), e32s(), next.p, inertia.p, nullptr, 0.0, dt * dt, rho, lf.p, true,
-                                       false, red(), stream);
+      launch_elem_energy_grad32(e64(), e32s(), s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false, red(),
+                                stream);
     if (profiling) prof_end(e0, e1, PK_GRAD, 0);
     gather_forces<float>(nullptr, 0.0, true);
     sync_scalars();
@@ -970,6 +988,7 @@ struct TimeStep {
       }
       // backtracking line search; each trial forms energy, forces and the curvature pair at u + alpha d
       const double Escale = (e32 ? params.ls_energy_slack32 : params.ls_energy_slack) * E0_scale;
+      if (e32) split32();  // the trials' base point
       double alpha = 1.0, gd = 0.0, dn = 0.0;
       bool have_gd = false, accepted = false;
       auto trial = [&](double a) {
@@ -1129,6 +1148,7 @@ struct TimeStep {
       double alpha = 1.0;
       double Et = 0, Et_scale = 0;
       const double slack = (e32 ? params.ls_energy_slack32 : params.ls_energy_slack) * Escale;
+      if (e32) split32();  // the trials' base point
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
         launch_trial<S>(s.x.p, alpha, true, e32);
         sync_scalars();
