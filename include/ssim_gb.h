@@ -121,7 +121,7 @@ typedef struct {
                              arithmetic while the residual is above elem32_switch times the target, then in
                              FP64 (the stopping test always sees an FP64 residual); 0 keeps every evaluation FP64 */
   double ls_energy_slack32; /* Armijo round-off slack of the FP32 evaluations, times their term-magnitude sum */
-  double elem32_switch;   /* residual / target below which the FP32 phase ends (100) */
+  double elem32_switch;   /* residual / target below which the FP32 phase ends (10) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

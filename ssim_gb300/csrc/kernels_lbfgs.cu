@@ -150,21 +150,22 @@ __global__ void __launch_bounds__(LB)
   __shared__ double shred[LB / 32][NV];
   __shared__ double tot[NV];
   __shared__ bool am_last;
-  const int u = blockIdx.x * LB + threadIdx.x;
   S acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) acc[k] = S(0);
-  if (u < nv) {
+  // a grid of a few blocks per SM striding over the vertices: the block sums and the last block's sum
+  // over the grid (NV values per block) stay short
+  for (int u = blockIdx.x * LB + threadIdx.x; u < nv; u += gridDim.x * LB) {
     const V4<S> gv = mk4<S>((S)g[3 * u], (S)g[3 * u + 1], (S)g[3 * u + 2]);
     const V4<S> yn = h.y[h.n - 1][u];
 #pragma unroll
     for (int j = 0; j < kLbfgsMaxCompact; ++j) {
       if (j < h.n) {
         const V4<S> sv = h.s[j][u], yv = h.y[j][u];
-        acc[4 * j + 0] = dot3<S>(sv, gv);
-        acc[4 * j + 1] = dot3<S>(yv, gv);
-        acc[4 * j + 2] = dot3<S>(sv, yn);
-        acc[4 * j + 3] = dot3<S>(yv, yn);
+        acc[4 * j + 0] += dot3<S>(sv, gv);
+        acc[4 * j + 1] += dot3<S>(yv, gv);
+        acc[4 * j + 2] += dot3<S>(sv, yn);
+        acc[4 * j + 3] += dot3<S>(yv, yn);
       }
     }
   }
@@ -286,10 +287,22 @@ __global__ void __launch_bounds__(LB)
 
 }  // namespace
 
+// 2 blocks per SM (each thread then sums several vertices in FP32 before the block sums)
+int multidot_grid(int nv) {
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
+                                                 cudaSuccess || nsm <= 0)
+      nsm = 132;
+  }
+  return std::max(1, std::min(div_up(nv, LB), 2 * nsm));
+}
+
 template <typename S>
 void launch_lbfgs_multidot(int nv, const double* g, const LbfgsHist<S>& h, double* partials, double* tab,
                            unsigned int* counter, cudaStream_t st) {
-  lbfgs_multidot_kernel<S><<<div_up(nv, LB), LB, 0, st>>>(nv, g, h, partials, tab, counter);
+  lbfgs_multidot_kernel<S><<<multidot_grid(nv), LB, 0, st>>>(nv, g, h, partials, tab, counter);
   after_launch("lbfgs_multidot");
 }
 

@@ -1560,7 +1560,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->stop_floor = 1e-12;
   p->mixed_elem32 = 1;
   p->ls_energy_slack32 = 1e-6;
-  p->elem32_switch = 100.0;
+  p->elem32_switch = 10.0;
 }
 
 ssim_gb_status ssim_gb_mesh_csr_nnz(const int32_t* cells, int32_t nt, int32_t nv, int64_t* nnz) {
