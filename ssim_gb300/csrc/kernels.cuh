@@ -173,8 +173,10 @@ template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
                      V4<S>* q, bool first, const Reduce& red, cudaStream_t st, bool kron = false);
 // the whole PCG loop (after launch_pcg_setup*) in one cooperative launch: variant 1 standard PCG (bitwise
-// the two-launch iterates), 2 Chronopoulos-Gear PCG; gsync: 3 + ceil(ceil(nv / 256) / 32) zeroed words of
-// barrier state; false if the device cannot launch it cooperatively (the caller runs the two-launch loop)
+// the two-launch iterates), 2 Chronopoulos-Gear PCG; gsync: grid_sync_words(nv) words of barrier state
+// (zeroed by the launch); false if the device cannot launch it cooperatively (the caller runs the
+// two-launch loop)
+size_t grid_sync_words(int nv);
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,

@@ -455,14 +455,19 @@ __global__ void __launch_bounds__(SB)
 // the FP64 reduction runs once per barrier (the FP64 pipe is narrow on GB300).  Arrays written inside the
 // loop are read with plain loads only after a barrier, whose acquire side orders them after the writers'
 // release (the cooperative-groups grid sync pattern); the scalars are read with L2 loads.
+// Every counter and release word sits on its own 128-byte line (kSyncStride words apart): the waiting
+// blocks poll release words that no atomic touches, and the atomics of one counter do not share a line
+// with another's.
+constexpr int kSyncStride = 16;
 struct GridSync {
   unsigned long long* arrive;  // plain-barrier arrivals since the launch (never reset within it)
   unsigned long long* top;     // arrivals of completed groups at the reducing barriers
   unsigned long long* release; // reducing barriers completed (written by the one that completes each)
-  unsigned long long* group;   // [ngroups] arrivals of each group's virtual blocks
+  unsigned long long* group;   // [ngroups] arrivals of each group's virtual blocks, kSyncStride apart
   int ngroups;
   unsigned int extra;  // arrivals beyond the grid / the groups (test hook; 0 in normal use)
   long long spin_limit;
+  unsigned long long* prelease;  // plain barriers completed (written by the last arrival of each)
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long* p) {
@@ -486,15 +491,19 @@ __device__ __forceinline__ bool wait_at_least(const unsigned long long* p, unsig
   return true;
 }
 
-// Barrier number k (0-based within the launch) without a reduction: the counter only grows, so nobody
-// resets or releases anything; each block waits until all (k + 1) * grid arrivals have happened.
+// Barrier number k (0-based within the launch) without a reduction: the arrival counter only grows; the
+// block whose arrival completes the (k + 1)-th round publishes k + 1 in the release word the others poll.
 __device__ __forceinline__ bool plain_barrier(const GridSync& gs, unsigned long long k) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    atomicAdd(gs.arrive, 1ull);
-    ok = wait_at_least(gs.arrive, (k + 1) * (unsigned long long)(gridDim.x + gs.extra), gs.spin_limit);
+    const unsigned long long target = (k + 1) * (unsigned long long)(gridDim.x + gs.extra);
+    if (atomicAdd(gs.arrive, 1ull) == target - 1) {
+      __threadfence();
+      st_release_gpu(gs.prelease, k + 1);
+    }
+    ok = wait_at_least(gs.prelease, k + 1, gs.spin_limit);
   }
   __syncthreads();
   return ok != 0;
@@ -517,7 +526,7 @@ __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long
       int last = 0;
       if (lane == 0) {
         __threadfence();
-        last = atomicAdd(gs.group + g, 1ull) == (kr + 1) * (unsigned long long)gsize - 1;
+        last = atomicAdd(gs.group + (size_t)g * kSyncStride, 1ull) == (kr + 1) * (unsigned long long)gsize - 1;
         if (last) __threadfence();
       }
       last = __shfl_sync(0xffffffffu, last, 0);
@@ -1055,6 +1064,8 @@ void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V
   after_launch("pcg_spmv");
 }
 
+size_t grid_sync_words(int nv) { return (size_t)kSyncStride * (4 + ((size_t)div_up(nv, SB) + 31) / 32); }
+
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
@@ -1074,10 +1085,16 @@ bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv
   if (max_blocks > 0) grid = std::min(grid, max_blocks);
   if (grid < 1) return true;
   const int ngroups = (div_up(A.nv, SB) + 31) / 32;
-  SSIM_CUDA(cudaMemsetAsync(gsync, 0, (3 + (size_t)ngroups) * sizeof(unsigned long long), st));
+  SSIM_CUDA(cudaMemsetAsync(gsync, 0, grid_sync_words(A.nv) * sizeof(unsigned long long), st));
   SSIM_CUDA(cudaMemsetAsync(&red.sc->wait_failed, 0, sizeof(int32_t), st));
-  GridSync gs{gsync, gsync + 1, gsync + 2, gsync + 3, ngroups, (unsigned int)extra,
-              spin_limit > 0 ? spin_limit : (1LL << 25)};
+  GridSync gs{gsync,
+              gsync + kSyncStride,
+              gsync + 2 * kSyncStride,
+              gsync + 4 * kSyncStride,
+              ngroups,
+              (unsigned int)extra,
+              spin_limit > 0 ? spin_limit : (1LL << 25),
+              gsync + 3 * kSyncStride};
   SellMatrix a = A;
   Reduce rd = red;
   void* args[] = {(void*)&a,  (void*)&vals, (void*)&dinv, (void*)&x,         (void*)&r,  (void*)&z,

@@ -435,7 +435,7 @@ struct TimeStep {
     sc.zero(stream);
     counter.alloc(1);
     counter.zero(stream);
-    gsync.alloc(3 + (size_t)(div_up(nv, 256) + 31) / 32);
+    gsync.alloc(grid_sync_words(nv));
     gsync.zero(stream);
     const size_t maxgrid = (size_t)std::max(div_up(nt, 64), div_up(std::max(3 * nv, topo.nslots), 256)) + 1;
     partials.alloc(maxgrid * 4);
