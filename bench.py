@@ -346,6 +346,19 @@ def cpu_baseline(workload, max_seconds, max_steps, stepper="newton"):
     return {"value": None, "unavailable": (r.stderr or "no output")[-300:]}
 
 
+def max_over_ranks(values):
+    """Element-wise maximum of ``values`` over the ranks of the process group (the values themselves when
+    there is no group): every replica's timings reduced to the job's (slowest rank) before rank 0 reports."""
+    import torch
+    import torch.distributed as tdist
+
+    if not (tdist.is_available() and tdist.is_initialized()):
+        return list(values)
+    t = torch.tensor(list(values), dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return t.tolist()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,19 +410,9 @@ def main():
             dist.destroy_process_group()
         return
 
-    import torch
-
     r = run_gpu_arm(args, scene)
-    # max over ranks of the device time
-    t_mixed = r["ms_mixed"]
-    if dist:
-        import torch.distributed as tdist
-
-        t = torch.tensor([t_mixed, r["ms_fp64"], r["e2e_s"]], dtype=torch.float64)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        t_mixed, ms_fp64, e2e_s = t.tolist()
-    else:
-        ms_fp64, e2e_s = r["ms_fp64"], r["e2e_s"]
+    # the job's times are the slowest replica's
+    t_mixed, ms_fp64, e2e_s = max_over_ranks([r["ms_mixed"], r["ms_fp64"], r["e2e_s"]])
     steps_total = args.steps * world
     value = steps_total / (t_mixed / 1e3)
     fp64_value = steps_total / (ms_fp64 / 1e3)
