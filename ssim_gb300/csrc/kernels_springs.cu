@@ -39,33 +39,51 @@ __device__ __forceinline__ void edge_vec(const SpringData& sp, const double* __r
   }
 }
 
+// FP64 spring pass.  FP64 arithmetic is scarce on GB300, so the pass spends it where the digits matter:
+// the edge vector, |e|, l - L, the energy and the forces (one rsqrt gives both l = |e|^2 rsqrt and the
+// force factor's 1/l); the trial direction's difference d_i - d_j is formed in the direction's own type,
+// and the energy's term magnitude (used only as the round-off scale of the line search) in FP32.
 template <typename SD, bool FORCES, bool TRIAL>
 __global__ void __launch_bounds__(PB)
     spring_energy_grad_kernel(SpringData sp, const double* __restrict__ u, const V4<SD>* __restrict__ d,
                               double alpha, double dt2, double* __restrict__ lf, Reduce red) {
-  __shared__ double shred[PB / 32][2];
+  __shared__ double shred[PB / 32][1];
+  __shared__ double shred2[PB / 32][1];
   const int s = blockIdx.x * PB + threadIdx.x;
-  double energy = 0, escale = 0;
+  double energy[1] = {0.0};
+  float escale[1] = {0.f};
   if (s < sp.ns) {
-    int i, j;
+    const int2 c = sp.ends[s];
+    const int i = c.x, j = c.y;
     double e[3];
-    edge_vec<SD, TRIAL>(sp, u, d, alpha, s, i, j, e);
-    const double l = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
-    const double L = sp.rest[s], k = sp.k[s];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) e[k] = (sp.X[3 * i + k] - sp.X[3 * j + k]) + (u[3 * i + k] - u[3 * j + k]);
+    if (TRIAL) {
+      const V4<SD> di = d[i], dj = d[j];
+      e[0] += alpha * (double)(di.x - dj.x);
+      e[1] += alpha * (double)(di.y - dj.y);
+      e[2] += alpha * (double)(di.z - dj.z);
+    }
+    const double l2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+    const double rl = l2 > 0.0 ? rsqrt(l2) : 0.0;
+    const double l = l2 * rl;
+    const double L = sp.rest[s], kk = dt2 * sp.k[s];
     const double dl = l - L;
-    energy = 0.5 * dt2 * k * dl * dl;
-    escale = 0.5 * dt2 * k * (l * l + L * L);  // magnitude of the terms whose difference dl is
+    energy[0] = 0.5 * kk * dl * dl;
+    escale[0] = 0.5f * (float)kk * ((float)l2 + (float)L * (float)L);
     if (FORCES) {
-      const double c = l > 0 ? dt2 * k * dl / l : 0.0;
+      const double cf = kk * dl * rl;
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        lf[(size_t)s * 6 + q] = c * e[q];
-        lf[(size_t)s * 6 + 3 + q] = -c * e[q];
+        lf[(size_t)s * 6 + q] = cf * e[q];
+        lf[(size_t)s * 6 + 3 + q] = -cf * e[q];
       }
     }
   }
-  double v2[2] = {energy, escale};
-  block_sum<2, PB>(v2, shred);
+  block_sum<1, PB>(energy, shred);
+  double sc1[1];
+  block_sum_s<1, PB, float>(escale, sc1, shred2);
+  double v2[2] = {energy[0], sc1[0]};
   double tot[2];
   if (grid_sum_last<2, PB>(v2, red.partials, red.counter, tot)) {
     if (TRIAL) {
