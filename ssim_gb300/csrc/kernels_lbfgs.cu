@@ -289,14 +289,10 @@ __global__ void __launch_bounds__(LB)
 
 // 2 blocks per SM (each thread then sums several vertices in FP32 before the block sums)
 int multidot_grid(int nv) {
-  static int nsm = 0;
-  if (nsm == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
-                                                 cudaSuccess || nsm <= 0)
-      nsm = 132;
-  }
-  return std::max(1, std::min(div_up(nv, LB), 2 * nsm));
+  int dev = 0, nsm = 0;
+  SSIM_CUDA(cudaGetDevice(&dev));
+  SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  return std::max(1, std::min(div_up(nv, LB), 2 * std::max(nsm, 1)));
 }
 
 template <typename S>
