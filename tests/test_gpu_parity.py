@@ -651,3 +651,30 @@ def test_mixed_fp32_elements_confirmed_in_fp64(scene_name):
         ot.step_next()
     uo = ot.get("deformation")
     assert rel(states[0], uo) <= 1e-4 and rel(states[1], uo) <= 1e-4
+
+
+def test_two_handles_step_concurrently_from_threads():
+    """One handle per stream, several handles at once: two handles stepped from two host threads at the same
+    time give bitwise the states of the same handles stepped one after the other."""
+    import threading
+
+    scene = scenes.cube10()
+    params = g.default_params(stop_mode=1, rel_tol=1e-8)
+
+    def run(ts, out, k):
+        for _ in range(4):
+            ts.step()
+        out[k] = ts.get("deformation")
+
+    seq = {}
+    for k, prec in enumerate(("mixed", "fp64")):
+        run(scenes.build_timestep(scene, precision=prec, params=params), seq, k)
+    handles = [scenes.build_timestep(scene, precision=prec, params=params) for prec in ("mixed", "fp64")]
+    par = {}
+    threads = [threading.Thread(target=run, args=(handles[k], par, k)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for k in range(2):
+        assert np.array_equal(par[k], seq[k])
