@@ -227,7 +227,11 @@ def run_gpu_arm(args, scene):
     pin_targ = torch.zeros((3, fixed.size), dtype=torch.float64).pin_memory()
     facades = {"newton": fem.tet_newton_cuda, "lbfgs": fem.tet_lbfgs_cuda, "pd": fem.tet_lbfgs_pd,
                "ncg_ext": fem.tet_ncg_cuda_ext_ai}
-    if scene.get("springs") or scene.get("tri2d") or args.stepper not in facades:
+    targ_np = pin_targ.numpy()
+    if scene.get("vertex_offsets") is not None:  # batched instances: the batch handle (per-instance stopping)
+        s = _HandleFacade(scenes.build_batch_timestep(scene, precision="mixed", params=params))
+        s.step_.reset(args.stepper)
+    elif scene.get("springs") or scene.get("tri2d") or args.stepper not in facades:
         # springs, triangles and the plain NCG have no libssim facade: the TimeStep handle itself
         s = _HandleFacade(scenes.build_timestep(scene, precision="mixed", stepper=args.stepper, params=params))
     else:
@@ -236,11 +240,15 @@ def run_gpu_arm(args, scene):
         if scene.get("E_cells") is not None:
             s.step_.set_material(scene["E_cells"], None)
         s.add_gravity(scene["gravity"])
+        # the Dirichlet set before reset(): reset builds the PD matrix with its identity rows
+        # (projective_dynamics.hpp:90-91); the per-step marking below only refreshes the same targets
+        s.mark_dirichlet_batched(fixed, targ_np)
         s.reset()
     if scene.get("u0") is not None:  # the scene's initial state, as the device-timed runs start from
         for f in ("deformation", "prev_deform"):
             s.step_.set(f, scene["u0"])
-    targ_np = pin_targ.numpy()
+    if scene.get("velocity") is not None:
+        s.step_.set("velocity", scene["velocity"])
     for _ in range(args.warmup):
         s.mark_dirichlet_batched(fixed, targ_np)
         s.step()
