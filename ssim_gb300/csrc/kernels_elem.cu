@@ -335,9 +335,10 @@ struct ElemSel<double> {
 
 // One thread per tet: K_e = dt^2 V_e pfpx^T H+ pfpx (the gather weight V_e and alpha = dt^2 of
 // time_step.hpp:646-651 folded in), written as the 10 upper 3x3 vertex blocks, staged through shared
-// memory so the global writes are contiguous.
+// memory so the global writes are contiguous.  Launch bounds of 8 blocks per SM (128 registers, a few
+// spills) beat the unconstrained 168 registers: 168 against 192 us per launch at 1.02M tets.
 template <typename S, bool XF>
-__global__ void __launch_bounds__(HB)
+__global__ void __launch_bounds__(HB, 8)
     elem_hessian_kernel(ElemFP64 e64, ElemFP32 e32, const double* __restrict__ X, const double* __restrict__ u,
                         const float4* __restrict__ xf, S dt2, int spsd, S* __restrict__ Kbuf) {
   __shared__ S stage[HB * 90];
