@@ -376,7 +376,7 @@ def main():
     ap.add_argument("--workload", default="beam1m",
                     help="beam1m (default), beam_small, cube10, bar, batch, cloth512, cloth_small, sheet2d")
     ap.add_argument("--stepper", default="newton", choices=["newton", "lbfgs", "pd", "ncg", "ncg_ext"],
-                    help="stepper of the timed GPU runs (the CPU baseline is Newton)")
+                    help="stepper of the timed GPU runs (and of the CPU baseline, Newton for ncg / ncg_ext)")
     ap.add_argument("--pd-kappa", type=int, default=0, choices=[0, 1, 2],
                     help="PD diffusivity: 0 the reference's (E, nu) slots, 1 Lame, 2 per element")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)

@@ -70,7 +70,7 @@ def test_csr_pattern_bit_exact(oracle, make):
     assert np.array_equal(ci, cio)
 
 
-def test_survey_sizes():
+def test_benchmark_mesh_sizes():
     """Mesh sizes of the benchmark configs (T, V, nnz)."""
     X, T = mesh.kuhn_box((10, 10, 10))
     assert T.shape[0] == 6000 and X.shape[0] == 1331
