@@ -51,6 +51,31 @@ def reference_box(nx=11):
     )
 
 
+def reference_beam(nx=6):
+    """The reference's own time-step harness (tests/fem_time_step/main.cpp:39-86): unit_box(4nx, nx, nx)
+    stretched 4x along x ([0,4] x [0,1]^2; nx = 6: 864 vertices, 2,875 tets), the first nx^2 vertices (the
+    x = 0 face) fixed, gravity -9.8 on y, dt = 1e-2, E = 1e6, nu = 0.4, rho = 10, threshold 1e-3 (the
+    reference's absolute rule), 200 steps."""
+    X, T = mesh.unit_box(4 * nx, nx, nx)
+    X = X.copy()
+    X[:, 0] *= 4.0
+    return dict(
+        name=f"reference_beam_unit_box{4 * nx}x{nx}x{nx}_{T.shape[0]}tets",
+        X=X,
+        cells=T,
+        dt=1e-2,
+        E=1e6,
+        nu=0.4,
+        rho=10.0,
+        fixed=np.arange(nx * nx),
+        gravity=(0.0, -9.8, 0.0),
+        steps=200,
+        rtol=1e-3,
+        u0=None,
+        E_cells=None,
+    )
+
+
 def bar(nx=80, ny=20, nz=20, seed=2):
     """Single large bar: 80x20x20 hex over [0,4]x[0,1]^2 (h=0.05) x 6 = 192,000 tets; interior vertices
     jittered U(-0.1h, 0.1h) (SplitMix64 seed 2); E=1e6, nu=0.4, rho=1000; initial state stretched 1.5x

@@ -678,3 +678,26 @@ def test_two_handles_step_concurrently_from_threads():
         t.join()
     for k in range(2):
         assert np.array_equal(par[k], seq[k])
+
+
+def test_reference_harness_scene_step_by_step():
+    """The reference's own time-step harness (tests/fem_time_step/main.cpp:39-86: unit_box(24, 6, 6) x 4 in x,
+    x = 0 face fixed, gravity on y, rho 10, threshold 1e-3 under the reference's absolute rule) with the
+    default Newton settings: the same Newton iteration count every step as the oracle (its loose threshold
+    often accepts the inertial prediction), and the same states to the PCG tolerance."""
+    from oracle import pyoracle
+
+    sc = scenes.reference_beam()
+    ts = scenes.build_timestep(sc, precision="fp64", stepper="newton", params=g.default_params(), rtol=sc["rtol"])
+    ot = scenes.build_oracle(sc, rtol=sc["rtol"])
+    op = pyoracle.default_params()
+    iters, iters_o = [], []
+    for _ in range(20):
+        ts.step()
+        iters.append(ts.stats()["newton_iters"])
+        ot.prepare_step()
+        _, sto = ot.compute_step("newton", op)
+        ot.step_next()
+        iters_o.append(sto["newton_iters"])
+    assert iters == iters_o
+    assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-6
