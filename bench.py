@@ -30,9 +30,11 @@ METRIC = "Newton steps/s @1M tets: mixed vs FP64 plain at 1e-6 residual; adjoint
 
 
 def newton_params(g):
-    """Solver settings shared by the mixed and FP64 GPU paths and the CPU baseline."""
+    """Solver settings shared by the mixed and FP64 GPU paths and the CPU baseline.  The inexact-Newton
+    forcing eta = min(0.1, max(0.05, |g|/|g0|)): on the 1.02M-tet beam a floor of 0.05 took 55.3 steps/s
+    against 46.1 for 0.01 with 169 against 165 Newton iterations over 20 steps."""
     return g.default_params(
-        stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=1e-2, cg_max_iters=5000,
+        stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, cg_max_iters=5000,
         max_newton_iters=100, cg_check_every=16, precond=2, max_lbfgs_iters=20000,
     )
 
@@ -476,7 +478,7 @@ def main():
             "data": "synthetic (seeded SplitMix64 material)",
             "config": {
                 "workload": scene["name"], cells_key: T, "vertices": V, "dofs": 3 * V,
-                "solver": ("Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(1e-2, "
+                "solver": ("Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(5e-2, "
                            "|g|/|g0|)); mixed: Chronopoulos-Gear PCG in one cooperative launch per solve, FP64: two "
                            "launches per PCG iteration") if args.stepper == "newton" else
                           f"{args.stepper}, stop |g| <= 1e-6 |g0| (per instance for batches)",
