@@ -163,6 +163,7 @@ def run_gpu_arm(args, scene):
     stream = torch.cuda.current_stream()
     params = newton_params(g)
     params.pd_kappa_mode = args.pd_kappa
+    params.pcg_persistent = args.pcg_variant
     result = {}
     launches0 = g.launch_count()
 
@@ -381,6 +382,8 @@ def main():
                     help="stepper of the timed GPU runs (and of the CPU baseline, Newton for ncg / ncg_ext)")
     ap.add_argument("--pd-kappa", type=int, default=0, choices=[0, 1, 2],
                     help="PD diffusivity: 0 the reference's (E, nu) slots, 1 Lame, 2 per element")
+    ap.add_argument("--pcg-variant", type=int, default=3, choices=[0, 1, 2, 3, 4],
+                    help="ssim_gb_params.pcg_persistent of the GPU arms (3: automatic; 4: pipelined PCG)")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
@@ -437,13 +440,17 @@ def main():
         p = prof["pcg_iteration"]
         avg_s = p["total_ms"] / p["launches"] / 1e3
         algo = spmv_algo + 7 * s_b * n
-        roofline = {"kernel": "cgcg_persistent_kernel<float> (whole Chronopoulos-Gear PCG solve in one cooperative "
-                              "launch; unit = one PCG iteration: symmetric SELL-32 SpMV + dots, grid reduction, "
-                              "vector update, grid barrier)",
+        pipe = args.pcg_variant == 4
+        roofline = {"kernel": ("pipe_persistent_kernel<float> (whole pipelined PCG solve in one cooperative launch; "
+                               "unit = one PCG iteration: symmetric SELL-32 SpMV of m = M w fused with the vector "
+                               "recurrences and dots, one reducing grid barrier)") if pipe else
+                              ("cgcg_persistent_kernel<float> (whole Chronopoulos-Gear PCG solve in one cooperative "
+                               "launch; unit = one PCG iteration: symmetric SELL-32 SpMV + dots, grid reduction, "
+                               "vector update, grid barrier)"),
                     "bound": "hbm", "achieved": round(algo / avg_s / 1e9, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(algo / avg_s / 1e9 / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_iteration": algo, "avg_iteration_us": round(avg_s * 1e6, 2),
-                    "iterations_timed": p["launches"], "traffic": ncu_traffic(args.workload, "cgcg_persistent"),
+                    "iterations_timed": p["launches"], "traffic": ncu_traffic(args.workload, "pipe_persistent" if pipe else "cgcg_persistent"),
                     "format_bytes_per_iteration": round(p["bytes_per_launch"]),
                     "format_frac": round(p["bytes_per_launch"] / avg_s / 1e9 / peak, 4)}
     elif prof and prof["pcg_spmv"]["launches"] > 0:

@@ -104,7 +104,12 @@ typedef struct {
                              1: the same PCG in one cooperative launch per solve (grid barriers, no host
                              round trips; bitwise the iterates of 0); 2: Chronopoulos-Gear PCG in one
                              launch (one reduction per iteration; equal to 0 up to rounding);
-                             3 (default): 2 in mixed precision, 0 in FP64 (the faster on GB300) */
+                             3 (default): 2 in mixed precision, 0 in FP64 (the faster on GB300);
+                             4: pipelined PCG in one launch (one grid barrier per iteration, two more vertex
+                             vectors, Chronopoulos-Gear after pcg_pipe_iters iterations; equal to 0 up to
+                             rounding, but in FP32 its true residual drifts from the recursive one with the
+                             iterations and the condition number: for loose solves of well-conditioned
+                             systems only) */
   int64_t pcg_spin_limit; /* polls before a grid-barrier wait gives up (SSIM_GB_ERR_DEVICE_TIMEOUT); 0 = default
                              (2^25 polls, about a second) */
   int32_t pcg_barrier_extra; /* test hook: arrivals a grid barrier waits for beyond the grid; 0 in normal use,
@@ -122,6 +127,8 @@ typedef struct {
                              FP64 (the stopping test always sees an FP64 residual); 0 keeps every evaluation FP64 */
   double ls_energy_slack32; /* Armijo round-off slack of the FP32 evaluations, times their term-magnitude sum */
   double elem32_switch;   /* residual / target below which the FP32 phase ends (10) */
+  int32_t pcg_pipe_iters; /* pipelined PCG (pcg_persistent 4) continues as Chronopoulos-Gear PCG after this many
+                             iterations (80), bounding the drift of its recursive residual in long solves */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

@@ -173,15 +173,16 @@ template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
                      V4<S>* q, bool first, const Reduce& red, cudaStream_t st, bool kron = false);
 // the whole PCG loop (after launch_pcg_setup*) in one cooperative launch: variant 1 standard PCG (bitwise
-// the two-launch iterates), 2 Chronopoulos-Gear PCG; gsync: grid_sync_words(nv) words of barrier state
-// (zeroed by the launch); false if the device cannot launch it cooperatively (the caller runs the
-// two-launch loop)
+// the two-launch iterates), 2 Chronopoulos-Gear PCG, 4 pipelined PCG (one grid barrier per iteration;
+// pm: 2 nv vectors of scratch; Chronopoulos-Gear after pipe_iters iterations); gsync: grid_sync_words(nv)
+// words of barrier state (zeroed by the launch); false if the device cannot launch it cooperatively (the
+// caller runs the two-launch loop)
 size_t grid_sync_words(int nv);
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st,
-                           bool kron = false);
+                           bool kron = false, V4<S>* pm = nullptr, int pipe_iters = 0);
 // kron: vals holds one value per slot (the matrix is (scalar) (x) I3); launch_kron_extract makes that form
 // from a 9-value store and sets *not_kron when some block is not a multiple of I3
 template <typename S>

@@ -68,13 +68,8 @@ __global__ void __launch_bounds__(SB)
 #pragma unroll
   for (int i = 0; i < 9; ++i) acc[i] = S(0);
   if (Kbuf != nullptr) {
-    const int c1 = cptr[q + 1];
-    for (int c = cptr[q]; c < c1; ++c) {
-      const int code = csrc[c];
-      const S* k = Kbuf + (size_t)(code & 0x7fffffff) * 9;
-      S kv[9];
-#pragma unroll
-      for (int i = 0; i < 9; ++i) kv[i] = k[i];
+    // contributions in pairs: 18 independent block loads in flight per thread (the gathers are latency-bound)
+    auto add = [&](int code, const S (&kv)[9]) {
       if (code >= 0) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) acc[i] += kv[i];
@@ -84,6 +79,29 @@ __global__ void __launch_bounds__(SB)
 #pragma unroll
           for (int b = 0; b < 3; ++b) acc[a * 3 + b] += kv[b * 3 + a];
       }
+    };
+    const int c1 = cptr[q + 1];
+    int c = cptr[q];
+    for (; c + 2 <= c1; c += 2) {
+      const int code0 = csrc[c], code1 = csrc[c + 1];
+      const S* k0 = Kbuf + (size_t)(code0 & 0x7fffffff) * 9;
+      const S* k1 = Kbuf + (size_t)(code1 & 0x7fffffff) * 9;
+      S kv0[9], kv1[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        kv0[i] = k0[i];
+        kv1[i] = k1[i];
+      }
+      add(code0, kv0);
+      add(code1, kv1);
+    }
+    if (c < c1) {
+      const int code = csrc[c];
+      const S* k = Kbuf + (size_t)(code & 0x7fffffff) * 9;
+      S kv[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) kv[i] = k[i];
+      add(code, kv);
     }
   }
   const int u = A.slot_row[q];
@@ -695,6 +713,168 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
   if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
 }
 
+// Pipelined PCG (Ghysels & Vanroose, "Hiding global synchronization latency in the preconditioned
+// Conjugate Gradient algorithm", Parallel Computing 40(7), 2014): the Chronopoulos-Gear scalars with the
+// SpMV applied to m = M w instead of u, so a vector phase reads nothing that another block writes in the
+// same phase except m, and ONE reducing grid barrier per iteration both sums the dots and orders m's
+// writes (Chronopoulos-Gear needs a second, plain barrier for u).  Invariants in exact arithmetic:
+// u = M r, w = A u, m = M w, s = A p, z = A M s.  M is the per-vertex block-Jacobi inverse, so u = M r
+// and M s are formed from r and s where needed instead of carried by recurrences (equal in exact
+// arithmetic), which leaves x, r, w, p, s, z and a double-buffered m:
+//   prologue:  w = A u0, m_0 = M w;     partials (r, u), (w, u), (r, r)          -> reduction 0
+//   phase k:   n = A m_k;  z = n + beta z,  s = w + beta s,  p = M r + beta p;
+//              x += alpha p,  r -= alpha s,  w -= alpha z;  m_{k+1} = M w;
+//              partials of the new r, u = M r, w                                -> reduction k + 1
+// The scalars (cgcg_after) and the stop rule are those of the Chronopoulos-Gear kernel.  The gap between
+// the recursive and the true residual grows with the iterations and with the condition number (in FP32
+// it reaches the tolerance of long, ill-conditioned solves), so after pipe_iters iterations the solve
+// continues as Chronopoulos-Gear PCG from the same state (x, r, p, s, w; u = M r), whose SpMV recomputes
+// w = A u every iteration.
+template <typename S>
+__device__ __forceinline__ V4<S> block_jacobi(const V4<S>* __restrict__ dinv, int u, S a0, S a1, S a2) {
+  const V4<S> d0 = dinv[3 * u], d1 = dinv[3 * u + 1], d2 = dinv[3 * u + 2];
+  return mk4<S>(d0.x * a0 + d0.y * a1 + d0.z * a2, d1.x * a0 + d1.y * a1 + d1.z * a2,
+                d2.x * a0 + d2.y * a1 + d2.z * a2);
+}
+
+template <typename S, bool KRON>
+__device__ __forceinline__ void pipe_first_row(const SellMatrix& A, const S* __restrict__ vals,
+                                               const V4<S>* __restrict__ dinv, const V4<S>* u0, const V4<S>* r,
+                                               V4<S>* w, V4<S>* m, int u, int (*sidx)[32], S (&part)[3]) {
+  part[0] = part[1] = part[2] = S(0);
+  if (u >= A.nv) return;
+  S a0, a1, a2;
+  row_product_t<S, true, KRON>(A, vals, u, u0, nullptr, S(0), sidx, a0, a1, a2);
+  w[u] = mk4<S>(a0, a1, a2);
+  m[u] = block_jacobi<S>(dinv, u, a0, a1, a2);
+  const V4<S> uu = u0[u], ru = r[u];
+  part[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
+  part[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
+  part[2] = ru.x * ru.x + ru.y * ru.y + ru.z * ru.z;
+}
+
+template <typename S, bool KRON>
+__device__ __forceinline__ void pipe_row(const SellMatrix& A, const S* __restrict__ vals, const V4<S>* __restrict__ dinv,
+                                         bool first, S alpha, S beta, const V4<S>* mk, V4<S>* mn, V4<S>* x,
+                                         V4<S>* r, V4<S>* z, V4<S>* p, V4<S>* sv, V4<S>* w, int u,
+                                         int (*sidx)[32], S (&part)[3]) {
+  part[0] = part[1] = part[2] = S(0);
+  if (u >= A.nv) return;
+  S n0, n1, n2;
+  row_product_t<S, true, KRON>(A, vals, u, mk, nullptr, S(0), sidx, n0, n1, n2);
+  V4<S> ru = r[u], wu = w[u];
+  const V4<S> uu = block_jacobi<S>(dinv, u, ru.x, ru.y, ru.z);
+  V4<S> zu = mk4<S>(n0, n1, n2), su = wu, pu = uu;
+  if (!first) {
+    const V4<S> zo = z[u], so = sv[u], po = p[u];
+    zu = mk4<S>(n0 + beta * zo.x, n1 + beta * zo.y, n2 + beta * zo.z);
+    su = mk4<S>(wu.x + beta * so.x, wu.y + beta * so.y, wu.z + beta * so.z);
+    pu = mk4<S>(uu.x + beta * po.x, uu.y + beta * po.y, uu.z + beta * po.z);
+  }
+  V4<S> xu = x[u];
+  xu.x += alpha * pu.x;
+  xu.y += alpha * pu.y;
+  xu.z += alpha * pu.z;
+  ru.x -= alpha * su.x;
+  ru.y -= alpha * su.y;
+  ru.z -= alpha * su.z;
+  wu.x -= alpha * zu.x;
+  wu.y -= alpha * zu.y;
+  wu.z -= alpha * zu.z;
+  z[u] = zu;
+  sv[u] = su;
+  p[u] = pu;
+  x[u] = xu;
+  r[u] = ru;
+  w[u] = wu;
+  mn[u] = block_jacobi<S>(dinv, u, wu.x, wu.y, wu.z);
+  const V4<S> un = block_jacobi<S>(dinv, u, ru.x, ru.y, ru.z);
+  part[0] = ru.x * un.x + ru.y * un.y + ru.z * un.z;
+  part[1] = wu.x * un.x + wu.y * un.y + wu.z * un.z;
+  part[2] = ru.x * ru.x + ru.y * ru.y + ru.z * ru.z;
+}
+
+// One solve of pipelined PCG.  On entry (pcg_setup): x = 0, r = b, z = M r.  z is read as u0 by the
+// prologue only and then holds A M s (u = M r again after the switch to Chronopoulos-Gear); m has room
+// for 2 nv vectors.
+template <typename S, bool KRON>
+__global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
+    pipe_persistent_kernel(SellMatrix A, const S* __restrict__ vals, const V4<S>* __restrict__ dinv, V4<S>* x,
+                           V4<S>* r, V4<S>* z, V4<S>* p, V4<S>* sv, V4<S>* w, V4<S>* m, int max_iters, Reduce red,
+                           GridSync gs, int pipe_iters) {
+  __shared__ double shred[SB / 32][3];
+  __shared__ int sidx[SB / 32][ST_K][32];
+  __shared__ double s_alpha, s_beta;
+  __shared__ int s_done;
+  DevScalars* sc = red.sc;
+  if (threadIdx.x == 0) s_done = *(volatile int*)&sc->done;
+  __syncthreads();
+  if (s_done) return;
+  const int nv = A.nv;
+  const int nvb = (nv + SB - 1) / SB;
+  double* part = red.partials;
+  double* gsum = red.partials + 3 * (size_t)nvb;
+  auto publish = [&](int vb, S (&pr)[3]) {
+    double bs[3];
+    block_sum_s<3, SB, S>(pr, bs, shred);
+    if (threadIdx.x == 0) {
+      part[3 * vb] = bs[0];
+      part[3 * vb + 1] = bs[1];
+      part[3 * vb + 2] = bs[2];
+    }
+    __syncthreads();
+  };
+  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    S pr[3];
+    pipe_first_row<S, KRON>(A, vals, dinv, z, r, w, m, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5], pr);
+    publish(vb, pr);
+  }
+  bool ok = true;
+  for (int k = 0;; ++k) {
+    ok = reduce_barrier<3>(gs, (unsigned long long)k, part, gsum, nvb,
+                           [&](const double (&t)[3]) { cgcg_after(sc, t[0], t[1], t[2], max_iters); });
+    if (!ok) break;
+    if (threadIdx.x == 0) {
+      s_done = __ldcg(&sc->done);
+      s_alpha = __ldcg(&sc->alpha);
+      s_beta = __ldcg(&sc->beta);
+    }
+    __syncthreads();
+    if (s_done) break;
+    const S alpha = (S)s_alpha, beta = (S)s_beta;
+    if (k < pipe_iters) {
+      const V4<S>* mk = m + (size_t)(k & 1) * nv;
+      V4<S>* mn = m + (size_t)((k + 1) & 1) * nv;
+      for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+        S pr[3];
+        pipe_row<S, KRON>(A, vals, dinv, k == 0, alpha, beta, mk, mn, x, r, z, p, sv, w, vb * SB + threadIdx.x,
+                          sidx[threadIdx.x >> 5], pr);
+        publish(vb, pr);
+      }
+      continue;
+    }
+    // Chronopoulos-Gear from here on: its phase B (u = M r, w the current A u), a plain barrier for u, its
+    // phase A (w = A u and the dots)
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int u = vb * SB + threadIdx.x;
+      if (k == pipe_iters && u < nv) {
+        const V4<S> ru = r[u];
+        z[u] = block_jacobi<S>(dinv, u, ru.x, ru.y, ru.z);
+      }
+      cgcg_update_row<S>(nv, k == 0, alpha, beta, dinv, z, w, p, sv, x, r, u);
+    }
+    ok = plain_barrier(gs, (unsigned long long)(k - pipe_iters));
+    if (!ok) break;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      S pr[3];
+      cgcg_spmv_row<S, KRON>(A, vals, z, r, w, vb * SB + threadIdx.x, sidx[threadIdx.x >> 5], pr);
+      publish(vb, pr);
+    }
+  }
+  // a barrier wait gave up: flag it (the host clears the flag before the launch) and leave
+  if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
+}
+
 // Standard PCG in one launch: the two-launch loop's phases (SpMV forming p = z + beta p_old, then the
 // update) separated by reducing grid barriers; the last block runs the same reductions and epilogues as
 // the two-launch kernels, so the iterates are bitwise theirs.
@@ -1069,16 +1249,20 @@ size_t grid_sync_words(int nv) { return (size_t)kSyncStride * (4 + ((size_t)div_
 template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
-                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st, bool kron) {
+                           long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st, bool kron,
+                           V4<S>* pm, int pipe_iters) {
   int dev = 0, coop = 0, nsm = 0, per_sm = 0;
   SSIM_CUDA(cudaGetDevice(&dev));
   SSIM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return false;
+  if (variant == 4 && pm == nullptr) return false;
   SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const void* fn = variant == 2 ? (kron ? (const void*)cgcg_persistent_kernel<S, true>
-                                        : (const void*)cgcg_persistent_kernel<S, false>)
-                                 : (kron ? (const void*)pcg_persistent_kernel<S, true>
-                                         : (const void*)pcg_persistent_kernel<S, false>);
+  const void* fn = variant == 4   ? (kron ? (const void*)pipe_persistent_kernel<S, true>
+                                          : (const void*)pipe_persistent_kernel<S, false>)
+                   : variant == 2 ? (kron ? (const void*)cgcg_persistent_kernel<S, true>
+                                          : (const void*)cgcg_persistent_kernel<S, false>)
+                                  : (kron ? (const void*)pcg_persistent_kernel<S, true>
+                                          : (const void*)pcg_persistent_kernel<S, false>);
   SSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SB, 0));
   if (per_sm < 1) return false;
   int grid = std::min(div_up(A.nv, SB), per_sm * nsm);
@@ -1099,7 +1283,10 @@ bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv
   Reduce rd = red;
   void* args[] = {(void*)&a,  (void*)&vals, (void*)&dinv, (void*)&x,         (void*)&r,  (void*)&z,
                   (void*)&p0, (void*)&p1,   (void*)&q,    (void*)&max_iters, (void*)&rd, (void*)&gs};
-  SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), args, 0, st));
+  // pipelined: p = p0, s = p1, w = q, then the two m vectors
+  void* pargs[] = {(void*)&a,  (void*)&vals, (void*)&dinv, (void*)&x,         (void*)&r,  (void*)&z,  (void*)&p0,
+                   (void*)&p1, (void*)&q,    (void*)&pm,   (void*)&max_iters, (void*)&rd, (void*)&gs, (void*)&pipe_iters};
+  SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), variant == 4 ? pargs : args, 0, st));
   after_launch("pcg_persistent");
   return true;
 }
@@ -1237,7 +1424,7 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
   template bool launch_pcg_persistent<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, V4<S>*, V4<S>*,       \
                                          V4<S>*, V4<S>*, V4<S>*, int, const Reduce&, unsigned long long*,        \
                                          long long,                                                               \
-                                         int, int, int, cudaStream_t, bool);                                      \
+                                         int, int, int, cudaStream_t, bool, V4<S>*, int);                         \
   template void launch_dot_gd<S>(int, const double*, const V4<S>*, const Reduce&, cudaStream_t);                 \
   template void launch_csr_dof_spmv<S>(int, const int*, const int*, const S*, const V4<S>*, V4<S>*, cudaStream_t); \
   template void launch_axpy_update<S>(int, double, const V4<S>*, const double*, double*, float4*, cudaStream_t); \

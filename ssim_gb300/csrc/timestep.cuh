@@ -55,6 +55,7 @@ struct Solver {
   DBuf<S> K, vals, mvals;  // element blocks, system values, mass values (SELL)
   DBuf<S> slot_mass;
   DBuf<V4<S>> x, r, z, p0, p1, q, dinv, tmp;
+  DBuf<V4<S>> pm;  // the pipelined PCG's double-buffered m = M w (2 nv), allocated on first use
   // L-BFGS / PD: direction, two-loop work vector, history ring, PD matrix and its preconditioner
   DBuf<V4<S>> ld, lq;
   std::vector<std::unique_ptr<DBuf<V4<S>>>> hs, hy;
@@ -68,7 +69,7 @@ struct Solver {
     for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &pd_svals, &ncg_L, &ncg_Lt}) b->release();
     pd_kron = false;
     ncg_version = -1;
-    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &ld, &lq, &pd_dinv}) b->release();
+    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &pm, &ld, &lq, &pd_dinv}) b->release();
     hs.clear();
     hy.clear();
   }
@@ -756,13 +757,20 @@ struct TimeStep {
                bool kron = false) {
     Solver<S>& s = solver<S>();
     int variant = params.pcg_persistent;
+    // automatic: FP64 runs two launches per iteration (its FP64 dots and updates make the persistent
+    // kernels slower on GB300), FP32 Chronopoulos-Gear.  Pipelined PCG (4) is opt-in: its recursive
+    // residual drifts from the true one in FP32 by an amount that grows with the iterations and the
+    // condition number, which a loose tolerance does not cover for ill-conditioned systems (cloth, thin
+    // sheets)
     if (variant == 3) variant = sizeof(S) == 4 ? 2 : 0;
     if (variant) {
       const bool prof = profiling && profile_spmv;
       if (prof) SSIM_CUDA(cudaEventRecord(ev[0], stream));
+      if (variant == 4 && s.pm.n < 2 * (size_t)nv) s.pm.alloc(2 * (size_t)nv);
       const bool ran = launch_pcg_persistent<S>(A(), vals, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters,
                                                 red(), gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra,
-                                                params.pcg_max_blocks, variant, stream, kron);
+                                                params.pcg_max_blocks, variant, stream, kron, s.pm.p,
+                                                params.pcg_pipe_iters);
       if (ran) {
         if (prof) SSIM_CUDA(cudaEventRecord(ev[1], stream));
         sync_scalars();
