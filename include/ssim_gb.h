@@ -270,8 +270,9 @@ SSIM_GB_API ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, cons
 SSIM_GB_API ssim_gb_status ssim_gb_pcg(ssim_gb_timestep* h, const double* b, double* x, double rtol, int32_t max_iters,
                            int32_t* iters, double* rel_residual);
 
-/* ---- batched instances (extension; SURVEY config 4): the mesh handed to ssim_gb_create is a disjoint
- * union of independent meshes whose vertices occupy the contiguous ranges vertex_offsets[i] ..
+/* ---- batched instances (extension; e.g. 256 cubes of 4-24 hexes a side in one handle): the mesh handed
+ * to ssim_gb_create is a disjoint union of independent meshes whose vertices occupy the contiguous ranges
+ * vertex_offsets[i] ..
  * vertex_offsets[i+1]-1 (num_instances + 1 offsets, first 0, last V).  Every kernel runs over the whole
  * union; with stop_mode 1 each instance must meet |g_i| <= rel_tol |g_i0| on its own. */
 SSIM_GB_API ssim_gb_status ssim_gb_set_instances(ssim_gb_timestep* h, const int32_t* vertex_offsets,
