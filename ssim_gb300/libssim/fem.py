@@ -86,17 +86,20 @@ class _TimeStepWrapper:
     def add_gravity(self, gravity):
         self.step_.add_gravity(gravity)
 
+    # The getters return [3, V] / [4, T] arrays with the memory of the reference's Eigen Matrix3Xd /
+    # Matrix4Xi results (column-major: one vertex's x, y, z adjacent), i.e. the transposed view of a fresh
+    # [V, 3] copy: no second copy per call.
     def vertices(self):
-        return np.ascontiguousarray(self.step_.vertices().T)
+        return self.step_.vertices().T
 
     def cells(self):
-        return np.ascontiguousarray(self.step_.cells().T)
+        return self.step_.cells().T
 
     def deformation(self):
-        return np.ascontiguousarray(self.step_.deformation().T)
+        return self.step_.deformation().T
 
     def forces(self):
-        return np.ascontiguousarray(self.step_.forces().T)
+        return self.step_.forces().T
 
     def update_energy_and_gradients(self):
         return self.step_.update_energy_and_gradients(True)

@@ -305,7 +305,7 @@ class TimeStep:
 
     # ---------------------------------------------------------------- state
     def get(self, field: str) -> np.ndarray:
-        out = np.zeros(self.n)
+        out = np.empty(self.n)
         self._c(self._L.ssim_gb_get_field(self._h, _lib.FIELDS[field], dptr(out)))
         return out.reshape(-1, 3)
 
