@@ -48,6 +48,8 @@ def make_scene(name):
         return scenes.beam(40, 20, 14, h=0.05)
     if name == "cube10":
         return scenes.cube10()
+    if name == "refbox":
+        return scenes.reference_box()
     if name == "bar":
         return scenes.bar()
     if name == "batch":
@@ -377,7 +379,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam1m",
-                    help="beam1m (default), beam_small, cube10, bar, batch, cloth512, cloth_small, sheet2d")
+                    help="beam1m (default), beam_small, cube10, refbox, bar, batch, cloth512, cloth_small, sheet2d")
     ap.add_argument("--stepper", default="newton", choices=["newton", "lbfgs", "pd", "ncg", "ncg_ext"],
                     help="stepper of the timed GPU runs (and of the CPU baseline, Newton for ncg / ncg_ext)")
     ap.add_argument("--pd-kappa", type=int, default=0, choices=[0, 1, 2],
