@@ -151,7 +151,7 @@ __device__ __forceinline__ V4<S> load_x(const V4<S>* x0, const V4<S>* x1, S beta
 template <typename S, int U, bool KRON = false>
 __device__ __forceinline__ void upper_chunk(const S* __restrict__ vb, const int (&c)[U], const V4<S>* x0,
                                             const V4<S>* x1, S beta, int k, S& a0, S& a1, S& a2) {
-  if (KRON) {
+  if constexpr (KRON) {
     S v[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) v[j] = vb[(size_t)(k + j) * 32];
@@ -164,28 +164,28 @@ __device__ __forceinline__ void upper_chunk(const S* __restrict__ vb, const int 
       a1 += v[j] * xv[j].y;
       a2 += v[j] * xv[j].z;
     }
-    return;
-  }
-  S v[U][9];
+  } else {
+    S v[U][9];
 #pragma unroll
-  for (int j = 0; j < U; ++j)
+    for (int j = 0; j < U; ++j)
 #pragma unroll
-    for (int m = 0; m < 9; ++m) v[j][m] = vb[(size_t)(k + j) * 288 + 32 * m];
-  V4<S> xv[U];
+      for (int m = 0; m < 9; ++m) v[j][m] = vb[(size_t)(k + j) * 288 + 32 * m];
+    V4<S> xv[U];
 #pragma unroll
-  for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
+    for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
 #pragma unroll
-  for (int j = 0; j < U; ++j) {
-    a0 += v[j][0] * xv[j].x + v[j][1] * xv[j].y + v[j][2] * xv[j].z;
-    a1 += v[j][3] * xv[j].x + v[j][4] * xv[j].y + v[j][5] * xv[j].z;
-    a2 += v[j][6] * xv[j].x + v[j][7] * xv[j].y + v[j][8] * xv[j].z;
+    for (int j = 0; j < U; ++j) {
+      a0 += v[j][0] * xv[j].x + v[j][1] * xv[j].y + v[j][2] * xv[j].z;
+      a1 += v[j][3] * xv[j].x + v[j][4] * xv[j].y + v[j][5] * xv[j].z;
+      a2 += v[j][6] * xv[j].x + v[j][7] * xv[j].y + v[j][8] * xv[j].z;
+    }
   }
 }
 
 template <typename S, int U, bool KRON = false>
 __device__ __forceinline__ void lower_chunk(const S* __restrict__ vals, const int (&q)[U], const int (&c)[U],
                                             const V4<S>* x0, const V4<S>* x1, S beta, S& a0, S& a1, S& a2) {
-  if (KRON) {  // v I3 is its own transpose
+  if constexpr (KRON) {  // v I3 is its own transpose
     S v[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) v[j] = vals[q[j]];
@@ -198,24 +198,24 @@ __device__ __forceinline__ void lower_chunk(const S* __restrict__ vals, const in
       a1 += v[j] * xv[j].y;
       a2 += v[j] * xv[j].z;
     }
-    return;
-  }
-  S v[U][9];
+  } else {
+    S v[U][9];
 #pragma unroll
-  for (int j = 0; j < U; ++j) {
-    const S* p = vals + sell_base(q[j]);
+    for (int j = 0; j < U; ++j) {
+      const S* p = vals + sell_base(q[j]);
 #pragma unroll
-    for (int m = 0; m < 9; ++m) v[j][m] = p[32 * m];
-  }
-  V4<S> xv[U];
+      for (int m = 0; m < 9; ++m) v[j][m] = p[32 * m];
+    }
+    V4<S> xv[U];
 #pragma unroll
-  for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
-  // (A_wu)^T x_w: column a of the stored block times x
+    for (int j = 0; j < U; ++j) xv[j] = load_x<S>(x0, x1, beta, c[j]);
+    // (A_wu)^T x_w: column a of the stored block times x
 #pragma unroll
-  for (int j = 0; j < U; ++j) {
-    a0 += v[j][0] * xv[j].x + v[j][3] * xv[j].y + v[j][6] * xv[j].z;
-    a1 += v[j][1] * xv[j].x + v[j][4] * xv[j].y + v[j][7] * xv[j].z;
-    a2 += v[j][2] * xv[j].x + v[j][5] * xv[j].y + v[j][8] * xv[j].z;
+    for (int j = 0; j < U; ++j) {
+      a0 += v[j][0] * xv[j].x + v[j][3] * xv[j].y + v[j][6] * xv[j].z;
+      a1 += v[j][1] * xv[j].x + v[j][4] * xv[j].y + v[j][7] * xv[j].z;
+      a2 += v[j][2] * xv[j].x + v[j][5] * xv[j].y + v[j][8] * xv[j].z;
+    }
   }
 }
 
