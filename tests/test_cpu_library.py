@@ -131,3 +131,4 @@ def test_ctypes_structs_mirror_header(cname, pycls):
     # the library's defaults round-trip through the Python struct
     p = g.default_params()
     assert p.pcg_persistent == 3 and p.pcg_barrier_extra == 0 and p.pcg_spin_limit == 0
+    assert p.pcg_pipe_iters == 80 and p.elem32_switch == 10.0 and p.mixed_elem32 == 1
