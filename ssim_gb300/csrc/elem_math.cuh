@@ -129,6 +129,37 @@ __host__ __device__ __forceinline__ S snh_eval_small(const S* G, S lam, S mu, S*
   return S(0.5) * (t1 + t2);
 }
 
+// The 2D stable Neo-Hookean (stable_neohookean.hpp with Ndim 2: Psi = 1/2 [mu (Ic - 2) + lambda (J - alpha)^2
+// - mu log(Ic + delta)] - Psi(I), alpha = 1 + (1 - 1/(2 + delta)) mu / lambda) in the displacement gradient
+// G = F - I (row-major 2x2), for FP32 evaluation of small strains: with s = Ic - 2 = 2 tr G + |G|^2,
+// J - 1 = tr G + det G, h = (1 - 1/(2 + delta)) mu = lambda (alpha - 1) and C = cof G = [[G11, -G10],
+// [-G01, G00]] (so cof F = I + C):
+//   Psi - Psi(I) = 1/2 [ mu (s - log1p(s / (2 + delta))) + lambda (J - 1)(J - 1) - 2 h (J - 1) ]
+//   P = lambda (J - 1)(I + C) + h (G - C) + mu s / ((2 + delta)(2 + delta + s)) (I + G),
+// the expansion of P = lambda (J - alpha) cof F + mu (1 - 1/(Ic + delta)) F in which the rest terms
+// (lambda (1 - alpha) + h = 0) cancel analytically; scale returns the magnitude sum of the terms.
+template <typename S, bool STRESS>
+__host__ __device__ __forceinline__ S snh2_eval_small(const S* G, S lam, S mu, S delta, S* P, S& scale) {
+  const S trG = G[0] + G[3];
+  const S s = S(2) * trG + (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + G[3] * G[3]);
+  const S Jm1 = trG + (G[0] * G[3] - G[1] * G[2]);
+  const S b = S(2) + delta;
+  const S h = (S(1) - S(1) / b) * mu;
+  const S lg = log1p(s / b);
+  if (STRESS) {
+    const S C[4] = {G[3], -G[2], -G[1], G[0]};
+    const S lj = lam * Jm1, q = mu * s / (b * (b + s));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const S id = (k == 0 || k == 3) ? S(1) : S(0);
+      P[k] = lj * (id + C[k]) + h * (G[k] - C[k]) + q * (id + G[k]);
+    }
+  }
+  const S t1 = mu * (s - lg), t2 = lam * Jm1 * Jm1 - S(2) * h * Jm1;
+  scale = S(0.5) * (mu * (fabs(s) + fabs(lg)) + lam * Jm1 * Jm1 + S(2) * h * fabs(Jm1));
+  return S(0.5) * (t1 + t2);
+}
+
 // per-element constants of snh_eval
 template <typename S>
 __host__ __device__ __forceinline__ void snh_constants(S lam, S mu, S& alpha, S& psi0) {

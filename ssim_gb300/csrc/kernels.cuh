@@ -148,6 +148,11 @@ void launch_tri_energy_grad(const ElemFP64& el, const double* u, const double* x
                             cudaStream_t st);
 template <typename S>
 void launch_tri_hessian(const ElemFP64& el, const double* u, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
+// the FP32 pass of the mixed path for triangles (as launch_elem_energy_grad32): delta32 the per-element
+// FP32 stable Neo-Hookean delta, forces lf32[t][3][3] for launch_vertex_gather32
+void launch_tri_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const float* delta32, const Split32& sp,
+                              const float4* d, double alpha, double dt2, double rho, float* lf32, bool with_forces,
+                              bool trial, const Reduce& red, cudaStream_t st);
 
 // ---------------- element Hessian ----------------
 template <typename S>

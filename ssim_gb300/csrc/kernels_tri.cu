@@ -10,6 +10,7 @@
 //   linear 2D (linear.hpp:23-68) from G = F - I.
 // The projection clamps the eigenvalues of the 4x4 H at 1e-3 (time_step.hpp:44-52), eigenvectors by cyclic
 // Jacobi rotations in registers.
+#include "elem_math.cuh"
 #include "kernels.cuh"
 
 namespace ssim_gb {
@@ -281,6 +282,99 @@ __global__ void __launch_bounds__(TB)
     }
 }
 
+// FP32 element pass of the mixed path (the triangle analogue of elem_energy_grad32_kernel): displacement
+// differences from the per-vertex FP32 split ((hi_j - hi_i) + (lo_j - lo_i) + alpha (d_j - d_i)), inertia
+// offsets from w = u - x~ rounded once per vertex, the strain-relative 2D stable Neo-Hookean
+// (snh2_eval_small) or the linear model, FP32 forces lf32[t][3][3] (z = 0) for vertex_gather32; energy
+// and its magnitude sum summed in FP64 across warps, blocks and the grid.
+template <bool FORCES, bool TRIAL>
+__global__ void __launch_bounds__(TB)
+    tri_energy_grad32_kernel(ElemFP64 el, ElemFP32 ef, const float* __restrict__ delta32, Split32 sp,
+                             const float4* __restrict__ d, float alpha, float dt2, float rho, float* __restrict__ lf32,
+                             Reduce red) {
+  __shared__ double shred[TB / 32][2];
+  const int e = blockIdx.x * TB + threadIdx.x;
+  float part[2] = {0.f, 0.f};
+  if (e < el.nt) {
+    const int4 c = el.cells[e];
+    const int vid[3] = {c.x, c.y, c.z};
+    float4 hv[3], lv[3], dv[3];
+    float dd[3][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      hv[i] = sp.uh[vid[i]];
+      lv[i] = sp.ul[vid[i]];
+      const float4 wv = sp.w[vid[i]];
+      if (TRIAL) dv[i] = d[vid[i]];
+      dd[i][0] = TRIAL ? wv.x + alpha * dv[i].x : wv.x;
+      dd[i][1] = TRIAL ? wv.y + alpha * dv[i].y : wv.y;
+    }
+    float Dm[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) Dm[k] = ef.dminv[(size_t)k * el.nt + e];
+    // Du(r, k) = (x_{k+1} - x_0)_r from the split, G = Du Dm^-1
+    float Du[4];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      float a0 = (hv[k + 1].x - hv[0].x) + (lv[k + 1].x - lv[0].x);
+      float a1 = (hv[k + 1].y - hv[0].y) + (lv[k + 1].y - lv[0].y);
+      if (TRIAL) {
+        a0 += alpha * (dv[k + 1].x - dv[0].x);
+        a1 += alpha * (dv[k + 1].y - dv[0].y);
+      }
+      Du[0 * 2 + k] = a0;
+      Du[1 * 2 + k] = a1;
+    }
+    float G[4];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 2; ++cc) G[r * 2 + cc] = Du[r * 2 + 0] * Dm[0 * 2 + cc] + Du[r * 2 + 1] * Dm[1 * 2 + cc];
+    const float lam = ef.lam[e], mu = ef.mu[e], A = ef.vol[e];
+    float P[4], sc;
+    const float psi = el.model == 1 ? linear2_eval<float, FORCES>(G, lam, mu, P, sc)
+                                    : snh2_eval_small<float, FORCES>(G, lam, mu, delta32[e], P, sc);
+    const float m = rho * A * (1.0f / 12.0f);
+    const float sd[2] = {dd[0][0] + dd[1][0] + dd[2][0], dd[0][1] + dd[1][1] + dd[2][1]};
+    float q = sd[0] * sd[0] + sd[1] * sd[1];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) q += dd[i][0] * dd[i][0] + dd[i][1] * dd[i][1];
+    if (FORCES) {
+      const float sA = dt2 * A;
+      float out[9];
+      float tot[2] = {0.f, 0.f};
+#pragma unroll
+      for (int i = 1; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const float h = P[j * 2 + 0] * Dm[(i - 1) * 2 + 0] + P[j * 2 + 1] * Dm[(i - 1) * 2 + 1];
+          tot[j] += h;
+          out[i * 3 + j] = sA * h + m * (dd[i][j] + sd[j]);
+        }
+#pragma unroll
+      for (int j = 0; j < 2; ++j) out[j] = -sA * tot[j] + m * (dd[0][j] + sd[j]);
+      out[2] = out[5] = out[8] = 0.f;
+      float* dst = lf32 + (size_t)e * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dst[k] = out[k];
+    }
+    part[0] = dt2 * A * psi + 0.5f * m * q;
+    part[1] = dt2 * A * sc + 0.5f * m * q;
+  }
+  double v2[2];
+  block_sum_s<2, TB, float>(part, v2, shred);
+  double tot[2];
+  if (grid_sum_last<2, TB>(v2, red.partials, red.counter, tot)) {
+    if (TRIAL) {
+      red.sc->trial_energy = tot[0];
+      red.sc->trial_energy_scale = tot[1];
+    } else {
+      red.sc->energy = tot[0];
+      red.sc->energy_scale = tot[1];
+    }
+  }
+}
+
 }  // namespace
 
 template <typename SD>
@@ -297,6 +391,23 @@ void launch_tri_energy_grad(const ElemFP64& el, const double* u, const double* x
   else
     tri_energy_grad_kernel<SD, false, false><<<grid, TB, 0, st>>>(el, u, xt, d, alpha, dt2, rho, lf, red);
   after_launch("tri_energy_grad");
+}
+
+void launch_tri_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const float* delta32, const Split32& sp,
+                              const float4* d, double alpha, double dt2, double rho, float* lf32, bool with_forces,
+                              bool trial, const Reduce& red, cudaStream_t st) {
+  if (el.nt <= 0) return;
+  const int grid = div_up(el.nt, TB);
+  const float a = (float)alpha, f_dt2 = (float)dt2, f_rho = (float)rho;
+  if (trial && with_forces)
+    tri_energy_grad32_kernel<true, true><<<grid, TB, 0, st>>>(el, ef, delta32, sp, d, a, f_dt2, f_rho, lf32, red);
+  else if (trial)
+    tri_energy_grad32_kernel<false, true><<<grid, TB, 0, st>>>(el, ef, delta32, sp, d, a, f_dt2, f_rho, lf32, red);
+  else if (with_forces)
+    tri_energy_grad32_kernel<true, false><<<grid, TB, 0, st>>>(el, ef, delta32, sp, d, a, f_dt2, f_rho, lf32, red);
+  else
+    tri_energy_grad32_kernel<false, false><<<grid, TB, 0, st>>>(el, ef, delta32, sp, d, a, f_dt2, f_rho, lf32, red);
+  after_launch("tri_energy_grad32");
 }
 
 template <typename S>

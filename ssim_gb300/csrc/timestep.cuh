@@ -105,6 +105,7 @@ struct TimeStep {
   DBuf<int4> dcells;
   DBuf<double> dminv, vol, lam, mu, snh_alpha, snh_psi0, snh_delta;
   DBuf<float> fdminv, fvol, flam, fmu;
+  DBuf<float> fdelta;  // triangles: the 2D stable Neo-Hookean delta per element in FP32
   // ---- device: state [n] (time_step.hpp:668-679)
   DBuf<double> deformation, prev_deform, inertia, next, velocity, ext_accel, forces, dbc_values, work;
   DBuf<int8_t> dof_type;
@@ -169,7 +170,7 @@ struct TimeStep {
     uh32.alloc(nv);
     ul32.alloc(nv);
     w32.alloc(nv);
-    if (!springs && !tri2d) lf32t.alloc(12 * (size_t)nt);
+    if (!springs) lf32t.alloc((tri2d ? 9 : 12) * (size_t)nt);
     launch_split32(nv, next.p, inertia.p, uh32.p, ul32.p, w32.p, stream);
   }
 
@@ -177,11 +178,14 @@ struct TimeStep {
   // fp32: the FP32 element / spring arithmetic of the mixed path's early iterations
   template <typename S>
   void launch_trial(const V4<S>* d, double alpha, bool forces, bool fp32 = false) {
-    if (fp32 && !tri2d) {
+    if (fp32) {
       if constexpr (std::is_same<S, float>::value) {
         if (springs)
           launch_spring_energy_grad32<float>(spd(), s32(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt,
                                              forces ? sp_lf32.p : nullptr, forces, true, red(), stream);
+        else if (tri2d)
+          launch_tri_energy_grad32(e64(), e32s(), fdelta.p, s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
+                                   forces, true, red(), stream);
         else
           launch_elem_energy_grad32(e64(), e32s(), s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
                                     forces, true, red(), stream);
@@ -211,7 +215,7 @@ struct TimeStep {
     } else if (springs)
       launch_spring_gather<S>(nv, vptr.p, vinc.p, lf.p, vmass.p, next.p, d, alpha, inertia.p, mask.p, forces.p, red(),
                               stream);
-    else if (fp32 && !tri2d)
+    else if (fp32)
       launch_vertex_gather32(nv, vptr.p, vinc.p, lf32t.p, mask.p, forces.p, red(), stream);
     else
       launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
@@ -480,6 +484,8 @@ struct TimeStep {
         p0[e] = 0.5 * (l[e] * (1 - al[e]) * (1 - al[e]) - m[e] * std::log(2 + dl[e]));
       }
       snh_delta.upload(dl, stream);
+      std::vector<float> df(dl.begin(), dl.end());
+      fdelta.upload(df, stream);
     } else {
       for (int e = 0; e < nt; ++e) snh_constants<double>(l[e], m[e], al[e], p0[e]);
     }
@@ -667,6 +673,9 @@ struct TimeStep {
     if (springs)
       launch_spring_energy_grad32<float>(spd(), s32(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt,
                                          sp_lf32.p, true, false, red(), stream);
+    else if (tri2d)
+      launch_tri_energy_grad32(e64(), e32s(), fdelta.p, s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false,
+                               red(), stream);
     else
       launch_elem_energy_grad32(e64(), e32s(), s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false, red(),
                                 stream);
@@ -913,7 +922,7 @@ struct TimeStep {
     int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
     // mixed precision: FP32 element / spring arithmetic until the residual is within elem32_switch times
     // the target or a line search runs out, FP64 after that and for the stopping test
-    bool e32 = mixed() && params.mixed_elem32 != 0 && !tri2d, e32_stall = false;
+    bool e32 = mixed() && params.mixed_elem32 != 0, e32_stall = false;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
@@ -1105,7 +1114,7 @@ struct TimeStep {
     // mixed precision: the inner iterations evaluate energy and forces with FP32 element arithmetic (the
     // small-strain forms); the stopping test is then confirmed with an FP64 evaluation, and if the FP64
     // residual is above the target (or the FP32 residual stalls) the remaining iterations run in FP64
-    bool e32 = mixed() && params.mixed_elem32 != 0 && !tri2d;
+    bool e32 = mixed() && params.mixed_elem32 != 0;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);

@@ -145,6 +145,32 @@ def test_mixed_newton_residual():
     assert rel(ts.get("deformation"), ot.get("deformation")) <= 1e-5
 
 
+def test_mixed_lbfgs_fp32_phase():
+    """Mixed-precision L-BFGS on triangles runs its early iterations with the FP32 triangle pass
+    (strain-relative 2D stable Neo-Hookean on the per-vertex FP32 split) and confirms in FP64: every step
+    reaches 1e-6 |g0| and the state matches the all-FP64-evaluation run and the oracle's L-BFGS."""
+    from oracle import pyoracle
+
+    sc = scenes.sheet2d(33, 17)
+    states = []
+    for e32 in (1, 0):
+        params = g.default_params(stop_mode=1, rel_tol=1e-6, max_lbfgs_iters=20000, mixed_elem32=e32)
+        ts = scenes.build_timestep(sc, precision="mixed", stepper="lbfgs", params=params)
+        for _ in range(3):
+            ts.step()
+            st = ts.stats()
+            assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"], st
+        states.append(ts.get("deformation"))
+    op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, max_lbfgs_iters=20000)
+    ot = scenes.build_oracle(sc)
+    for _ in range(3):
+        ot.prepare_step()
+        ot.compute_step("lbfgs", op)
+        ot.step_next()
+    uo = ot.get("deformation")
+    assert rel(states[0], uo) <= 1e-4 and rel(states[1], uo) <= 1e-4
+
+
 def test_2d_errors():
     X2, T = mesh.unit_square(3, 3)
     with pytest.raises(ValueError):

@@ -689,14 +689,15 @@ def test_pd_per_element_diffusivity():
     assert res[0][0] == 0 or res[0][1] > res[2][1], res
 
 
-@pytest.mark.parametrize("scene_name", ["cube10", "bar"])
+@pytest.mark.parametrize("scene_name", ["cube10", "bar", "sheet2d"])
 def test_mixed_fp32_elements_confirmed_in_fp64(scene_name):
     """Mixed Newton with FP32 element arithmetic in its inner iterations (small-strain forms) and an FP64
     confirmation of the stopping test: every step ends with an FP64 residual <= 1e-6 |g0| (the stats report
     the FP64 evaluation), and the state matches the all-FP64-evaluation mixed run and the FP64 oracle."""
     from oracle import pyoracle
 
-    scene = scenes.cube10() if scene_name == "cube10" else scenes.bar(20, 6, 6)
+    scene = {"cube10": scenes.cube10, "bar": lambda: scenes.bar(20, 6, 6),
+             "sheet2d": lambda: scenes.sheet2d(33, 17)}[scene_name]()
     states = []
     for e32 in (1, 0):
         params = g.default_params(stop_mode=1, rel_tol=1e-6, mixed_elem32=e32)
