@@ -29,14 +29,30 @@ sys.path.insert(0, ROOT)
 METRIC = "Newton steps/s @1M tets: mixed vs FP64 plain at 1e-6 residual; adjoint ms/step"
 
 
+# Solver settings shared by the mixed and FP64 GPU arms and by the CPU arm (the oracle).  The inexact-Newton
+# forcing eta = min(0.1, max(0.05, |g|/|g0|)): on the 1.02M-tet beam a floor of 0.05 took 55.3 steps/s
+# against 46.1 for 0.01 with 169 against 165 Newton iterations over 20 steps.
+SOLVER = dict(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, cg_max_iters=5000,
+              max_newton_iters=100, precond=2, max_lbfgs_iters=20000)
+GPU_ONLY = dict(cg_check_every=16)  # how often the two-launch PCG reads its stop test (no effect on iterates)
+
+
 def newton_params(g):
-    """Solver settings shared by the mixed and FP64 GPU paths and the CPU baseline.  The inexact-Newton
-    forcing eta = min(0.1, max(0.05, |g|/|g0|)): on the 1.02M-tet beam a floor of 0.05 took 55.3 steps/s
-    against 46.1 for 0.01 with 169 against 165 Newton iterations over 20 steps."""
-    return g.default_params(
-        stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, cg_max_iters=5000,
-        max_newton_iters=100, cg_check_every=16, precond=2, max_lbfgs_iters=20000,
-    )
+    """SOLVER as the GPU library's parameter block."""
+    return g.default_params(**SOLVER, **GPU_ONLY)
+
+
+def oracle_params():
+    """SOLVER as the oracle's parameter block (no call into the GPU library)."""
+    from oracle import pyoracle
+
+    return pyoracle.default_params(**SOLVER)
+
+
+SOLVER_TEXT = {
+    "newton": "Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(5e-2, |g|/|g0|)), "
+              "backtracking Armijo 0.3",
+}
 
 
 def make_scene(name):
@@ -184,14 +200,18 @@ def run_gpu_arm(args, scene):
             tdist.barrier()
 
     def timed_run(precision, steps, warmup, profile=False):
-        # restart from rest: same initial state for every run
+        # restart from the scene's initial state: the same start for every run; the state after the first
+        # (untimed) step is kept for the comparison with the oracle's first step
         ts.set_precision(precision)
         ts.reset(args.stepper)
         for f in ("deformation", "prev_deform"):
             ts.set(f, zeros if scene.get("u0") is None else scene["u0"])
         ts.set("velocity", v0)
-        for _ in range(warmup):
+        first = None
+        for i in range(warmup):
             ts.step()
+            if i == 0:
+                first = ts.get("deformation")
         ts.profile(profile)
         torch.cuda.synchronize()
         barrier()
@@ -209,21 +229,21 @@ def run_gpu_arm(args, scene):
         launches = g.launch_count() - l0
         prof = {k: ts.profile_read(k) for k in ("pcg_spmv", "pcg_iteration")} if profile else None
         ts.profile(False)
-        return ts, ms, stats, launches, prof
+        return ts, ms, stats, launches, prof, first
 
     # ---- headline: mixed precision, inputs resident
     with ClockSampler(dev) as clk:
-        ts, ms_mixed, st_mixed, launches, _ = timed_run("mixed", args.steps, args.warmup)
+        ts, ms_mixed, st_mixed, launches, _, first_mixed = timed_run("mixed", args.steps, args.warmup)
     clocks = clk.summary()
     solve_log = ts.solve_log()
     if args.arms == "mixed":
         return dict(ms_mixed=ms_mixed, ms_fp64=float("nan"), st_mixed=st_mixed, st_fp64=[], launches=launches,
                     prof=None, clocks=clocks, e2e_s=float("nan"), h2d=0, d2h=0, total_launches=0,
-                    solve_log=solve_log)
+                    solve_log=solve_log, first={"mixed": first_mixed})
     # ---- roofline of the dominant kernel (PCG SpMV), events around each launch, same workload
-    _, _, _, _, prof = timed_run("mixed", min(args.steps, 3), 1, profile=True)
+    _, _, _, _, prof, _ = timed_run("mixed", min(args.steps, 3), 1, profile=True)
     # ---- plain FP64 on the same steps
-    _, ms_fp64, st_fp64, _, _ = timed_run("fp64", args.steps, args.warmup)
+    _, ms_fp64, st_fp64, _, _, first_fp64 = timed_run("fp64", args.steps, args.warmup)
     # ---- e2e through the reference-facing API: per step h2d of the Dirichlet targets (pinned), the step,
     # d2h of the deformation (pinned)
     from ssim_gb300.libssim import fem
@@ -272,9 +292,16 @@ def run_gpu_arm(args, scene):
         ms_mixed=ms_mixed, ms_fp64=ms_fp64, st_mixed=st_mixed, st_fp64=st_fp64, launches=launches, prof=prof,
         clocks=clocks, e2e_s=e2e_s, h2d=fixed.size * 3 * 8 + fixed.size * 4, d2h=d.size * 8,
         total_launches=g.launch_count() - launches0, nnz=ts.nnz, solve_log=solve_log,
+        first={"mixed": first_mixed, "fp64": first_fp64},
     )
     if args.adjoint:
-        result["adjoint"] = [run_adjoint("mixed"), run_adjoint("fp64")]
+        mixed, g_mixed = run_adjoint("mixed")
+        fp64, g_fp64 = run_adjoint("fp64")
+        # the mixed gradients against the FP64 ones (both arms at the same 1e-6 tolerances)
+        for k, (a, b) in enumerate(zip(g_mixed, g_fp64)):
+            mixed[("grad_E_rel_err_vs_fp64", "grad_v0_rel_err_vs_fp64")[k]] = float(
+                ((a - b).norm() / b.norm()).item())
+        result["adjoint"] = [mixed, fp64]
     return result
 
 
@@ -313,42 +340,56 @@ def run_adjoint(precision, n=32, steps=40, checkpoint_every=8):
             "forward_ms_per_step": round((t1 - t0) * 1e3 / steps, 3),
             "adjoint_ms_per_step": round((t2 - t1) * 1e3 / steps, 3),
             "adjoint_cg_iters_per_step": round((eng.cg_iters - it0) / steps, 1),
-            "grad_finite": bool(torch.isfinite(E.grad).all().item() and torch.isfinite(v0.grad).all().item())}
+            "grad_finite": bool(torch.isfinite(E.grad).all().item() and torch.isfinite(v0.grad).all().item())}, \
+        (E.grad.detach().clone(), v0.grad.detach().clone())
 
 
-def cpu_baseline_inproc(scene, max_seconds, max_steps, method="newton"):
-    """The FP64 oracle on this host's cores: whole steps (``method``: newton, lbfgs or pd) of the same
-    workload from rest, as many as fit in ``max_seconds`` (at least one, at most ``max_steps``)."""
+def cpu_baseline_inproc(scene, max_seconds, max_steps, warmup=0, method="newton", dump=None):
+    """The FP64 oracle on this host's cores over the GPU arm's step window: ``warmup`` untimed steps of the
+    same workload from its initial state, then whole timed steps (``method``: newton, lbfgs or pd) as many
+    as fit in ``max_seconds`` (at least one, at most ``max_steps``).  ``dump``: a path where the state after
+    the first step is saved (float64 [V, 3]) for the comparison with the GPU arms."""
     from oracle import pyoracle
-    from ssim_gb300 import scenes
+    from oracle import scenes as oscenes
 
-    import ssim_gb300 as g
+    op = oracle_params()
+    ot = oscenes.build_oracle(scene)
+    done = 0
 
-    gp = newton_params(g)
-    op = pyoracle.default_params(stop_mode=1, rel_tol=gp.rel_tol, cg_forcing=1, cg_rtol=gp.cg_rtol,
-                                 cg_eta_min=gp.cg_eta_min, cg_max_iters=gp.cg_max_iters,
-                                 max_newton_iters=gp.max_newton_iters, precond=gp.precond,
-                                 max_lbfgs_iters=gp.max_lbfgs_iters)
-    ot = scenes.build_oracle(scene)
-    t0 = time.perf_counter()
-    steps = 0
-    while True:
+    def one_step():
+        nonlocal done
         ot.prepare_step()
         ot.compute_step(method, op)
         ot.step_next()
-        steps += 1
-        if steps >= max_steps or time.perf_counter() - t0 >= max_seconds:
+        done += 1
+        if done == 1 and dump:
+            np.save(dump, ot.get("deformation"))
+
+    t0 = time.perf_counter()
+    for _ in range(warmup):
+        one_step()
+    t_warm = time.perf_counter() - t0
+    timed, spent = 0, 0.0
+    while True:
+        t1 = time.perf_counter()
+        one_step()
+        spent += time.perf_counter() - t1  # excludes the one-off state dump after the first step
+        timed += 1
+        if timed >= max_steps or spent >= max_seconds:
             break
-    dt = time.perf_counter() - t0
-    return {"value": steps / dt, "unit": "steps/s", "cores": pyoracle.num_threads(), "kind": "port",
-            "sample": f"{steps} backward-Euler {method} step(s) of the same workload from rest, FP64 oracle "
-                      f"(C++/OpenMP restatement of the reference path), {dt:.1f} s, no warm-up (CPU)"}
+    return {"value": timed / spent, "unit": "steps/s", "cores": pyoracle.num_threads(), "kind": "port",
+            "sample": f"steps {warmup + 1}-{warmup + timed} of the same workload from its initial state "
+                      f"({warmup} untimed warm-up step(s), {t_warm:.1f} s), {method}, FP64 oracle (C++/OpenMP "
+                      f"restatement of the reference path), {spent:.1f} s timed on the host CPU"}
 
 
-def cpu_baseline(workload, max_seconds, max_steps, stepper="newton"):
+def cpu_baseline(workload, max_seconds, max_steps, warmup, stepper="newton", dump=None):
     """Runs the CPU baseline in a fresh process so its OpenMP pool does not share the process with torch."""
     cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
-           "--cpu-seconds", str(max_seconds), "--steps", str(max_steps), "--warmup", "0", "--stepper", stepper]
+           "--cpu-seconds", str(max_seconds), "--steps", str(max_steps), "--warmup", str(warmup),
+           "--stepper", stepper]
+    if dump:
+        cmd += ["--dump-first-state", dump]
     env = dict(os.environ)
     for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
         env.pop(k, None)
@@ -357,6 +398,25 @@ def cpu_baseline(workload, max_seconds, max_steps, stepper="newton"):
         if line.startswith("{"):
             return json.loads(line)["cpu_baseline"]
     return {"value": None, "unavailable": (r.stderr or "no output")[-300:]}
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| over all entries."""
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+def bench_config(scene, stepper, world):
+    """The ``config`` object of both arms' lines (identical, so the two lines describe the same run)."""
+    T, V = scene["cells"].shape[0], scene["X"].shape[0]
+    cells_key = "springs" if scene.get("springs") else ("triangles" if scene.get("tri2d") else "tets")
+    return {
+        "workload": scene["name"], cells_key: T, "vertices": V, "dofs": 3 * V, "stepper": stepper,
+        "solver": SOLVER_TEXT.get(stepper, f"{stepper}, stop |g| <= 1e-6 |g0| (per instance for batches)"),
+        "precision": "GPU value: FP32 Hessian/assembly/PCG vectors with FP64 energy/gradient/state/dots; "
+                     "fp64_plain and the CPU reference: FP64 throughout",
+        "parallelism": "replicas" if world > 1 else "1 GPU",
+        "l2": "working set per step ~1 GB > L2 (no explicit flush)",
+    }
 
 
 def max_over_ranks(values):
@@ -388,6 +448,7 @@ def main():
                     help="ssim_gb_params.pcg_persistent of the GPU arms (3: automatic; 4: pipelined PCG)")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dump-first-state", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the differentiable-rollout timing (32^3 cube, 40 steps)")
@@ -404,19 +465,21 @@ def main():
         dist.init_process_group("gloo")
 
     scene = make_scene(args.workload)
-    T, V = scene["cells"].shape[0], scene["X"].shape[0]
-    cells_key = "springs" if scene.get("springs") else ("triangles" if scene.get("tri2d") else "tets")
+    T = scene["cells"].shape[0]
+    config = bench_config(scene, args.stepper, world)
+    cells_key = next(k for k in ("tets", "springs", "triangles") if k in config)
+    cpu_method = args.stepper if args.stepper in ("newton", "lbfgs", "pd") else "newton"
 
     if args.impl == "reference":
+        # the reference's CPU path (its restatement: the reference itself does not build here) over the GPU
+        # arm's step window; nothing of the GPU library is loaded
         if rank == 0:
-            method = args.stepper if args.stepper in ("newton", "lbfgs", "pd") else "newton"
-            cb = cpu_baseline_inproc(scene, args.cpu_seconds, max(1, args.steps), method)
+            cb = cpu_baseline_inproc(scene, args.cpu_seconds, max(1, args.steps), args.warmup, cpu_method,
+                                     args.dump_first_state)
             line = {
                 "metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-                "config": {"workload": scene["name"], cells_key: T, "vertices": V,
-                           "solver": f"{method} (Newton: block-Jacobi PCG), stop 1e-6 rel"},
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)", "config": config,
                 "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             }
@@ -436,7 +499,7 @@ def main():
     roofline = None
     # algorithmic bytes of one SpMV of the system matrix as a scalar CSR in FP32 (the reference's format):
     # nnz (value + column) + row pointers + x read + y written; one PCG iteration adds 7 n-vectors
-    s_b, n = 4, 3 * V
+    s_b, n = 4, 3 * scene["X"].shape[0]
     spmv_algo = r.get("nnz", 0) * (s_b + 4) + 4 * (n + 1) + 2 * s_b * n
     if prof and prof["pcg_iteration"]["launches"] > 0:
         p = prof["pcg_iteration"]
@@ -452,7 +515,8 @@ def main():
                     "bound": "hbm", "achieved": round(algo / avg_s / 1e9, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(algo / avg_s / 1e9 / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_iteration": algo, "avg_iteration_us": round(avg_s * 1e6, 2),
-                    "iterations_timed": p["launches"], "traffic": ncu_traffic(args.workload, "pipe_persistent" if pipe else "cgcg_persistent"),
+                    "iterations_timed": p["launches"],
+                    "traffic": ncu_traffic(args.workload, "pipe_persistent" if pipe else "cgcg_persistent"),
                     "format_bytes_per_iteration": round(p["bytes_per_launch"]),
                     "format_frac": round(p["bytes_per_launch"] / avg_s / 1e9 / peak, 4)}
     elif prof and prof["pcg_spmv"]["launches"] > 0:
@@ -468,10 +532,20 @@ def main():
     st = r["st_mixed"]
     stf = r["st_fp64"]
     if rank == 0:
-        cb = None
+        cb, err = None, None
         if not args.no_cpu_baseline:
-            cb = cpu_baseline(args.workload, args.cpu_seconds, args.steps,
-                              args.stepper if args.stepper in ("newton", "lbfgs", "pd") else "newton")
+            import tempfile
+
+            with tempfile.TemporaryDirectory() as tmp:
+                dump = os.path.join(tmp, "oracle_first_state.npy")
+                cb = cpu_baseline(args.workload, args.cpu_seconds, args.steps, args.warmup, cpu_method, dump)
+                if os.path.exists(dump):
+                    uo = np.load(dump)
+                    err = {k: rel_err(v, uo) for k, v in r.get("first", {}).items() if v is not None}
+                    err.update(after_steps=1, measure="max|u_gpu - u_oracle| / max|u_oracle| after the first step "
+                               "from the scene's initial state, every arm (and the oracle) at the bench's solver "
+                               "settings (Newton stop 1e-6 relative)")
+        rel_res = [s["grad_norm"] / s["grad_norm0"] if s["grad_norm0"] > 0 else 0.0 for s in st]
         line = {
             "metric": METRIC,
             "value": round(value, 4),
@@ -485,33 +559,32 @@ def main():
             "vs_baseline": None,
             "dtype": "f32+f64",
             "data": "synthetic (seeded SplitMix64 material)",
-            "config": {
-                "workload": scene["name"], cells_key: T, "vertices": V, "dofs": 3 * V,
-                "solver": ("Newton, stop |g| <= 1e-6 |g0|, block-Jacobi PCG with forcing eta = min(1e-1, max(5e-2, "
-                           "|g|/|g0|)); mixed: Chronopoulos-Gear PCG in one cooperative launch per solve, FP64: two "
-                           "launches per PCG iteration") if args.stepper == "newton" else
-                          f"{args.stepper}, stop |g| <= 1e-6 |g0| (per instance for batches)",
-                "precision": "mixed: FP32 Hessian/assembly/PCG vectors, FP64 energy/gradient/state/dots",
-                "parallelism": "replicas" if world > 1 else "1 GPU",
-                "l2": "working set per step ~1 GB > L2 (no explicit flush)",
-            },
+            "config": config,
             "fp64_plain": {"value": round(fp64_value, 4), "unit": "steps/s", "ms_per_step": round(ms_fp64 / args.steps, 3),
-                           "newton_iters": [s["newton_iters"] for s in stf], "cg_iters": [s["cg_iters_total"] for s in stf]},
+                           "newton_iters": sum(s["newton_iters"] for s in stf),
+                           "cg_iters": sum(s["cg_iters_total"] for s in stf)},
             "mixed_over_fp64": round(value / fp64_value, 3),
-            "newton_iters": [s["newton_iters"] for s in st],
-            "cg_iters": [s["cg_iters_total"] for s in st],
-            "rel_residual": [s["grad_norm"] / s["grad_norm0"] if s["grad_norm0"] > 0 else 0.0 for s in st],
+            "newton_iters": sum(s["newton_iters"] for s in st),
+            "cg_iters": sum(s["cg_iters_total"] for s in st),
+            "max_rel_residual": max(rel_res) if rel_res else None,
+            "err_vs_oracle": err,
             f"{cells_key}_per_s": round(T * value, 1),
-            "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
-            "adjoint": r.get("adjoint"),
             "e2e": {"value": round(steps_total / e2e_s, 4), "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": r["launches"],
-            "pcg_iters_per_solve_from_reset": r.get("solve_log"),
             "roofline": roofline,
             "cpu_baseline": cb,
             "clocks": r["clocks"],
+            "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
+            "adjoint": r.get("adjoint"),
         }
+        # per-step detail (Newton / PCG iteration counts, residuals, PCG length of every solve) on stderr
+        print(json.dumps({"detail": {"newton_iters": [s["newton_iters"] for s in st],
+                                     "cg_iters": [s["cg_iters_total"] for s in st], "rel_residual": rel_res,
+                                     "fp64_newton_iters": [s["newton_iters"] for s in stf],
+                                     "fp64_cg_iters": [s["cg_iters_total"] for s in stf],
+                                     "pcg_iters_per_solve_from_reset": r.get("solve_log")}}),
+              file=sys.stderr, flush=True)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

@@ -301,9 +301,11 @@ SSIM_GB_API ssim_gb_status ssim_gb_set_field_device(ssim_gb_timestep* h, int32_t
  * Inputs (device): X, u, x_tilde [V,3] float64; cells [T,4] int32, 16-byte aligned; dminv [T,3,3] (rows of
  * Dm^-1, ssim_gb_get_dminv's layout); rest_volume, lambda, mu [T].  Output: *energy_out (device, one
  * double), written on `stream` (a cudaStream_t; NULL = the legacy default stream).
- * Scratch: a fixed 128 KiB array inside the library, held by every GPU that loads it until the process
+ * Scratch: a fixed 64 KiB array inside the library, held by every GPU that loads it until the process
  * exits.  num_cells above SSIM_GB_NOALLOC_MAX_CELLS is rejected (SSIM_GB_ERR_INVALID_ARGUMENT).  The first
- * call on a device looks up that array's device address; make that first call before any stream capture.
+ * call on a device, and the first in each further CUDA context of it (a non-primary context, or the primary
+ * context re-created after cudaDeviceReset), looks up that array's device address; make that first call
+ * before any stream capture.
  * All calls share the array: calls that overlap on the GPU (different streams, or different host threads
  * without ordering) race and give wrong results; calls queued on one stream are safe. */
 #define SSIM_GB_NOALLOC_MAX_CELLS (1 << 20)

@@ -6,6 +6,7 @@
 // device memory it is given (a framework's caching allocator or a fixed memory budget set at start-up), or a
 // loop that must not pay an allocation's latency or risk its failure once it is running.  They hand in
 // every input and the output; this file brings the rest with it.
+#include <cuda.h>  // CUcontext / CUresult types only: cuCtxGetCurrent is fetched through the runtime
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -21,14 +22,36 @@ namespace {
 
 constexpr int NB = 128;  // threads per block, one tet per thread
 
-// Scratch of the deterministic grid reduction: two partial sums (energy, its term scale) per block, then
-// the arrival counter.  Every GPU that loads the library holds these 128 KiB until the process exits.
+// Scratch of the deterministic grid reduction: one partial sum per block, then the arrival counter.
+// Every GPU that loads the library holds these 64 KiB until the process exits.
 constexpr int kMaxBlocks = SSIM_GB_NOALLOC_MAX_CELLS / NB;
-static __device__ __align__(256) double g_noalloc_scratch[2 * kMaxBlocks + 32];
+static __device__ __align__(256) double g_noalloc_scratch[kMaxBlocks + 32];
 
-// per-device address of g_noalloc_scratch, looked up once per device
+// Address of g_noalloc_scratch per device, with the CUDA context it was looked up in: a symbol's device
+// address belongs to a context, so a call made in another context (a non-primary context, or the primary
+// context re-created after cudaDeviceReset) looks it up again.
 std::mutex g_mutex;
 double* g_scratch_ptr[64] = {nullptr};
+CUcontext g_scratch_ctx[64] = {nullptr};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+
+// the calling thread's current context, or nullptr if the driver entry point is not available
+CUcontext current_context() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  CUcontext c = nullptr;
+  if (fn == nullptr || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
 
 // The value-only variant of the element energy kernel (kernels_elem.cu, elem_energy_grad_kernel): same
 // per-tet terms, the reference's AoS [T,3,3] Dm^-1 layout, and the reduction's partials and counter in the
@@ -39,9 +62,9 @@ __global__ void __launch_bounds__(NB)
                           const double* __restrict__ vol, const double* __restrict__ lam_e,
                           const double* __restrict__ mu_e, int nt, double dt2, double rho, double* scratch,
                           double* out) {
-  __shared__ double shred[NB / 32][2];
+  __shared__ double shred[NB / 32][1];
   const int e = blockIdx.x * NB + threadIdx.x;
-  double energy = 0, escale = 0;
+  double energy = 0;
   if (e < nt) {
     const int4 c = cells[e];
     const int vid[4] = {c.x, c.y, c.z, c.w};
@@ -73,13 +96,12 @@ __global__ void __launch_bounds__(NB)
 #pragma unroll
     for (int i = 0; i < 4; ++i) q += dd[i][0] * dd[i][0] + dd[i][1] * dd[i][1] + dd[i][2] * dd[i][2];
     energy = dt2 * V * snh_energy<double>(F, lam, mu) + 0.5 * m * q;
-    escale = dt2 * V * snh_energy_scale<double>(F, lam, mu) + 0.5 * m * q;
   }
-  double v2[2] = {energy, escale};
-  block_sum<2, NB>(v2, shred);
-  double tot[2];
-  unsigned int* counter = reinterpret_cast<unsigned int*>(scratch + 2 * kMaxBlocks);
-  if (grid_sum_last<2, NB>(v2, scratch, counter, tot)) *out = tot[0];
+  double v1[1] = {energy};
+  block_sum<1, NB>(v1, shred);
+  double tot[1];
+  unsigned int* counter = reinterpret_cast<unsigned int*>(scratch + kMaxBlocks);
+  if (grid_sum_last<1, NB>(v1, scratch, counter, tot)) *out = tot[0];
 }
 
 }  // namespace
@@ -109,10 +131,12 @@ extern "C" SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, co
   }
   double* scratch = nullptr;
   {
+    const CUcontext ctx = current_context();
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (g_scratch_ptr[dev] == nullptr) {
-      // first call on this device: the device address of the fixed scratch array (host code cannot use the
-      // symbol itself, which names a host-side stand-in)
+    if (g_scratch_ptr[dev] == nullptr || ctx == nullptr || ctx != g_scratch_ctx[dev]) {
+      // first call on this device (or in this context): the device address of the fixed scratch array (host
+      // code cannot use the symbol itself, which names a host-side stand-in).  Without the driver's context
+      // query the lookup runs on every call.
       void* p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || p == nullptr) {
@@ -120,13 +144,14 @@ extern "C" SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, co
         return fail(SSIM_GB_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       }
       g_scratch_ptr[dev] = static_cast<double*>(p);
+      g_scratch_ctx[dev] = ctx;
     }
     scratch = g_scratch_ptr[dev];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the arrival counter must start at zero (each completed call leaves it at zero; clearing it here also
   // recovers from a call that did not complete)
-  unsigned int* counter = reinterpret_cast<unsigned int*>(scratch + 2 * kMaxBlocks);
+  unsigned int* counter = reinterpret_cast<unsigned int*>(scratch + kMaxBlocks);
   const cudaError_t me = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
   if (me != cudaSuccess) {
     cudaGetLastError();

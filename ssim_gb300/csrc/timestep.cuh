@@ -175,6 +175,14 @@ struct TimeStep {
   }
 
   // element / spring pass at u = next (+ alpha d): energy (+ local forces into lf) into the trial scalars;
+  // the per-triangle FP32 delta that the stable Neo-Hookean FP32 triangle pass reads (the linear model reads
+  // none); refuses to hand the kernel a missing array
+  const float* tri_delta32() const {
+    if (elastic_model != SSIM_GB_MODEL_LINEAR && fdelta.p == nullptr)
+      throw state_error("the FP32 triangle pass needs the per-element delta: the material is not uploaded");
+    return fdelta.p;
+  }
+
   // fp32: the FP32 element / spring arithmetic of the mixed path's early iterations
   template <typename S>
   void launch_trial(const V4<S>* d, double alpha, bool forces, bool fp32 = false) {
@@ -184,8 +192,8 @@ struct TimeStep {
           launch_spring_energy_grad32<float>(spd(), s32(), next.p, inertia.p, vmass.p, nv, d, alpha, dt * dt,
                                              forces ? sp_lf32.p : nullptr, forces, true, red(), stream);
         else if (tri2d)
-          launch_tri_energy_grad32(e64(), e32s(), fdelta.p, s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
-                                   forces, true, red(), stream);
+          launch_tri_energy_grad32(e64(), e32s(), tri_delta32(), s32(), d, alpha, dt * dt, rho,
+                                   forces ? lf32t.p : nullptr, forces, true, red(), stream);
         else
           launch_elem_energy_grad32(e64(), e32s(), s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
                                     forces, true, red(), stream);
@@ -674,7 +682,7 @@ struct TimeStep {
       launch_spring_energy_grad32<float>(spd(), s32(), next.p, inertia.p, vmass.p, nv, nullptr, 0.0, dt * dt,
                                          sp_lf32.p, true, false, red(), stream);
     else if (tri2d)
-      launch_tri_energy_grad32(e64(), e32s(), fdelta.p, s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false,
+      launch_tri_energy_grad32(e64(), e32s(), tri_delta32(), s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false,
                                red(), stream);
     else
       launch_elem_energy_grad32(e64(), e32s(), s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false, red(),

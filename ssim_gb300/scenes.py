@@ -2,7 +2,7 @@
 
 Each scene returns a dict with the mesh, the material, the boundary and the
 time-stepping settings; ``build_timestep`` turns it into a GPU ``TimeStep`` and
-the tests feed the same dict to the oracle.  No public dataset is involved.
+the tests set the same dict up on the oracle (oracle/scenes.py).  No public dataset is involved.
 """
 from __future__ import annotations
 
@@ -204,7 +204,7 @@ def build_timestep(scene, precision="fp64", stepper="newton", params=None, rtol=
         ts = TimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"], scene["rho"])
     ts.set_precision(precision)
     if scene.get("E_cells") is not None:
-        ts.set_material(scene["E_cells"], None)
+        ts.set_material(scene["E_cells"], scene.get("nu_cells"))
     if len(scene["fixed"]):
         ts.mark_dirichlet_batched(scene["fixed"], np.zeros((len(scene["fixed"]), 3)))
     if any(scene["gravity"]):
@@ -217,34 +217,8 @@ def build_timestep(scene, precision="fp64", stepper="newton", params=None, rtol=
     if scene.get("u0") is not None:
         ts.set("deformation", scene["u0"])
         ts.set("prev_deform", scene["u0"])
-    return ts
-
-
-def build_oracle(scene, rtol=None):
-    """The same scene on the FP64 CPU oracle (test infrastructure)."""
-    from oracle import pyoracle
-
-    if scene.get("springs"):
-        ts = pyoracle.OracleTimeStep.springs(scene["X"], scene["cells"], scene["k"],
-                                             vertex_mass=scene["vertex_mass"], time_step=scene["dt"])
-    elif scene.get("tri2d"):
-        ts = pyoracle.OracleTimeStep.tri2d(scene["X2"], scene["cells"], scene["dt"], scene["E"], scene["nu"],
-                                           scene["rho"])
-    else:
-        ts = pyoracle.OracleTimeStep(scene["X"], scene["cells"], scene["dt"], scene["E"], scene["nu"],
-                                     scene["rho"])
-    if scene.get("E_cells") is not None:
-        ts.set_material(scene["E_cells"], None)
-    if len(scene["fixed"]):
-        ts.mark_dirichlet(scene["fixed"])
-    if any(scene["gravity"]):
-        ts.add_gravity(scene["gravity"])
-    if rtol is not None:
-        ts.set_threshold(rtol)
-    ts.reset()
-    if scene.get("u0") is not None:
-        ts.set("deformation", scene["u0"])
-        ts.set("prev_deform", scene["u0"])
+    if scene.get("velocity") is not None:
+        ts.set("velocity", scene["velocity"])
     return ts
 
 
@@ -308,19 +282,3 @@ def build_batch_timestep(batch, precision="mixed", params=None):
     ts.reset("newton")
     ts.set("velocity", batch["velocity"])
     return ts
-
-
-def batch_instance_oracle(batch, i):
-    """Instance i of the batch on the FP64 oracle (test infrastructure)."""
-    from oracle import pyoracle
-
-    a, b = batch["vertex_offsets"][i], batch["vertex_offsets"][i + 1]
-    X = batch["X"][a:b]
-    cells = batch["cells"]
-    sel = (cells[:, 0] >= a) & (cells[:, 0] < b)
-    T = cells[sel] - a
-    ot = pyoracle.OracleTimeStep(X, T, batch["dt"], batch["E_inst"][i], batch["nu_inst"][i], batch["rho"])
-    ot.mark_dirichlet(np.where(X[:, 2] == 0.0)[0])
-    ot.reset()
-    ot.set("velocity", batch["velocity"][a:b])
-    return ot

@@ -5,6 +5,7 @@ import pytest
 
 import ssim_gb300 as g
 from ssim_gb300 import mesh, scenes
+from oracle import scenes as oscenes
 
 pytestmark = pytest.mark.gpu
 
@@ -29,7 +30,7 @@ def _drop_z(ot, which="sysmatrix"):
 def test_rest_shape_pattern_mass():
     sc = _small()
     ts = scenes.build_timestep(sc, stepper="none")
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     assert ts.dim == 2
     assert rel(ts.rest_volume(), ot.rest_vol()) <= 1e-15
     assert rel(ts.dminv().reshape(-1, 4), ot.dminv().reshape(-1, 9)[:, :4]) <= 1e-15
@@ -49,7 +50,7 @@ def test_rest_shape_pattern_mass():
 def test_energy_gradient_hessian(model):
     sc = _small()
     ts = scenes.build_timestep(sc, stepper="none")
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     ts.set_elastic_model(model)
     ot.set_model(model)
     rng = np.random.default_rng(11)
@@ -86,7 +87,7 @@ def test_newton_trajectory_fp64_and_2dof_export():
     params = g.default_params(stop_mode=1, rel_tol=1e-11, cg_rtol=1e-13, cg_max_iters=20000, stop_floor=0.0)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-11, cg_rtol=1e-13, cg_max_iters=20000, stop_floor=0.0)
     ts = scenes.build_timestep(sc, precision="fp64", stepper="newton", params=params)
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     for _ in range(5):
         ts.step()
         st = ts.stats()
@@ -116,7 +117,7 @@ def test_lbfgs_pd_fp64(method):
                               stop_floor=0.0)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, stop_floor=0.0)
     ts = scenes.build_timestep(sc, precision="fp64", stepper=method, params=params)
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     for _ in range(3):
         ts.step()
         st = ts.stats()
@@ -134,7 +135,7 @@ def test_mixed_newton_residual():
     params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-2, cg_eta_min=1e-4)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12)
     ts = scenes.build_timestep(sc, precision="mixed", stepper="newton", params=params)
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     for _ in range(4):
         ts.step()
         st = ts.stats()
@@ -162,13 +163,15 @@ def test_mixed_lbfgs_fp32_phase():
             assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"], st
         states.append(ts.get("deformation"))
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, max_lbfgs_iters=20000)
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     for _ in range(3):
         ot.prepare_step()
         ot.compute_step("lbfgs", op)
         ot.step_next()
     uo = ot.get("deformation")
     assert rel(states[0], uo) <= 1e-4 and rel(states[1], uo) <= 1e-4
+    # the FP32 triangle pass did run: its iterates differ from the all-FP64-evaluation run's
+    assert not np.array_equal(states[0], states[1])
 
 
 def test_2d_errors():

@@ -5,6 +5,7 @@ import pytest
 
 import ssim_gb300 as g
 from ssim_gb300 import scenes
+from oracle import scenes as oscenes
 
 pytestmark = pytest.mark.gpu
 
@@ -20,7 +21,7 @@ def test_batch_matches_instances_fp64():
     params = g.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000, precond=2,
                               stop_floor=0.0)
     ts = scenes.build_batch_timestep(batch, precision="fp64", params=params)
-    ots = [scenes.batch_instance_oracle(batch, i) for i in range(5)]
+    ots = [oscenes.batch_instance_oracle(batch, i) for i in range(5)]
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000, precond=2,
                                  stop_floor=0.0)
     for _ in range(3):

@@ -9,6 +9,7 @@ import pytest
 
 import ssim_gb300 as g
 from ssim_gb300 import scenes
+from oracle import scenes as oscenes
 
 pytestmark = pytest.mark.gpu
 
@@ -27,7 +28,7 @@ def _small(n=12):
 def test_pattern_and_mass():
     sc = _small()
     ts = scenes.build_timestep(sc, stepper="none")
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     rp, ci = ts.csr_pattern()
     rpo, cio = ot.csr_pattern()
     assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
@@ -39,7 +40,7 @@ def test_pattern_and_mass():
 def test_energy_gradient_hessian():
     sc = _small()
     ts = scenes.build_timestep(sc, stepper="none")
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     rng = np.random.default_rng(21)
     v = rng.uniform(-1, 1, sc["X"].shape)
     u = rng.uniform(-1, 1, sc["X"].shape) * 0.02
@@ -74,7 +75,7 @@ def test_steppers_fp64_match_oracle(method):
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-12, cg_max_iters=20000,
                                  max_lbfgs_iters=50000, max_newton_iters=200)
     ts = scenes.build_timestep(sc, precision="fp64", stepper=method, params=params)
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     for _ in range(3):
         ts.prepare_step()
         ts.compute_step()
@@ -103,7 +104,7 @@ def test_steppers_mixed_reach_residual(method):
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12, cg_max_iters=20000,
                                  max_newton_iters=200)
     ts = scenes.build_timestep(sc, precision="mixed", stepper=method, params=params)
-    ot = scenes.build_oracle(sc)
+    ot = oscenes.build_oracle(sc)
     for _ in range(3):
         ts.step()
         st = ts.stats()

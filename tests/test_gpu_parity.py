@@ -9,6 +9,7 @@ import pytest
 
 import ssim_gb300 as g
 from ssim_gb300 import mesh, scenes
+from oracle import scenes as oscenes
 
 pytestmark = pytest.mark.gpu
 
@@ -152,7 +153,7 @@ def test_mixed_kernels_close_to_fp64():
 
 def _run(scene, precision, params, oracle_params, steps, rtol=None):
     ts = scenes.build_timestep(scene, precision=precision, params=params, rtol=rtol)
-    ot = scenes.build_oracle(scene, rtol=rtol)
+    ot = oscenes.build_oracle(scene, rtol=rtol)
     hist = []
     for _ in range(steps):
         ts.prepare_step()
@@ -302,7 +303,7 @@ def test_lbfgs_and_pd_fp64(method):
     params = g.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-11, max_lbfgs_iters=20000, precond=2)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000)
     ts = scenes.build_timestep(scene, precision="fp64", stepper=method, params=params)
-    ot = scenes.build_oracle(scene)
+    ot = oscenes.build_oracle(scene)
     for _ in range(3):
         ts.prepare_step()
         ts.compute_step()
@@ -326,7 +327,7 @@ def test_lbfgs_history_compact_and_two_loop(history):
     params = g.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, lbfgs_history=history)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, lbfgs_history=history)
     ts = scenes.build_timestep(scene, precision="fp64", stepper="lbfgs", params=params)
-    ot = scenes.build_oracle(scene)
+    ot = oscenes.build_oracle(scene)
     for _ in range(2):
         ts.step()
         st = ts.stats()
@@ -372,7 +373,7 @@ def test_pd_partly_fixed_vertices_fall_back_to_blocks():
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=20000, stop_floor=0.0)
     for partial in (False, True):
         ts = scenes.build_timestep(scene, precision="fp64", stepper="none", params=params)
-        ot = scenes.build_oracle(scene)
+        ot = oscenes.build_oracle(scene)
         if partial:  # the bottom face may slide in x and y
             X = scene["X"]
             t = ts.dof_type().copy()
@@ -398,7 +399,7 @@ def test_pd_matrix_matches_oracle():
 
     scene = scenes.cube10()
     ts = scenes.build_timestep(scene, precision="fp64", stepper="pd", params=g.default_params(precond=2))
-    ot = scenes.build_oracle(scene)
+    ot = oscenes.build_oracle(scene)
     A = ot.pd_matrix_values()
     assert np.all(np.isfinite(A))
     # first L-BFGS-PD iteration direction is -A^{-1} g: compare after one prepare_step at rest + gravity
@@ -425,7 +426,7 @@ def test_forward_euler_matches_oracle():
 
     scene = scenes.cube10()
     ts = scenes.build_timestep(scene, precision="fp64", stepper="forward_euler")
-    ot = scenes.build_oracle(scene)
+    ot = oscenes.build_oracle(scene)
     for _ in range(3):
         ts.prepare_step()
         r = ts.compute_step()
@@ -445,7 +446,7 @@ def test_h0_stepper_fp64():
     scene = scenes.cube10()
     params = g.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-11, max_lbfgs_iters=5000, precond=2)
     ts = scenes.build_timestep(scene, precision="fp64", stepper="h0", params=params)
-    ot = scenes.build_oracle(scene)
+    ot = oscenes.build_oracle(scene)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9, max_lbfgs_iters=5000)
     for _ in range(3):
         ts.prepare_step()
@@ -679,7 +680,7 @@ def test_pd_per_element_diffusivity():
         res[mode] = (st["converged"], st["newton_iters"], st["grad_norm"] / st["grad_norm0"])
         if mode == 2:
             assert st["converged"] == 1, st
-            ot = scenes.build_oracle(scene)
+            ot = oscenes.build_oracle(scene)
             ot.set_pd_diffusivity_mode(2)
             ot.prepare_step()
             _, sto = ot.compute_step("pd", pyoracle.default_params(stop_mode=1, rel_tol=1e-8, max_lbfgs_iters=400))
@@ -712,7 +713,7 @@ def test_mixed_fp32_elements_confirmed_in_fp64(scene_name):
             assert abs(np.linalg.norm(ts.get("forces")) - st["grad_norm"]) <= 1e-9 * st["grad_norm0"]
             ts.step_next()
         states.append(ts.get("deformation"))
-    ot = scenes.build_oracle(scene)
+    ot = oscenes.build_oracle(scene)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-10, cg_rtol=1e-12)
     for _ in range(4):
         ot.prepare_step()
@@ -720,6 +721,8 @@ def test_mixed_fp32_elements_confirmed_in_fp64(scene_name):
         ot.step_next()
     uo = ot.get("deformation")
     assert rel(states[0], uo) <= 1e-4 and rel(states[1], uo) <= 1e-4
+    # the FP32 pass did run: its iterates differ from the all-FP64-evaluation run's (within the tolerance)
+    assert not np.array_equal(states[0], states[1])
 
 
 def test_two_handles_step_concurrently_from_threads():
@@ -758,7 +761,7 @@ def test_reference_harness_scene_step_by_step():
 
     sc = scenes.reference_beam()
     ts = scenes.build_timestep(sc, precision="fp64", stepper="newton", params=g.default_params(), rtol=sc["rtol"])
-    ot = scenes.build_oracle(sc, rtol=sc["rtol"])
+    ot = oscenes.build_oracle(sc, rtol=sc["rtol"])
     op = pyoracle.default_params()
     iters, iters_o = [], []
     for _ in range(20):

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from ssim_gb300 import scenes
+from oracle import scenes as oscenes
 
 
 def _dense(ts, which="sysmatrix"):
@@ -117,7 +118,7 @@ def test_spring_steppers_agree(oracle):
     sc = scenes.cloth(8, h=0.05, k=1e3, areal_density=0.5, dt=1e-2)
     outs = {}
     for method in ("newton", "lbfgs", "pd"):
-        ts = scenes.build_oracle(sc, rtol=1e-10)
+        ts = oscenes.build_oracle(sc, rtol=1e-10)
         p = oracle.default_params(max_newton_iters=100000, max_lbfgs_iters=100000)
         for _ in range(2):
             ts.prepare_step()
