@@ -387,7 +387,7 @@ def cpu_baseline(workload, max_seconds, max_steps, warmup, stepper="newton", dum
     """Runs the CPU baseline in a fresh process so its OpenMP pool does not share the process with torch."""
     cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
            "--cpu-seconds", str(max_seconds), "--steps", str(max_steps), "--warmup", str(warmup),
-           "--stepper", stepper]
+           "--stepper", stepper, "--precond", str(SOLVER["precond"])]
     if dump:
         cmd += ["--dump-first-state", dump]
     env = dict(os.environ)
@@ -446,6 +446,8 @@ def main():
                     help="PD diffusivity: 0 the reference's (E, nu) slots, 1 Lame, 2 per element")
     ap.add_argument("--pcg-variant", type=int, default=3, choices=[0, 1, 2, 3, 4],
                     help="ssim_gb_params.pcg_persistent of the GPU arms (3: automatic; 4: pipelined PCG)")
+    ap.add_argument("--precond", type=int, default=None, choices=[1, 2, 3],
+                    help="PCG preconditioner of every arm (1 Jacobi, 2 block-Jacobi, 3 slice); default: the bench's")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-first-state", default=None, help=argparse.SUPPRESS)
@@ -453,6 +455,8 @@ def main():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the differentiable-rollout timing (32^3 cube, 40 steps)")
     args = ap.parse_args()
+    if args.precond is not None:
+        SOLVER["precond"] = args.precond
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
 

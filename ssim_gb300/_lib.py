@@ -68,6 +68,7 @@ class Params(C.Structure):
         ("ls_energy_slack32", C.c_double),
         ("elem32_switch", C.c_double),
         ("pcg_pipe_iters", C.c_int32),
+        ("fused_assembly", C.c_int32),
     ]
 
     def as_dict(self):

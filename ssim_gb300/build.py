@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libssim_gb300.so")
-SOURCES = ["kernels_elem.cu", "kernels_sparse.cu", "kernels_adjoint.cu", "kernels_springs.cu", "kernels_lbfgs.cu", "kernels_tri.cu",
+SOURCES = ["kernels_elem.cu", "kernels_sparse.cu", "kernels_adjoint.cu", "kernels_springs.cu", "kernels_lbfgs.cu", "kernels_tri.cu", "kernels_fused.cu",
            "timestep.cu",
            "topology.cpp", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

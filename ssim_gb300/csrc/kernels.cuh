@@ -95,6 +95,48 @@ struct SellMatrix {
   const int* lo_col;    // [nlslots] block column (own row for padding)
 };
 
+// 3x3 preconditioner rows from a diagonal block a (row-major): 0 identity, 1 Jacobi, 2 block-Jacobi
+// (inverse of the symmetric block by its adjugate; falls back to Jacobi if the block is singular).
+template <typename S>
+__device__ __forceinline__ void precond_rows(const S* a, int precond, V4<S>* out) {
+  S m[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m[i] = S(0);
+  if (precond == 2 || precond == 3) {  // 3: the slice preconditioner starts from (and falls back to) these
+    const S c0 = a[4] * a[8] - a[5] * a[7], c1 = a[5] * a[6] - a[3] * a[8], c2 = a[3] * a[7] - a[4] * a[6];
+    const S det = a[0] * c0 + a[1] * c1 + a[2] * c2;
+    if (det > S(0) && isfinite(det)) {
+      const S id = S(1) / det;
+      m[0] = c0 * id;
+      m[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+      m[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+      m[3] = c1 * id;
+      m[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+      m[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+      m[6] = c2 * id;
+      m[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+      m[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+      // symmetrise (the block is symmetric; keeps the preconditioner exactly symmetric)
+      const S m01 = S(0.5) * (m[1] + m[3]), m02 = S(0.5) * (m[2] + m[6]), m12 = S(0.5) * (m[5] + m[7]);
+      m[1] = m[3] = m01;
+      m[2] = m[6] = m02;
+      m[5] = m[7] = m12;
+    } else {
+      precond = 1;
+    }
+  }
+  if (precond == 1) {
+    m[0] = a[0] != S(0) ? S(1) / a[0] : S(1);
+    m[4] = a[4] != S(0) ? S(1) / a[4] : S(1);
+    m[8] = a[8] != S(0) ? S(1) / a[8] : S(1);
+  } else if (precond == 0) {
+    m[0] = m[4] = m[8] = S(1);
+  }
+  out[0] = mk4<S>(m[0], m[1], m[2]);
+  out[1] = mk4<S>(m[3], m[4], m[5]);
+  out[2] = mk4<S>(m[6], m[7], m[8]);
+}
+
 // ---------------- element kernels (FP64 energy / gradient) ----------------
 // lf[e] = dt^2 V_e * local elastic force + element inertia force M_e (u - x_tilde); energy reduced into
 // sc->energy.  When trial, u is replaced by u + alpha * d and the energy goes to sc->trial_energy (forces
@@ -161,6 +203,18 @@ void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double*
 
 // ---------------- assembly / sparse ----------------
 // precond: 0 identity, 1 Jacobi (diagonal of the diagonal block), 2 block-Jacobi (inverse 3x3 block)
+// element Hessian and assembly in one pass for tets (kernels_fused.cu): CTA b owns the block rows of slices
+// [spc b, spc (b + 1)); fptr / felem / fcode are the lists of topology.h's FusedLists.  Writes vals (and the
+// preconditioner rows dinv) exactly as launch_elem_hessian followed by launch_assemble would, up to the
+// order of the FP sums
+template <typename S>
+void launch_fused_hessian(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
+                          const float4* xf, double dt2, bool spsd, const SellMatrix& A, int nslices, int spc,
+                          int ncta, const int* fptr, const int* felem, const uint16_t* fcode, const S* slot_mass,
+                          const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st);
+// entries per chunk of the fused kernel's lists (the rank of a block counts within a chunk)
+int fused_chunk();
+
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
                      const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st);
@@ -173,7 +227,8 @@ void launch_export_csr(const SellMatrix& A, const int* bptr, const int* slot_k, 
 // ---------------- PCG (fused) ----------------
 template <typename S>
 void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
-                      double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st);
+                      double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st,
+                      const V4<S>* lmat = nullptr);
 template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
                      V4<S>* q, bool first, const Reduce& red, cudaStream_t st, bool kron = false);
@@ -187,7 +242,7 @@ template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st,
-                           bool kron = false, V4<S>* pm = nullptr, int pipe_iters = 0);
+                           bool kron = false, V4<S>* pm = nullptr, int pipe_iters = 0, const V4<S>* lmat = nullptr);
 // kron: vals holds one value per slot (the matrix is (scalar) (x) I3); launch_kron_extract makes that form
 // from a 9-value store and sets *not_kron when some block is not a multiple of I3
 template <typename S>
@@ -198,7 +253,13 @@ void launch_csr_dof_spmv(int n, const int* rp, const int* ci, const S* vals, con
                          cudaStream_t st);
 template <typename S>
 void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
-                       int max_iters, const Reduce& red, cudaStream_t st);
+                       int max_iters, const Reduce& red, cudaStream_t st, const V4<S>* lmat = nullptr);
+// the slice preconditioner (precond 3): per 32-row slice the block LDL^T factorisation of the slice's
+// block-tridiagonal part, D^-1 into dinv and L into lmat (3 rows per vertex each); block-Jacobi rows and
+// L = 0 for a slice whose pivots are not all positive definite.  With lmat, the PCG kernels apply the slice
+// solve instead of the per-vertex rows (the pipelined variant falls back to Chronopoulos-Gear)
+template <typename S>
+void launch_slice_factor(const SellMatrix& A, int nslices, const S* vals, V4<S>* dinv, V4<S>* lmat, cudaStream_t st);
 
 // ---------------- vector kernels ----------------
 template <typename S>
@@ -269,7 +330,7 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
 // PCG setup from an S right-hand side (the PD stepper's inner solve)
 template <typename S>
 void launch_pcg_setup_v(int nv, const V4<S>* b, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
-                        double rtol, int max_iters, const Reduce& red, cudaStream_t st);
+                        double rtol, int max_iters, const Reduce& red, cudaStream_t st, const V4<S>* lmat = nullptr);
 template <typename S>
 void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st);
 

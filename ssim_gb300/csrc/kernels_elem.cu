@@ -1,8 +1,7 @@
 // kernels_elem.cu -- element-parallel kernels: FP64 energy / gradient (update_energy_and_gradients,
 // time_step.hpp:577-624), the vertex gather of element forces (global_composer.hpp:36-66 +
 // time_step.hpp:608-617) and the element Hessian (wrapped_pfpx, time_step.hpp:23-60, 626-651).
-#include "elem_math.cuh"
-#include "kernels.cuh"
+#include "hessian_elem.cuh"
 
 namespace ssim_gb {
 
@@ -316,23 +315,6 @@ __global__ void __launch_bounds__(GB)
 }
 
 // ------------------------------------------------------------------ element Hessian
-template <typename S>
-struct ElemSel;
-template <>
-struct ElemSel<float> {
-  __device__ static const float* dminv(const ElemFP64&, const ElemFP32& b) { return b.dminv; }
-  __device__ static float vol(const ElemFP64&, const ElemFP32& b, int e) { return b.vol[e]; }
-  __device__ static float lam(const ElemFP64&, const ElemFP32& b, int e) { return b.lam[e]; }
-  __device__ static float mu(const ElemFP64&, const ElemFP32& b, int e) { return b.mu[e]; }
-};
-template <>
-struct ElemSel<double> {
-  __device__ static const double* dminv(const ElemFP64& a, const ElemFP32&) { return a.dminv; }
-  __device__ static double vol(const ElemFP64& a, const ElemFP32&, int e) { return a.vol[e]; }
-  __device__ static double lam(const ElemFP64& a, const ElemFP32&, int e) { return a.lam[e]; }
-  __device__ static double mu(const ElemFP64& a, const ElemFP32&, int e) { return a.mu[e]; }
-};
-
 // One thread per tet: K_e = dt^2 V_e pfpx^T H+ pfpx (the gather weight V_e and alpha = dt^2 of
 // time_step.hpp:646-651 folded in), written as the 10 upper 3x3 vertex blocks, staged through shared
 // memory so the global writes are contiguous.  Launch bounds of 8 blocks per SM (128 registers, a few
@@ -346,47 +328,8 @@ __global__ void __launch_bounds__(HB, 8)
   const int e0 = blockIdx.x * HB;
   const int e = e0 + threadIdx.x;
   if (e < nt) {
-    const int4 c = e64.cells[e];
-    const int vid[4] = {c.x, c.y, c.z, c.w};
-    S x[4][3];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (XF) {
-        const float4 p = xf[vid[i]];
-        x[i][0] = (S)p.x;
-        x[i][1] = (S)p.y;
-        x[i][2] = (S)p.z;
-      } else {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) x[i][k] = (S)(X[vid[i] * 3 + k] + u[vid[i] * 3 + k]);
-      }
-    }
-    const S* dm = ElemSel<S>::dminv(e64, e32);
-    S Dm[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Dm[k] = dm[(size_t)k * nt + e];
-    S F[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc)
-        F[r * 3 + cc] = (x[1][r] - x[0][r]) * Dm[0 * 3 + cc] + (x[2][r] - x[0][r]) * Dm[1 * 3 + cc] +
-                        (x[3][r] - x[0][r]) * Dm[2 * 3 + cc];
-    S D[4][3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      D[1][j] = Dm[0 * 3 + j];
-      D[2][j] = Dm[1 * 3 + j];
-      D[3][j] = Dm[2 * 3 + j];
-      D[0][j] = -(Dm[0 * 3 + j] + Dm[1 * 3 + j] + Dm[2 * 3 + j]);
-    }
     S K[78];
-    if (e64.model == 1)
-      linear_stiffness<S>(D, ElemSel<S>::lam(e64, e32, e), ElemSel<S>::mu(e64, e32, e), spsd != 0,
-                          dt2 * ElemSel<S>::vol(e64, e32, e), K);
-    else
-      element_stiffness<S>(F, D, ElemSel<S>::lam(e64, e32, e), ElemSel<S>::mu(e64, e32, e), spsd != 0,
-                           dt2 * ElemSel<S>::vol(e64, e32, e), K);
+    element_hessian_at<S, XF>(e64, e32, X, u, xf, dt2, spsd, e, K);
     S* st = stage + threadIdx.x * 90;
     int blk = 0;
 #pragma unroll

@@ -63,13 +63,15 @@ struct Solver {
   DBuf<S> pd_svals;      // the PD matrix as (scalar) (x) I3: one value per slot, when its blocks allow
   bool pd_kron = false;
   DBuf<V4<S>> pd_dinv;
+  DBuf<V4<S>> lmat, pd_lmat;  // slice preconditioner factors (precond 3) of the system / the H0 matrix
+  bool pd_slice = false;      // the H0 matrix carries the slice factors (pd_lmat)
   DBuf<S> ncg_L, ncg_Lt;  // NCG preconditioner factor and its transpose on the CSR pattern
   long ncg_version = -1;
   void release() {
     for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &pd_svals, &ncg_L, &ncg_Lt}) b->release();
     pd_kron = false;
     ncg_version = -1;
-    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &pm, &ld, &lq, &pd_dinv}) b->release();
+    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &pm, &ld, &lq, &pd_dinv, &lmat, &pd_lmat}) b->release();
     hs.clear();
     hy.clear();
   }
@@ -113,6 +115,11 @@ struct TimeStep {
   DBuf<float4> xf;
   // ---- device: topology
   DBuf<int32_t> vptr, vinc, sl_off, sl_col, slot_row, cptr, csrc, bptr, slot_k, slot_kt, lo_off, lo_src, lo_col;
+  // lists of the fused element-Hessian + assembly kernel (tets; topology.h FusedLists)
+  DBuf<int32_t> fptr, felem;
+  DBuf<uint16_t> fcode;
+  int fused_ncta = 0, fused_spc = 0;
+  bool fused_ok = false;
   DBuf<double> lf, csr_out;
   // ---- device: solver
   Solver<float> sf;
@@ -467,6 +474,20 @@ struct TimeStep {
     lo_src.upload(topo.lo_src, stream);
     lo_col.upload(topo.lo_col, stream);
     lf.alloc((size_t)3 * cv * nt);
+    if (cv == 4) {
+      // 4 slices (128 block rows) per CTA of the fused Hessian + assembly kernel
+      FusedLists fl;
+      build_fused_lists(topo, cells.data(), 4, fused_chunk(), fl);
+      fused_ok = fl.ok;
+      if (fl.ok) {
+        fptr.upload(fl.ptr, stream);
+        felem.upload(fl.elem, stream);
+        fcode.upload(fl.code, stream);
+        fused_ncta = fl.ncta;
+        fused_spc = fl.slices_per_cta;
+        SSIM_CUDA(cudaStreamSynchronize(stream));  // the host lists go out of scope
+      }
+    }
   }
 
   // material: per element Lame parameters (basic_elast.hpp:10-20) and the stable Neo-Hookean constants
@@ -616,7 +637,6 @@ struct TimeStep {
 
   template <typename S>
   void alloc_solver(Solver<S>& s) {
-    s.K.alloc((size_t)9 * (topo.cv * (topo.cv + 1) / 2) * nt);
     s.vals.alloc(9 * (size_t)topo.nslots);
     s.vals.zero(stream);
     s.mvals.release();
@@ -729,6 +749,16 @@ struct TimeStep {
     Solver<S>& s = solver<S>();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
+    if (!springs && !tri2d && fused_ok && params.fused_assembly) {
+      launch_fused_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, A(), topo.nslices,
+                              fused_spc, fused_ncta, fptr.p, felem.p, fcode.p, s.slot_mass.p, mask.p, filter, s.vals.p,
+                              s.dinv.p, params.precond, stream);
+      if (profiling) prof_end(e0, e1, PK_HESS, 0);
+      slice_factor<S>(s);
+      return;
+    }
+    // two kernels through the per-element block buffer (allocated on first use)
+    s.K.alloc((size_t)9 * (topo.cv * (topo.cv + 1) / 2) * nt);
     if (springs)
       launch_spring_hessian<S>(spd(), next.p, dt * dt, spsd, s.K.p, stream);
     else if (tri2d)
@@ -740,6 +770,19 @@ struct TimeStep {
     launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
                        params.precond, stream);
     if (profiling) prof_end(e0, e1, PK_ASM, 0);
+    slice_factor<S>(s);
+  }
+
+  // precond 3: the slice preconditioner's factors from the assembled values
+  template <typename S>
+  void slice_factor(Solver<S>& s) {
+    if (params.precond != 3) return;
+    s.lmat.alloc(3 * (size_t)nv);
+    launch_slice_factor<S>(A(), topo.nslices, s.vals.p, s.dinv.p, s.lmat.p, stream);
+  }
+  template <typename S>
+  const V4<S>* slice_lmat(Solver<S>& s) const {
+    return params.precond == 3 && s.lmat.p != nullptr ? s.lmat.p : nullptr;
   }
 
   void hessian_any(bool spsd, bool filter) {
@@ -756,22 +799,23 @@ struct TimeStep {
   template <typename S>
   int pcg(const double* b, bool negate, double eta, int max_iters, double* rel_res) {
     Solver<S>& s = solver<S>();
-    launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
-    return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true);
+    const V4<S>* lm = slice_lmat<S>(s);
+    launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream, lm);
+    return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true, false, lm);
   }
 
   // PCG on another matrix of the same block pattern (the PD matrix) with an S right-hand side
   template <typename S>
   int pcg_on(const S* vals, const V4<S>* dinv, const V4<S>* b, double eta, int max_iters, double* rel_res,
-             bool kron = false) {
+             bool kron = false, const V4<S>* lmat = nullptr) {
     Solver<S>& s = solver<S>();
-    launch_pcg_setup_v<S>(nv, b, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, red(), stream);
-    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false, kron);
+    launch_pcg_setup_v<S>(nv, b, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, red(), stream, lmat);
+    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false, kron, lmat);
   }
 
   template <typename S>
   int pcg_loop(const S* vals, const V4<S>* dinv, int max_iters, double* rel_res, bool profile_spmv,
-               bool kron = false) {
+               bool kron = false, const V4<S>* lmat = nullptr) {
     Solver<S>& s = solver<S>();
     int variant = params.pcg_persistent;
     // automatic: FP64 runs two launches per iteration (its FP64 dots and updates make the persistent
@@ -787,7 +831,7 @@ struct TimeStep {
       const bool ran = launch_pcg_persistent<S>(A(), vals, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters,
                                                 red(), gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra,
                                                 params.pcg_max_blocks, variant, stream, kron, s.pm.p,
-                                                params.pcg_pipe_iters);
+                                                params.pcg_pipe_iters, lmat);
       if (ran) {
         if (prof) SSIM_CUDA(cudaEventRecord(ev[1], stream));
         sync_scalars();
@@ -818,7 +862,7 @@ struct TimeStep {
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c], stream));
         launch_pcg_spmv<S>(A(), vals, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream, kron);
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c + 1], stream));
-        launch_pcg_update<S>(nv, pnew, s.q.p, dinv, s.x.p, s.r.p, s.z.p, max_iters, red(), stream);
+        launch_pcg_update<S>(nv, pnew, s.q.p, dinv, s.x.p, s.r.p, s.z.p, max_iters, red(), stream, lmat);
       }
       sync_scalars();
       if (prof) {
@@ -905,6 +949,12 @@ struct TimeStep {
                                 stream));
       SSIM_CUDA(cudaMemcpyAsync(s.pd_dinv.p, s.dinv.p, sizeof(V4<S>) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice,
                                 stream));
+      s.pd_slice = slice_lmat<S>(s) != nullptr;
+      if (s.pd_slice) {
+        s.pd_lmat.alloc(3 * (size_t)nv);
+        SSIM_CUDA(cudaMemcpyAsync(s.pd_lmat.p, s.lmat.p, sizeof(V4<S>) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice,
+                                  stream));
+      }
       s.pd_kron = false;  // the projected Hessian is not a multiple of I3 per block
       pd = true;
     }
@@ -989,7 +1039,7 @@ struct TimeStep {
                                stream);
           double rr = 0;
           st.cg_iters_total += pcg_on<S>(s.pd_kron ? s.pd_svals.p : s.pd_vals.p, s.pd_dinv.p, q, pd_tol,
-                                       params.cg_max_iters, &rr, s.pd_kron);
+                                       params.cg_max_iters, &rr, s.pd_kron, h0 && s.pd_slice ? s.pd_lmat.p : nullptr);
           if (i0 >= 0)
             launch_lbfgs_pass<S>(nv, z, nullptr, z, nullptr, nullptr, nullptr, 0.0, nullptr, 1.0, s.hy[i0]->p,
                                  rho_h[i0], bb + i0, red(), stream);
@@ -1078,8 +1128,11 @@ struct TimeStep {
     return up * (9.0 * s + 4.0) + lo * 8.0 + 2.0 * (topo.nslices + 1) * 4 + 4.0 * nv * 4 * s;
   }
 
-  // bytes one PCG update pass moves: p, q, x, r read, x, r, z written, the 3x3 preconditioner blocks
-  double update_bytes(size_t s) const { return 7.0 * nv * 4 * s + 3.0 * nv * 4 * s; }
+  // bytes one PCG update pass moves: p, q, x, r read, x, r, z written, the 3x3 preconditioner blocks (and
+  // the slice preconditioner's L blocks with precond 3)
+  double update_bytes(size_t s) const {
+    return 7.0 * nv * 4 * s + (params.precond == 3 ? 6.0 : 3.0) * nv * 4 * s;
+  }
 
   // ------------------------------------------------------------------ adjoint of one step
   // The handle's next_deform holds u_{n+1}.  ubar, vbar (device [n]) hold the adjoint of (u_{n+1}, v_{n+1}) on

@@ -301,4 +301,72 @@ void slot_pd_values_2d(const Topology& t, const int32_t* cells, const double* X,
   }
 }
 
+void build_fused_lists(const Topology& t, const int32_t* cells, int slices_per_cta, int chunk, FusedLists& f) {
+  f = FusedLists();
+  if (t.cv != 4 || slices_per_cta <= 0 || chunk <= 0) return;
+  const int rows = 32 * slices_per_cta;
+  const int ncta = (t.nslices + slices_per_cta - 1) / slices_per_cta;
+  f.slices_per_cta = slices_per_cta;
+  f.chunk = chunk;
+  f.ncta = ncta;
+  for (int b = 0; b < ncta; ++b) {
+    const int s0 = b * slices_per_cta, s1 = std::min(t.nslices, s0 + slices_per_cta);
+    if (t.sl_off[s1] - t.sl_off[s0] > 1024) return;  // local slots need more than 10 bits
+  }
+  // the CTAs whose rows hold a block of element e, each once, ascending
+  auto ctas_of = [&](int e, int (&out)[10]) {
+    const int32_t* c = cells + 4 * (size_t)e;
+    int n = 0;
+    for (int v = 0; v < 4; ++v)
+      for (int w = v; w < 4; ++w) {
+        const int b = std::min(c[v], c[w]) / rows;
+        bool seen = false;
+        for (int k = 0; k < n; ++k) seen |= out[k] == b;
+        if (!seen) out[n++] = b;
+      }
+    std::sort(out, out + n);
+    return n;
+  };
+  f.ptr.assign(ncta + 1, 0);
+  for (int e = 0; e < t.nt; ++e) {
+    int cs[10];
+    const int n = ctas_of(e, cs);
+    for (int k = 0; k < n; ++k) f.ptr[cs[k] + 1]++;
+  }
+  for (int b = 0; b < ncta; ++b) f.ptr[b + 1] += f.ptr[b];
+  f.elem.assign(f.ptr[ncta], 0);
+  {
+    std::vector<int32_t> cur(f.ptr.begin(), f.ptr.end() - 1);
+    for (int e = 0; e < t.nt; ++e) {
+      int cs[10];
+      const int n = ctas_of(e, cs);
+      for (int k = 0; k < n; ++k) f.elem[cur[cs[k]]++] = e;
+    }
+  }
+  f.code.assign(10 * (size_t)f.ptr[ncta], kFusedSkip);
+  std::vector<int32_t> stamp(1024), count(1024);
+  for (int b = 0; b < ncta; ++b) {
+    const int q0 = t.sl_off[b * slices_per_cta];
+    std::fill(stamp.begin(), stamp.end(), -1);
+    for (int p = f.ptr[b]; p < f.ptr[b + 1]; ++p) {
+      const int e = f.elem[p], ch = (p - f.ptr[b]) / chunk;
+      const int32_t* c = cells + 4 * (size_t)e;
+      for (int v = 0; v < 4; ++v)
+        for (int w = v; w < 4; ++w) {
+          const int a = c[v], d = c[w], u = std::min(a, d);
+          if (u / rows != b) continue;
+          const int ls = upper_slot(t, u, std::max(a, d)) - q0;
+          if (stamp[ls] != ch) {
+            stamp[ls] = ch;
+            count[ls] = 0;
+          }
+          const int rank = count[ls]++;
+          if (rank > 31) return;  // ok stays false
+          f.code[10 * (size_t)p + upper_block_id(v, w)] = (uint16_t)(ls | ((a > d) ? 1 << 10 : 0) | (rank << 11));
+        }
+    }
+  }
+  f.ok = true;
+}
+
 }  // namespace ssim_gb

@@ -36,6 +36,27 @@ struct Topology {
   std::vector<int32_t> vptr, vinc;
 };
 
+// Lists of the fused element-Hessian + assembly kernel (tets).  CTA b owns the block rows of slices
+// [spc b, spc (b + 1)) (spc = slices per CTA, 32 rows each), i.e. the upper slots
+// [sl_off[spc b], sl_off[spc (b + 1)]), and computes the Hessian of every element that has an upper block
+// (a vertex pair v <= w of the element, row min(cell[v], cell[w])) in one of its rows; an element whose
+// blocks fall in several CTAs' rows is computed by each of them.  ptr / elem: per CTA its elements,
+// ascending.  code: per entry, one 16-bit code per upper block in upper_block_id order: 0xffff when the
+// block's row belongs to another CTA, else the local slot (bits 0-9, relative to the CTA's first slot), the
+// transposed flag (bit 10: the block enters its slot transposed, cell[v] > cell[w]) and the rank (bits
+// 11-15): how many earlier entries of the same chunk (chunk consecutive entries of the CTA's list) add to
+// that slot.  The kernel adds the blocks of a chunk rank by rank, so every slot sums its contributions in
+// the list's order (deterministic, no atomics).  ok is false when a CTA has more than 1024 local slots or
+// a rank exceeds 31; the mesh then keeps the two-kernel path.
+struct FusedLists {
+  int slices_per_cta = 0, chunk = 0, ncta = 0;
+  bool ok = false;
+  std::vector<int32_t> ptr, elem;
+  std::vector<uint16_t> code;
+};
+constexpr uint16_t kFusedSkip = 0xffff;
+void build_fused_lists(const Topology& t, const int32_t* cells, int slices_per_cta, int chunk, FusedLists& f);
+
 // validates the cell indices (throws ssim_gb::invalid_argument) and builds everything above; cells are
 // [nt][cv] with cv = 4 (tets), 3 (triangles) or 2 (springs)
 void build_topology(int nv, int nt, const int32_t* cells, Topology& t, int cv = 4);

@@ -68,5 +68,6 @@ def test_cpp_header_steps_like_python_binding(tmp_path):
         ts.prepare_step()
         ts.compute_step()
         ts.step_next()
+        assert ts.stats()["converged"] == 1
     assert np.array_equal(u_cpp, ts.get("deformation"))
     assert u_cpp[:, 2].min() < 0
