@@ -446,8 +446,8 @@ def main():
                     help="PD diffusivity: 0 the reference's (E, nu) slots, 1 Lame, 2 per element")
     ap.add_argument("--pcg-variant", type=int, default=3, choices=[0, 1, 2, 3, 4],
                     help="ssim_gb_params.pcg_persistent of the GPU arms (3: automatic; 4: pipelined PCG)")
-    ap.add_argument("--precond", type=int, default=None, choices=[1, 2, 3],
-                    help="PCG preconditioner of every arm (1 Jacobi, 2 block-Jacobi, 3 slice); default: the bench's")
+    ap.add_argument("--precond", type=int, default=None, choices=[1, 2],
+                    help="PCG preconditioner of every arm (1 Jacobi, 2 block-Jacobi); default: the bench's")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-first-state", default=None, help=argparse.SUPPRESS)

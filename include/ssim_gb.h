@@ -129,11 +129,12 @@ typedef struct {
   double elem32_switch;   /* residual / target below which the FP32 phase ends (10) */
   int32_t pcg_pipe_iters; /* pipelined PCG (pcg_persistent 4) continues as Chronopoulos-Gear PCG after this many
                              iterations (80), bounding the drift of its recursive residual in long solves */
-  int32_t fused_assembly; /* tets: 1 (default) evaluates the element Hessians inside the assembly, each CTA summing
-                             the blocks of its own rows in shared memory (no per-element blocks in memory; the
-                             elements on a CTA's row boundary are evaluated by each CTA they touch); 0 runs the
-                             element Hessian and the assembly as two kernels through a per-element block buffer.
-                             Both sum the same terms, in different orders */
+  int32_t fused_assembly; /* tets: 0 (default) runs the element Hessian and the assembly as two kernels through a
+                             per-element block buffer; 1 evaluates the element Hessians inside the assembly, each
+                             CTA summing the blocks of its own rows in shared memory (no per-element blocks in
+                             memory, but every element is evaluated by each CTA whose rows it touches: 2.3x the
+                             element work on a lexicographically numbered box, measured slower on GB300).  Both
+                             give the same values bit for bit (each slot sums its blocks in element order) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

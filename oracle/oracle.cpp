@@ -828,8 +828,7 @@ int pcg(const orc_ts& s, const Vec& vals, const double* b, double* x, double rto
         double* rel_res) {
   const int n = s.n;
   Vec r(n), z(n), p(n), q(n);
-  // preconditioner as one 3x3 block per vertex: 0 identity, 1 Jacobi (diagonal), 2 block-Jacobi (also the
-  // starting point and the fall-back of 3, the slice preconditioner below)
+  // preconditioner as one 3x3 block per vertex: 0 identity, 1 Jacobi (diagonal), 2 block-Jacobi
   Vec P(9 * (size_t)s.nv, 0.0);
   for (int u = 0; u < s.nv; ++u) {
     double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -839,7 +838,7 @@ int pcg(const orc_ts& s, const Vec& vals, const double* b, double* x, double rto
         if (c >= 3 * u && c < 3 * u + 3) a[i * 3 + (c - 3 * u)] = vals[k];
       }
     double* m = &P[9 * (size_t)u];
-    int mode = precond == 3 ? 2 : precond;
+    int mode = precond;
     if (mode == 2) {
       const double det = det3(a);
       if (det > 0 && std::isfinite(det)) {
@@ -858,103 +857,7 @@ int pcg(const orc_ts& s, const Vec& vals, const double* b, double* x, double rto
       for (int i = 0; i < 3; ++i) m[i * 4] = 1.0;
     }
   }
-  // 3: the slice preconditioner.  Vertices are grouped in slices of 32 consecutive ids (32s .. 32s+31); the
-  // preconditioner is the block-tridiagonal part of each slice's diagonal block (the couplings of vertex u
-  // with u - 1 and u + 1 in the same slice), applied through its block LDL^T factorization:
-  //   D_0 = A_00;  L_i = A_{i,i-1} D_{i-1}^-1,  D_i = A_ii - L_i A_{i-1,i}   (i = 1 .. 31)
-  //   y_i = r_i - L_i y_{i-1};  w_i = D_i^-1 y_i;  z_i = w_i - L_{i+1}^T z_{i+1}.
-  // A slice with a pivot D_i that is not symmetric positive definite keeps block-Jacobi (L = 0, the rows
-  // of mode 2 above).
-  Vec Lm;
-  if (precond == 3) {
-    Lm.assign(9 * (size_t)s.nv, 0.0);
-    auto block = [&](int u, int w, double* a) {  // the 3x3 block (u, w), zero if not in the pattern
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) a[i * 3 + j] = 0.0;
-      for (int i = 0; i < 3; ++i)
-        for (int k = s.row_ptr[3 * u + i]; k < s.row_ptr[3 * u + i + 1]; ++k) {
-          const int c = s.col_idx[k];
-          if (c >= 3 * w && c < 3 * w + 3) a[i * 3 + (c - 3 * w)] = vals[k];
-        }
-    };
-    auto spd = [](const double* d) {
-      const double m2 = d[0] * d[4] - d[1] * d[3], m3 = det3(d);
-      return d[0] > 0 && m2 > 0 && m3 > 0 && std::isfinite(m3);
-    };
-    auto inv_sym = [](const double* d, double* m) {  // the inverse, made exactly symmetric
-      inv3(d, m);
-      m[1] = m[3] = 0.5 * (m[1] + m[3]);
-      m[2] = m[6] = 0.5 * (m[2] + m[6]);
-      m[5] = m[7] = 0.5 * (m[5] + m[7]);
-    };
-    const int nsl = (s.nv + 31) / 32;
-    for (int sl = 0; sl < nsl; ++sl) {
-      const int u0 = 32 * sl, u1 = std::min(s.nv, u0 + 32);
-      std::vector<double> Dinv(9 * (size_t)(u1 - u0)), L(9 * (size_t)(u1 - u0), 0.0);
-      bool ok = true;
-      double D[9], Dp[9];
-      block(u0, u0, D);
-      ok = spd(D);
-      if (ok) inv_sym(D, &Dinv[0]);
-      for (int u = u0 + 1; ok && u < u1; ++u) {
-        double C[9], A[9];
-        block(u - 1, u, C);  // A_{u-1,u}; A_{u,u-1} = C^T
-        block(u, u, A);
-        const double* Di = &Dinv[9 * (size_t)(u - 1 - u0)];
-        double* Lu = &L[9 * (size_t)(u - u0)];
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j)
-            Lu[i * 3 + j] = C[0 * 3 + i] * Di[0 * 3 + j] + C[1 * 3 + i] * Di[1 * 3 + j] + C[2 * 3 + i] * Di[2 * 3 + j];
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j)
-            Dp[i * 3 + j] = A[i * 3 + j] - (Lu[i * 3 + 0] * C[0 * 3 + j] + Lu[i * 3 + 1] * C[1 * 3 + j] +
-                                            Lu[i * 3 + 2] * C[2 * 3 + j]);
-        for (int i = 0; i < 3; ++i)  // symmetric in exact arithmetic
-          for (int j = i + 1; j < 3; ++j) Dp[i * 3 + j] = Dp[j * 3 + i] = 0.5 * (Dp[i * 3 + j] + Dp[j * 3 + i]);
-        ok = spd(Dp);
-        if (ok) inv_sym(Dp, &Dinv[9 * (size_t)(u - u0)]);
-      }
-      if (!ok) continue;  // block-Jacobi rows (P) and L = 0
-      for (int u = u0; u < u1; ++u) {
-        double* m = &P[9 * (size_t)u];
-        const double* di = &Dinv[9 * (size_t)(u - u0)];
-        for (int k = 0; k < 9; ++k) m[k] = di[k];
-        for (int k = 0; k < 9; ++k) Lm[9 * (size_t)u + k] = L[9 * (size_t)(u - u0) + k];
-      }
-    }
-  }
   auto apply = [&](const Vec& in, Vec& out) {
-    if (precond == 3) {
-      const int nsl = (s.nv + 31) / 32;
-#pragma omp parallel for schedule(static)
-      for (int sl = 0; sl < nsl; ++sl) {
-        const int u0 = 32 * sl, u1 = std::min(s.nv, u0 + 32);
-        double y[32][3];
-        for (int u = u0; u < u1; ++u) {
-          const double* L = &Lm[9 * (size_t)u];
-          for (int i = 0; i < 3; ++i) {
-            double a = in[3 * u + i];
-            if (u > u0) a -= L[i * 3] * y[u - 1 - u0][0] + L[i * 3 + 1] * y[u - 1 - u0][1] + L[i * 3 + 2] * y[u - 1 - u0][2];
-            y[u - u0][i] = a;
-          }
-        }
-        for (int u = u0; u < u1; ++u) {
-          const double* m = &P[9 * (size_t)u];
-          double w[3];
-          for (int i = 0; i < 3; ++i) w[i] = m[i * 3] * y[u - u0][0] + m[i * 3 + 1] * y[u - u0][1] + m[i * 3 + 2] * y[u - u0][2];
-          for (int i = 0; i < 3; ++i) y[u - u0][i] = w[i];
-        }
-        for (int u = u1 - 1; u >= u0; --u) {
-          if (u + 1 < u1) {
-            const double* L = &Lm[9 * (size_t)(u + 1)];
-            const double* zn = y[u + 1 - u0];
-            for (int i = 0; i < 3; ++i) y[u - u0][i] -= L[0 * 3 + i] * zn[0] + L[1 * 3 + i] * zn[1] + L[2 * 3 + i] * zn[2];
-          }
-          for (int i = 0; i < 3; ++i) out[3 * u + i] = y[u - u0][i];
-        }
-      }
-      return;
-    }
 #pragma omp parallel for schedule(static)
     for (int u = 0; u < s.nv; ++u) {
       const double* m = &P[9 * (size_t)u];

@@ -102,7 +102,7 @@ __device__ __forceinline__ void precond_rows(const S* a, int precond, V4<S>* out
   S m[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) m[i] = S(0);
-  if (precond == 2 || precond == 3) {  // 3: the slice preconditioner starts from (and falls back to) these
+  if (precond == 2) {
     const S c0 = a[4] * a[8] - a[5] * a[7], c1 = a[5] * a[6] - a[3] * a[8], c2 = a[3] * a[7] - a[4] * a[6];
     const S det = a[0] * c0 + a[1] * c1 + a[2] * c2;
     if (det > S(0) && isfinite(det)) {
@@ -227,8 +227,7 @@ void launch_export_csr(const SellMatrix& A, const int* bptr, const int* slot_k, 
 // ---------------- PCG (fused) ----------------
 template <typename S>
 void launch_pcg_setup(int nv, const double* g, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
-                      double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st,
-                      const V4<S>* lmat = nullptr);
+                      double rtol, int max_iters, bool rhs_negate, const Reduce& red, cudaStream_t st);
 template <typename S>
 void launch_pcg_spmv(const SellMatrix& A, const S* vals, const V4<S>* z, const V4<S>* p_old, V4<S>* p_new,
                      V4<S>* q, bool first, const Reduce& red, cudaStream_t st, bool kron = false);
@@ -242,7 +241,7 @@ template <typename S>
 bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st,
-                           bool kron = false, V4<S>* pm = nullptr, int pipe_iters = 0, const V4<S>* lmat = nullptr);
+                           bool kron = false, V4<S>* pm = nullptr, int pipe_iters = 0);
 // kron: vals holds one value per slot (the matrix is (scalar) (x) I3); launch_kron_extract makes that form
 // from a 9-value store and sets *not_kron when some block is not a multiple of I3
 template <typename S>
@@ -253,13 +252,7 @@ void launch_csr_dof_spmv(int n, const int* rp, const int* ci, const S* vals, con
                          cudaStream_t st);
 template <typename S>
 void launch_pcg_update(int nv, const V4<S>* p, const V4<S>* q, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z,
-                       int max_iters, const Reduce& red, cudaStream_t st, const V4<S>* lmat = nullptr);
-// the slice preconditioner (precond 3): per 32-row slice the block LDL^T factorisation of the slice's
-// block-tridiagonal part, D^-1 into dinv and L into lmat (3 rows per vertex each); block-Jacobi rows and
-// L = 0 for a slice whose pivots are not all positive definite.  With lmat, the PCG kernels apply the slice
-// solve instead of the per-vertex rows (the pipelined variant falls back to Chronopoulos-Gear)
-template <typename S>
-void launch_slice_factor(const SellMatrix& A, int nslices, const S* vals, V4<S>* dinv, V4<S>* lmat, cudaStream_t st);
+                       int max_iters, const Reduce& red, cudaStream_t st);
 
 // ---------------- vector kernels ----------------
 template <typename S>
@@ -330,7 +323,7 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
 // PCG setup from an S right-hand side (the PD stepper's inner solve)
 template <typename S>
 void launch_pcg_setup_v(int nv, const V4<S>* b, const V4<S>* dinv, V4<S>* x, V4<S>* r, V4<S>* z, V4<S>* p0,
-                        double rtol, int max_iters, const Reduce& red, cudaStream_t st, const V4<S>* lmat = nullptr);
+                        double rtol, int max_iters, const Reduce& red, cudaStream_t st);
 template <typename S>
 void launch_from_vec4(int nv, const V4<S>* in, double* out, cudaStream_t st);
 

@@ -149,7 +149,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->mixed_elem32 = 1;
   p->ls_energy_slack32 = 1e-6;
   p->pcg_pipe_iters = 80;
-  p->fused_assembly = 1;
+  p->fused_assembly = 0;
   p->elem32_switch = 10.0;
 }
 
@@ -300,7 +300,7 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
   CHECK_H(h);
   if (!p) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null params");
   if (p->max_newton_iters < 0 || p->cg_max_iters < 0 || p->max_ls_iters < 1 || !(p->ls_shrink > 0 && p->ls_shrink < 1) ||
-      !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 3 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 2 ||
+      !(p->ls_energy_slack >= 0) || p->precond < 0 || p->precond > 2 || p->pd_kappa_mode < 0 || p->pd_kappa_mode > 2 ||
       p->pcg_persistent < 0 || p->pcg_persistent > 4 || p->pcg_spin_limit < 0 || p->pcg_barrier_extra < 0 ||
       p->pcg_max_blocks < 0 || p->ncg_max_iters < 0 || !(p->ncg_step0 > 0) || !(p->ncg_eta >= 0) ||
       p->ncg_expand < 0 || !(p->stop_floor >= 0) || p->mixed_elem32 < 0 || p->mixed_elem32 > 1 ||

@@ -63,15 +63,13 @@ struct Solver {
   DBuf<S> pd_svals;      // the PD matrix as (scalar) (x) I3: one value per slot, when its blocks allow
   bool pd_kron = false;
   DBuf<V4<S>> pd_dinv;
-  DBuf<V4<S>> lmat, pd_lmat;  // slice preconditioner factors (precond 3) of the system / the H0 matrix
-  bool pd_slice = false;      // the H0 matrix carries the slice factors (pd_lmat)
   DBuf<S> ncg_L, ncg_Lt;  // NCG preconditioner factor and its transpose on the CSR pattern
   long ncg_version = -1;
   void release() {
     for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &pd_svals, &ncg_L, &ncg_Lt}) b->release();
     pd_kron = false;
     ncg_version = -1;
-    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &pm, &ld, &lq, &pd_dinv, &lmat, &pd_lmat}) b->release();
+    for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &pm, &ld, &lq, &pd_dinv}) b->release();
     hs.clear();
     hy.clear();
   }
@@ -119,7 +117,7 @@ struct TimeStep {
   DBuf<int32_t> fptr, felem;
   DBuf<uint16_t> fcode;
   int fused_ncta = 0, fused_spc = 0;
-  bool fused_ok = false;
+  bool fused_ok = false, fused_built = false;
   DBuf<double> lf, csr_out;
   // ---- device: solver
   Solver<float> sf;
@@ -474,20 +472,26 @@ struct TimeStep {
     lo_src.upload(topo.lo_src, stream);
     lo_col.upload(topo.lo_col, stream);
     lf.alloc((size_t)3 * cv * nt);
-    if (cv == 4) {
-      // 4 slices (128 block rows) per CTA of the fused Hessian + assembly kernel
-      FusedLists fl;
-      build_fused_lists(topo, cells.data(), 4, fused_chunk(), fl);
-      fused_ok = fl.ok;
-      if (fl.ok) {
-        fptr.upload(fl.ptr, stream);
-        felem.upload(fl.elem, stream);
-        fcode.upload(fl.code, stream);
-        fused_ncta = fl.ncta;
-        fused_spc = fl.slices_per_cta;
-        SSIM_CUDA(cudaStreamSynchronize(stream));  // the host lists go out of scope
-      }
+  }
+
+  // the fused kernel's lists, built on its first use (4 slices = 128 block rows per CTA); false if the mesh
+  // is not a tet mesh or does not fit the lists' codes
+  bool fused_ready() {
+    if (fused_built) return fused_ok;
+    fused_built = true;
+    if (topo.cv != 4) return false;
+    FusedLists fl;
+    build_fused_lists(topo, cells.data(), 4, fused_chunk(), fl);
+    fused_ok = fl.ok;
+    if (fl.ok) {
+      fptr.upload(fl.ptr, stream);
+      felem.upload(fl.elem, stream);
+      fcode.upload(fl.code, stream);
+      fused_ncta = fl.ncta;
+      fused_spc = fl.slices_per_cta;
+      SSIM_CUDA(cudaStreamSynchronize(stream));  // the host lists go out of scope
     }
+    return fused_ok;
   }
 
   // material: per element Lame parameters (basic_elast.hpp:10-20) and the stable Neo-Hookean constants
@@ -749,12 +753,11 @@ struct TimeStep {
     Solver<S>& s = solver<S>();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
-    if (!springs && !tri2d && fused_ok && params.fused_assembly) {
+    if (!springs && !tri2d && params.fused_assembly && fused_ready()) {
       launch_fused_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, A(), topo.nslices,
                               fused_spc, fused_ncta, fptr.p, felem.p, fcode.p, s.slot_mass.p, mask.p, filter, s.vals.p,
                               s.dinv.p, params.precond, stream);
       if (profiling) prof_end(e0, e1, PK_HESS, 0);
-      slice_factor<S>(s);
       return;
     }
     // two kernels through the per-element block buffer (allocated on first use)
@@ -770,19 +773,6 @@ struct TimeStep {
     launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
                        params.precond, stream);
     if (profiling) prof_end(e0, e1, PK_ASM, 0);
-    slice_factor<S>(s);
-  }
-
-  // precond 3: the slice preconditioner's factors from the assembled values
-  template <typename S>
-  void slice_factor(Solver<S>& s) {
-    if (params.precond != 3) return;
-    s.lmat.alloc(3 * (size_t)nv);
-    launch_slice_factor<S>(A(), topo.nslices, s.vals.p, s.dinv.p, s.lmat.p, stream);
-  }
-  template <typename S>
-  const V4<S>* slice_lmat(Solver<S>& s) const {
-    return params.precond == 3 && s.lmat.p != nullptr ? s.lmat.p : nullptr;
   }
 
   void hessian_any(bool spsd, bool filter) {
@@ -799,23 +789,22 @@ struct TimeStep {
   template <typename S>
   int pcg(const double* b, bool negate, double eta, int max_iters, double* rel_res) {
     Solver<S>& s = solver<S>();
-    const V4<S>* lm = slice_lmat<S>(s);
-    launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream, lm);
-    return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true, false, lm);
+    launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
+    return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true);
   }
 
   // PCG on another matrix of the same block pattern (the PD matrix) with an S right-hand side
   template <typename S>
   int pcg_on(const S* vals, const V4<S>* dinv, const V4<S>* b, double eta, int max_iters, double* rel_res,
-             bool kron = false, const V4<S>* lmat = nullptr) {
+             bool kron = false) {
     Solver<S>& s = solver<S>();
-    launch_pcg_setup_v<S>(nv, b, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, red(), stream, lmat);
-    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false, kron, lmat);
+    launch_pcg_setup_v<S>(nv, b, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, red(), stream);
+    return pcg_loop<S>(vals, dinv, max_iters, rel_res, false, kron);
   }
 
   template <typename S>
   int pcg_loop(const S* vals, const V4<S>* dinv, int max_iters, double* rel_res, bool profile_spmv,
-               bool kron = false, const V4<S>* lmat = nullptr) {
+               bool kron = false) {
     Solver<S>& s = solver<S>();
     int variant = params.pcg_persistent;
     // automatic: FP64 runs two launches per iteration (its FP64 dots and updates make the persistent
@@ -831,7 +820,7 @@ struct TimeStep {
       const bool ran = launch_pcg_persistent<S>(A(), vals, dinv, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters,
                                                 red(), gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra,
                                                 params.pcg_max_blocks, variant, stream, kron, s.pm.p,
-                                                params.pcg_pipe_iters, lmat);
+                                                params.pcg_pipe_iters);
       if (ran) {
         if (prof) SSIM_CUDA(cudaEventRecord(ev[1], stream));
         sync_scalars();
@@ -862,7 +851,7 @@ struct TimeStep {
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c], stream));
         launch_pcg_spmv<S>(A(), vals, s.z.p, pold, pnew, s.q.p, k == 0, red(), stream, kron);
         if (prof) SSIM_CUDA(cudaEventRecord(ev[2 * c + 1], stream));
-        launch_pcg_update<S>(nv, pnew, s.q.p, dinv, s.x.p, s.r.p, s.z.p, max_iters, red(), stream, lmat);
+        launch_pcg_update<S>(nv, pnew, s.q.p, dinv, s.x.p, s.r.p, s.z.p, max_iters, red(), stream);
       }
       sync_scalars();
       if (prof) {
@@ -949,12 +938,6 @@ struct TimeStep {
                                 stream));
       SSIM_CUDA(cudaMemcpyAsync(s.pd_dinv.p, s.dinv.p, sizeof(V4<S>) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice,
                                 stream));
-      s.pd_slice = slice_lmat<S>(s) != nullptr;
-      if (s.pd_slice) {
-        s.pd_lmat.alloc(3 * (size_t)nv);
-        SSIM_CUDA(cudaMemcpyAsync(s.pd_lmat.p, s.lmat.p, sizeof(V4<S>) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice,
-                                  stream));
-      }
       s.pd_kron = false;  // the projected Hessian is not a multiple of I3 per block
       pd = true;
     }
@@ -1039,7 +1022,7 @@ struct TimeStep {
                                stream);
           double rr = 0;
           st.cg_iters_total += pcg_on<S>(s.pd_kron ? s.pd_svals.p : s.pd_vals.p, s.pd_dinv.p, q, pd_tol,
-                                       params.cg_max_iters, &rr, s.pd_kron, h0 && s.pd_slice ? s.pd_lmat.p : nullptr);
+                                       params.cg_max_iters, &rr, s.pd_kron);
           if (i0 >= 0)
             launch_lbfgs_pass<S>(nv, z, nullptr, z, nullptr, nullptr, nullptr, 0.0, nullptr, 1.0, s.hy[i0]->p,
                                  rho_h[i0], bb + i0, red(), stream);
@@ -1128,11 +1111,8 @@ struct TimeStep {
     return up * (9.0 * s + 4.0) + lo * 8.0 + 2.0 * (topo.nslices + 1) * 4 + 4.0 * nv * 4 * s;
   }
 
-  // bytes one PCG update pass moves: p, q, x, r read, x, r, z written, the 3x3 preconditioner blocks (and
-  // the slice preconditioner's L blocks with precond 3)
-  double update_bytes(size_t s) const {
-    return 7.0 * nv * 4 * s + (params.precond == 3 ? 6.0 : 3.0) * nv * 4 * s;
-  }
+  // bytes one PCG update pass moves: p, q, x, r read, x, r, z written, the 3x3 preconditioner blocks
+  double update_bytes(size_t s) const { return 7.0 * nv * 4 * s + 3.0 * nv * 4 * s; }
 
   // ------------------------------------------------------------------ adjoint of one step
   // The handle's next_deform holds u_{n+1}.  ubar, vbar (device [n]) hold the adjoint of (u_{n+1}, v_{n+1}) on
