@@ -135,6 +135,10 @@ typedef struct {
                              memory, but every element is evaluated by each CTA whose rows it touches: 2.3x the
                              element work on a lexicographically numbered box, measured slower on GB300).  Both
                              give the same values bit for bit (each slot sums its blocks in element order) */
+  int32_t mixed_delta;    /* mixed precision, Newton, tets with stable Neo-Hookean: 1 (default) evaluates the
+                             iterations after the FP32 phase as FP32 increments from the FP64 evaluation made at
+                             the switch (energy and forces = that evaluation's + increments whose rounding is
+                             relative to the increment); 0 evaluates them in FP64 */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

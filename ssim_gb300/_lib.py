@@ -69,6 +69,7 @@ class Params(C.Structure):
         ("elem32_switch", C.c_double),
         ("pcg_pipe_iters", C.c_int32),
         ("fused_assembly", C.c_int32),
+        ("mixed_delta", C.c_int32),
     ]
 
     def as_dict(self):

@@ -90,6 +90,80 @@ __host__ __device__ __forceinline__ S snh_eval(const S* F, S lam, S mu, S alpha,
   return S(0.5) * (t1 + t2 - t3) - psi0;
 }
 
+// cof(A + B) - cof(A) - cof(B): the part of the cofactor (quadratic in its argument) bilinear in A and B,
+// for cofactor()'s convention C[k] = F[a] F[b] - F[c] F[d]
+template <typename S>
+__host__ __device__ __forceinline__ void cofactor_cross(const S* A, const S* B, S* C) {
+  constexpr int idx[9][4] = {{4, 8, 5, 7}, {5, 6, 3, 8}, {3, 7, 4, 6}, {7, 2, 8, 1}, {8, 0, 6, 2},
+                             {6, 1, 7, 0}, {1, 5, 2, 4}, {2, 3, 0, 5}, {0, 4, 1, 3}};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int a = idx[k][0], b = idx[k][1], c = idx[k][2], d = idx[k][3];
+    C[k] = A[a] * B[b] + B[a] * A[b] - A[c] * B[d] - B[c] * A[d];
+  }
+}
+
+// The stable Neo-Hookean energy and PK1 increments between the displacement gradients Gr and Gr + dG,
+// written so that each term is proportional to dG (rounding relative to the increment, not to the stress):
+// with F = Fr + dG, s = Ic - 3, a(s) = 1 - 1/(s + 4), c1 = -3/4 mu / lambda,
+//   ds   = 2 Fr:dG + |dG|^2
+//   dJ   = cof(Fr):dG + Fr:cof(dG) + det(dG)                       (det of a sum of 3x3 matrices)
+//   dcof = cross(Fr, dG) + cof(dG)
+//   da   = ds / ((sr + 4)(sr + ds + 4))
+//   dP   = lambda [(Jr - alpha) dcof + dJ (cof Fr + dcof)] + mu [a(sr) dG + da (Fr + dG)]
+//   dPsi = 1/2 [ mu (ds - log1p(ds / (sr + 4))) + lambda dJ ((J - 1) + (Jr - 1) + 2 c1) ]
+// (the differences of snh_eval_small's energy and stress, expanded exactly).  The reference quantities
+// (Fr, cof Fr, sr, Jr - 1) only scale the increment's terms, so their own rounding perturbs the result
+// relative to the increment too.
+template <typename S>
+__host__ __device__ __forceinline__ S snh_increment(const S* Gr, const S* dG, S lam, S mu, S* dP) {
+  S Fr[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Fr[k] = Gr[k] + (k % 4 == 0 ? S(1) : S(0));
+  // reference: sr = 2 tr Gr + |Gr|^2, Jr - 1 from the principal minors of Gr (as snh_eval_small)
+  const S trGr = Gr[0] + Gr[4] + Gr[8];
+  S n2 = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) n2 += Gr[k] * Gr[k];
+  const S sr = S(2) * trGr + n2;
+  S cGr[9];
+  cofactor(Gr, cGr);
+  const S Jr1 = trGr + (cGr[0] + cGr[4] + cGr[8]) + (Gr[0] * cGr[0] + Gr[1] * cGr[1] + Gr[2] * cGr[2]);
+  S cFr[9];
+  cofactor(Fr, cFr);
+  // increments
+  S fd = 0, d2 = 0, cd = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    fd += Fr[k] * dG[k];
+    d2 += dG[k] * dG[k];
+    cd += cFr[k] * dG[k];
+  }
+  const S ds = S(2) * fd + d2;
+  S cdG[9], dC[9];
+  cofactor(dG, cdG);
+  cofactor_cross(Fr, dG, dC);
+  S fc = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    fc += Fr[k] * cdG[k];
+    dC[k] += cdG[k];
+  }
+  const S detdG = dG[0] * cdG[0] + dG[1] * cdG[1] + dG[2] * cdG[2];
+  const S dJ = cd + fc + detdG;
+  const S c1 = S(-0.75) * mu / lam;
+  const S Jm_r = Jr1 + c1;  // Jr - alpha
+  const S ar = (sr + S(3)) / (sr + S(4));
+  const S da = ds / ((sr + S(4)) * (sr + ds + S(4)));
+  if (dP != nullptr) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      dP[k] = lam * (Jm_r * dC[k] + dJ * (cFr[k] + dC[k])) + mu * (ar * dG[k] + da * (Fr[k] + dG[k]));
+  }
+  const S dlog = log1p(ds / (sr + S(4)));
+  return S(0.5) * (mu * (ds - dlog) + lam * dJ * ((Jr1 + dJ) + Jr1 + S(2) * c1));
+}
+
 // The stable Neo-Hookean energy and PK1 written in the displacement gradient G = F - I so that no O(mu) or
 // O(lambda) terms cancel (for FP32 evaluation of small strains): with s = Ic - 3 = 2 tr G + |G|^2,
 // J - 1 = tr G + (principal 2x2 minors of G) + det G, c1 = 1 - alpha = -3/4 mu / lambda:

@@ -152,6 +152,16 @@ void launch_split32(int nv, const double* u, const double* xt, float4* uh, float
 void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
                                double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
                                const Reduce& red, cudaStream_t st);
+// increment evaluation from a reference u_r (the mixed Newton's iterations after the FP32 phase): ref = the
+// FP32 split of u_r and w = u_r - x~, db = u_b - u_r; energy e_ref + increment into the (trial) energy,
+// escale_ref as its round-off scale; local force increments into lf32 (see kernels_elem.cu)
+void launch_elem_delta32(const ElemFP64& el, const ElemFP32& ef, const Split32& ref, const float4* db, const float4* d,
+                         double alpha, double dt2, double rho, double e_ref, double escale_ref, float* lf32,
+                         bool with_forces, bool trial, const Reduce& red, cudaStream_t st);
+// g = gref + the gathered increments (Dirichlet dofs zeroed), |g|^2 into sc->gnorm2
+void launch_vertex_gather_delta32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
+                                  const double* gref, double* g, const Reduce& red, cudaStream_t st);
+void launch_delta_base(int nv, const double* u, const double* uref, float4* db, cudaStream_t st);
 void launch_vertex_gather32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
                             double* g, const Reduce& red, cudaStream_t st);
 // mass-spring energy (+ spring forces into lf[s][2][3]) at u (+ alpha d), plus the lumped inertia energy

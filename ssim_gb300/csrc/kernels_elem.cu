@@ -249,6 +249,163 @@ __global__ void __launch_bounds__(EB)
   }
 }
 
+// The mixed Newton's iterations after the switch from the FP32 pass: energy and forces as increments from a
+// reference state u_r evaluated once in FP64 (its energy e_ref and forces, which the gather adds back).  Per
+// element the stable Neo-Hookean increment between G_r and G_r + dG in FP32 (snh_increment: rounding
+// relative to the increment, not to the stress), the consistent-mass inertia increment
+// (M_e (d_r + x))^T-terms with d_r = u_r - x~ and x = u - u_r, and the local force increments.  Vertex data:
+// ref = the FP32 split (hi, lo) of u_r and w = u_r - x~ (split32_kernel at u_r); db = u_b - u_r at the line
+// search's base point; the trial point is u_b + alpha d.
+template <bool FORCES, bool TRIAL>
+__global__ void __launch_bounds__(EB)
+    elem_delta32_kernel(ElemFP64 el, ElemFP32 ef, Split32 ref, const float4* __restrict__ db,
+                        const float4* __restrict__ d, float alpha, float dt2, float rho, double e_ref,
+                        double escale_ref, float* __restrict__ lf32, Reduce red) {
+  __shared__ float stage[FORCES ? EB * 12 : 1];
+  __shared__ double shred[EB / 32][1];
+  const int e0 = blockIdx.x * EB;
+  const int e = e0 + threadIdx.x;
+  float part[1] = {0.f};
+  float lfv[12];
+  if (e < el.nt) {
+    const int4 c = el.cells[e];
+    const int vid[4] = {c.x, c.y, c.z, c.w};
+    float4 hv[4], lv[4], wv[4];
+    float x[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      hv[i] = ref.uh[vid[i]];
+      lv[i] = ref.ul[vid[i]];
+      wv[i] = ref.w[vid[i]];
+      const float4 b = db[vid[i]];
+      x[i][0] = b.x;
+      x[i][1] = b.y;
+      x[i][2] = b.z;
+      if (TRIAL) {
+        const float4 dv = d[vid[i]];
+        x[i][0] += alpha * dv.x;
+        x[i][1] += alpha * dv.y;
+        x[i][2] += alpha * dv.z;
+      }
+    }
+    float Dm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Dm[k] = ef.dminv[(size_t)k * el.nt + e];
+    float Gr[9], dG[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const float hr[3] = {comp<float>(hv[1], r) - comp<float>(hv[0], r) + (comp<float>(lv[1], r) - comp<float>(lv[0], r)),
+                           comp<float>(hv[2], r) - comp<float>(hv[0], r) + (comp<float>(lv[2], r) - comp<float>(lv[0], r)),
+                           comp<float>(hv[3], r) - comp<float>(hv[0], r) + (comp<float>(lv[3], r) - comp<float>(lv[0], r))};
+      const float xr[3] = {x[1][r] - x[0][r], x[2][r] - x[0][r], x[3][r] - x[0][r]};
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) {
+        Gr[r * 3 + cc] = hr[0] * Dm[0 * 3 + cc] + hr[1] * Dm[1 * 3 + cc] + hr[2] * Dm[2 * 3 + cc];
+        dG[r * 3 + cc] = xr[0] * Dm[0 * 3 + cc] + xr[1] * Dm[1 * 3 + cc] + xr[2] * Dm[2 * 3 + cc];
+      }
+    }
+    const float lam = ef.lam[e], mu = ef.mu[e], V = ef.vol[e];
+    const float m = rho * V * (1.0f / 20.0f);
+    float dP[9];
+    const float dpsi = snh_increment<float>(Gr, dG, lam, mu, FORCES ? dP : nullptr);
+    // inertia: 1/2 (d_r + x)^T M_e (d_r + x) - 1/2 d_r^T M_e d_r with M_e(i, j) = m (1 + delta_ij)
+    float sw[3], sx[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      sw[k] = comp<float>(wv[0], k) + comp<float>(wv[1], k) + comp<float>(wv[2], k) + comp<float>(wv[3], k);
+      sx[k] = x[0][k] + x[1][k] + x[2][k] + x[3][k];
+    }
+    float cross = sw[0] * sx[0] + sw[1] * sx[1] + sw[2] * sx[2];
+    float quad = sx[0] * sx[0] + sx[1] * sx[1] + sx[2] * sx[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        cross += comp<float>(wv[i], k) * x[i][k];
+        quad += x[i][k] * x[i][k];
+      }
+    if (FORCES) {
+      const float sV = dt2 * V;
+      float tot[3] = {0, 0, 0};
+#pragma unroll
+      for (int i = 1; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float h = dP[j * 3 + 0] * Dm[(i - 1) * 3 + 0] + dP[j * 3 + 1] * Dm[(i - 1) * 3 + 1] +
+                          dP[j * 3 + 2] * Dm[(i - 1) * 3 + 2];
+          tot[j] += h;
+          lfv[i * 3 + j] = sV * h + m * (x[i][j] + sx[j]);
+        }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) lfv[j] = -sV * tot[j] + m * (x[0][j] + sx[j]);
+    }
+    part[0] = dt2 * V * dpsi + m * cross + 0.5f * m * quad;
+  }
+  if (FORCES) {
+    if (e < el.nt) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) stage[threadIdx.x * 12 + k] = lfv[k];
+    }
+    __syncthreads();
+    const int nvalid = min(EB, el.nt - e0);
+    float* dst = lf32 + (size_t)e0 * 12;
+    for (int i = threadIdx.x; i < nvalid * 12; i += EB) dst[i] = stage[i];
+  }
+  double v1[1];
+  block_sum_s<1, EB, float>(part, v1, shred);
+  double tot[1];
+  if (grid_sum_last<1, EB>(v1, red.partials, red.counter, tot)) {
+    if (TRIAL) {
+      red.sc->trial_energy = e_ref + tot[0];
+      red.sc->trial_energy_scale = escale_ref;
+    } else {
+      red.sc->energy = e_ref + tot[0];
+      red.sc->energy_scale = escale_ref;
+    }
+  }
+}
+
+// forces as the reference's FP64 forces plus the FP32 local force increments lf32[(e, i)][3] summed per
+// vertex, Dirichlet dofs zeroed; |g|^2 in FP64
+__global__ void __launch_bounds__(256)
+    vertex_gather_delta32_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
+                                 const float* __restrict__ lf32, const uint8_t* __restrict__ mask,
+                                 const double* __restrict__ gref, double* __restrict__ g, Reduce red) {
+  __shared__ double shred[256 / 32][1];
+  const int v = blockIdx.x * 256 + threadIdx.x;
+  double part[1] = {0.0};
+  if (v < nv) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    const int k1 = vptr[v + 1];
+    for (int k = vptr[v]; k < k1; ++k) {
+      const float* s = lf32 + (size_t)vinc[k] * 3;
+      a0 += s[0];
+      a1 += s[1];
+      a2 += s[2];
+    }
+    const uint8_t mk = mask[v];
+    const double g0 = (mk & 1) ? 0.0 : gref[3 * v] + (double)a0;
+    const double g1 = (mk & 2) ? 0.0 : gref[3 * v + 1] + (double)a1;
+    const double g2 = (mk & 4) ? 0.0 : gref[3 * v + 2] + (double)a2;
+    g[3 * v] = g0;
+    g[3 * v + 1] = g1;
+    g[3 * v + 2] = g2;
+    part[0] = g0 * g0 + g1 * g1 + g2 * g2;
+  }
+  block_sum<1, 256>(part, shred);
+  double tot[1];
+  if (grid_sum_last<1, 256>(part, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+}
+
+// x_b = u - u_ref per vertex, rounded once to FP32 (the base point of the increment evaluations)
+__global__ void __launch_bounds__(256)
+    delta_base_kernel(int nv, const double* __restrict__ u, const double* __restrict__ uref, float4* __restrict__ db) {
+  const int v = blockIdx.x * 256 + threadIdx.x;
+  if (v >= nv) return;
+  db[v] = make_float4((float)(u[3 * v] - uref[3 * v]), (float)(u[3 * v + 1] - uref[3 * v + 1]),
+                      (float)(u[3 * v + 2] - uref[3 * v + 2]), 0.f);
+}
+
 // forces from FP32 local forces lf32[(e, i)][3], summed per vertex in FP32, Dirichlet dofs zeroed; |g|^2
 __global__ void __launch_bounds__(256)
     vertex_gather32_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
@@ -399,6 +556,36 @@ void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Spl
   else
     elem_energy_grad32_kernel<false, false><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
   after_launch("elem_energy_grad32");
+}
+
+void launch_elem_delta32(const ElemFP64& el, const ElemFP32& ef, const Split32& ref, const float4* db, const float4* d,
+                         double alpha, double dt2, double rho, double e_ref, double escale_ref, float* lf32,
+                         bool with_forces, bool trial, const Reduce& red, cudaStream_t st) {
+  if (el.nt <= 0) return;
+  const int grid = div_up(el.nt, EB);
+  const float f_dt2 = (float)dt2, f_rho = (float)rho, a = (float)alpha;
+  if (trial && with_forces)
+    elem_delta32_kernel<true, true><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+  else if (trial)
+    elem_delta32_kernel<false, true><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+  else if (with_forces)
+    elem_delta32_kernel<true, false><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+  else
+    elem_delta32_kernel<false, false><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+  after_launch("elem_delta32");
+}
+
+void launch_vertex_gather_delta32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
+                                  const double* gref, double* g, const Reduce& red, cudaStream_t st) {
+  if (nv <= 0) return;
+  vertex_gather_delta32_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, vptr, vinc, lf32, mask, gref, g, red);
+  after_launch("vertex_gather_delta32");
+}
+
+void launch_delta_base(int nv, const double* u, const double* uref, float4* db, cudaStream_t st) {
+  if (nv <= 0) return;
+  delta_base_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, u, uref, db);
+  after_launch("delta_base");
 }
 
 void launch_vertex_gather32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,

@@ -171,6 +171,33 @@ struct TimeStep {
   DBuf<float4> uh32, ul32, w32;
   DBuf<float> lf32t;
   Split32 s32() const { return Split32{uh32.p, ul32.p, w32.p}; }
+  // the reference of the increment evaluations (mixed Newton after the FP32 phase): u_r, its FP64 forces and
+  // energy, and the base point offset u_b - u_r; the FP32 split of u_r lives in uh32 / ul32 / w32
+  DBuf<double> uref, gref;
+  DBuf<float4> db32;
+  double e_ref = 0, escale_ref = 0;
+  bool delta_supported() const {
+    return !springs && !tri2d && elastic_model == SSIM_GB_MODEL_STABLE_NEOHOOKEAN && params.mixed_delta != 0;
+  }
+  // u_r = next, whose FP64 energy E and forces were just evaluated
+  void set_delta_reference(double E, double Escale) {
+    uref.alloc(n);
+    gref.alloc(n);
+    db32.alloc(nv);
+    SSIM_CUDA(cudaMemcpyAsync(uref.p, next.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    SSIM_CUDA(cudaMemcpyAsync(gref.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    split32();
+    e_ref = E;
+    escale_ref = Escale;
+  }
+  void delta_base() { launch_delta_base(nv, next.p, uref.p, db32.p, stream); }
+  void delta_trial(const float4* d, double alpha) {
+    launch_elem_delta32(e64(), e32s(), s32(), db32.p, d, alpha, dt * dt, rho, e_ref, escale_ref, lf32t.p, true, true,
+                        red(), stream);
+  }
+  void delta_gather() {
+    launch_vertex_gather_delta32(nv, vptr.p, vinc.p, lf32t.p, mask.p, gref.p, forces.p, red(), stream);
+  }
   void split32() {
     uh32.alloc(nv);
     ul32.alloc(nv);
@@ -1156,6 +1183,8 @@ struct TimeStep {
     // small-strain forms); the stopping test is then confirmed with an FP64 evaluation, and if the FP64
     // residual is above the target (or the FP32 residual stalls) the remaining iterations run in FP64
     bool e32 = mixed() && params.mixed_elem32 != 0;
+    // after the FP32 phase: FP32 increments from the FP64 evaluation at the switch (delta)
+    bool delta = false;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double Escale = hsc->energy_scale;
     double gn = std::sqrt(hsc->gnorm2);
@@ -1169,6 +1198,12 @@ struct TimeStep {
       E0 = energy_grad();
       Escale = hsc->energy_scale;
       gn = std::sqrt(hsc->gnorm2);
+      if constexpr (std::is_same<S, float>::value) {
+        if (delta_supported()) {
+          set_delta_reference(E0, Escale);
+          delta = true;
+        }
+      }
     };
     int it = 0;
     for (;; ++it) {
@@ -1179,6 +1214,12 @@ struct TimeStep {
       const double tgt = params.stop_mode == 0 ? abs_tol : params.rel_tol * g0;
       if (e32 && (gn <= params.elem32_switch * tgt || stall >= 2)) {
         to_fp64();
+        st.grad_norm = gn;
+        st.energy = E0;
+      } else if (delta && stall >= 3) {
+        // the increments have grown with little progress: a fresh FP64 reference at the current state
+        to_fp64();
+        stall = 0;
         st.grad_norm = gn;
         st.energy = E0;
       }
@@ -1207,8 +1248,18 @@ struct TimeStep {
       double Et = 0, Et_scale = 0;
       const double slack = (e32 ? params.ls_energy_slack32 : params.ls_energy_slack) * Escale;
       if (e32) split32();  // the trials' base point
+      if constexpr (std::is_same<S, float>::value) {
+        if (delta) delta_base();
+      }
       for (int ls = 0; ls < params.max_ls_iters; ++ls) {
-        launch_trial<S>(s.x.p, alpha, true, e32);
+        if constexpr (std::is_same<S, float>::value) {
+          if (delta)
+            delta_trial(s.x.p, alpha);
+          else
+            launch_trial<S>(s.x.p, alpha, true, e32);
+        } else {
+          launch_trial<S>(s.x.p, alpha, true, e32);
+        }
         sync_scalars();
         st.ls_steps_total++;
         Et = hsc->trial_energy;
@@ -1217,7 +1268,10 @@ struct TimeStep {
         if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
       launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
-      gather_forces<S>(nullptr, 0.0, e32);
+      if (delta)
+        delta_gather();
+      else
+        gather_forces<S>(nullptr, 0.0, e32);
       sync_scalars();
       if (!std::isfinite(Et) || !std::isfinite(hsc->gnorm2))
         throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
