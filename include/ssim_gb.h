@@ -154,6 +154,23 @@ typedef struct {
   double elapsed_ms;
 } ssim_gb_step_stats;
 
+/* Launch shapes chosen by ssim_gb_autotune (extension: the reference has no GPU kernels of its own) */
+typedef struct {
+  int32_t elem_block;     /* threads per block of the FP32 element passes (0: not tuned, the default 128) */
+  int32_t hessian_block;  /* threads per block of the element Hessian kernel (default 64) */
+  int32_t assembly_block; /* threads per block of the assembly kernel (default 256) */
+  int32_t gather_block;   /* threads per block of the FP32 force gathers (0: not tuned, the default 256) */
+  int32_t pcg_persistent; /* the PCG variant chosen (ssim_gb_params.pcg_persistent) */
+  int32_t pcg_max_blocks; /* the persistent PCG's grid cap chosen (ssim_gb_params.pcg_max_blocks) */
+  int32_t fused_assembly; /* ssim_gb_params.fused_assembly chosen */
+  int32_t from_cache;     /* 1: an earlier sweep of the same shape in this process decided (nothing timed) */
+  double elem_us;         /* per launch of the chosen element pass (0 when not timed) */
+  double hessian_us;      /* Hessian + assembly with the chosen shapes */
+  double pcg_solve_ms;    /* one PCG solve to 5e-2 relative residual with the chosen variant and grid */
+  int32_t pcg_iterations; /* iterations of that solve */
+  int32_t candidates;     /* configurations timed */
+} ssim_gb_tuning;
+
 typedef struct ssim_gb_timestep ssim_gb_timestep;
 
 /* ---- library ---- */
@@ -324,6 +341,19 @@ SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, const double*
                                                   const double* rest_volume, const double* lambda_,
                                                   const double* mu, int32_t num_cells, double time_step,
                                                   double density, void* stream, double* energy_out);
+
+/* ---- launch-shape autotuning (extension) ----
+ * A one-time sweep on this handle's own data (call after reset(), between steps): the block sizes of the
+ * FP32 element pass (64 / 128 / 256), the element Hessian (32 / 64 / 128), the assembly (128 / 256 / 512)
+ * and the FP32 force gather (128 / 256 / 512), the persistent PCG's variant (mixed: standard or
+ * Chronopoulos-Gear; FP64: two launches or Chronopoulos-Gear) and grid (one block per 256 rows or four per
+ * SM), and the fused or two-kernel Hessian assembly.  Each candidate runs once untimed and then timed by
+ * CUDA events on the handle's stream; the fastest is applied to the handle (the shapes, and pcg_persistent,
+ * pcg_max_blocks, fused_assembly in its parameters).  The choice is cached for the process by (vertices,
+ * cells, nonzero blocks, precision, instances, cell kind): a later handle of the same shape gets it without
+ * timing (from_cache = 1).  The deformation and the other state are left as they were; the forces view is
+ * restored. */
+SSIM_GB_API ssim_gb_status ssim_gb_autotune(ssim_gb_timestep* h, ssim_gb_tuning* out);
 
 /* ---- profiling (CUDA events on the handle's stream around the element, assembly and PCG launches) ---- */
 SSIM_GB_API ssim_gb_status ssim_gb_profile_enable(ssim_gb_timestep* h, int32_t enable);

@@ -93,6 +93,27 @@ class StepStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("elem_block", C.c_int32),
+        ("hessian_block", C.c_int32),
+        ("assembly_block", C.c_int32),
+        ("gather_block", C.c_int32),
+        ("pcg_persistent", C.c_int32),
+        ("pcg_max_blocks", C.c_int32),
+        ("fused_assembly", C.c_int32),
+        ("from_cache", C.c_int32),
+        ("elem_us", C.c_double),
+        ("hessian_us", C.c_double),
+        ("pcg_solve_ms", C.c_double),
+        ("pcg_iterations", C.c_int32),
+        ("candidates", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SsimGbError(RuntimeError):
     """A CUDA, state or out-of-memory failure reported by the library."""
 
@@ -183,6 +204,7 @@ _SIGS = {
     "ssim_gb_adjoint_step": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, _I, _I]),
     "ssim_gb_get_field_device": (C.c_int, [_H, C.c_int32, C.c_void_p]),
     "ssim_gb_set_field_device": (C.c_int, [_H, C.c_int32, C.c_void_p]),
+    "ssim_gb_autotune": (C.c_int, [_H, C.POINTER(Tuning)]),
     "ssim_gb_profile_enable": (C.c_int, [_H, C.c_int32]),
     "ssim_gb_profile_read": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), _D, _D]),
     "ssim_gb_synchronize": (C.c_int, [_H]),

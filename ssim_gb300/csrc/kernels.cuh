@@ -14,6 +14,7 @@
 //   lf           double[T][4][3] scaled element forces awaiting the vertex gather
 //   vectors      vec4<S>[V]  CG vectors, one padded xyz triple per vertex
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -59,6 +60,18 @@ struct ElemFP32 {
 
 // per-vertex FP32 split of the state for the FP32 element / spring passes: uh + ul = u (to ~2^-48),
 // w = u - x~ rounded once
+// Calls fn(std::integral_constant<int, B>) for the block size B in the candidate list equal to `block`
+// (the first candidate if none is): the run-time choice of a launch's block size among compiled variants
+template <int... Bs, typename Fn>
+inline void dispatch_block(int block, Fn&& fn) {
+  bool done = false;
+  ((!done && block == Bs ? (fn(std::integral_constant<int, Bs>{}), done = true) : false), ...);
+  if (!done) {
+    constexpr int first[] = {Bs...};
+    fn(std::integral_constant<int, first[0]>{});
+  }
+}
+
 struct Split32 {
   const float4* uh;
   const float4* ul;
@@ -151,19 +164,19 @@ void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* 
 void launch_split32(int nv, const double* u, const double* xt, float4* uh, float4* ul, float4* w, cudaStream_t st);
 void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
                                double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
-                               const Reduce& red, cudaStream_t st);
+                               const Reduce& red, cudaStream_t st, int block = 0);
 // increment evaluation from a reference u_r (the mixed Newton's iterations after the FP32 phase): ref = the
 // FP32 split of u_r and w = u_r - x~, db = u_b - u_r; energy e_ref + increment into the (trial) energy,
 // escale_ref as its round-off scale; local force increments into lf32 (see kernels_elem.cu)
 void launch_elem_delta32(const ElemFP64& el, const ElemFP32& ef, const Split32& ref, const float4* db, const float4* d,
                          double alpha, double dt2, double rho, double e_ref, double escale_ref, float* lf32,
-                         bool with_forces, bool trial, const Reduce& red, cudaStream_t st);
+                         bool with_forces, bool trial, const Reduce& red, cudaStream_t st, int block = 0);
 // g = gref + the gathered increments (Dirichlet dofs zeroed), |g|^2 into sc->gnorm2
 void launch_vertex_gather_delta32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
-                                  const double* gref, double* g, const Reduce& red, cudaStream_t st);
+                                  const double* gref, double* g, const Reduce& red, cudaStream_t st, int block = 0);
 void launch_delta_base(int nv, const double* u, const double* uref, float4* db, cudaStream_t st);
 void launch_vertex_gather32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
-                            double* g, const Reduce& red, cudaStream_t st);
+                            double* g, const Reduce& red, cudaStream_t st, int block = 0);
 // mass-spring energy (+ spring forces into lf[s][2][3]) at u (+ alpha d), plus the lumped inertia energy
 template <typename SD>
 void launch_spring_energy_grad(const SpringData& sp, const double* u, const double* xt, const double* m, int nv,
@@ -209,7 +222,7 @@ void launch_tri_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const floa
 // ---------------- element Hessian ----------------
 template <typename S>
 void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
-                         const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st);
+                         const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st, int block = 0);
 
 // ---------------- assembly / sparse ----------------
 // precond: 0 identity, 1 Jacobi (diagonal of the diagonal block), 2 block-Jacobi (inverse 3x3 block)
@@ -227,7 +240,7 @@ int fused_chunk();
 
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
-                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st);
+                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st, int block = 0);
 template <typename S>
 void launch_spmv(const SellMatrix& A, const S* vals, const V4<S>* x, V4<S>* y, cudaStream_t st);
 template <typename S>

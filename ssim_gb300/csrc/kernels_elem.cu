@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256)
   if (w != nullptr) w[v] = make_float4(o[0], o[1], o[2], 0.f);
 }
 
-template <bool FORCES, bool TRIAL>
+template <bool FORCES, bool TRIAL, int EB>
 __global__ void __launch_bounds__(EB)
     elem_energy_grad32_kernel(ElemFP64 el, ElemFP32 ef, Split32 sp, const float4* __restrict__ d, float alpha,
                               float dt2, float rho, float* __restrict__ lf32, Reduce red) {
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(EB)
 // (M_e (d_r + x))^T-terms with d_r = u_r - x~ and x = u - u_r, and the local force increments.  Vertex data:
 // ref = the FP32 split (hi, lo) of u_r and w = u_r - x~ (split32_kernel at u_r); db = u_b - u_r at the line
 // search's base point; the trial point is u_b + alpha d.
-template <bool FORCES, bool TRIAL>
+template <bool FORCES, bool TRIAL, int EB>
 __global__ void __launch_bounds__(EB)
     elem_delta32_kernel(ElemFP64 el, ElemFP32 ef, Split32 ref, const float4* __restrict__ db,
                         const float4* __restrict__ d, float alpha, float dt2, float rho, double e_ref,
@@ -367,12 +367,13 @@ __global__ void __launch_bounds__(EB)
 
 // forces as the reference's FP64 forces plus the FP32 local force increments lf32[(e, i)][3] summed per
 // vertex, Dirichlet dofs zeroed; |g|^2 in FP64
-__global__ void __launch_bounds__(256)
+template <int B>
+__global__ void __launch_bounds__(B)
     vertex_gather_delta32_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
                                  const float* __restrict__ lf32, const uint8_t* __restrict__ mask,
                                  const double* __restrict__ gref, double* __restrict__ g, Reduce red) {
-  __shared__ double shred[256 / 32][1];
-  const int v = blockIdx.x * 256 + threadIdx.x;
+  __shared__ double shred[B / 32][1];
+  const int v = blockIdx.x * B + threadIdx.x;
   double part[1] = {0.0};
   if (v < nv) {
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
@@ -392,9 +393,9 @@ __global__ void __launch_bounds__(256)
     g[3 * v + 2] = g2;
     part[0] = g0 * g0 + g1 * g1 + g2 * g2;
   }
-  block_sum<1, 256>(part, shred);
+  block_sum<1, B>(part, shred);
   double tot[1];
-  if (grid_sum_last<1, 256>(part, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+  if (grid_sum_last<1, B>(part, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
 }
 
 // x_b = u - u_ref per vertex, rounded once to FP32 (the base point of the increment evaluations)
@@ -407,12 +408,13 @@ __global__ void __launch_bounds__(256)
 }
 
 // forces from FP32 local forces lf32[(e, i)][3], summed per vertex in FP32, Dirichlet dofs zeroed; |g|^2
-__global__ void __launch_bounds__(256)
+template <int B>
+__global__ void __launch_bounds__(B)
     vertex_gather32_kernel(int nv, const int* __restrict__ vptr, const int* __restrict__ vinc,
                            const float* __restrict__ lf32, const uint8_t* __restrict__ mask, double* __restrict__ g,
                            Reduce red) {
-  __shared__ double shred[256 / 32][1];
-  const int v = blockIdx.x * 256 + threadIdx.x;
+  __shared__ double shred[B / 32][1];
+  const int v = blockIdx.x * B + threadIdx.x;
   float part[1] = {0.f};
   if (v < nv) {
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
@@ -433,9 +435,9 @@ __global__ void __launch_bounds__(256)
     part[0] = a0 * a0 + a1 * a1 + a2 * a2;
   }
   double v1[1];
-  block_sum_s<1, 256, float>(part, v1, shred);
+  block_sum_s<1, B, float>(part, v1, shred);
   double tot[1];
-  if (grid_sum_last<1, 256>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
+  if (grid_sum_last<1, B>(v1, red.partials, red.counter, tot)) red.sc->gnorm2 = tot[0];
 }
 
 constexpr int GB = 256;
@@ -476,8 +478,8 @@ __global__ void __launch_bounds__(GB)
 // time_step.hpp:646-651 folded in), written as the 10 upper 3x3 vertex blocks, staged through shared
 // memory so the global writes are contiguous.  Launch bounds of 8 blocks per SM (128 registers, a few
 // spills) beat the unconstrained 168 registers: 168 against 192 us per launch at 1.02M tets.
-template <typename S, bool XF>
-__global__ void __launch_bounds__(HB, 8)
+template <typename S, bool XF, int HB>
+__global__ void __launch_bounds__(HB, 512 / HB)
     elem_hessian_kernel(ElemFP64 e64, ElemFP32 e32, const double* __restrict__ X, const double* __restrict__ u,
                         const float4* __restrict__ xf, S dt2, int spsd, S* __restrict__ Kbuf) {
   __shared__ S stage[HB * 90];
@@ -543,45 +545,54 @@ void launch_split32(int nv, const double* u, const double* xt, float4* uh, float
 
 void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
                                double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
-                               const Reduce& red, cudaStream_t st) {
+                               const Reduce& red, cudaStream_t st, int block) {
   if (el.nt <= 0) return;
-  const int grid = div_up(el.nt, EB);
   const float f_dt2 = (float)dt2, f_rho = (float)rho, a = (float)alpha;
-  if (trial && with_forces)
-    elem_energy_grad32_kernel<true, true><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
-  else if (trial)
-    elem_energy_grad32_kernel<false, true><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
-  else if (with_forces)
-    elem_energy_grad32_kernel<true, false><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
-  else
-    elem_energy_grad32_kernel<false, false><<<grid, EB, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    const int grid = div_up(el.nt, b);
+    if (trial && with_forces)
+      elem_energy_grad32_kernel<true, true, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+    else if (trial)
+      elem_energy_grad32_kernel<false, true, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+    else if (with_forces)
+      elem_energy_grad32_kernel<true, false, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+    else
+      elem_energy_grad32_kernel<false, false, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+  };
+  dispatch_block<64, 128, 256>(block == 0 ? EB : block, go);
   after_launch("elem_energy_grad32");
 }
-
 void launch_elem_delta32(const ElemFP64& el, const ElemFP32& ef, const Split32& ref, const float4* db, const float4* d,
                          double alpha, double dt2, double rho, double e_ref, double escale_ref, float* lf32,
-                         bool with_forces, bool trial, const Reduce& red, cudaStream_t st) {
+                         bool with_forces, bool trial, const Reduce& red, cudaStream_t st, int block) {
   if (el.nt <= 0) return;
-  const int grid = div_up(el.nt, EB);
   const float f_dt2 = (float)dt2, f_rho = (float)rho, a = (float)alpha;
-  if (trial && with_forces)
-    elem_delta32_kernel<true, true><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
-  else if (trial)
-    elem_delta32_kernel<false, true><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
-  else if (with_forces)
-    elem_delta32_kernel<true, false><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
-  else
-    elem_delta32_kernel<false, false><<<grid, EB, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    const int grid = div_up(el.nt, b);
+    if (trial && with_forces)
+      elem_delta32_kernel<true, true, b><<<grid, b, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+    else if (trial)
+      elem_delta32_kernel<false, true, b><<<grid, b, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+    else if (with_forces)
+      elem_delta32_kernel<true, false, b><<<grid, b, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+    else
+      elem_delta32_kernel<false, false, b><<<grid, b, 0, st>>>(el, ef, ref, db, d, a, f_dt2, f_rho, e_ref, escale_ref, lf32, red);
+  };
+  dispatch_block<64, 128, 256>(block == 0 ? EB : block, go);
   after_launch("elem_delta32");
 }
-
 void launch_vertex_gather_delta32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
-                                  const double* gref, double* g, const Reduce& red, cudaStream_t st) {
+                                  const double* gref, double* g, const Reduce& red, cudaStream_t st, int block) {
   if (nv <= 0) return;
-  vertex_gather_delta32_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, vptr, vinc, lf32, mask, gref, g, red);
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    vertex_gather_delta32_kernel<b><<<div_up(nv, b), b, 0, st>>>(nv, vptr, vinc, lf32, mask, gref, g, red);
+  };
+  dispatch_block<128, 256, 512>(block == 0 ? 256 : block, go);
   after_launch("vertex_gather_delta32");
 }
-
 void launch_delta_base(int nv, const double* u, const double* uref, float4* db, cudaStream_t st) {
   if (nv <= 0) return;
   delta_base_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, u, uref, db);
@@ -589,12 +600,15 @@ void launch_delta_base(int nv, const double* u, const double* uref, float4* db, 
 }
 
 void launch_vertex_gather32(int nv, const int* vptr, const int* vinc, const float* lf32, const uint8_t* mask,
-                            double* g, const Reduce& red, cudaStream_t st) {
+                            double* g, const Reduce& red, cudaStream_t st, int block) {
   if (nv <= 0) return;
-  vertex_gather32_kernel<<<div_up(nv, 256), 256, 0, st>>>(nv, vptr, vinc, lf32, mask, g, red);
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    vertex_gather32_kernel<b><<<div_up(nv, b), b, 0, st>>>(nv, vptr, vinc, lf32, mask, g, red);
+  };
+  dispatch_block<128, 256, 512>(block == 0 ? 256 : block, go);
   after_launch("vertex_gather32");
 }
-
 void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double* lf, const uint8_t* mask,
                           double* g, const Reduce& red, cudaStream_t st) {
   if (nv <= 0) return;
@@ -604,18 +618,21 @@ void launch_vertex_gather(int nv, const int* vptr, const int* vinc, const double
 
 template <typename S>
 void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
-                         const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st) {
+                         const float4* xf, double dt2, bool spsd, S* Kbuf, cudaStream_t st, int block) {
   if (e64.nt <= 0) return;
-  const int grid = div_up(e64.nt, HB);
-  if (xf != nullptr)
-    elem_hessian_kernel<S, true><<<grid, HB, 0, st>>>(e64, e32, X, u, xf, (S)dt2, spsd ? 1 : 0, Kbuf);
-  else
-    elem_hessian_kernel<S, false><<<grid, HB, 0, st>>>(e64, e32, X, u, xf, (S)dt2, spsd ? 1 : 0, Kbuf);
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    const int grid = div_up(e64.nt, b);
+    if (xf != nullptr)
+      elem_hessian_kernel<S, true, b><<<grid, b, 0, st>>>(e64, e32, X, u, xf, (S)dt2, spsd ? 1 : 0, Kbuf);
+    else
+      elem_hessian_kernel<S, false, b><<<grid, b, 0, st>>>(e64, e32, X, u, xf, (S)dt2, spsd ? 1 : 0, Kbuf);
+  };
+  dispatch_block<32, 64, 128>(block == 0 ? HB : block, go);
   after_launch("elem_hessian");
-}
-template void launch_elem_hessian<float>(const ElemFP64&, const ElemFP32&, const double*, const double*,
-                                         const float4*, double, bool, float*, cudaStream_t);
+}template void launch_elem_hessian<float>(const ElemFP64&, const ElemFP32&, const double*, const double*,
+                                         const float4*, double, bool, float*, cudaStream_t, int);
 template void launch_elem_hessian<double>(const ElemFP64&, const ElemFP32&, const double*, const double*,
-                                          const float4*, double, bool, double*, cudaStream_t);
+                                          const float4*, double, bool, double*, cudaStream_t, int);
 
 }  // namespace ssim_gb

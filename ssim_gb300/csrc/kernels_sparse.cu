@@ -15,12 +15,12 @@ __device__ __forceinline__ size_t sell_base(int q) { return (size_t)9 * (size_t)
 // symmetric matrix) adds its precomputed list of element blocks (global_composer.hpp:103-119 builds the
 // same map entry by entry) to the consistent-mass block, then applies the Dirichlet identity filter
 // (boundary.hpp:53-67).  One thread per slot, no atomics: deterministic.
-template <typename S>
-__global__ void __launch_bounds__(SB)
+template <typename S, int B>
+__global__ void __launch_bounds__(B)
     assemble_kernel(SellMatrix A, const int* __restrict__ cptr, const int* __restrict__ csrc,
                     const S* __restrict__ Kbuf, const S* __restrict__ slot_mass, const uint8_t* __restrict__ mask,
                     int filter, S* __restrict__ vals, V4<S>* __restrict__ dinv, int precond) {
-  const int q = blockIdx.x * SB + threadIdx.x;
+  const int q = blockIdx.x * B + threadIdx.x;
   if (q >= A.nslots) return;
   S acc[9];
 #pragma unroll
@@ -1166,10 +1166,15 @@ void launch_kron_extract(const SellMatrix& A, const S* vals, S* svals, int* not_
 
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
-                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st) {
+                     const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st,
+                     int block) {
   if (A.nslots <= 0) return;
-  assemble_kernel<S><<<div_up(A.nslots, SB), SB, 0, st>>>(A, cptr, csrc, Kbuf, slot_mass, mask, filter ? 1 : 0,
-                                                          vals, dinv, precond);
+  auto go = [&](auto Bc) {
+    constexpr int b = decltype(Bc)::value;
+    assemble_kernel<S, b><<<div_up(A.nslots, b), b, 0, st>>>(A, cptr, csrc, Kbuf, slot_mass, mask, filter ? 1 : 0,
+                                                             vals, dinv, precond);
+  };
+  dispatch_block<128, 256, 512>(block == 0 ? SB : block, go);
   after_launch("assemble");
 }
 
@@ -1372,7 +1377,7 @@ void launch_instance_norms(int ninst, const int* voff, const double* g, double* 
 
 #define SSIM_INST(S)                                                                                              \
   template void launch_assemble<S>(const SellMatrix&, const int*, const int*, const S*, const S*, const uint8_t*, \
-                                   bool, S*, V4<S>*, int, cudaStream_t);                                          \
+                                   bool, S*, V4<S>*, int, cudaStream_t, int);                                     \
   template void launch_spmv<S>(const SellMatrix&, const S*, const V4<S>*, V4<S>*, cudaStream_t);                 \
   template void launch_kron_extract<S>(const SellMatrix&, const S*, S*, int*, cudaStream_t);                     \
   template void launch_export_csr<S>(const SellMatrix&, const int*, const int*, const int*, const S*, double*,   \

@@ -745,6 +745,14 @@ ssim_gb_status ssim_gb_adjoint_step(ssim_gb_timestep* h, double* ubar, double* v
   API_CATCH(h)
 }
 
+ssim_gb_status ssim_gb_autotune(ssim_gb_timestep* h, ssim_gb_tuning* out) {
+  CHECK_H(h);
+  API_TRY
+  const ssim_gb_tuning r = h->ts.autotune();
+  if (out) *out = r;
+  API_CATCH(h)
+}
+
 ssim_gb_status ssim_gb_get_field_device(ssim_gb_timestep* h, int32_t field, double* dst) {
   CHECK_H(h);
   API_TRY

@@ -7,8 +7,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -171,6 +174,11 @@ struct TimeStep {
   DBuf<float4> uh32, ul32, w32;
   DBuf<float> lf32t;
   Split32 s32() const { return Split32{uh32.p, ul32.p, w32.p}; }
+  // block sizes chosen by autotune() for the element pass, the Hessian, the assembly and the gather (0: the
+  // kernels' defaults)
+  struct Shapes {
+    int elem = 0, hess = 0, assem = 0, gather = 0;
+  } shapes;
   // the reference of the increment evaluations (mixed Newton after the FP32 phase): u_r, its FP64 forces and
   // energy, and the base point offset u_b - u_r; the FP32 split of u_r lives in uh32 / ul32 / w32
   DBuf<double> uref, gref;
@@ -193,10 +201,10 @@ struct TimeStep {
   void delta_base() { launch_delta_base(nv, next.p, uref.p, db32.p, stream); }
   void delta_trial(const float4* d, double alpha) {
     launch_elem_delta32(e64(), e32s(), s32(), db32.p, d, alpha, dt * dt, rho, e_ref, escale_ref, lf32t.p, true, true,
-                        red(), stream);
+                        red(), stream, shapes.elem);
   }
   void delta_gather() {
-    launch_vertex_gather_delta32(nv, vptr.p, vinc.p, lf32t.p, mask.p, gref.p, forces.p, red(), stream);
+    launch_vertex_gather_delta32(nv, vptr.p, vinc.p, lf32t.p, mask.p, gref.p, forces.p, red(), stream, shapes.gather);
   }
   void split32() {
     uh32.alloc(nv);
@@ -228,7 +236,7 @@ struct TimeStep {
                                    forces ? lf32t.p : nullptr, forces, true, red(), stream);
         else
           launch_elem_energy_grad32(e64(), e32s(), s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
-                                    forces, true, red(), stream);
+                                    forces, true, red(), stream, shapes.elem);
       } else {
         throw state_error("the FP32 element pass takes FP32 directions");
       }
@@ -256,7 +264,7 @@ struct TimeStep {
       launch_spring_gather<S>(nv, vptr.p, vinc.p, lf.p, vmass.p, next.p, d, alpha, inertia.p, mask.p, forces.p, red(),
                               stream);
     else if (fp32)
-      launch_vertex_gather32(nv, vptr.p, vinc.p, lf32t.p, mask.p, forces.p, red(), stream);
+      launch_vertex_gather32(nv, vptr.p, vinc.p, lf32t.p, mask.p, forces.p, red(), stream, shapes.gather);
     else
       launch_vertex_gather(nv, vptr.p, vinc.p, lf.p, mask.p, forces.p, red(), stream);
   }
@@ -737,7 +745,7 @@ struct TimeStep {
                                red(), stream);
     else
       launch_elem_energy_grad32(e64(), e32s(), s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false, red(),
-                                stream);
+                                stream, shapes.elem);
     if (profiling) prof_end(e0, e1, PK_GRAD, 0);
     gather_forces<float>(nullptr, 0.0, true);
     sync_scalars();
@@ -794,11 +802,12 @@ struct TimeStep {
     else if (tri2d)
       launch_tri_hessian<S>(e64(), next.p, dt * dt, spsd, s.K.p, stream);
     else
-      launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream);
+      launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream,
+                             shapes.hess);
     if (profiling) prof_end(e0, e1, PK_HESS, 0);
     if (profiling) prof_begin(e0, e1);
     launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
-                       params.precond, stream);
+                       params.precond, stream, shapes.assem);
     if (profiling) prof_end(e0, e1, PK_ASM, 0);
   }
 
@@ -1482,6 +1491,169 @@ struct TimeStep {
     st.elapsed_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     stats = st;
     return st.grad_norm;
+  }
+
+  // ------------------------------------------------------------------ launch-shape autotuning
+  // ssim_gb_autotune: times candidate launch shapes on this handle's data and applies the fastest; the
+  // choice is cached per process by the problem's shape (see ssim_gb.h).
+  using TuneKey = std::tuple<int, int, long long, int, int, int>;
+  static std::map<TuneKey, ssim_gb_tuning>& tune_cache() {
+    static std::map<TuneKey, ssim_gb_tuning> m;
+    return m;
+  }
+  static std::mutex& tune_mutex() {
+    static std::mutex m;
+    return m;
+  }
+  void apply_tuning(const ssim_gb_tuning& t) {
+    shapes.elem = t.elem_block;
+    shapes.hess = t.hessian_block;
+    shapes.assem = t.assembly_block;
+    shapes.gather = t.gather_block;
+    params.pcg_persistent = t.pcg_persistent;
+    params.pcg_max_blocks = t.pcg_max_blocks;
+    params.fused_assembly = t.fused_assembly;
+  }
+  ssim_gb_tuning autotune() {
+    if (!has_reset) throw state_error("autotune() before reset()");
+    const TuneKey key{nv, nt, topo.nnzb, mixed() ? 1 : 0, ninst, springs ? 2 : (tri2d ? 1 : 0)};
+    {
+      std::lock_guard<std::mutex> lock(tune_mutex());
+      auto it = tune_cache().find(key);
+      if (it != tune_cache().end()) {
+        ssim_gb_tuning t = it->second;
+        apply_tuning(t);
+        t.from_cache = 1;
+        return t;
+      }
+    }
+    ssim_gb_tuning t{};
+    if (mixed())
+      tune_impl<float>(t);
+    else
+      tune_impl<double>(t);
+    apply_tuning(t);
+    t.from_cache = 0;
+    std::lock_guard<std::mutex> lock(tune_mutex());
+    tune_cache()[key] = t;
+    return t;
+  }
+  // mean time of f over reps launches after one untimed launch, CUDA events on the handle's stream (ms)
+  template <typename F>
+  double time_launches(F&& f, int reps = 3) {
+    cudaEvent_t a, b;
+    SSIM_CUDA(cudaEventCreate(&a));
+    SSIM_CUDA(cudaEventCreate(&b));
+    f();
+    SSIM_CUDA(cudaEventRecord(a, stream));
+    for (int r = 0; r < reps; ++r) f();
+    SSIM_CUDA(cudaEventRecord(b, stream));
+    SSIM_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    SSIM_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / reps;
+  }
+  template <typename S>
+  void tune_impl(ssim_gb_tuning& t) {
+    Solver<S>& s = solver<S>();
+    const bool tets = !springs && !tri2d;
+    DBuf<double> keep, rhs;
+    keep.alloc(n);
+    SSIM_CUDA(cudaMemcpyAsync(keep.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    int count = 0;
+    // FP32 element pass and force gather (the mixed path's tet kernels)
+    if constexpr (std::is_same<S, float>::value) {
+      if (tets) {
+        split32();
+        double best = 1e300;
+        for (int b : {64, 128, 256}) {
+          const double ms = time_launches([&] {
+            launch_elem_energy_grad32(e64(), e32s(), s32(), s.x.p, 0.0, dt * dt, rho, lf32t.p, true, true, red(),
+                                      stream, b);
+          });
+          ++count;
+          if (ms < best) best = ms, t.elem_block = b;
+        }
+        t.elem_us = best * 1e3;
+        best = 1e300;
+        for (int b : {128, 256, 512}) {
+          const double ms = time_launches(
+              [&] { launch_vertex_gather32(nv, vptr.p, vinc.p, lf32t.p, mask.p, forces.p, red(), stream, b); });
+          ++count;
+          if (ms < best) best = ms, t.gather_block = b;
+        }
+      }
+    }
+    // element Hessian and assembly: block sizes of the two kernels, against the fused kernel
+    if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+    const float4* xfp = mixed() ? xf.p : nullptr;
+    t.hessian_block = 0;
+    t.assembly_block = 0;
+    double hbest = 1e300, abest = 1e300;
+    s.K.alloc((size_t)9 * (topo.cv * (topo.cv + 1) / 2) * nt);
+    if (tets) {
+      for (int b : {32, 64, 128}) {
+        const double ms = time_launches(
+            [&] { launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, xfp, dt * dt, true, s.K.p, stream, b); });
+        ++count;
+        if (ms < hbest) hbest = ms, t.hessian_block = b;
+      }
+    } else {
+      hbest = 0;
+      hessian<S>(true, true);  // the springs' / triangles' element blocks for the assembly timings
+    }
+    for (int b : {128, 256, 512}) {
+      const double ms = time_launches([&] {
+        launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, true, s.vals.p, s.dinv.p,
+                           params.precond, stream, b);
+      });
+      ++count;
+      if (ms < abest) abest = ms, t.assembly_block = b;
+    }
+    t.hessian_us = (hbest + abest) * 1e3;
+    t.fused_assembly = 0;
+    if (tets && fused_ready()) {
+      const double ms = time_launches([&] {
+        launch_fused_hessian<S>(e64(), e32(), dX.p, next.p, xfp, dt * dt, true, A(), topo.nslices, fused_spc,
+                                fused_ncta, fptr.p, felem.p, fcode.p, s.slot_mass.p, mask.p, true, s.vals.p, s.dinv.p,
+                                params.precond, stream);
+      });
+      ++count;
+      if (ms < hbest + abest) t.fused_assembly = 1, t.hessian_us = ms * 1e3;
+    }
+    // PCG on the assembled matrix: variant and persistent grid, one solve to 5e-2 from a fixed right-hand side
+    std::vector<double> ones(n, 1.0);
+    rhs.upload(ones, stream);
+    int nsm = 0, dev = 0;
+    SSIM_CUDA(cudaGetDevice(&dev));
+    SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const std::vector<int> variants = mixed() ? std::vector<int>{2, 1} : std::vector<int>{0, 2};
+    std::vector<int> grids = {0};
+    if (4 * nsm < div_up(nv, 256)) grids.push_back(4 * nsm);
+    const int keep_variant = params.pcg_persistent, keep_grid = params.pcg_max_blocks;
+    const size_t log0 = solve_log.size();
+    double pbest = 1e300;
+    t.pcg_persistent = keep_variant;
+    t.pcg_max_blocks = keep_grid;
+    for (int v : variants)
+      for (int gcap : grids) {
+        if (v == 0 && gcap != 0) continue;  // the two-launch loop has no persistent grid
+        params.pcg_persistent = v;
+        params.pcg_max_blocks = gcap;
+        int iters = 0;
+        const double ms = time_launches([&] { iters = pcg<S>(rhs.p, false, 5e-2, params.cg_max_iters, nullptr); }, 2);
+        ++count;
+        if (ms < pbest) pbest = ms, t.pcg_persistent = v, t.pcg_max_blocks = gcap, t.pcg_iterations = iters;
+      }
+    params.pcg_persistent = keep_variant;
+    params.pcg_max_blocks = keep_grid;
+    solve_log.resize(log0);
+    t.pcg_solve_ms = pbest;
+    t.candidates = count;
+    SSIM_CUDA(cudaMemcpyAsync(forces.p, keep.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    SSIM_CUDA(cudaStreamSynchronize(stream));
   }
 
   // ------------------------------------------------------------------ profiling

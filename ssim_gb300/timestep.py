@@ -392,6 +392,15 @@ class TimeStep:
         return g, g0
 
     # ---------------------------------------------------------------- profiling
+    def autotune(self) -> dict:
+        """One-time sweep of launch shapes on this handle's data (ssim_gb_autotune): block sizes of the element
+        pass, the Hessian, the assembly and the gather, the PCG variant and grid, fused or two-kernel assembly;
+        the fastest is applied and cached for the process by problem shape.  Returns the chosen shapes and
+        their timings."""
+        t = _lib.Tuning()
+        self._c(self._L.ssim_gb_autotune(self._h, C.byref(t)))
+        return t.as_dict()
+
     def profile(self, enable: bool = True):
         self._c(self._L.ssim_gb_profile_enable(self._h, int(enable)))
 
