@@ -199,6 +199,8 @@ def run_gpu_arm(args, scene):
         if tdist.is_available() and tdist.is_initialized():
             tdist.barrier()
 
+    tuning = {}
+
     def timed_run(precision, steps, warmup, profile=False):
         # restart from the scene's initial state: the same start for every run; the state after the first
         # (untimed) step is kept for the comparison with the oracle's first step
@@ -207,6 +209,8 @@ def run_gpu_arm(args, scene):
         for f in ("deformation", "prev_deform"):
             ts.set(f, zeros if scene.get("u0") is None else scene["u0"])
         ts.set("velocity", v0)
+        if args.autotune:  # launch shapes for this precision (swept once, then from the process cache)
+            tuning[precision] = ts.autotune()
         first = None
         for i in range(warmup):
             ts.step()
@@ -239,7 +243,7 @@ def run_gpu_arm(args, scene):
     if args.arms == "mixed":
         return dict(ms_mixed=ms_mixed, ms_fp64=float("nan"), st_mixed=st_mixed, st_fp64=[], launches=launches,
                     prof=None, clocks=clocks, e2e_s=float("nan"), h2d=0, d2h=0, total_launches=0,
-                    solve_log=solve_log, first={"mixed": first_mixed})
+                    solve_log=solve_log, first={"mixed": first_mixed}, tuning=tuning)
     # ---- roofline of the dominant kernel (PCG SpMV), events around each launch, same workload
     _, _, _, _, prof, _ = timed_run("mixed", min(args.steps, 3), 1, profile=True)
     # ---- plain FP64 on the same steps
@@ -269,6 +273,8 @@ def run_gpu_arm(args, scene):
         # (projective_dynamics.hpp:90-91); the per-step marking below only refreshes the same targets
         s.mark_dirichlet_batched(fixed, targ_np)
         s.reset()
+    if args.autotune:  # the same shape as the device-timed handle: the cached choice, nothing timed
+        s.step_.autotune()
     if scene.get("u0") is not None:  # the scene's initial state, as the device-timed runs start from
         for f in ("deformation", "prev_deform"):
             s.step_.set(f, scene["u0"])
@@ -292,7 +298,7 @@ def run_gpu_arm(args, scene):
         ms_mixed=ms_mixed, ms_fp64=ms_fp64, st_mixed=st_mixed, st_fp64=st_fp64, launches=launches, prof=prof,
         clocks=clocks, e2e_s=e2e_s, h2d=fixed.size * 3 * 8 + fixed.size * 4, d2h=d.size * 8,
         total_launches=g.launch_count() - launches0, nnz=ts.nnz, solve_log=solve_log,
-        first={"mixed": first_mixed, "fp64": first_fp64},
+        first={"mixed": first_mixed, "fp64": first_fp64}, tuning=tuning,
     )
     if args.adjoint:
         mixed, g_mixed = run_adjoint("mixed")
@@ -452,6 +458,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-first-state", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the kernels' default launch shapes (no ssim_gb_autotune sweep before the timed runs)")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the differentiable-rollout timing (32^3 cube, 40 steps)")
     args = ap.parse_args()
@@ -579,6 +587,9 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cb,
             "clocks": r["clocks"],
+            "tuning": {k: {f: v[f] for f in ("elem_block", "hessian_block", "assembly_block", "gather_block",
+                                             "pcg_persistent", "pcg_max_blocks", "fused_assembly", "candidates")}
+                       for k, v in r.get("tuning", {}).items()} or None,
             "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
             "adjoint": r.get("adjoint"),
         }
