@@ -182,6 +182,8 @@ def run_gpu_arm(args, scene):
     params = newton_params(g)
     params.pd_kappa_mode = args.pd_kappa
     params.pcg_persistent = args.pcg_variant
+    if args.pcg_half is not None:
+        params.pcg_half_matrix = args.pcg_half
     result = {}
     launches0 = g.launch_count()
 
@@ -209,7 +211,10 @@ def run_gpu_arm(args, scene):
         for f in ("deformation", "prev_deform"):
             ts.set(f, zeros if scene.get("u0") is None else scene["u0"])
         ts.set("velocity", v0)
-        if args.autotune:  # launch shapes for this precision (swept once, then from the process cache)
+        if args.tuning is not None and precision == "mixed":  # pinned shapes: nothing swept
+            ts.set_tuning(args.tuning)
+            tuning[precision] = dict(args.tuning, pinned=True)
+        elif args.autotune:  # launch shapes for this precision (swept once, then from the process cache)
             tuning[precision] = ts.autotune()
         first = None
         for i in range(warmup):
@@ -273,7 +278,9 @@ def run_gpu_arm(args, scene):
         # (projective_dynamics.hpp:90-91); the per-step marking below only refreshes the same targets
         s.mark_dirichlet_batched(fixed, targ_np)
         s.reset()
-    if args.autotune:  # the same shape as the device-timed handle: the cached choice, nothing timed
+    if args.tuning is not None:
+        s.step_.set_tuning(args.tuning)
+    elif args.autotune:  # the same shape as the device-timed handle: the cached choice, nothing timed
         s.step_.autotune()
     if scene.get("u0") is not None:  # the scene's initial state, as the device-timed runs start from
         for f in ("deformation", "prev_deform"):
@@ -452,6 +459,8 @@ def main():
                     help="PD diffusivity: 0 the reference's (E, nu) slots, 1 Lame, 2 per element")
     ap.add_argument("--pcg-variant", type=int, default=3, choices=[0, 1, 2, 3, 4],
                     help="ssim_gb_params.pcg_persistent of the GPU arms (3: automatic; 4: pipelined PCG)")
+    ap.add_argument("--pcg-half", type=int, default=None, choices=[0, 1],
+                    help="FP16 copy of the scaled system matrix for the loose PCG solves (default: the library's)")
     ap.add_argument("--precond", type=int, default=None, choices=[1, 2],
                     help="PCG preconditioner of every arm (1 Jacobi, 2 block-Jacobi); default: the bench's")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
@@ -460,6 +469,10 @@ def main():
     ap.add_argument("--arms", default="all", choices=["all", "mixed"], help="mixed: only the headline timed run")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the kernels' default launch shapes (no ssim_gb_autotune sweep before the timed runs)")
+    ap.add_argument("--tuning", type=json.loads, default=None,
+                    help="apply this launch-shape tuning (a JSON object as the bench line's 'tuning' reports for the "
+                         "mixed arm) to the mixed runs instead of sweeping; for profiling runs, whose tools distort "
+                         "the sweep's timings")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the differentiable-rollout timing (32^3 cube, 40 steps)")
     args = ap.parse_args()
@@ -587,8 +600,9 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cb,
             "clocks": r["clocks"],
-            "tuning": {k: {f: v[f] for f in ("elem_block", "hessian_block", "assembly_block", "gather_block",
-                                             "pcg_persistent", "pcg_max_blocks", "fused_assembly", "candidates")}
+            "tuning": {k: {f: v.get(f, 0) for f in ("elem_block", "hessian_block", "assembly_block", "gather_block",
+                                                    "pcg_persistent", "pcg_max_blocks", "fused_assembly",
+                                                    "pcg_half_matrix", "candidates", "pinned")}
                        for k, v in r.get("tuning", {}).items()} or None,
             "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
             "adjoint": r.get("adjoint"),

@@ -75,7 +75,12 @@ typedef enum {
   SSIM_GB_DBC_VALUES = 7
 } ssim_gb_field;
 
-typedef enum { SSIM_GB_SYSMATRIX = 0, SSIM_GB_MASS = 1, SSIM_GB_MASS_FILTERED = 2 } ssim_gb_matrix;
+typedef enum {
+  SSIM_GB_SYSMATRIX = 0,
+  SSIM_GB_MASS = 1,
+  SSIM_GB_MASS_FILTERED = 2,
+  SSIM_GB_SYSMATRIX_HALF = 3 /* ssim_gb_spmv only, mixed precision: the FP16 copy of pcg_half_matrix */
+} ssim_gb_matrix;
 
 /* Solver settings.  Defaults (ssim_gb_default_params) follow the reference where it fixes a value:
  * max 1000 Newton iterations and Armijo 0.3 (backward_euler.hpp:21-22), stopping rule
@@ -139,6 +144,14 @@ typedef struct {
                              iterations after the FP32 phase as FP32 increments from the FP64 evaluation made at
                              the switch (energy and forces = that evaluation's + increments whose rounding is
                              relative to the increment); 0 evaluates them in FP64 */
+  int32_t pcg_half_matrix; /* mixed precision: 1 (default) runs the persistent Chronopoulos-Gear PCG solves whose relative
+                             tolerance is at least half_matrix_min_rtol on an FP16 copy of the Jacobi-scaled system
+                             matrix (S K S, S = diag(K)^-1/2, both triangles, one 16-byte load per block; remade
+                             after each assembly): the same iterates up to the FP16 rounding of the scaled values
+                             (~5e-4 relative), about 60% of the FP32 symmetric format's SpMV time on a 1M-tet
+                             mesh; ssim_gb_autotune turns it off where its per-assembly conversion costs more than
+                             it saves.  0 keeps every solve on the FP32 values */
+  double half_matrix_min_rtol; /* tighter solves (adjoint, tight forcing) stay on the FP32 values (1e-2) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
@@ -169,6 +182,8 @@ typedef struct {
   double pcg_solve_ms;    /* one PCG solve to 5e-2 relative residual with the chosen variant and grid */
   int32_t pcg_iterations; /* iterations of that solve */
   int32_t candidates;     /* configurations timed */
+  int32_t pcg_half_matrix; /* ssim_gb_params.pcg_half_matrix chosen (mixed: the persistent Chronopoulos-Gear
+                              solve timed on the FP16 copy, its conversion included, and on the FP32 values) */
 } ssim_gb_tuning;
 
 typedef struct ssim_gb_timestep ssim_gb_timestep;
@@ -354,6 +369,12 @@ SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, const double*
  * timing (from_cache = 1).  The deformation and the other state are left as they were; the forces view is
  * restored. */
 SSIM_GB_API ssim_gb_status ssim_gb_autotune(ssim_gb_timestep* h, ssim_gb_tuning* out);
+/* Applies a tuning found earlier (by ssim_gb_autotune in this or another process) without timing anything:
+ * elem_block in {0, 64, 128, 256}, hessian_block in {0, 32, 64, 128}, assembly_block and gather_block in
+ * {0, 128, 256, 512} (0: the compiled default), pcg_persistent 0..4, pcg_max_blocks >= 0, fused_assembly and
+ * pcg_half_matrix 0 or 1; the timing and cache fields are ignored.  Anything else: SSIM_GB_ERR_INVALID_ARGUMENT, nothing
+ * applied. */
+SSIM_GB_API ssim_gb_status ssim_gb_set_tuning(ssim_gb_timestep* h, const ssim_gb_tuning* t);
 
 /* ---- profiling (CUDA events on the handle's stream around the element, assembly and PCG launches) ---- */
 SSIM_GB_API ssim_gb_status ssim_gb_profile_enable(ssim_gb_timestep* h, int32_t enable);

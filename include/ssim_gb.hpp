@@ -229,6 +229,14 @@ class basic_time_step {
     return t;
   }
 
+  // ---- launch shapes (extension): sweep once, or apply a tuning saved from an earlier sweep
+  ssim_gb_tuning autotune() {
+    ssim_gb_tuning t{};
+    chk(ssim_gb_autotune(h_, &t));
+    return t;
+  }
+  basic_time_step& set_tuning(const ssim_gb_tuning& t) { return chk(ssim_gb_set_tuning(h_, &t)); }
+
   // ---- energy, gradient, Hessian (time_step.hpp:577-658)
   double update_energy_and_gradients(bool is_deform_grad_updated = false) {
     double e = 0;

@@ -32,7 +32,7 @@ FIELDS = {
     "forces": 6,
     "dbc_values": 7,
 }
-MATRICES = {"sysmatrix": 0, "mass": 1, "mass_filtered": 2}
+MATRICES = {"sysmatrix": 0, "mass": 1, "mass_filtered": 2, "sysmatrix_half": 3}
 PROFILE_KERNELS = {"pcg_spmv": 0, "elem_hessian": 1, "assemble": 2, "elem_grad": 3, "pcg_update": 4, "pcg_iteration": 5}
 
 
@@ -70,6 +70,8 @@ class Params(C.Structure):
         ("pcg_pipe_iters", C.c_int32),
         ("fused_assembly", C.c_int32),
         ("mixed_delta", C.c_int32),
+        ("pcg_half_matrix", C.c_int32),
+        ("half_matrix_min_rtol", C.c_double),
     ]
 
     def as_dict(self):
@@ -108,6 +110,7 @@ class Tuning(C.Structure):
         ("pcg_solve_ms", C.c_double),
         ("pcg_iterations", C.c_int32),
         ("candidates", C.c_int32),
+        ("pcg_half_matrix", C.c_int32),
     ]
 
     def as_dict(self):
@@ -205,6 +208,7 @@ _SIGS = {
     "ssim_gb_get_field_device": (C.c_int, [_H, C.c_int32, C.c_void_p]),
     "ssim_gb_set_field_device": (C.c_int, [_H, C.c_int32, C.c_void_p]),
     "ssim_gb_autotune": (C.c_int, [_H, C.POINTER(Tuning)]),
+    "ssim_gb_set_tuning": (C.c_int, [_H, C.POINTER(Tuning)]),
     "ssim_gb_profile_enable": (C.c_int, [_H, C.c_int32]),
     "ssim_gb_profile_read": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), _D, _D]),
     "ssim_gb_synchronize": (C.c_int, [_H]),

@@ -265,6 +265,40 @@ bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv
                            V4<S>* p0, V4<S>* p1, V4<S>* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                            long long spin_limit, int extra, int max_blocks, int variant, cudaStream_t st,
                            bool kron = false, V4<S>* pm = nullptr, int pipe_iters = 0);
+// FP16 copy of the Jacobi-scaled system matrix for the mixed Newton's loose PCG solves.  With s_a =
+// 1/sqrt(K_aa) per dof and S = diag(s), the copy holds K~ = S K S (|K~_ij| <= 1 for an SPD K) in both
+// triangles, full block SELL-32 (build_full_sell): per entry one 16-byte load of the block's first eight
+// values and one 2-byte load of the ninth.  PCG on K~ with the scaled block-Jacobi (S B S)^-1 makes the
+// same iterates as PCG on K with B^-1 up to the FP16 rounding of K~ (about 5e-4 relative per value): the
+// scalars (r, u), (w, u) are invariant, the stop test uses (r, r) of the unscaled residual, and the
+// solution is unscaled (x = S x~) before the kernel returns.
+struct HalfMatrix {
+  int nv;
+  const int* off;       // [nslices + 1] entry offset of each slice (multiple of 32)
+  const int* col;       // [nfs] block column, own row for padding
+  const uint4* v8;      // [nfs] values 0..7 of the scaled block (row-major), FP16
+  const uint16_t* v1;   // [nfs] value 8, FP16 bits
+  const float4* scale;  // [nv] s_a
+  const float4* iscale; // [nv] 1 / s_a
+};
+// scale, inverse scale and the scaled block-Jacobi rows (precond 0 / 1 / 2 on S B S) from the diagonal blocks
+// of the FP32 symmetric values
+void launch_half_prepare(const SellMatrix& A, const float* vals, int precond, float4* scale, float4* iscale,
+                         float4* dinv16, cudaStream_t st);
+// the FP16 values of every full entry from the FP32 symmetric values (src: build_full_sell's sources)
+void launch_half_convert(const SellMatrix& A, const int* off, const int* col, const int* src, const float* vals,
+                         const float4* scale, uint4* v8, uint16_t* v1, cudaStream_t st);
+// PCG setup in the scaled space: r~ = S (negate ? -b : b), z~ = M~ r~, x = p0 = 0; partials (r~, z~) and
+// (r, r) of the unscaled residual
+void launch_pcg_setup_half(const HalfMatrix& H, const double* b, const float4* dinv16, float4* x, float4* r, float4* z,
+                           float4* p0, double rtol, int max_iters, bool negate, const Reduce& red, cudaStream_t st);
+// Chronopoulos-Gear PCG on the FP16 copy in one cooperative launch (as launch_pcg_persistent variant 2);
+// x holds the unscaled solution on return.  false if the device cannot launch it cooperatively.
+bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float4* r, float4* z, float4* p0,
+                     float4* p1, float4* q, int max_iters, const Reduce& red, unsigned long long* gsync,
+                     long long spin_limit, int extra, int max_blocks, cudaStream_t st);
+// y = S^-1 K~ S^-1 x (the FP16 copy applied in the unscaled space); xs: nv vectors of scratch
+void launch_half_spmv(const HalfMatrix& H, const float4* x, float4* xs, float4* y, cudaStream_t st);
 // kron: vals holds one value per slot (the matrix is (scalar) (x) I3); launch_kron_extract makes that form
 // from a 9-value store and sets *not_kron when some block is not a multiple of I3
 template <typename S>

@@ -1,6 +1,8 @@
 // kernels_sparse.cu -- CSR/SELL assembly, SpMV, the fused Jacobi-PCG and the state-update vector kernels.
 #include <algorithm>
 
+#include <cuda_fp16.h>
+
 #include "kernels.cuh"
 
 namespace ssim_gb {
@@ -490,43 +492,92 @@ __device__ __forceinline__ bool plain_barrier(const GridSync& gs, unsigned long 
 }
 
 // Reducing barrier number kr: every block has written the partials of its virtual blocks (NV doubles each,
-// part[NV * vb]); warp 0 of each block marks them arrived in their groups of 32; the block completing a
-// group sums it (warp_group_sum) into gsum[g], and the block completing the last group sums the group
-// sums (warp_top_sum, the order of grid_sum_last_tree), runs epi(tot) in its lane 0 and releases everyone.
-// Returns false in every thread of a block whose wait gave up.
+// part[NV * vb]); warp 0 of each block marks them arrived in their groups of 32 virtual blocks, and the block
+// completing a group marks the group arrived at the top counter.  The block completing the last group sums
+// everything in the order of grid_sum_last_tree (each group of 32 by warp_group_sum's shuffle tree, then the
+// group sums by warp_top_sum's), runs epi(tot) in its thread 0 and releases everyone.  Only that block reads
+// partials, with all its warps at once (up to kTopPass groups per warp in flight), so the critical path holds
+// two atomics, one round of L2 reads and the release; grids of more than kTopGroups groups keep the group sums
+// in gsum (global) instead of shared memory.  Returns false in every thread of a block whose wait gave up.
+constexpr int kTopGroups = 64, kTopPass = 3;
+
+template <int NV>
+__device__ __forceinline__ void shfl_tree(double (&v)[NV]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+}
+
 template <int NV, typename EPI>
 __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long long kr, const double* part,
                                                double* gsum, int nvb, EPI&& epi) {
-  __shared__ int ok;
+  __shared__ int ok, s_top;
+  __shared__ double s_gsum[kTopGroups][NV];
   __syncthreads();
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
+    int top_any = 0;
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       const int g = vb >> 5, gsize = min(32, nvb - 32 * g);
-      int last = 0;
-      if (lane == 0) {
-        fence_acq_rel_gpu();
-        last = atomicAdd(gs.group + (size_t)g * kSyncStride, 1ull) == (kr + 1) * (unsigned long long)gsize - 1;
-        if (last) fence_acq_rel_gpu();
-      }
-      last = __shfl_sync(0xffffffffu, last, 0);
-      __syncwarp();
-      if (!last) continue;
-      double v[NV];
-      warp_group_sum<NV>(part, 32 * g, gsize, v);
       int top = 0;
       if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) gsum[g * NV + k] = v[k];
         fence_acq_rel_gpu();
-        top = atomicAdd(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
-        if (top) fence_acq_rel_gpu();
+        if (atomicAdd(gs.group + (size_t)g * kSyncStride, 1ull) == (kr + 1) * (unsigned long long)gsize - 1) {
+          fence_acq_rel_gpu();
+          top = atomicAdd(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
+          if (top) fence_acq_rel_gpu();
+        }
       }
-      top = __shfl_sync(0xffffffffu, top, 0);
-      __syncwarp();
-      if (!top) continue;
+      top_any |= top;
+    }
+    if (lane == 0) s_top = top_any;
+  }
+  __syncthreads();
+  if (s_top) {  // this block completed the last group: every partial has been released to it
+    const int ng = gs.ngroups, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const bool shared_sums = ng <= kTopGroups;
+    for (int g0 = warp; g0 < ng; g0 += kTopPass * nwarps) {
+      double v[kTopPass][NV];
+#pragma unroll
+      for (int j = 0; j < kTopPass; ++j) {
+        const int vb = 32 * (g0 + j * nwarps) + lane;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[j][k] = vb < nvb ? __ldcg(part + (size_t)vb * NV + k) : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < kTopPass; ++j) {
+        const int g = g0 + j * nwarps;
+        shfl_tree<NV>(v[j]);
+        if (lane == 0 && g < ng) {
+#pragma unroll
+          for (int k = 0; k < NV; ++k) {
+            if (shared_sums)
+              s_gsum[g][k] = v[j][k];
+            else
+              gsum[(size_t)g * NV + k] = v[j][k];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
       double tot[NV];
-      warp_top_sum<NV>(gsum, gs.ngroups, tot);
+      if (shared_sums) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) tot[k] = 0.0;
+        for (int c0 = 0; c0 < ng; c0 += 32) {
+          double v[NV];
+#pragma unroll
+          for (int k = 0; k < NV; ++k) v[k] = c0 + lane < ng ? s_gsum[c0 + lane][k] : 0.0;
+          shfl_tree<NV>(v);
+#pragma unroll
+          for (int k = 0; k < NV; ++k) tot[k] += v[k];
+        }
+      } else {
+        warp_top_sum<NV>(gsum, ng, tot);
+      }
       if (lane == 0) {
         epi(tot);
         fence_acq_rel_gpu();
@@ -672,6 +723,236 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
     if (!ok) break;
   }
   // a barrier wait gave up: flag it (the host clears the flag before the launch) and leave
+  if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
+}
+
+// ------------------------------------------------------------------ FP16 copy of the scaled matrix
+// (kernels.cuh, HalfMatrix).  The diagonal block of row u is its first upper slot.
+__global__ void __launch_bounds__(SB)
+    half_prepare_kernel(SellMatrix A, const float* __restrict__ vals, int precond, float4* __restrict__ scale,
+                        float4* __restrict__ iscale, float4* __restrict__ dinv16) {
+  const int u = blockIdx.x * SB + threadIdx.x;
+  if (u >= A.nv) return;
+  const int q = A.sl_off[u >> 5] + (u & 31);
+  const bool own = A.slot_row[q] == u;  // false only for a vertex that no cell uses (all-zero row)
+  const size_t base = sell_base(q);
+  float b[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) b[c] = own ? vals[base + 32 * c] : 0.f;
+  float sc[3], isc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float d = b[4 * a];
+    if (d > 0.f && isfinite(d)) {
+      isc[a] = sqrtf(d);
+      sc[a] = 1.f / isc[a];
+    } else {
+      sc[a] = isc[a] = 1.f;
+    }
+  }
+  float bt[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) bt[3 * a + c] = b[3 * a + c] * sc[a] * sc[c];
+  precond_rows<float>(bt, precond, dinv16 + 3 * (size_t)u);
+  scale[u] = make_float4(sc[0], sc[1], sc[2], 0.f);
+  iscale[u] = make_float4(isc[0], isc[1], isc[2], 0.f);
+}
+
+__device__ __forceinline__ unsigned int pack_half2(float lo, float hi) {
+  return (unsigned int)__half_as_ushort(__float2half_rn(lo)) | ((unsigned int)__half_as_ushort(__float2half_rn(hi)) << 16);
+}
+
+// one thread per block row, its entries in slot order (stores coalesced across the slice's lanes)
+__global__ void __launch_bounds__(SB)
+    half_convert_kernel(int nv, const int* __restrict__ off, const int* __restrict__ col, const int* __restrict__ src,
+                        const float* __restrict__ vals, const float4* __restrict__ scale, uint4* __restrict__ v8,
+                        uint16_t* __restrict__ v1) {
+  const int u = blockIdx.x * SB + threadIdx.x;
+  if (u >= nv) return;
+  const int lane = u & 31, sl = u >> 5;
+  const int b = off[sl], W = (off[sl + 1] - b) >> 5;
+  const float4 su = scale[u];
+  const float sa[3] = {su.x, su.y, su.z};
+  for (int k = 0; k < W; ++k) {
+    const int e = b + 32 * k + lane;
+    const unsigned int code = (unsigned int)src[e];
+    const bool tr = (code >> 31) != 0u;
+    const size_t base = sell_base((int)(code & 0x7fffffffu));
+    const float4 sw4 = scale[col[e]];
+    const float sw[3] = {sw4.x, sw4.y, sw4.z};
+    float v[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) v[c] = vals[base + 32 * c];
+    float h[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) h[3 * a + c] = (tr ? v[3 * c + a] : v[3 * a + c]) * sa[a] * sw[c];
+    v8[e] = make_uint4(pack_half2(h[0], h[1]), pack_half2(h[2], h[3]), pack_half2(h[4], h[5]),
+                       pack_half2(h[6], h[7]));
+    v1[e] = __half_as_ushort(__float2half_rn(h[8]));
+  }
+}
+
+__device__ __forceinline__ float2 unpack_half2(unsigned int w) {
+  return __half22float2(__halves2half2(__ushort_as_half((unsigned short)(w & 0xffffu)),
+                                       __ushort_as_half((unsigned short)(w >> 16))));
+}
+
+// y~_u = sum_k K~_{u,w_k} x_{w_k}: column indices staged per warp (cp.async, up to ST_K per row), then two
+// entries at a time: one 16-byte and one 2-byte value load and one x gather each
+__device__ __forceinline__ void half_row_product(const HalfMatrix& H, int u, const float4* x, int (*sidx)[32],
+                                                 float& a0, float& a1, float& a2) {
+  const int lane = u & 31, sl = u >> 5;
+  const int b = H.off[sl], W = (H.off[sl + 1] - b) >> 5;
+  const int* cb = H.col + b + lane;
+  const int ns = min(W, ST_K);
+  for (int k = 0; k < ns; ++k) cp_async4(&sidx[k][lane], cb + k * 32);
+  cp_async_wait_all();
+  auto col = [&](int k) { return k < ST_K ? sidx[k][lane] : cb[k * 32]; };
+  a0 = a1 = a2 = 0.f;
+  auto fma_block = [&](const uint4& p, uint16_t h8, const float4& xv) {
+    const float2 f01 = unpack_half2(p.x), f23 = unpack_half2(p.y), f45 = unpack_half2(p.z), f67 = unpack_half2(p.w);
+    const float f8 = __half2float(__ushort_as_half(h8));
+    a0 += f01.x * xv.x + f01.y * xv.y + f23.x * xv.z;
+    a1 += f23.y * xv.x + f45.x * xv.y + f45.y * xv.z;
+    a2 += f67.x * xv.x + f67.y * xv.y + f8 * xv.z;
+  };
+  const size_t e0 = (size_t)b + lane;
+  int k = 0;
+  for (; k + 2 <= W; k += 2) {
+    const uint4 p0 = H.v8[e0 + 32 * (size_t)k], p1 = H.v8[e0 + 32 * (size_t)(k + 1)];
+    const uint16_t h0 = H.v1[e0 + 32 * (size_t)k], h1 = H.v1[e0 + 32 * (size_t)(k + 1)];
+    const float4 x0 = x[col(k)], x1 = x[col(k + 1)];
+    fma_block(p0, h0, x0);
+    fma_block(p1, h1, x1);
+  }
+  if (k < W) fma_block(H.v8[e0 + 32 * (size_t)k], H.v1[e0 + 32 * (size_t)k], x[col(k)]);
+}
+
+__global__ void __launch_bounds__(SB)
+    half_spmv_kernel(HalfMatrix H, const float4* __restrict__ x, float4* __restrict__ xs, float4* __restrict__ y,
+                     int phase) {
+  __shared__ int sidx[SB / 32][ST_K][32];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  if (u >= H.nv) return;
+  if (phase == 0) {  // xs = S^-1 x
+    const float4 xv = x[u], is = H.iscale[u];
+    xs[u] = make_float4(xv.x * is.x, xv.y * is.y, xv.z * is.z, 0.f);
+    return;
+  }
+  float a0, a1, a2;
+  half_row_product(H, u, xs, sidx[threadIdx.x >> 5], a0, a1, a2);
+  const float4 is = H.iscale[u];
+  y[u] = make_float4(a0 * is.x, a1 * is.y, a2 * is.z, 0.f);
+}
+
+__global__ void __launch_bounds__(SB)
+    pcg_setup_half_kernel(HalfMatrix H, const double* __restrict__ g, const float4* __restrict__ dinv16,
+                          float4* __restrict__ x, float4* __restrict__ r, float4* __restrict__ z,
+                          float4* __restrict__ p0, double rtol, int max_iters, int negate, Reduce red) {
+  __shared__ double shred[SB / 32][2];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  float part[2] = {0.f, 0.f};
+  if (u < H.nv) {
+    const double sg = negate ? -1.0 : 1.0;
+    const float r0 = (float)(sg * g[u * 3 + 0]), r1 = (float)(sg * g[u * 3 + 1]), r2 = (float)(sg * g[u * 3 + 2]);
+    const float4 sc = H.scale[u];
+    const float t0 = r0 * sc.x, t1 = r1 * sc.y, t2 = r2 * sc.z;
+    const float4 d0 = dinv16[3 * u], d1 = dinv16[3 * u + 1], d2 = dinv16[3 * u + 2];
+    const float z0 = d0.x * t0 + d0.y * t1 + d0.z * t2;
+    const float z1 = d1.x * t0 + d1.y * t1 + d1.z * t2;
+    const float z2 = d2.x * t0 + d2.y * t1 + d2.z * t2;
+    x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+    r[u] = make_float4(t0, t1, t2, 0.f);
+    z[u] = make_float4(z0, z1, z2, 0.f);
+    p0[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+    part[0] = t0 * z0 + t1 * z1 + t2 * z2;
+    part[1] = r0 * r0 + r1 * r1 + r2 * r2;
+  }
+  double bs[2];
+  block_sum_s<2, SB, float>(part, bs, shred);
+  double tot[2];
+  if (grid_sum_last<2, SB>(bs, red.partials, red.counter, tot)) {
+    DevScalars* sc = red.sc;
+    sc->rz = tot[0];
+    sc->rz_old = 1.0;
+    sc->rr = tot[1];
+    sc->rr0 = tot[1];
+    sc->tol2 = rtol * rtol * tot[1];
+    sc->iters = 0;
+    sc->status = 0;
+    sc->done = (tot[1] <= sc->tol2 || tot[1] == 0.0 || max_iters <= 0) ? 1 : 0;
+  }
+}
+
+// Chronopoulos-Gear PCG (cgcg_persistent_kernel) in the scaled space of the FP16 copy: the SpMV reads the
+// full entries, the third dot is (r, r) of the unscaled residual r = S^-1 r~, and every block unscales its
+// own rows of x after the last iteration.
+__global__ void __launch_bounds__(SB, 5)
+    cgcg_half_kernel(HalfMatrix H, const float4* __restrict__ dinv16, float4* x, float4* r, float4* z, float4* p0,
+                     float4* p1, float4* q, int max_iters, Reduce red, GridSync gs) {
+  __shared__ double shred[SB / 32][3];
+  __shared__ int sidx[SB / 32][ST_K][32];
+  __shared__ double s_alpha, s_beta;
+  __shared__ int s_done;
+  DevScalars* sc = red.sc;
+  if (threadIdx.x == 0) s_done = *(volatile int*)&sc->done;
+  __syncthreads();
+  if (s_done) return;
+  const int nvb = (H.nv + SB - 1) / SB;
+  double* part = red.partials;
+  double* gsum = red.partials + 3 * (size_t)nvb;
+  bool ok = true;
+  for (int k = 0;; ++k) {
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int u = vb * SB + threadIdx.x;
+      float pr[3] = {0.f, 0.f, 0.f};
+      if (u < H.nv) {
+        float a0, a1, a2;
+        half_row_product(H, u, z, sidx[threadIdx.x >> 5], a0, a1, a2);
+        q[u] = make_float4(a0, a1, a2, 0.f);
+        const float4 uu = z[u], ru = r[u], is = H.iscale[u];
+        pr[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
+        pr[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
+        const float t0 = ru.x * is.x, t1 = ru.y * is.y, t2 = ru.z * is.z;
+        pr[2] = t0 * t0 + t1 * t1 + t2 * t2;
+      }
+      double bs[3];
+      block_sum_s<3, SB, float>(pr, bs, shred);
+      if (threadIdx.x == 0) {
+        part[3 * vb] = bs[0];
+        part[3 * vb + 1] = bs[1];
+        part[3 * vb + 2] = bs[2];
+      }
+      __syncthreads();
+    }
+    ok = reduce_barrier<3>(gs, (unsigned long long)k, part, gsum, nvb,
+                           [&](const double (&t)[3]) { cgcg_after(sc, t[0], t[1], t[2], max_iters); });
+    if (!ok) break;
+    if (threadIdx.x == 0) {
+      s_done = __ldcg(&sc->done);
+      s_alpha = __ldcg(&sc->alpha);
+      s_beta = __ldcg(&sc->beta);
+    }
+    __syncthreads();
+    if (s_done) break;
+    const float alpha = (float)s_alpha, beta = (float)s_beta;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x)
+      cgcg_update_row<float>(H.nv, k == 0, alpha, beta, dinv16, z, q, p0, p1, x, r, vb * SB + threadIdx.x);
+    ok = plain_barrier(gs, (unsigned long long)k);
+    if (!ok) break;
+  }
+  // x = S x~ (rows of this block only: no other block reads x)
+  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    const int u = vb * SB + threadIdx.x;
+    if (u < H.nv) {
+      const float4 xv = x[u], s4 = H.scale[u];
+      x[u] = make_float4(xv.x * s4.x, xv.y * s4.y, xv.z * s4.z, 0.f);
+    }
+  }
   if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
 }
 
@@ -1255,6 +1536,69 @@ bool launch_pcg_persistent(const SellMatrix& A, const S* vals, const V4<S>* dinv
                    (void*)&p1, (void*)&q,    (void*)&pm,   (void*)&max_iters, (void*)&rd, (void*)&gs, (void*)&pipe_iters};
   SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), variant == 4 ? pargs : args, 0, st));
   after_launch("pcg_persistent");
+  return true;
+}
+
+void launch_half_prepare(const SellMatrix& A, const float* vals, int precond, float4* scale, float4* iscale,
+                         float4* dinv16, cudaStream_t st) {
+  if (A.nv <= 0) return;
+  half_prepare_kernel<<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, precond, scale, iscale, dinv16);
+  after_launch("half_prepare");
+}
+
+void launch_half_convert(const SellMatrix& A, const int* off, const int* col, const int* src, const float* vals,
+                         const float4* scale, uint4* v8, uint16_t* v1, cudaStream_t st) {
+  if (A.nv <= 0) return;
+  half_convert_kernel<<<div_up(A.nv, SB), SB, 0, st>>>(A.nv, off, col, src, vals, scale, v8, v1);
+  after_launch("half_convert");
+}
+
+void launch_pcg_setup_half(const HalfMatrix& H, const double* b, const float4* dinv16, float4* x, float4* r, float4* z,
+                           float4* p0, double rtol, int max_iters, bool negate, const Reduce& red, cudaStream_t st) {
+  if (H.nv <= 0) return;
+  pcg_setup_half_kernel<<<div_up(H.nv, SB), SB, 0, st>>>(H, b, dinv16, x, r, z, p0, rtol, max_iters, negate ? 1 : 0,
+                                                          red);
+  after_launch("pcg_setup_half");
+}
+
+void launch_half_spmv(const HalfMatrix& H, const float4* x, float4* xs, float4* y, cudaStream_t st) {
+  if (H.nv <= 0) return;
+  half_spmv_kernel<<<div_up(H.nv, SB), SB, 0, st>>>(H, x, xs, y, 0);
+  half_spmv_kernel<<<div_up(H.nv, SB), SB, 0, st>>>(H, x, xs, y, 1);
+  after_launch("half_spmv");
+}
+
+bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float4* r, float4* z, float4* p0,
+                     float4* p1, float4* q, int max_iters, const Reduce& red, unsigned long long* gsync,
+                     long long spin_limit, int extra, int max_blocks, cudaStream_t st) {
+  int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+  SSIM_CUDA(cudaGetDevice(&dev));
+  SSIM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) return false;
+  SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const void* fn = (const void*)cgcg_half_kernel;
+  SSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SB, 0));
+  if (per_sm < 1) return false;
+  int grid = std::min(div_up(H.nv, SB), per_sm * nsm);
+  if (max_blocks > 0) grid = std::min(grid, max_blocks);
+  if (grid < 1) return true;
+  const int ngroups = (div_up(H.nv, SB) + 31) / 32;
+  SSIM_CUDA(cudaMemsetAsync(gsync, 0, grid_sync_words(H.nv) * sizeof(unsigned long long), st));
+  SSIM_CUDA(cudaMemsetAsync(&red.sc->wait_failed, 0, sizeof(int32_t), st));
+  GridSync gs{gsync,
+              gsync + kSyncStride,
+              gsync + 2 * kSyncStride,
+              gsync + 4 * kSyncStride,
+              ngroups,
+              (unsigned int)extra,
+              spin_limit > 0 ? spin_limit : (1LL << 25),
+              gsync + 3 * kSyncStride};
+  HalfMatrix h = H;
+  Reduce rd = red;
+  void* args[] = {(void*)&h,  (void*)&dinv16, (void*)&x, (void*)&r,         (void*)&z,  (void*)&p0,
+                  (void*)&p1, (void*)&q,      (void*)&max_iters, (void*)&rd, (void*)&gs};
+  SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), args, 0, st));
+  after_launch("pcg_half");
   return true;
 }
 

@@ -1,4 +1,5 @@
 // timestep.cu -- the C ABI of include/ssim_gb.h over the time-step object of timestep.cuh.
+#include <initializer_list>
 #include "timestep.cuh"
 
 // ==================================================================== C ABI
@@ -151,6 +152,8 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->pcg_pipe_iters = 80;
   p->fused_assembly = 0;
   p->mixed_delta = 1;
+  p->pcg_half_matrix = 1;
+  p->half_matrix_min_rtol = 1e-2;
   p->elem32_switch = 10.0;
 }
 
@@ -306,7 +309,8 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
       p->pcg_max_blocks < 0 || p->ncg_max_iters < 0 || !(p->ncg_step0 > 0) || !(p->ncg_eta >= 0) ||
       p->ncg_expand < 0 || !(p->stop_floor >= 0) || p->mixed_elem32 < 0 || p->mixed_elem32 > 1 ||
       !(p->ls_energy_slack32 >= 0) || !(p->elem32_switch >= 1) || p->pcg_pipe_iters < 0 || (p->fused_assembly != 0 && p->fused_assembly != 1) ||
-      (p->mixed_delta != 0 && p->mixed_delta != 1) ||
+      (p->mixed_delta != 0 && p->mixed_delta != 1) || (p->pcg_half_matrix != 0 && p->pcg_half_matrix != 1) ||
+      !(p->half_matrix_min_rtol >= 0) ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;
@@ -669,8 +673,21 @@ ssim_gb_status ssim_gb_spmv(ssim_gb_timestep* h, int32_t which, const double* x,
   CHECK_H(h);
   API_TRY
   TimeStep& t = h->ts;
-  if (!x || !y || which < 0 || which > 2) throw ssim_gb::invalid_argument("invalid matrix or null buffer");
+  if (!x || !y || which < 0 || which > 3) throw ssim_gb::invalid_argument("invalid matrix or null buffer");
   if (!t.has_reset) throw ssim_gb::state_error("spmv before reset()");
+  if (which == SSIM_GB_SYSMATRIX_HALF) {
+    if (!t.mixed()) throw ssim_gb::invalid_argument("the FP16 system matrix exists in mixed precision only");
+    if (!t.half_ready()) throw ssim_gb::invalid_argument("the pattern does not fit the FP16 matrix's indices");
+    t.half_refresh();
+    ssim_gb::Solver<float>& s = t.sf;
+    SSIM_CUDA(cudaMemcpyAsync(t.work.p, x, sizeof(double) * t.n, cudaMemcpyHostToDevice, t.stream));
+    ssim_gb::launch_to_vec4<float>(t.nv, t.work.p, s.tmp.p, false, t.stream);
+    ssim_gb::launch_half_spmv(t.half_matrix(), s.tmp.p, s.r.p, s.q.p, t.stream);
+    ssim_gb::launch_from_vec4<float>(t.nv, s.q.p, t.work.p, t.stream);
+    SSIM_CUDA(cudaMemcpyAsync(y, t.work.p, sizeof(double) * t.n, cudaMemcpyDeviceToHost, t.stream));
+    SSIM_CUDA(cudaStreamSynchronize(t.stream));
+    return SSIM_GB_OK;
+  }
   if (t.mixed())
     do_spmv<float>(t, which, x, y);
   else
@@ -751,6 +768,23 @@ ssim_gb_status ssim_gb_autotune(ssim_gb_timestep* h, ssim_gb_tuning* out) {
   const ssim_gb_tuning r = h->ts.autotune();
   if (out) *out = r;
   API_CATCH(h)
+}
+
+ssim_gb_status ssim_gb_set_tuning(ssim_gb_timestep* h, const ssim_gb_tuning* t) {
+  CHECK_H(h);
+  if (!t) return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "null tuning");
+  auto one_of = [](int v, std::initializer_list<int> set) {
+    for (int x : set)
+      if (v == x) return true;
+    return false;
+  };
+  if (!one_of(t->elem_block, {0, 64, 128, 256}) || !one_of(t->hessian_block, {0, 32, 64, 128}) ||
+      !one_of(t->assembly_block, {0, 128, 256, 512}) || !one_of(t->gather_block, {0, 128, 256, 512}) ||
+      t->pcg_persistent < 0 || t->pcg_persistent > 4 || t->pcg_max_blocks < 0 ||
+      (t->fused_assembly != 0 && t->fused_assembly != 1) || (t->pcg_half_matrix != 0 && t->pcg_half_matrix != 1))
+    return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid tuning (block size outside its candidate set)");
+  h->ts.apply_tuning(*t);
+  return SSIM_GB_OK;
 }
 
 ssim_gb_status ssim_gb_get_field_device(ssim_gb_timestep* h, int32_t field, double* dst) {

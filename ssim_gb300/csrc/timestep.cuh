@@ -121,6 +121,15 @@ struct TimeStep {
   DBuf<uint16_t> fcode;
   int fused_ncta = 0, fused_spc = 0;
   bool fused_ok = false, fused_built = false;
+  // FP16 copy of the scaled system matrix for the mixed Newton's loose PCG solves (kernels.cuh HalfMatrix):
+  // pattern built on first use, values made from the FP32 assembly before the first solve that reads them
+  DBuf<int32_t> h16off, h16col, h16src;
+  DBuf<uint4> h16v8;
+  DBuf<uint16_t> h16v1;
+  DBuf<float4> h16scale, h16iscale, h16dinv;
+  bool h16_ok = false, h16_built = false;
+  long long nfs = 0;
+  long long asm_count = 0, h16_count = -1;  // assemblies of the FP32 values; the one the copy was made from
   DBuf<double> lf, csr_out;
   // ---- device: solver
   Solver<float> sf;
@@ -529,6 +538,42 @@ struct TimeStep {
     return fused_ok;
   }
 
+  bool half_ready() {
+    if (h16_built) return h16_ok;
+    h16_built = true;
+    std::vector<int32_t> off, col, src;
+    h16_ok = build_full_sell(topo, off, col, src);
+    if (!h16_ok) return false;
+    nfs = (long long)col.size();
+    h16off.upload(off, stream);
+    h16col.upload(col, stream);
+    h16src.upload(src, stream);
+    SSIM_CUDA(cudaStreamSynchronize(stream));  // the host lists go out of scope
+    return true;
+  }
+  HalfMatrix half_matrix() const {
+    return HalfMatrix{nv, h16off.p, h16col.p, h16v8.p, h16v1.p, h16scale.p, h16iscale.p};
+  }
+  // the FP16 copy of the current FP32 system values (remade only after a new assembly)
+  void half_refresh() {
+    h16v8.alloc((size_t)nfs);
+    h16v1.alloc((size_t)nfs);
+    h16scale.alloc(nv);
+    h16iscale.alloc(nv);
+    h16dinv.alloc(3 * (size_t)nv);
+    if (h16_count == asm_count) return;
+    launch_half_prepare(A(), sf.vals.p, params.precond, h16scale.p, h16iscale.p, h16dinv.p, stream);
+    launch_half_convert(A(), h16off.p, h16col.p, h16src.p, sf.vals.p, h16scale.p, h16v8.p, h16v1.p, stream);
+    h16_count = asm_count;
+  }
+  // the FP16 copy serves a solve when it is enabled, the tolerance is loose enough for its rounding, the
+  // solve would run the persistent Chronopoulos-Gear kernel, and the pattern fits
+  bool use_half(double rtol) {
+    if (!mixed() || params.pcg_half_matrix != 1 || !(rtol >= params.half_matrix_min_rtol)) return false;
+    const int variant = params.pcg_persistent == 3 ? 2 : params.pcg_persistent;
+    return variant == 2 && half_ready();
+  }
+
   // material: per element Lame parameters (basic_elast.hpp:10-20) and the stable Neo-Hookean constants
   void upload_material() {
     std::vector<double> l(nt), m(nt);
@@ -592,6 +637,9 @@ struct TimeStep {
       sd.slot_mass.upload(smass, stream);
       alloc_solver(sd);
       sf.release();
+      h16v8.release();
+      h16v1.release();
+      h16_count = -1;
     }
     launch_build_mask(nv, dof_type.p, mask.p, stream);
     if (stepper == SSIM_GB_STEPPER_PD) {
@@ -786,6 +834,7 @@ struct TimeStep {
   template <typename S>
   void hessian(bool spsd, bool filter) {
     Solver<S>& s = solver<S>();
+    ++asm_count;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
     if (!springs && !tri2d && params.fused_assembly && fused_ready()) {
@@ -825,8 +874,41 @@ struct TimeStep {
   template <typename S>
   int pcg(const double* b, bool negate, double eta, int max_iters, double* rel_res) {
     Solver<S>& s = solver<S>();
+    if constexpr (std::is_same<S, float>::value) {
+      int it = 0;
+      if (use_half(eta) && pcg_half(b, negate, eta, max_iters, rel_res, &it)) return it;
+    }
     launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
     return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true);
+  }
+
+  // PCG on the FP16 copy of the scaled system matrix (Chronopoulos-Gear, one cooperative launch); false if
+  // the device cannot launch it cooperatively (the caller then runs the FP32 matrix)
+  bool pcg_half(const double* b, bool negate, double eta, int max_iters, double* rel_res, int* iters) {
+    Solver<float>& s = sf;
+    half_refresh();
+    const HalfMatrix H = half_matrix();
+    launch_pcg_setup_half(H, b, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
+    if (profiling) SSIM_CUDA(cudaEventRecord(ev[0], stream));
+    const bool ran = launch_pcg_half(H, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters, red(),
+                                     gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra, params.pcg_max_blocks,
+                                     stream);
+    if (!ran) return false;
+    if (profiling) SSIM_CUDA(cudaEventRecord(ev[1], stream));
+    sync_scalars();
+    if (hsc->wait_failed) throw device_timeout("a grid-barrier wait of the persistent PCG kernel gave up");
+    if (profiling) {
+      float ms = 0;
+      SSIM_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      prof_ms[PK_PCG] += ms;
+      prof_launch[PK_PCG] += hsc->iters;
+      prof_bytes[PK_PCG] = half_spmv_bytes() + update_bytes(sizeof(float));
+    }
+    if (rel_res) *rel_res = hsc->rr0 > 0 ? std::sqrt(hsc->rr / hsc->rr0) : 0.0;
+    if (hsc->status == 2) throw numerical_error("PCG produced a non-finite residual");
+    if (solve_log.size() < (1u << 20)) solve_log.push_back(hsc->iters);
+    *iters = hsc->iters;
+    return true;
   }
 
   // PCG on another matrix of the same block pattern (the PD matrix) with an S right-hand side
@@ -1147,6 +1229,9 @@ struct TimeStep {
     return up * (9.0 * s + 4.0) + lo * 8.0 + 2.0 * (topo.nslices + 1) * 4 + 4.0 * nv * 4 * s;
   }
 
+  // bytes one SpMV on the FP16 copy moves: 18 B of values and a 4-byte column per entry, the gathered vector
+  // and the product once, the inverse scale for the unscaled residual norm
+  double half_spmv_bytes() const { return 22.0 * (double)nfs + 3.0 * nv * 16.0; }
   // bytes one PCG update pass moves: p, q, x, r read, x, r, z written, the 3x3 preconditioner blocks
   double update_bytes(size_t s) const { return 7.0 * nv * 4 * s + 3.0 * nv * 4 * s; }
 
@@ -1513,6 +1598,7 @@ struct TimeStep {
     params.pcg_persistent = t.pcg_persistent;
     params.pcg_max_blocks = t.pcg_max_blocks;
     params.fused_assembly = t.fused_assembly;
+    params.pcg_half_matrix = t.pcg_half_matrix;
   }
   ssim_gb_tuning autotune() {
     if (!has_reset) throw state_error("autotune() before reset()");
@@ -1612,6 +1698,7 @@ struct TimeStep {
       ++count;
       if (ms < abest) abest = ms, t.assembly_block = b;
     }
+    ++asm_count;  // the timed assemblies rewrote the system values
     t.hessian_us = (hbest + abest) * 1e3;
     t.fused_assembly = 0;
     if (tets && fused_ready()) {
@@ -1633,22 +1720,33 @@ struct TimeStep {
     std::vector<int> grids = {0};
     if (4 * nsm < div_up(nv, 256)) grids.push_back(4 * nsm);
     const int keep_variant = params.pcg_persistent, keep_grid = params.pcg_max_blocks;
+    const int keep_half = params.pcg_half_matrix;
     const size_t log0 = solve_log.size();
     double pbest = 1e300;
     t.pcg_persistent = keep_variant;
     t.pcg_max_blocks = keep_grid;
+    t.pcg_half_matrix = keep_half;
     for (int v : variants)
-      for (int gcap : grids) {
-        if (v == 0 && gcap != 0) continue;  // the two-launch loop has no persistent grid
-        params.pcg_persistent = v;
-        params.pcg_max_blocks = gcap;
-        int iters = 0;
-        const double ms = time_launches([&] { iters = pcg<S>(rhs.p, false, 5e-2, params.cg_max_iters, nullptr); }, 2);
-        ++count;
-        if (ms < pbest) pbest = ms, t.pcg_persistent = v, t.pcg_max_blocks = gcap, t.pcg_iterations = iters;
-      }
+      for (int gcap : grids)
+        for (int half : {0, 1}) {
+          if (v == 0 && gcap != 0) continue;  // the two-launch loop has no persistent grid
+          if (half && (v != 2 || !mixed() || !half_ready())) continue;  // the FP16 copy serves only these
+          params.pcg_persistent = v;
+          params.pcg_max_blocks = gcap;
+          params.pcg_half_matrix = half;
+          int iters = 0;
+          // the FP16 candidate pays its conversion in every timed solve, as each Newton solve follows an assembly
+          const double ms = time_launches([&] {
+            h16_count = -1;
+            iters = pcg<S>(rhs.p, false, 5e-2, params.cg_max_iters, nullptr);
+          }, 2);
+          ++count;
+          if (ms < pbest)
+            pbest = ms, t.pcg_persistent = v, t.pcg_max_blocks = gcap, t.pcg_iterations = iters, t.pcg_half_matrix = half;
+        }
     params.pcg_persistent = keep_variant;
     params.pcg_max_blocks = keep_grid;
+    params.pcg_half_matrix = keep_half;
     solve_log.resize(log0);
     t.pcg_solve_ms = pbest;
     t.candidates = count;

@@ -177,6 +177,39 @@ int upper_slot(const Topology& t, int u, int w) {
   return t.sl_off[u >> 5] + 32 * (find_pos(t, u, w) - lo) + (u & 31);
 }
 
+bool build_full_sell(const Topology& t, std::vector<int32_t>& off, std::vector<int32_t>& col,
+                     std::vector<int32_t>& src) {
+  off.assign(t.nslices + 1, 0);
+  long long total = 0;
+  for (int s = 0; s < t.nslices; ++s) {
+    int w = 0;
+    for (int u = 32 * s; u < std::min(t.nv, 32 * s + 32); ++u) w = std::max(w, t.bptr[u + 1] - t.bptr[u]);
+    total += 32LL * w;
+    if (total >= (1LL << 31)) return false;
+    off[s + 1] = (int32_t)total;
+  }
+  col.assign(total, 0);
+  src.assign(total, t.zero_slot);
+  for (int s = 0; s < t.nslices; ++s) {
+    const int W = (off[s + 1] - off[s]) / 32;
+    for (int lane = 0; lane < 32; ++lane) {
+      const int u = 32 * s + lane;
+      const int deg = u < t.nv ? t.bptr[u + 1] - t.bptr[u] : 0;
+      for (int k = 0; k < W; ++k) {
+        const int e = off[s] + 32 * k + lane;
+        if (k < deg) {
+          const int w = t.bcol[t.bptr[u] + k];
+          col[e] = w;
+          src[e] = w >= u ? upper_slot(t, u, w) : (int32_t)(0x80000000u | (uint32_t)upper_slot(t, w, u));
+        } else {
+          col[e] = u < t.nv ? u : 0;
+        }
+      }
+    }
+  }
+  return true;
+}
+
 void csr_pattern(const Topology& t, int32_t* row_ptr, int32_t* col_idx) {
   row_ptr[0] = 0;
   for (int u = 0; u < t.nv; ++u) {

@@ -61,6 +61,15 @@ void build_fused_lists(const Topology& t, const int32_t* cells, int slices_per_c
 // [nt][cv] with cv = 4 (tets), 3 (triangles) or 2 (springs)
 void build_topology(int nv, int nt, const int32_t* cells, Topology& t, int cv = 4);
 
+// Both triangles of the block pattern in SELL-32 (the FP16 copy of the system matrix that the mixed Newton's
+// loose PCG solves read): slice s = block rows 32s..32s+31, width = the slice's largest degree; entry
+// off[s] + 32k + lane holds row u = 32s + lane's k-th neighbour w (ascending) in col and, in src, the upper slot
+// holding block (min(u, w), max(u, w)) with bit 31 set when the entry is that slot's transpose (w < u).
+// Padding entries: column u (0 past the last row) and the all-zero slot.  false if the entries do not fit
+// 31-bit indices.
+bool build_full_sell(const Topology& t, std::vector<int32_t>& off, std::vector<int32_t>& col,
+                     std::vector<int32_t>& src);
+
 // the upper-triangular block id of the local vertex pair (v <= w) used by the element Hessian kernel
 inline int upper_block_id(int v, int w) { return v * 4 - (v * (v - 1)) / 2 + (w - v); }
 

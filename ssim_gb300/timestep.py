@@ -401,6 +401,16 @@ class TimeStep:
         self._c(self._L.ssim_gb_autotune(self._h, C.byref(t)))
         return t.as_dict()
 
+    def set_tuning(self, tuning: dict):
+        """Applies a tuning found earlier (ssim_gb_set_tuning): the shape and PCG keys of an autotune() result;
+        missing keys are 0 (the compiled defaults, the two-launch or standard PCG, unfused assembly, the FP32
+        matrix in every solve)."""
+        t = _lib.Tuning()
+        for k in ("elem_block", "hessian_block", "assembly_block", "gather_block", "pcg_persistent",
+                  "pcg_max_blocks", "fused_assembly", "pcg_half_matrix"):
+            setattr(t, k, int(tuning.get(k, 0)))
+        self._c(self._L.ssim_gb_set_tuning(self._h, C.byref(t)))
+
     def profile(self, enable: bool = True):
         self._c(self._L.ssim_gb_profile_enable(self._h, int(enable)))
 

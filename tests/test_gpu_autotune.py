@@ -4,7 +4,8 @@ block sizes, PCG variant / grid and assembly path, cached per process by problem
 Checked: the choices come from the candidate sets and the sweep timed them; a second handle of the same
 shape takes the cached choice without timing; the forces view and the deformation are left as they were;
 and a tuned handle steps to the same states as an untuned one up to the solver tolerance (tuning changes
-launch shapes and the PCG variant, not the equations), in both precisions and for a batch of instances.
+launch shapes and the PCG variant, not the equations), in both precisions and for a batch of instances;
+and a saved tuning applied with ssim_gb_set_tuning, with out-of-set values rejected.
 """
 import numpy as np
 import pytest
@@ -38,16 +39,19 @@ def test_autotune_choices_cache_and_states(precision):
         assert t["pcg_persistent"] in (0, 2)
     assert t["hessian_block"] in (32, 64, 128) and t["assembly_block"] in (128, 256, 512)
     assert t["fused_assembly"] in (0, 1) and t["pcg_solve_ms"] > 0 and t["pcg_iterations"] > 0
+    if precision == "mixed":
+        assert t["pcg_half_matrix"] in (0, 1) and (t["pcg_half_matrix"] == 0 or t["pcg_persistent"] == 2)
     assert np.array_equal(ts.get("deformation"), u) and np.array_equal(ts.get("forces"), f)
     p = ts.params
     assert (p.pcg_persistent, p.pcg_max_blocks, p.fused_assembly) == (t["pcg_persistent"], t["pcg_max_blocks"],
                                                                       t["fused_assembly"])
+    assert p.pcg_half_matrix == t["pcg_half_matrix"]
     # a second handle of the same shape: the cached choice
     ts2 = scenes.build_timestep(scene, precision=precision, params=_params())
     t2 = ts2.autotune()
     assert t2["from_cache"] == 1
     for k in ("elem_block", "hessian_block", "assembly_block", "gather_block", "pcg_persistent", "pcg_max_blocks",
-              "fused_assembly"):
+              "fused_assembly", "pcg_half_matrix"):
         assert t2[k] == t[k]
     # tuned and untuned handles step to the same states up to the tolerance
     ref = scenes.build_timestep(scene, precision=precision, params=_params())
@@ -70,3 +74,27 @@ def test_autotune_batch():
     gi, gi0 = ts.instance_residuals()
     assert np.all(gi <= 1e-8 * gi0)
     assert rel(ts.get("deformation"), ref.get("deformation")) <= 1e-6
+
+
+def test_set_tuning_applies_a_saved_choice():
+    """ssim_gb_set_tuning: a tuning from an earlier sweep applied to a fresh handle without timing
+    anything; values outside the candidate sets are rejected and leave the handle as it was."""
+    scene = scenes.bar(24, 8, 8)
+    ts = scenes.build_timestep(scene, precision="mixed", params=_params())
+    saved = {"elem_block": 256, "hessian_block": 32, "assembly_block": 512, "gather_block": 128,
+             "pcg_persistent": 2, "pcg_max_blocks": 0, "fused_assembly": 0, "pcg_half_matrix": 1}
+    ts.set_tuning(saved)
+    p = ts.params
+    assert (p.pcg_persistent, p.pcg_max_blocks, p.fused_assembly, p.pcg_half_matrix) == (2, 0, 0, 1)
+    ref = scenes.build_timestep(scene, precision="mixed", params=_params())
+    for _ in range(2):
+        ts.step()
+        ref.step()
+        assert ts.stats()["converged"] == 1
+    assert rel(ts.get("deformation"), ref.get("deformation")) <= 1e-6
+    for bad in ({"elem_block": 96}, {"hessian_block": 256}, {"assembly_block": 64}, {"gather_block": 1024},
+                {"pcg_persistent": 5}, {"pcg_max_blocks": -1}, {"fused_assembly": 2}, {"pcg_half_matrix": 2}):
+        with pytest.raises(ValueError, match="invalid tuning"):
+            ts.set_tuning(dict(saved, **bad))
+    p = ts.params
+    assert (p.pcg_persistent, p.pcg_max_blocks, p.fused_assembly, p.pcg_half_matrix) == (2, 0, 0, 1)

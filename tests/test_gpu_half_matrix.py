@@ -1,0 +1,107 @@
+"""The FP16 copy of the Jacobi-scaled system matrix (pcg_half_matrix = 1): the mixed Newton's loose PCG
+solves run on K~ = S K S (S = diag(K)^-1/2) stored in FP16, both triangles, full block SELL-32.
+
+Checked, against the FP64 oracle's matrix and the FP32 symmetric values on the same state:
+* the copy applied in the unscaled space (ssim_gb_spmv, SSIM_GB_SYSMATRIX_HALF) equals K x within the FP16
+  rounding of the scaled values: 2e-3 of max|K x| (a scaled value carries 2^-11 relative rounding; a row
+  sums about 15 blocks of mixed sign);
+* a PCG solve to 5e-2 on the copy leaves a TRUE residual |b - K x| / |b| within the requested tolerance
+  plus the copy's rounding (5e-2 + 5e-3) and takes the FP32 path's iteration count within 10% + 2; a solve
+  tighter than half_matrix_min_rtol runs on the FP32 values (bitwise the FP32 path's result);
+* Newton steps with the copy converge like the FP32 matrix's (the same stopping test on FP64 residuals):
+  states within 1e-5, Newton iterations per step within 1, total PCG iterations within 15%.
+"""
+import numpy as np
+import pytest
+
+import ssim_gb300 as g
+from ssim_gb300 import mesh, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _pair(half):
+    from oracle import pyoracle
+
+    X, T = mesh.kuhn_box((12, 6, 5), (1.2, 0.6, 0.5))
+    X = mesh.jitter_interior(X, 0.01, 11)
+    E = 10.0 ** mesh.uniform(12, T.shape[0], 4.0, 6.0)
+    fixed = np.where(X[:, 0] == 0.0)[0]
+    ts = g.TimeStep(X, T, 1e-2, 1e5, 0.45, 1000.0)
+    ts.set_material(E, None)
+    ts.mark_dirichlet_batched(fixed, np.zeros((fixed.size, 3)))
+    ts.set_precision("mixed")
+    ts.set_params(g.default_params(precond=2, pcg_half_matrix=half, cg_max_iters=20000))
+    ts.reset("newton")
+    ot = pyoracle.OracleTimeStep(X, T, 1e-2, 1e5, 0.45, 1000.0)
+    ot.set_material(E, None)
+    ot.mark_dirichlet(fixed)
+    ot.reset()
+    u = np.random.default_rng(13).uniform(-1, 1, X.shape) * 0.02
+    for t in (ts, ot):
+        t.set("next_deform", u)
+        t.update_hessian(False, True, True)
+    return ts, ot, X
+
+
+def test_half_spmv_matches_matrix():
+    ts, ot, X = _pair(1)
+    for seed in (14, 15):
+        x = np.random.default_rng(seed).normal(size=X.shape)
+        y64 = ot.spmv(x).reshape(-1, 3)
+        y32 = ts.spmv(x)
+        yh = ts.spmv(x, "sysmatrix_half")
+        assert rel(y32, y64) <= 1e-5
+        assert rel(yh, y64) <= 2e-3, rel(yh, y64)
+        assert rel(yh, y32) <= 2e-3
+    # FP64 handles have no FP16 copy
+    ts64 = g.TimeStep(*mesh.kuhn_box((3, 2, 2), (0.3, 0.2, 0.2)), 1e-2, 1e5, 0.45, 1000.0)
+    ts64.reset("newton")
+    with pytest.raises(ValueError, match="mixed precision only"):
+        ts64.spmv(np.zeros((ts64.num_vertices, 3)), "sysmatrix_half")
+
+
+def test_half_pcg_true_residual_and_iterations():
+    ts_h, ot, X = _pair(1)
+    ts_f, _, _ = _pair(0)
+    b = np.random.default_rng(16).normal(size=X.shape)
+    nb = np.linalg.norm(b)
+    xh, ith, rrh = ts_h.pcg(b, rtol=5e-2)
+    xf, itf, rrf = ts_f.pcg(b, rtol=5e-2)
+    true_h = np.linalg.norm(b.reshape(-1) - ot.spmv(xh)) / nb
+    true_f = np.linalg.norm(b.reshape(-1) - ot.spmv(xf)) / nb
+    assert rrh <= 5e-2 and rrf <= 5e-2
+    assert true_f <= 5e-2 + 1e-4, true_f
+    assert true_h <= 5e-2 + 5e-3, (true_h, rrh)
+    assert abs(ith - itf) <= 0.1 * itf + 2, (ith, itf)
+    # tighter than half_matrix_min_rtol: the FP32 values, bitwise the FP32 handle's solve
+    xh2, ith2, _ = ts_h.pcg(b, rtol=1e-6)
+    xf2, itf2, _ = ts_f.pcg(b, rtol=1e-6)
+    assert ith2 == itf2 and np.array_equal(xh2, xf2)
+
+
+@pytest.mark.parametrize("name", ["beam_small", "bar_small", "cube10"])
+def test_newton_with_half_matrix(name):
+    scene = {"beam_small": lambda: scenes.beam(40, 20, 14, h=0.05), "bar_small": lambda: scenes.bar(20, 6, 6),
+             "cube10": scenes.cube10}[name]()
+    runs = {}
+    for half in (1, 0):
+        params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2,
+                                  precond=2, pcg_half_matrix=half)
+        ts = scenes.build_timestep(scene, precision="mixed", params=params)
+        newton, cg = [], 0
+        for _ in range(4):
+            ts.step()
+            st = ts.stats()
+            assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"], (half, st)
+            newton.append(st["newton_iters"])
+            cg += st["cg_iters_total"]
+        runs[half] = (ts.get("deformation"), newton, cg)
+    (uh, nh, ch), (uf, nf, cf) = runs[1], runs[0]
+    assert rel(uh, uf) <= 1e-5
+    assert all(abs(a - b) <= 1 for a, b in zip(nh, nf)), (nh, nf)
+    assert abs(ch - cf) <= 0.15 * cf, (ch, cf)

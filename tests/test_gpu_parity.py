@@ -190,14 +190,16 @@ def test_newton_trajectory_fp64_tight():
 def test_reference_box_scene(precision):
     """The reference's unit_box(11, 11, 11) (5 tets per hex, 5,000 tets) with its harness conventions
     (tests/fem_time_step/main.cpp:54-67: x = 0 face fixed, gravity on y, E 1e6, nu 0.4, rho 10): 5 Newton
-    steps to 1e-9 (FP64, matching the oracle's trajectory to 1e-10) or 1e-6 (mixed, within 1e-5 of it)."""
+    steps to 1e-9 (FP64, matching the oracle's trajectory to 1e-10) or 1e-7 (mixed, within 1e-5 of it; on
+    this stiff, light scene a 1e-6 residual leaves state errors up to about 2e-5, wherever in that band the
+    iterates of a given PCG matrix happen to stop)."""
     from oracle import pyoracle
 
     scene = scenes.reference_box()
     if precision == "fp64":
         params = g.default_params(stop_mode=1, rel_tol=1e-9, cg_rtol=1e-12, cg_max_iters=20000)
     else:
-        params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-2, cg_eta_min=1e-4)
+        params = g.default_params(stop_mode=1, rel_tol=1e-7, cg_forcing=1, cg_rtol=1e-2, cg_eta_min=1e-4)
     op = pyoracle.default_params(stop_mode=1, rel_tol=1e-9 if precision == "fp64" else 1e-10, cg_rtol=1e-12,
                                  cg_max_iters=20000)
     ts, ot, hist = _run(scene, precision, params, op, 5)
