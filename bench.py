@@ -602,7 +602,7 @@ def main():
             "clocks": r["clocks"],
             "tuning": {k: {f: v.get(f, 0) for f in ("elem_block", "hessian_block", "assembly_block", "gather_block",
                                                     "pcg_persistent", "pcg_max_blocks", "fused_assembly",
-                                                    "pcg_half_matrix", "candidates", "pinned")}
+                                                    "pcg_half_matrix", "elem_regcap", "candidates", "pinned")}
                        for k, v in r.get("tuning", {}).items()} or None,
             "adjoint_ms_per_step": r["adjoint"][0]["adjoint_ms_per_step"] if r.get("adjoint") else None,
             "adjoint": r.get("adjoint"),

@@ -184,6 +184,8 @@ typedef struct {
   int32_t candidates;     /* configurations timed */
   int32_t pcg_half_matrix; /* ssim_gb_params.pcg_half_matrix chosen (mixed: the persistent Chronopoulos-Gear
                               solve timed on the FP16 copy, its conversion included, and on the FP32 values) */
+  int32_t elem_regcap;    /* 1: the FP32 element pass's variant capped at 64 registers a thread (more resident
+                             warps for its dependent gathers) */
 } ssim_gb_tuning;
 
 typedef struct ssim_gb_timestep ssim_gb_timestep;
@@ -371,8 +373,8 @@ SSIM_GB_API ssim_gb_status ssim_gb_energy_noalloc(const double* X, const double*
 SSIM_GB_API ssim_gb_status ssim_gb_autotune(ssim_gb_timestep* h, ssim_gb_tuning* out);
 /* Applies a tuning found earlier (by ssim_gb_autotune in this or another process) without timing anything:
  * elem_block in {0, 64, 128, 256}, hessian_block in {0, 32, 64, 128}, assembly_block and gather_block in
- * {0, 128, 256, 512} (0: the compiled default), pcg_persistent 0..4, pcg_max_blocks >= 0, fused_assembly and
- * pcg_half_matrix 0 or 1; the timing and cache fields are ignored.  Anything else: SSIM_GB_ERR_INVALID_ARGUMENT, nothing
+ * {0, 128, 256, 512} (0: the compiled default), pcg_persistent 0..4, pcg_max_blocks >= 0, fused_assembly,
+ * pcg_half_matrix and elem_regcap 0 or 1; the timing and cache fields are ignored.  Anything else: SSIM_GB_ERR_INVALID_ARGUMENT, nothing
  * applied. */
 SSIM_GB_API ssim_gb_status ssim_gb_set_tuning(ssim_gb_timestep* h, const ssim_gb_tuning* t);
 

@@ -111,6 +111,7 @@ class Tuning(C.Structure):
         ("pcg_iterations", C.c_int32),
         ("candidates", C.c_int32),
         ("pcg_half_matrix", C.c_int32),
+        ("elem_regcap", C.c_int32),
     ]
 
     def as_dict(self):

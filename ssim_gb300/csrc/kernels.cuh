@@ -164,7 +164,7 @@ void launch_elem_energy_grad(const ElemFP64& el, const double* X, const double* 
 void launch_split32(int nv, const double* u, const double* xt, float4* uh, float4* ul, float4* w, cudaStream_t st);
 void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
                                double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
-                               const Reduce& red, cudaStream_t st, int block = 0);
+                               const Reduce& red, cudaStream_t st, int block = 0, int regcap = 0);
 // increment evaluation from a reference u_r (the mixed Newton's iterations after the FP32 phase): ref = the
 // FP32 split of u_r and w = u_r - x~, db = u_b - u_r; energy e_ref + increment into the (trial) energy,
 // escale_ref as its round-off scale; local force increments into lf32 (see kernels_elem.cu)

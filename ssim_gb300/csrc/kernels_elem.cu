@@ -147,8 +147,8 @@ __global__ void __launch_bounds__(256)
   if (w != nullptr) w[v] = make_float4(o[0], o[1], o[2], 0.f);
 }
 
-template <bool FORCES, bool TRIAL, int EB>
-__global__ void __launch_bounds__(EB)
+template <bool FORCES, bool TRIAL, int EB, int MINB = 1>
+__global__ void __launch_bounds__(EB, MINB)
     elem_energy_grad32_kernel(ElemFP64 el, ElemFP32 ef, Split32 sp, const float4* __restrict__ d, float alpha,
                               float dt2, float rho, float* __restrict__ lf32, Reduce red) {
   __shared__ float stage[FORCES ? EB * 12 : 1];
@@ -545,20 +545,29 @@ void launch_split32(int nv, const double* u, const double* xt, float4* uh, float
 
 void launch_elem_energy_grad32(const ElemFP64& el, const ElemFP32& ef, const Split32& sp, const float4* d,
                                double alpha, double dt2, double rho, float* lf32, bool with_forces, bool trial,
-                               const Reduce& red, cudaStream_t st, int block) {
+                               const Reduce& red, cudaStream_t st, int block, int regcap) {
   if (el.nt <= 0) return;
   const float f_dt2 = (float)dt2, f_rho = (float)rho, a = (float)alpha;
-  auto go = [&](auto B) {
-    constexpr int b = decltype(B)::value;
+  // regcap: the variant compiled for 1024 / b resident blocks per SM (at most 64 registers a thread: more warps
+  // in flight for the dependent vertex gathers, a few bytes of spill)
+  auto launch = [&](auto B, auto M) {
+    constexpr int b = decltype(B)::value, m = decltype(M)::value;
     const int grid = div_up(el.nt, b);
     if (trial && with_forces)
-      elem_energy_grad32_kernel<true, true, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+      elem_energy_grad32_kernel<true, true, b, m><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
     else if (trial)
-      elem_energy_grad32_kernel<false, true, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+      elem_energy_grad32_kernel<false, true, b, m><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
     else if (with_forces)
-      elem_energy_grad32_kernel<true, false, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+      elem_energy_grad32_kernel<true, false, b, m><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
     else
-      elem_energy_grad32_kernel<false, false, b><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+      elem_energy_grad32_kernel<false, false, b, m><<<grid, b, 0, st>>>(el, ef, sp, d, a, f_dt2, f_rho, lf32, red);
+  };
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    if (regcap)
+      launch(B, std::integral_constant<int, 1024 / b>{});
+    else
+      launch(B, std::integral_constant<int, 1>{});
   };
   dispatch_block<64, 128, 256>(block == 0 ? EB : block, go);
   after_launch("elem_energy_grad32");

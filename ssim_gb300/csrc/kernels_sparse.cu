@@ -492,92 +492,43 @@ __device__ __forceinline__ bool plain_barrier(const GridSync& gs, unsigned long 
 }
 
 // Reducing barrier number kr: every block has written the partials of its virtual blocks (NV doubles each,
-// part[NV * vb]); warp 0 of each block marks them arrived in their groups of 32 virtual blocks, and the block
-// completing a group marks the group arrived at the top counter.  The block completing the last group sums
-// everything in the order of grid_sum_last_tree (each group of 32 by warp_group_sum's shuffle tree, then the
-// group sums by warp_top_sum's), runs epi(tot) in its thread 0 and releases everyone.  Only that block reads
-// partials, with all its warps at once (up to kTopPass groups per warp in flight), so the critical path holds
-// two atomics, one round of L2 reads and the release; grids of more than kTopGroups groups keep the group sums
-// in gsum (global) instead of shared memory.  Returns false in every thread of a block whose wait gave up.
-constexpr int kTopGroups = 64, kTopPass = 3;
-
-template <int NV>
-__device__ __forceinline__ void shfl_tree(double (&v)[NV]) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-  }
-}
-
+// part[NV * vb]); warp 0 of each block marks them arrived in their groups of 32; the block completing a
+// group sums it (warp_group_sum) into gsum[g], and the block completing the last group sums the group
+// sums (warp_top_sum, the order of grid_sum_last_tree), runs epi(tot) in its lane 0 and releases everyone.
+// Returns false in every thread of a block whose wait gave up.
 template <int NV, typename EPI>
 __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long long kr, const double* part,
                                                double* gsum, int nvb, EPI&& epi) {
-  __shared__ int ok, s_top;
-  __shared__ double s_gsum[kTopGroups][NV];
+  __shared__ int ok;
   __syncthreads();
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
-    int top_any = 0;
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       const int g = vb >> 5, gsize = min(32, nvb - 32 * g);
-      int top = 0;
+      int last = 0;
       if (lane == 0) {
         fence_acq_rel_gpu();
-        if (atomicAdd(gs.group + (size_t)g * kSyncStride, 1ull) == (kr + 1) * (unsigned long long)gsize - 1) {
-          fence_acq_rel_gpu();
-          top = atomicAdd(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
-          if (top) fence_acq_rel_gpu();
-        }
+        last = atomicAdd(gs.group + (size_t)g * kSyncStride, 1ull) == (kr + 1) * (unsigned long long)gsize - 1;
+        if (last) fence_acq_rel_gpu();
       }
-      top_any |= top;
-    }
-    if (lane == 0) s_top = top_any;
-  }
-  __syncthreads();
-  if (s_top) {  // this block completed the last group: every partial has been released to it
-    const int ng = gs.ngroups, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const bool shared_sums = ng <= kTopGroups;
-    for (int g0 = warp; g0 < ng; g0 += kTopPass * nwarps) {
-      double v[kTopPass][NV];
+      last = __shfl_sync(0xffffffffu, last, 0);
+      __syncwarp();
+      if (!last) continue;
+      double v[NV];
+      warp_group_sum<NV>(part, 32 * g, gsize, v);
+      int top = 0;
+      if (lane == 0) {
 #pragma unroll
-      for (int j = 0; j < kTopPass; ++j) {
-        const int vb = 32 * (g0 + j * nwarps) + lane;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) v[j][k] = vb < nvb ? __ldcg(part + (size_t)vb * NV + k) : 0.0;
+        for (int k = 0; k < NV; ++k) gsum[g * NV + k] = v[k];
+        fence_acq_rel_gpu();
+        top = atomicAdd(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
+        if (top) fence_acq_rel_gpu();
       }
-#pragma unroll
-      for (int j = 0; j < kTopPass; ++j) {
-        const int g = g0 + j * nwarps;
-        shfl_tree<NV>(v[j]);
-        if (lane == 0 && g < ng) {
-#pragma unroll
-          for (int k = 0; k < NV; ++k) {
-            if (shared_sums)
-              s_gsum[g][k] = v[j][k];
-            else
-              gsum[(size_t)g * NV + k] = v[j][k];
-          }
-        }
-      }
-    }
-    __syncthreads();
-    if (warp == 0) {
+      top = __shfl_sync(0xffffffffu, top, 0);
+      __syncwarp();
+      if (!top) continue;
       double tot[NV];
-      if (shared_sums) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) tot[k] = 0.0;
-        for (int c0 = 0; c0 < ng; c0 += 32) {
-          double v[NV];
-#pragma unroll
-          for (int k = 0; k < NV; ++k) v[k] = c0 + lane < ng ? s_gsum[c0 + lane][k] : 0.0;
-          shfl_tree<NV>(v);
-#pragma unroll
-          for (int k = 0; k < NV; ++k) tot[k] += v[k];
-        }
-      } else {
-        warp_top_sum<NV>(gsum, ng, tot);
-      }
+      warp_top_sum<NV>(gsum, gs.ngroups, tot);
       if (lane == 0) {
         epi(tot);
         fence_acq_rel_gpu();

@@ -781,7 +781,8 @@ ssim_gb_status ssim_gb_set_tuning(ssim_gb_timestep* h, const ssim_gb_tuning* t) 
   if (!one_of(t->elem_block, {0, 64, 128, 256}) || !one_of(t->hessian_block, {0, 32, 64, 128}) ||
       !one_of(t->assembly_block, {0, 128, 256, 512}) || !one_of(t->gather_block, {0, 128, 256, 512}) ||
       t->pcg_persistent < 0 || t->pcg_persistent > 4 || t->pcg_max_blocks < 0 ||
-      (t->fused_assembly != 0 && t->fused_assembly != 1) || (t->pcg_half_matrix != 0 && t->pcg_half_matrix != 1))
+      (t->fused_assembly != 0 && t->fused_assembly != 1) || (t->pcg_half_matrix != 0 && t->pcg_half_matrix != 1) ||
+      (t->elem_regcap != 0 && t->elem_regcap != 1))
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid tuning (block size outside its candidate set)");
   h->ts.apply_tuning(*t);
   return SSIM_GB_OK;

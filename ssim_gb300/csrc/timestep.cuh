@@ -187,6 +187,7 @@ struct TimeStep {
   // kernels' defaults)
   struct Shapes {
     int elem = 0, hess = 0, assem = 0, gather = 0;
+    int elem_regcap = 0;  // the FP32 element pass's 64-register variant
   } shapes;
   // the reference of the increment evaluations (mixed Newton after the FP32 phase): u_r, its FP64 forces and
   // energy, and the base point offset u_b - u_r; the FP32 split of u_r lives in uh32 / ul32 / w32
@@ -245,7 +246,7 @@ struct TimeStep {
                                    forces ? lf32t.p : nullptr, forces, true, red(), stream);
         else
           launch_elem_energy_grad32(e64(), e32s(), s32(), d, alpha, dt * dt, rho, forces ? lf32t.p : nullptr,
-                                    forces, true, red(), stream, shapes.elem);
+                                    forces, true, red(), stream, shapes.elem, shapes.elem_regcap);
       } else {
         throw state_error("the FP32 element pass takes FP32 directions");
       }
@@ -793,7 +794,7 @@ struct TimeStep {
                                red(), stream);
     else
       launch_elem_energy_grad32(e64(), e32s(), s32(), nullptr, 0.0, dt * dt, rho, lf32t.p, true, false, red(),
-                                stream, shapes.elem);
+                                stream, shapes.elem, shapes.elem_regcap);
     if (profiling) prof_end(e0, e1, PK_GRAD, 0);
     gather_forces<float>(nullptr, 0.0, true);
     sync_scalars();
@@ -1595,6 +1596,7 @@ struct TimeStep {
     shapes.hess = t.hessian_block;
     shapes.assem = t.assembly_block;
     shapes.gather = t.gather_block;
+    shapes.elem_regcap = t.elem_regcap;
     params.pcg_persistent = t.pcg_persistent;
     params.pcg_max_blocks = t.pcg_max_blocks;
     params.fused_assembly = t.fused_assembly;
@@ -1654,14 +1656,15 @@ struct TimeStep {
       if (tets) {
         split32();
         double best = 1e300;
-        for (int b : {64, 128, 256}) {
-          const double ms = time_launches([&] {
-            launch_elem_energy_grad32(e64(), e32s(), s32(), s.x.p, 0.0, dt * dt, rho, lf32t.p, true, true, red(),
-                                      stream, b);
-          });
-          ++count;
-          if (ms < best) best = ms, t.elem_block = b;
-        }
+        for (int b : {64, 128, 256})
+          for (int cap : {0, 1}) {
+            const double ms = time_launches([&] {
+              launch_elem_energy_grad32(e64(), e32s(), s32(), s.x.p, 0.0, dt * dt, rho, lf32t.p, true, true, red(),
+                                        stream, b, cap);
+            });
+            ++count;
+            if (ms < best) best = ms, t.elem_block = b, t.elem_regcap = cap;
+          }
         t.elem_us = best * 1e3;
         best = 1e300;
         for (int b : {128, 256, 512}) {

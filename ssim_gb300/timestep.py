@@ -407,7 +407,7 @@ class TimeStep:
         matrix in every solve)."""
         t = _lib.Tuning()
         for k in ("elem_block", "hessian_block", "assembly_block", "gather_block", "pcg_persistent",
-                  "pcg_max_blocks", "fused_assembly", "pcg_half_matrix"):
+                  "pcg_max_blocks", "fused_assembly", "pcg_half_matrix", "elem_regcap"):
             setattr(t, k, int(tuning.get(k, 0)))
         self._c(self._L.ssim_gb_set_tuning(self._h, C.byref(t)))
 

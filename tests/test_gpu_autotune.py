@@ -34,6 +34,7 @@ def test_autotune_choices_cache_and_states(precision):
     assert t["from_cache"] == 0 and t["candidates"] >= 8
     if precision == "mixed":
         assert t["elem_block"] in (64, 128, 256) and t["gather_block"] in (128, 256, 512)
+        assert t["elem_regcap"] in (0, 1)
         assert t["pcg_persistent"] in (1, 2)
     else:
         assert t["pcg_persistent"] in (0, 2)
@@ -51,7 +52,7 @@ def test_autotune_choices_cache_and_states(precision):
     t2 = ts2.autotune()
     assert t2["from_cache"] == 1
     for k in ("elem_block", "hessian_block", "assembly_block", "gather_block", "pcg_persistent", "pcg_max_blocks",
-              "fused_assembly", "pcg_half_matrix"):
+              "fused_assembly", "pcg_half_matrix", "elem_regcap"):
         assert t2[k] == t[k]
     # tuned and untuned handles step to the same states up to the tolerance
     ref = scenes.build_timestep(scene, precision=precision, params=_params())
@@ -82,7 +83,7 @@ def test_set_tuning_applies_a_saved_choice():
     scene = scenes.bar(24, 8, 8)
     ts = scenes.build_timestep(scene, precision="mixed", params=_params())
     saved = {"elem_block": 256, "hessian_block": 32, "assembly_block": 512, "gather_block": 128,
-             "pcg_persistent": 2, "pcg_max_blocks": 0, "fused_assembly": 0, "pcg_half_matrix": 1}
+             "pcg_persistent": 2, "pcg_max_blocks": 0, "fused_assembly": 0, "pcg_half_matrix": 1, "elem_regcap": 1}
     ts.set_tuning(saved)
     p = ts.params
     assert (p.pcg_persistent, p.pcg_max_blocks, p.fused_assembly, p.pcg_half_matrix) == (2, 0, 0, 1)
@@ -93,8 +94,25 @@ def test_set_tuning_applies_a_saved_choice():
         assert ts.stats()["converged"] == 1
     assert rel(ts.get("deformation"), ref.get("deformation")) <= 1e-6
     for bad in ({"elem_block": 96}, {"hessian_block": 256}, {"assembly_block": 64}, {"gather_block": 1024},
-                {"pcg_persistent": 5}, {"pcg_max_blocks": -1}, {"fused_assembly": 2}, {"pcg_half_matrix": 2}):
+                {"pcg_persistent": 5}, {"pcg_max_blocks": -1}, {"fused_assembly": 2}, {"pcg_half_matrix": 2},
+                {"elem_regcap": 3}):
         with pytest.raises(ValueError, match="invalid tuning"):
             ts.set_tuning(dict(saved, **bad))
     p = ts.params
     assert (p.pcg_persistent, p.pcg_max_blocks, p.fused_assembly, p.pcg_half_matrix) == (2, 0, 0, 1)
+
+
+def test_register_capped_element_pass_is_bitwise_the_same():
+    """elem_regcap changes the element pass's register allocation, not its arithmetic: two handles that
+    differ only in it step to bitwise equal states."""
+    scene = scenes.bar(20, 6, 6)
+    base = {"elem_block": 128, "hessian_block": 64, "assembly_block": 256, "gather_block": 256,
+            "pcg_persistent": 2, "pcg_max_blocks": 0, "fused_assembly": 0, "pcg_half_matrix": 1}
+    states = []
+    for cap in (0, 1):
+        ts = scenes.build_timestep(scene, precision="mixed", params=_params())
+        ts.set_tuning(dict(base, elem_regcap=cap))
+        for _ in range(2):
+            ts.step()
+        states.append(ts.get("deformation"))
+    assert np.array_equal(states[0], states[1])
