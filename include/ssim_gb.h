@@ -152,6 +152,9 @@ typedef struct {
                              mesh; ssim_gb_autotune turns it off where its per-assembly conversion costs more than
                              it saves.  0 keeps every solve on the FP32 values */
   double half_matrix_min_rtol; /* tighter solves (adjoint, tight forcing) stay on the FP32 values (1e-2) */
+  int32_t half_hessian_blocks; /* tets: 1 (default) writes the element Hessian blocks of the assemblies whose solve
+                             runs on the FP16 copy in FP16 (a power-of-two scale per 3x3 block, 24 bytes a block
+                             instead of 36, three 8-byte loads in the assembly, FP32 sums); 0 keeps FP32 blocks */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */

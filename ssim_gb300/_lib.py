@@ -72,6 +72,7 @@ class Params(C.Structure):
         ("mixed_delta", C.c_int32),
         ("pcg_half_matrix", C.c_int32),
         ("half_matrix_min_rtol", C.c_double),
+        ("half_hessian_blocks", C.c_int32),
     ]
 
     def as_dict(self):

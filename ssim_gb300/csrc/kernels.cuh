@@ -241,6 +241,13 @@ int fused_chunk();
 template <typename S>
 void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, const S* Kbuf, const S* slot_mass,
                      const uint8_t* mask, bool filter, S* vals, V4<S>* dinv, int precond, cudaStream_t st, int block = 0);
+// the element Hessian blocks in FP16 (per block a power-of-two scale; 24 bytes a block instead of 36) and the
+// assembly that reads them (FP32 sums): the mixed Newton's assemblies whose solve runs on the FP16 matrix copy
+void launch_elem_hessian16(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
+                           const float4* xf, double dt2, bool spsd, uint2* K16, cudaStream_t st, int block = 0);
+void launch_assemble16(const SellMatrix& A, const int* cptr, const int* csrc, const uint2* K16, const float* slot_mass,
+                       const uint8_t* mask, bool filter, float* vals, float4* dinv, int precond, cudaStream_t st,
+                       int block = 0);
 template <typename S>
 void launch_spmv(const SellMatrix& A, const S* vals, const V4<S>* x, V4<S>* y, cudaStream_t st);
 template <typename S>

@@ -1,6 +1,10 @@
 // kernels_elem.cu -- element-parallel kernels: FP64 energy / gradient (update_energy_and_gradients,
 // time_step.hpp:577-624), the vertex gather of element forces (global_composer.hpp:36-66 +
 // time_step.hpp:608-617) and the element Hessian (wrapped_pfpx, time_step.hpp:23-60, 626-651).
+#include <cfloat>
+
+#include <cuda_fp16.h>
+
 #include "hessian_elem.cuh"
 
 namespace ssim_gb {
@@ -478,7 +482,29 @@ __global__ void __launch_bounds__(GB)
 // time_step.hpp:646-651 folded in), written as the 10 upper 3x3 vertex blocks, staged through shared
 // memory so the global writes are contiguous.  Launch bounds of 8 blocks per SM (128 registers, a few
 // spills) beat the unconstrained 168 registers: 168 against 192 us per launch at 1.02M tets.
-template <typename S, bool XF, int HB>
+// H16 (FP32 arithmetic only): each block written as twelve FP16 words, the nine values scaled by 2^-k and
+// k (the power of two that puts the block's largest magnitude in [2^14, 2^15)) in word 9: 24 bytes a block
+// instead of 36, read back with three 8-byte loads (kernels_sparse.cu assemble_kernel).
+__device__ __forceinline__ void pack_block16(const float* v, uint2* out) {
+  float m = 0.f;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m = fmaxf(m, fabsf(v[i]));
+  int k = 0;
+  if (m > 0.f && m <= FLT_MAX) k = ((__float_as_int(m) >> 23) & 0xff) - 127 - 14;  // floor(log2 m) - 14
+  k = max(-100, min(100, k));
+  const float inv = __int_as_float((127 - k) << 23);  // 2^-k, exact
+  unsigned short h[12];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) h[i] = __half_as_ushort(__float2half_rn(v[i] * inv));
+  h[9] = (unsigned short)(short)k;
+  h[10] = h[11] = 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    out[j] = make_uint2((unsigned int)h[4 * j] | ((unsigned int)h[4 * j + 1] << 16),
+                        (unsigned int)h[4 * j + 2] | ((unsigned int)h[4 * j + 3] << 16));
+}
+
+template <typename S, bool XF, int HB, bool H16 = false>
 __global__ void __launch_bounds__(HB, 512 / HB)
     elem_hessian_kernel(ElemFP64 e64, ElemFP32 e32, const double* __restrict__ X, const double* __restrict__ u,
                         const float4* __restrict__ xf, S dt2, int spsd, S* __restrict__ Kbuf) {
@@ -505,10 +531,32 @@ __global__ void __launch_bounds__(HB, 512 / HB)
         ++blk;
       }
   }
-  __syncthreads();
-  const int nvalid = min(HB, nt - e0);
-  S* dst = Kbuf + (size_t)e0 * 90;
-  for (int i = threadIdx.x; i < nvalid * 90; i += HB) dst[i] = stage[i];
+  if constexpr (H16) {
+    // pack this element's blocks in place of its own staged values, block by block: packed block b (bytes
+    // 24b..24b+23 of the thread's 360) ends before source block b + 1 starts (byte 36b + 36), and block b is
+    // read into registers before it is overwritten
+    if (e < nt) {
+      const float* st = stage + threadIdx.x * 90;
+      uint2* pk = reinterpret_cast<uint2*>(stage) + threadIdx.x * 45;
+#pragma unroll 1
+      for (int b = 0; b < 10; ++b) {
+        float v[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = st[9 * b + i];
+        pack_block16(v, pk + 3 * b);
+      }
+    }
+    __syncthreads();
+    const int nvalid = min(HB, nt - e0);
+    const uint2* src = reinterpret_cast<const uint2*>(stage);
+    uint2* dst = reinterpret_cast<uint2*>(Kbuf) + (size_t)e0 * 30;
+    for (int i = threadIdx.x; i < nvalid * 30; i += HB) dst[i] = src[(i / 30) * 45 + i % 30];
+  } else {
+    __syncthreads();
+    const int nvalid = min(HB, nt - e0);
+    S* dst = Kbuf + (size_t)e0 * 90;
+    for (int i = threadIdx.x; i < nvalid * 90; i += HB) dst[i] = stage[i];
+  }
 }
 
 }  // namespace
@@ -639,6 +687,21 @@ void launch_elem_hessian(const ElemFP64& e64, const ElemFP32& e32, const double*
   };
   dispatch_block<32, 64, 128>(block == 0 ? HB : block, go);
   after_launch("elem_hessian");
+}
+void launch_elem_hessian16(const ElemFP64& e64, const ElemFP32& e32, const double* X, const double* u,
+                           const float4* xf, double dt2, bool spsd, uint2* K16, cudaStream_t st, int block) {
+  if (e64.nt <= 0) return;
+  float* kb = reinterpret_cast<float*>(K16);
+  auto go = [&](auto B) {
+    constexpr int b = decltype(B)::value;
+    const int grid = div_up(e64.nt, b);
+    if (xf != nullptr)
+      elem_hessian_kernel<float, true, b, true><<<grid, b, 0, st>>>(e64, e32, X, u, xf, (float)dt2, spsd ? 1 : 0, kb);
+    else
+      elem_hessian_kernel<float, false, b, true><<<grid, b, 0, st>>>(e64, e32, X, u, xf, (float)dt2, spsd ? 1 : 0, kb);
+  };
+  dispatch_block<32, 64, 128>(block == 0 ? HB : block, go);
+  after_launch("elem_hessian16");
 }template void launch_elem_hessian<float>(const ElemFP64&, const ElemFP32&, const double*, const double*,
                                          const float4*, double, bool, float*, cudaStream_t, int);
 template void launch_elem_hessian<double>(const ElemFP64&, const ElemFP32&, const double*, const double*,

@@ -17,7 +17,22 @@ __device__ __forceinline__ size_t sell_base(int q) { return (size_t)9 * (size_t)
 // symmetric matrix) adds its precomputed list of element blocks (global_composer.hpp:103-119 builds the
 // same map entry by entry) to the consistent-mass block, then applies the Dirichlet identity filter
 // (boundary.hpp:53-67).  One thread per slot, no atomics: deterministic.
-template <typename S, int B>
+// one element block in the FP16 form of launch_elem_hessian16: three 8-byte words, nine FP16 values and the
+// power-of-two exponent k in word 9; value = half * 2^k (exact in FP32)
+__device__ __forceinline__ void load_block16(const uint2* __restrict__ K16, int blk, float (&kv)[9]) {
+  const uint2* p = K16 + 3 * (size_t)blk;
+  const uint2 w0 = p[0], w1 = p[1], w2 = p[2];
+  const unsigned int u[6] = {w0.x, w0.y, w1.x, w1.y, w2.x, w2.y};
+  const int k = (int)(short)(unsigned short)(u[4] >> 16);
+  const float sc = __int_as_float((127 + k) << 23);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const unsigned short h = (unsigned short)((u[i >> 1] >> (16 * (i & 1))) & 0xffffu);
+    kv[i] = __half2float(__ushort_as_half(h)) * sc;
+  }
+}
+
+template <typename S, int B, bool H16 = false>
 __global__ void __launch_bounds__(B)
     assemble_kernel(SellMatrix A, const int* __restrict__ cptr, const int* __restrict__ csrc,
                     const S* __restrict__ Kbuf, const S* __restrict__ slot_mass, const uint8_t* __restrict__ mask,
@@ -27,7 +42,36 @@ __global__ void __launch_bounds__(B)
   S acc[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) acc[i] = S(0);
-  if (Kbuf != nullptr) {
+  if constexpr (H16) {
+    const uint2* K16 = reinterpret_cast<const uint2*>(Kbuf);
+    const int c1 = cptr[q + 1];
+    int c = cptr[q];
+    auto add16 = [&](int code, const float (&kv)[9]) {
+      if (code >= 0) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) acc[i] += kv[i];
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) acc[a * 3 + b] += kv[b * 3 + a];
+      }
+    };
+    for (; c + 2 <= c1; c += 2) {
+      const int code0 = csrc[c], code1 = csrc[c + 1];
+      float kv0[9], kv1[9];
+      load_block16(K16, code0 & 0x7fffffff, kv0);
+      load_block16(K16, code1 & 0x7fffffff, kv1);
+      add16(code0, kv0);
+      add16(code1, kv1);
+    }
+    if (c < c1) {
+      const int code = csrc[c];
+      float kv[9];
+      load_block16(K16, code & 0x7fffffff, kv);
+      add16(code, kv);
+    }
+  } else if (Kbuf != nullptr) {
     // contributions in pairs: 18 independent block loads in flight per thread (the gathers are latency-bound)
     auto add = [&](int code, const S (&kv)[9]) {
       if (code >= 0) {
@@ -1408,6 +1452,20 @@ void launch_assemble(const SellMatrix& A, const int* cptr, const int* csrc, cons
   };
   dispatch_block<128, 256, 512>(block == 0 ? SB : block, go);
   after_launch("assemble");
+}
+
+void launch_assemble16(const SellMatrix& A, const int* cptr, const int* csrc, const uint2* K16, const float* slot_mass,
+                       const uint8_t* mask, bool filter, float* vals, float4* dinv, int precond, cudaStream_t st,
+                       int block) {
+  if (A.nslots <= 0) return;
+  const float* kb = reinterpret_cast<const float*>(K16);
+  auto go = [&](auto Bc) {
+    constexpr int b = decltype(Bc)::value;
+    assemble_kernel<float, b, true><<<div_up(A.nslots, b), b, 0, st>>>(A, cptr, csrc, kb, slot_mass, mask,
+                                                                        filter ? 1 : 0, vals, dinv, precond);
+  };
+  dispatch_block<128, 256, 512>(block == 0 ? SB : block, go);
+  after_launch("assemble16");
 }
 
 template <typename S>

@@ -56,6 +56,7 @@ struct DBuf {
 template <typename S>
 struct Solver {
   DBuf<S> K, vals, mvals;  // element blocks, system values, mass values (SELL)
+  DBuf<uint2> K16;         // element blocks in FP16 (launch_elem_hessian16), mixed Newton only
   DBuf<S> slot_mass;
   DBuf<V4<S>> x, r, z, p0, p1, q, dinv, tmp;
   DBuf<V4<S>> pm;  // the pipelined PCG's double-buffered m = M w (2 nv), allocated on first use
@@ -70,6 +71,7 @@ struct Solver {
   long ncg_version = -1;
   void release() {
     for (DBuf<S>* b : {&K, &vals, &mvals, &slot_mass, &pd_vals, &slot_pd, &pd_svals, &ncg_L, &ncg_Lt}) b->release();
+    K16.release();
     pd_kron = false;
     ncg_version = -1;
     for (DBuf<V4<S>>* b : {&x, &r, &z, &p0, &p1, &q, &dinv, &tmp, &pm, &ld, &lq, &pd_dinv}) b->release();
@@ -832,8 +834,9 @@ struct TimeStep {
   Solver<S>& solver();
 
   // update_hessian (time_step.hpp:626-658)
+  // k16: the element blocks in FP16 (tets, mixed precision; for assemblies whose solve runs on the FP16 copy)
   template <typename S>
-  void hessian(bool spsd, bool filter) {
+  void hessian(bool spsd, bool filter, bool k16 = false) {
     Solver<S>& s = solver<S>();
     ++asm_count;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -844,6 +847,18 @@ struct TimeStep {
                               s.dinv.p, params.precond, stream);
       if (profiling) prof_end(e0, e1, PK_HESS, 0);
       return;
+    }
+    if constexpr (std::is_same<S, float>::value) {
+      if (k16 && !springs && !tri2d) {
+        s.K16.alloc((size_t)30 * nt);
+        launch_elem_hessian16(e64(), e32(), dX.p, next.p, xf.p, dt * dt, spsd, s.K16.p, stream, shapes.hess);
+        if (profiling) prof_end(e0, e1, PK_HESS, 0);
+        if (profiling) prof_begin(e0, e1);
+        launch_assemble16(A(), cptr.p, csrc.p, s.K16.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
+                          params.precond, stream, shapes.assem);
+        if (profiling) prof_end(e0, e1, PK_ASM, 0);
+        return;
+      }
     }
     // two kernels through the per-element block buffer (allocated on first use)
     s.K.alloc((size_t)9 * (topo.cv * (topo.cv + 1) / 2) * nt);
@@ -1323,10 +1338,11 @@ struct TimeStep {
         break;
       }
       if (it >= params.max_newton_iters) break;
-      if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
-      hessian<S>(true, true);
       double eta = params.cg_rtol;
       if (params.cg_forcing == 1 && g0 > 0) eta = std::min(params.cg_rtol, std::max(params.cg_eta_min, gn / g0));
+      if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+      // a solve on the FP16 matrix copy can take FP16 element blocks too (half_hessian_blocks)
+      hessian<S>(true, true, std::is_same<S, float>::value && params.half_hessian_blocks == 1 && use_half(eta));
       double rr = 0;
       st.cg_iters_total += pcg<S>(forces.p, true, eta, params.cg_max_iters, &rr);
       launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);

@@ -9,7 +9,9 @@ Checked, against the FP64 oracle's matrix and the FP32 symmetric values on the s
   plus the copy's rounding (5e-2 + 5e-3) and takes the FP32 path's iteration count within 10% + 2; a solve
   tighter than half_matrix_min_rtol runs on the FP32 values (bitwise the FP32 path's result);
 * Newton steps with the copy converge like the FP32 matrix's (the same stopping test on FP64 residuals):
-  states within 1e-5, Newton iterations per step within 1, total PCG iterations within 15%.
+  states within 1e-5, Newton iterations per step within 1, total PCG iterations within 15%;
+* the FP16 element blocks of those assemblies (half_hessian_blocks): values within 1e-3 of max|K| of the
+  FP32-block assembly at the same state, and Newton steps as above.
 """
 import numpy as np
 import pytest
@@ -105,3 +107,47 @@ def test_newton_with_half_matrix(name):
     assert rel(uh, uf) <= 1e-5
     assert all(abs(a - b) <= 1 for a, b in zip(nh, nf)), (nh, nf)
     assert abs(ch - cf) <= 0.15 * cf, (ch, cf)
+
+
+def _one_newton_iteration(scene, half_blocks):
+    params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, precond=2,
+                              pcg_half_matrix=1, half_hessian_blocks=half_blocks, max_newton_iters=1)
+    ts = scenes.build_timestep(scene, precision="mixed", params=params)
+    ts.prepare_step()
+    ts.compute_step()
+    return ts
+
+
+def test_half_hessian_blocks_assembly():
+    """half_hessian_blocks = 1: the element blocks of a loose-solve assembly are written in FP16 with a
+    power-of-two scale per block and summed in FP32.  The first Newton iteration of the same step on two
+    handles assembles at the same state: the FP16-block values differ from the FP32-block values (the FP16
+    path ran) by at most 1e-3 of max|K| (a block's values carry 2^-11 of the block's largest magnitude; a
+    slot sums up to ~20 of them)."""
+    scene = scenes.bar(20, 6, 6)
+    k16 = _one_newton_iteration(scene, 1).values("sysmatrix")
+    k32 = _one_newton_iteration(scene, 0).values("sysmatrix")
+    assert not np.array_equal(k16, k32)
+    assert rel(k16, k32) <= 1e-3, rel(k16, k32)
+
+
+@pytest.mark.parametrize("name", ["beam_small", "bar_small"])
+def test_newton_with_half_hessian_blocks(name):
+    scene = {"beam_small": lambda: scenes.beam(40, 20, 14, h=0.05), "bar_small": lambda: scenes.bar(20, 6, 6)}[name]()
+    runs = {}
+    for hb in (1, 0):
+        params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2,
+                                  precond=2, pcg_half_matrix=1, half_hessian_blocks=hb)
+        ts = scenes.build_timestep(scene, precision="mixed", params=params)
+        newton, cg = [], 0
+        for _ in range(4):
+            ts.step()
+            st = ts.stats()
+            assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"], (hb, st)
+            newton.append(st["newton_iters"])
+            cg += st["cg_iters_total"]
+        runs[hb] = (ts.get("deformation"), newton, cg)
+    (u1, n1, c1), (u0, n0, c0) = runs[1], runs[0]
+    assert rel(u1, u0) <= 1e-5
+    assert all(abs(a - b) <= 1 for a, b in zip(n1, n0)), (n1, n0)
+    assert abs(c1 - c0) <= 0.15 * c0, (c1, c0)
