@@ -184,6 +184,8 @@ def run_gpu_arm(args, scene):
     params.pcg_persistent = args.pcg_variant
     if args.pcg_half is not None:
         params.pcg_half_matrix = args.pcg_half
+    if args.half_blocks is not None:
+        params.half_hessian_blocks = args.half_blocks
     result = {}
     launches0 = g.launch_count()
 
@@ -462,6 +464,8 @@ def main():
                     help="ssim_gb_params.pcg_persistent of the GPU arms (3: automatic; 4: pipelined PCG)")
     ap.add_argument("--pcg-half", type=int, default=None, choices=[0, 1],
                     help="FP16 copy of the scaled system matrix for the loose PCG solves (default: the library's)")
+    ap.add_argument("--half-blocks", type=int, default=None, choices=[0, 1],
+                    help="FP16 element Hessian blocks for the assemblies of those solves (default: the library's)")
     ap.add_argument("--precond", type=int, default=None, choices=[1, 2],
                     help="PCG preconditioner of every arm (1 Jacobi, 2 block-Jacobi); default: the bench's")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
