@@ -515,45 +515,36 @@ __global__ void __launch_bounds__(HB, 512 / HB)
   if (e < nt) {
     S K[78];
     element_hessian_at<S, XF>(e64, e32, X, u, xf, dt2, spsd, e, K);
-    S* st = stage + threadIdx.x * 90;
     int blk = 0;
 #pragma unroll
     for (int v = 0; v < 4; ++v)
 #pragma unroll
       for (int w = v; w < 4; ++w) {
+        S bv[9];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
           for (int b = 0; b < 3; ++b) {
             const int i = v * 3 + a, j = w * 3 + b;
-            st[blk * 9 + a * 3 + b] = (i <= j) ? K[kup(i, j)] : K[kup(j, i)];
+            bv[a * 3 + b] = (i <= j) ? K[kup(i, j)] : K[kup(j, i)];
           }
+        if constexpr (H16) {
+          // packed straight from registers: thread t's 30 words at 30 t (the element's global order)
+          pack_block16(bv, reinterpret_cast<uint2*>(stage) + threadIdx.x * 30 + 3 * blk);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 9; ++c) stage[threadIdx.x * 90 + blk * 9 + c] = bv[c];
+        }
         ++blk;
       }
   }
+  __syncthreads();
+  const int nvalid = min(HB, nt - e0);
   if constexpr (H16) {
-    // pack this element's blocks in place of its own staged values, block by block: packed block b (bytes
-    // 24b..24b+23 of the thread's 360) ends before source block b + 1 starts (byte 36b + 36), and block b is
-    // read into registers before it is overwritten
-    if (e < nt) {
-      const float* st = stage + threadIdx.x * 90;
-      uint2* pk = reinterpret_cast<uint2*>(stage) + threadIdx.x * 45;
-#pragma unroll 1
-      for (int b = 0; b < 10; ++b) {
-        float v[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) v[i] = st[9 * b + i];
-        pack_block16(v, pk + 3 * b);
-      }
-    }
-    __syncthreads();
-    const int nvalid = min(HB, nt - e0);
     const uint2* src = reinterpret_cast<const uint2*>(stage);
     uint2* dst = reinterpret_cast<uint2*>(Kbuf) + (size_t)e0 * 30;
-    for (int i = threadIdx.x; i < nvalid * 30; i += HB) dst[i] = src[(i / 30) * 45 + i % 30];
+    for (int i = threadIdx.x; i < nvalid * 30; i += HB) dst[i] = src[i];
   } else {
-    __syncthreads();
-    const int nvalid = min(HB, nt - e0);
     S* dst = Kbuf + (size_t)e0 * 90;
     for (int i = threadIdx.x; i < nvalid * 90; i += HB) dst[i] = stage[i];
   }
