@@ -155,6 +155,10 @@ typedef struct {
   int32_t half_hessian_blocks; /* tets: 1 (default) writes the element Hessian blocks of the assemblies whose solve
                              runs on the FP16 copy in FP16 (a power-of-two scale per 3x3 block, 24 bytes a block
                              instead of 36, three 8-byte loads in the assembly, FP32 sums); 0 keeps FP32 blocks */
+  double half_check_slack; /* after each Newton solve on the FP16 copy the true residual |g + K d| on the FP32
+                             values is computed with g . d; above half_check_slack (1.5) times the forcing eta
+                             times |g| the copy is too coarse for the system's conditioning and the handle's
+                             later solves use the FP32 values (until reset() or ssim_gb_set_params) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
@@ -168,6 +172,7 @@ typedef struct {
   double energy;
   double last_change;
   double elapsed_ms;
+  int32_t half_solves;    /* mixed Newton: solves of this step that ran on the FP16 copy of the scaled matrix */
 } ssim_gb_step_stats;
 
 /* Launch shapes chosen by ssim_gb_autotune (extension: the reference has no GPU kernels of its own) */

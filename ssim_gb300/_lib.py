@@ -73,6 +73,7 @@ class Params(C.Structure):
         ("pcg_half_matrix", C.c_int32),
         ("half_matrix_min_rtol", C.c_double),
         ("half_hessian_blocks", C.c_int32),
+        ("half_check_slack", C.c_double),
     ]
 
     def as_dict(self):
@@ -90,6 +91,7 @@ class StepStats(C.Structure):
         ("energy", C.c_double),
         ("last_change", C.c_double),
         ("elapsed_ms", C.c_double),
+        ("half_solves", C.c_int32),
     ]
 
     def as_dict(self):

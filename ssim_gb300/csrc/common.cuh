@@ -64,6 +64,7 @@ struct DevScalars {
   int32_t done;
   int32_t status;  // 0 ok, 1 breakdown (pq <= 0), 2 non-finite residual
   int32_t wait_failed;  // set by a persistent kernel whose grid-barrier wait gave up
+  double true_rr, true_bb;  // |b - K x|^2 on the FP32 values and |b|^2 after a solve on the FP16 copy
 };
 
 // Deterministic grid reduction: every block writes its partial sums, the last block to finish (found

@@ -304,6 +304,10 @@ void launch_pcg_setup_half(const HalfMatrix& H, const double* b, const float4* d
 bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float4* r, float4* z, float4* p0,
                      float4* p1, float4* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                      long long spin_limit, int extra, int max_blocks, cudaStream_t st);
+// after a solve on the FP16 copy: g . d, |d|^2 (as launch_dot_gd) and the solve's true residual on the FP32
+// symmetric values, |-g - K d|^2 and |g|^2 (sc->true_rr, sc->true_bb)
+void launch_dot_gd_check(const SellMatrix& A, const float* vals, const double* g, const float4* d, const Reduce& red,
+                         cudaStream_t st);
 // y = S^-1 K~ S^-1 x (the FP16 copy applied in the unscaled space); xs: nv vectors of scratch
 void launch_half_spmv(const HalfMatrix& H, const float4* x, float4* xs, float4* y, cudaStream_t st);
 // kron: vals holds one value per slot (the matrix is (scalar) (x) I3); launch_kron_extract makes that form

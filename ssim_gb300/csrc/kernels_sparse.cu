@@ -1219,6 +1219,36 @@ __global__ void __launch_bounds__(SB)
   }
 }
 
+// g . d and |d|^2 as dot_gd_kernel, with the solve's TRUE residual on the FP32 values: |-g - K d|^2 and |g|^2
+// (the check of a solve that ran on the FP16 copy of the scaled matrix)
+__global__ void __launch_bounds__(SB)
+    dot_gd_check_kernel(SellMatrix A, const float* __restrict__ vals, const double* __restrict__ g,
+                        const float4* __restrict__ d, Reduce red) {
+  __shared__ double shred[SB / 32][4];
+  __shared__ int sidx[SB / 32][ST_K][32];
+  const int u = blockIdx.x * SB + threadIdx.x;
+  double part[4] = {0, 0, 0, 0};
+  if (u < A.nv) {
+    float a0, a1, a2;
+    row_product_t<float, true>(A, vals, u, d, nullptr, 0.f, sidx[threadIdx.x >> 5], a0, a1, a2);
+    const float4 dv = d[u];
+    const double g0 = g[u * 3 + 0], g1 = g[u * 3 + 1], g2 = g[u * 3 + 2];
+    part[0] = g0 * (double)dv.x + g1 * (double)dv.y + g2 * (double)dv.z;
+    part[1] = (double)dv.x * dv.x + (double)dv.y * dv.y + (double)dv.z * dv.z;
+    const double r0 = -g0 - (double)a0, r1 = -g1 - (double)a1, r2 = -g2 - (double)a2;
+    part[2] = r0 * r0 + r1 * r1 + r2 * r2;
+    part[3] = g0 * g0 + g1 * g1 + g2 * g2;
+  }
+  block_sum<4, SB>(part, shred);
+  double tot[4];
+  if (grid_sum_last<4, SB>(part, red.partials, red.counter, tot)) {
+    red.sc->gd = tot[0];
+    red.sc->dnorm2 = tot[1];
+    red.sc->true_rr = tot[2];
+    red.sc->true_bb = tot[3];
+  }
+}
+
 template <typename S>
 __global__ void axpy_update_kernel(int nv, double alpha, const V4<S>* __restrict__ d, const double* __restrict__ X,
                                    double* __restrict__ u, float4* __restrict__ xf) {
@@ -1630,6 +1660,13 @@ template <typename S>
 void launch_dot_gd(int nv, const double* g, const V4<S>* d, const Reduce& red, cudaStream_t st) {
   dot_gd_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, g, d, red);
   after_launch("dot_gd");
+}
+
+void launch_dot_gd_check(const SellMatrix& A, const float* vals, const double* g, const float4* d, const Reduce& red,
+                         cudaStream_t st) {
+  if (A.nv <= 0) return;
+  dot_gd_check_kernel<<<div_up(A.nv, SB), SB, 0, st>>>(A, vals, g, d, red);
+  after_launch("dot_gd_check");
 }
 
 template <typename S>

@@ -155,6 +155,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->pcg_half_matrix = 1;
   p->half_matrix_min_rtol = 1e-2;
   p->half_hessian_blocks = 1;
+  p->half_check_slack = 1.5;
   p->elem32_switch = 10.0;
 }
 
@@ -312,9 +313,11 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
       !(p->ls_energy_slack32 >= 0) || !(p->elem32_switch >= 1) || p->pcg_pipe_iters < 0 || (p->fused_assembly != 0 && p->fused_assembly != 1) ||
       (p->mixed_delta != 0 && p->mixed_delta != 1) || (p->pcg_half_matrix != 0 && p->pcg_half_matrix != 1) ||
       !(p->half_matrix_min_rtol >= 0) || (p->half_hessian_blocks != 0 && p->half_hessian_blocks != 1) ||
+      !(p->half_check_slack > 0) ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;
+  h->ts.half_off = false;
   return SSIM_GB_OK;
 }
 

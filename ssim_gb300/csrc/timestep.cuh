@@ -132,6 +132,9 @@ struct TimeStep {
   bool h16_ok = false, h16_built = false;
   long long nfs = 0;
   long long asm_count = 0, h16_count = -1;  // assemblies of the FP32 values; the one the copy was made from
+  bool last_half = false;  // the last pcg() ran on the FP16 copy
+  bool half_off = false;   // a Newton solve on the copy missed its forcing on the FP32 values: not used again
+                           // until reset() or new parameters
   DBuf<double> lf, csr_out;
   // ---- device: solver
   Solver<float> sf;
@@ -572,7 +575,7 @@ struct TimeStep {
   // the FP16 copy serves a solve when it is enabled, the tolerance is loose enough for its rounding, the
   // solve would run the persistent Chronopoulos-Gear kernel, and the pattern fits
   bool use_half(double rtol) {
-    if (!mixed() || params.pcg_half_matrix != 1 || !(rtol >= params.half_matrix_min_rtol)) return false;
+    if (half_off || !mixed() || params.pcg_half_matrix != 1 || !(rtol >= params.half_matrix_min_rtol)) return false;
     const int variant = params.pcg_persistent == 3 ? 2 : params.pcg_persistent;
     return variant == 2 && half_ready();
   }
@@ -619,6 +622,7 @@ struct TimeStep {
     if (!(rho >= 0)) throw invalid_argument("Density must be positive, got " + std::to_string(rho));
     if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NCG_EXT) throw invalid_argument("unknown stepper");
     stepper = stepper_kind;
+    half_off = false;
     for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
     if (!springs) upload_material();
     // consistent mass per slot (time_step.hpp:437-461) and the threshold (time_step.hpp:490-491):
@@ -890,9 +894,13 @@ struct TimeStep {
   template <typename S>
   int pcg(const double* b, bool negate, double eta, int max_iters, double* rel_res) {
     Solver<S>& s = solver<S>();
+    last_half = false;
     if constexpr (std::is_same<S, float>::value) {
       int it = 0;
-      if (use_half(eta) && pcg_half(b, negate, eta, max_iters, rel_res, &it)) return it;
+      if (use_half(eta) && pcg_half(b, negate, eta, max_iters, rel_res, &it)) {
+        last_half = true;
+        return it;
+      }
     }
     launch_pcg_setup<S>(nv, b, s.dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
     return pcg_loop<S>(s.vals.p, s.dinv.p, max_iters, rel_res, true);
@@ -1345,8 +1353,21 @@ struct TimeStep {
       hessian<S>(true, true, std::is_same<S, float>::value && params.half_hessian_blocks == 1 && use_half(eta));
       double rr = 0;
       st.cg_iters_total += pcg<S>(forces.p, true, eta, params.cg_max_iters, &rr);
-      launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
+      const bool checked = last_half;
+      st.half_solves += checked ? 1 : 0;
+      if constexpr (std::is_same<S, float>::value) {
+        if (checked)
+          launch_dot_gd_check(A(), s.vals.p, forces.p, s.x.p, red(), stream);
+        else
+          launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
+      } else {
+        launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
+      }
       sync_scalars();
+      // a solve on the FP16 copy whose true residual (FP32 values) misses the forcing by the slack: the copy's
+      // rounding is too coarse for this system's conditioning; later solves use the FP32 values
+      const double tr_max = params.half_check_slack * eta;
+      if (checked && hsc->true_bb > 0 && !(hsc->true_rr <= tr_max * tr_max * hsc->true_bb)) half_off = true;
       double gd = hsc->gd;
       const double dn = std::sqrt(hsc->dnorm2);
       if (!(gd < 0)) {  // not a descent direction: steepest descent
@@ -1749,7 +1770,8 @@ struct TimeStep {
       for (int gcap : grids)
         for (int half : {0, 1}) {
           if (v == 0 && gcap != 0) continue;  // the two-launch loop has no persistent grid
-          if (half && (v != 2 || !mixed() || !half_ready())) continue;  // the FP16 copy serves only these
+          // the FP16 copy serves only these, and only when enabled (the sweep may turn it off, never on)
+          if (half && (v != 2 || !mixed() || keep_half != 1 || !half_ready())) continue;
           params.pcg_persistent = v;
           params.pcg_max_blocks = gcap;
           params.pcg_half_matrix = half;

@@ -151,3 +151,37 @@ def test_newton_with_half_hessian_blocks(name):
     assert rel(u1, u0) <= 1e-5
     assert all(abs(a - b) <= 1 for a, b in zip(n1, n0)), (n1, n0)
     assert abs(c1 - c0) <= 0.15 * c0, (c1, c0)
+
+
+def test_half_solves_reported_and_checked():
+    """Every Newton solve on the copy is followed by its true residual on the FP32 values (fused with g . d):
+    on a well-conditioned beam every step's solves stay on the copy (half_solves = Newton iterations)."""
+    scene = scenes.beam(40, 20, 14, h=0.05)
+    params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, precond=2)
+    ts = scenes.build_timestep(scene, precision="mixed", params=params)
+    for _ in range(3):
+        ts.step()
+        st = ts.stats()
+        assert st["converged"] == 1 and st["half_solves"] == st["newton_iters"], st
+
+
+def test_half_fallback_to_fp32_values():
+    """A check that fails (here forced by half_check_slack = 0.5: no solve that stops at its forcing has a true
+    residual below half of it) turns the copy off for the handle: one solve on the copy, then the FP32 values,
+    the same converged trajectory as a handle that never used the copy; reset() turns it on again."""
+    scene = scenes.bar(20, 6, 6)
+    base = dict(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, precond=2)
+    ts = scenes.build_timestep(scene, precision="mixed", params=g.default_params(half_check_slack=0.5, **base))
+    ref = scenes.build_timestep(scene, precision="mixed", params=g.default_params(pcg_half_matrix=0, **base))
+    halves = []
+    for _ in range(3):
+        ts.step()
+        ref.step()
+        st = ts.stats()
+        assert st["converged"] == 1 and ref.stats()["converged"] == 1
+        halves.append(st["half_solves"])
+    assert halves == [1, 0, 0], halves
+    assert rel(ts.get("deformation"), ref.get("deformation")) <= 1e-5
+    ts.reset("newton")
+    ts.step()
+    assert ts.stats()["half_solves"] == 1
