@@ -601,6 +601,7 @@ def main():
             "mixed_over_fp64": round(value / fp64_value, 3),
             "newton_iters": sum(s["newton_iters"] for s in st),
             "cg_iters": sum(s["cg_iters_total"] for s in st),
+            "half_solves": sum(s.get("half_solves", 0) for s in st),
             "max_rel_residual": max(rel_res) if rel_res else None,
             "err_vs_oracle": err,
             f"{cells_key}_per_s": round(T * value, 1),
@@ -620,6 +621,8 @@ def main():
         # per-step detail (Newton / PCG iteration counts, residuals, PCG length of every solve) on stderr
         print(json.dumps({"detail": {"newton_iters": [s["newton_iters"] for s in st],
                                      "cg_iters": [s["cg_iters_total"] for s in st], "rel_residual": rel_res,
+                                     "half_solves": [s.get("half_solves", 0) for s in st],
+                                     "half_check": [round(s.get("half_check", 0.0), 3) for s in st],
                                      "fp64_newton_iters": [s["newton_iters"] for s in stf],
                                      "fp64_cg_iters": [s["cg_iters_total"] for s in stf],
                                      "pcg_iters_per_solve_from_reset": r.get("solve_log")}}),

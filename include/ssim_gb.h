@@ -156,9 +156,12 @@ typedef struct {
                              runs on the FP16 copy in FP16 (a power-of-two scale per 3x3 block, 24 bytes a block
                              instead of 36, three 8-byte loads in the assembly, FP32 sums); 0 keeps FP32 blocks */
   double half_check_slack; /* after each Newton solve on the FP16 copy the true residual |g + K d| on the FP32
-                             values is computed with g . d; above half_check_slack (1.5) times the forcing eta
+                             values is computed with g . d; above half_check_slack (1.2) times the forcing eta
                              times |g| the copy is too coarse for the system's conditioning and the handle's
-                             later solves use the FP32 values (until reset() or ssim_gb_set_params) */
+                             later solves use the FP32 values (until reset() or ssim_gb_set_params).  Measured
+                             ratios: 0.8-1.05 on the beams, bar and cube, up to 1.46 (2.7 with FP32 element
+                             blocks) on the reference's light, stiff unit box, where the copy costs Newton
+                             iterations */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
@@ -173,6 +176,7 @@ typedef struct {
   double last_change;
   double elapsed_ms;
   int32_t half_solves;    /* mixed Newton: solves of this step that ran on the FP16 copy of the scaled matrix */
+  double half_check;      /* the largest |g + K d| / (eta |g|) on the FP32 values among those solves (0: none) */
 } ssim_gb_step_stats;
 
 /* Launch shapes chosen by ssim_gb_autotune (extension: the reference has no GPU kernels of its own) */

@@ -92,6 +92,7 @@ class StepStats(C.Structure):
         ("last_change", C.c_double),
         ("elapsed_ms", C.c_double),
         ("half_solves", C.c_int32),
+        ("half_check", C.c_double),
     ]
 
     def as_dict(self):

@@ -155,7 +155,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->pcg_half_matrix = 1;
   p->half_matrix_min_rtol = 1e-2;
   p->half_hessian_blocks = 1;
-  p->half_check_slack = 1.5;
+  p->half_check_slack = 1.2;
   p->elem32_switch = 10.0;
 }
 

@@ -1367,7 +1367,10 @@ struct TimeStep {
       // a solve on the FP16 copy whose true residual (FP32 values) misses the forcing by the slack: the copy's
       // rounding is too coarse for this system's conditioning; later solves use the FP32 values
       const double tr_max = params.half_check_slack * eta;
-      if (checked && hsc->true_bb > 0 && !(hsc->true_rr <= tr_max * tr_max * hsc->true_bb)) half_off = true;
+      if (checked && hsc->true_bb > 0) {
+        st.half_check = std::max(st.half_check, std::sqrt(hsc->true_rr / hsc->true_bb) / eta);
+        if (!(hsc->true_rr <= tr_max * tr_max * hsc->true_bb)) half_off = true;
+      }
       double gd = hsc->gd;
       const double dn = std::sqrt(hsc->dnorm2);
       if (!(gd < 0)) {  // not a descent direction: steepest descent
