@@ -186,6 +186,8 @@ def run_gpu_arm(args, scene):
         params.pcg_half_matrix = args.pcg_half
     if args.half_blocks is not None:
         params.half_hessian_blocks = args.half_blocks
+    if args.speculate is not None:
+        params.speculative_hessian = args.speculate
     result = {}
     launches0 = g.launch_count()
 
@@ -466,6 +468,8 @@ def main():
                     help="FP16 copy of the scaled system matrix for the loose PCG solves (default: the library's)")
     ap.add_argument("--half-blocks", type=int, default=None, choices=[0, 1],
                     help="FP16 element Hessian blocks for the assemblies of those solves (default: the library's)")
+    ap.add_argument("--speculate", type=int, default=None, choices=[0, 1],
+                    help="assemble the next Newton matrix during the line search (default: the library's)")
     ap.add_argument("--precond", type=int, default=None, choices=[1, 2],
                     help="PCG preconditioner of every arm (1 Jacobi, 2 block-Jacobi); default: the bench's")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)

@@ -162,6 +162,13 @@ typedef struct {
                              ratios: 0.8-1.05 on the beams, bar and cube, up to 1.46 (2.7 with FP32 element
                              blocks) on the reference's light, stiff unit box, where the copy costs Newton
                              iterations */
+  int32_t speculative_hessian; /* mixed precision, tets, Newton: 1 assembles the next iteration's Hessian at the
+                             full step u + d on a second stream while the line search runs on the handle's
+                             stream; a full step accepted finds its matrix ready (the same values: the same FP32
+                             positions), a shorter one assembles again.  0 (default): after the line search.
+                             Measured on GB300: 304 against 299 steps/s on the 192k-tet bar, but 62.2 against
+                             63.9 on the 1.02M-tet beam and 9.37 against 9.83 on the 6.5M-tet batch (the
+                             Hessian's many small blocks hold the SMs the line search's kernels wait for) */
 } ssim_gb_params;
 
 /* Per compute_step statistics (the optim_result fields of backward_euler.hpp:28-32 and more). */
@@ -177,6 +184,7 @@ typedef struct {
   double elapsed_ms;
   int32_t half_solves;    /* mixed Newton: solves of this step that ran on the FP16 copy of the scaled matrix */
   double half_check;      /* the largest |g + K d| / (eta |g|) on the FP32 values among those solves (0: none) */
+  int32_t spec_hits;      /* Newton iterations whose matrix was assembled ahead of the line search (speculative_hessian) */
 } ssim_gb_step_stats;
 
 /* Launch shapes chosen by ssim_gb_autotune (extension: the reference has no GPU kernels of its own) */

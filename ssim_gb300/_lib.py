@@ -74,6 +74,7 @@ class Params(C.Structure):
         ("half_matrix_min_rtol", C.c_double),
         ("half_hessian_blocks", C.c_int32),
         ("half_check_slack", C.c_double),
+        ("speculative_hessian", C.c_int32),
     ]
 
     def as_dict(self):
@@ -93,6 +94,7 @@ class StepStats(C.Structure):
         ("elapsed_ms", C.c_double),
         ("half_solves", C.c_int32),
         ("half_check", C.c_double),
+        ("spec_hits", C.c_int32),
     ]
 
     def as_dict(self):

@@ -328,6 +328,9 @@ void launch_dot_gd(int nv, const double* g, const V4<S>* d, const Reduce& red, c
 template <typename S>
 void launch_axpy_update(int nv, double alpha, const V4<S>* d, const double* X, double* u, float4* xf,
                         cudaStream_t st);
+// xf = float(X + (u + d)): the positions after a full step, for an assembly made ahead of the line search
+template <typename S>
+void launch_full_step_xf(int nv, const V4<S>* d, const double* X, const double* u, float4* xf, cudaStream_t st);
 void launch_refresh_xf(int nv, const double* X, const double* u, float4* xf, cudaStream_t st);
 void launch_prepare_step(int n, double dt, const double* u, const double* v, const double* a,
                          const int8_t* dof_type, const double* dbc, double* xt, double* next, cudaStream_t st);

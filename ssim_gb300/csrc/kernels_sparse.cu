@@ -1249,6 +1249,20 @@ __global__ void __launch_bounds__(SB)
   }
 }
 
+// the FP32 positions of u + d: what axpy_update_kernel (alpha = 1) and refresh_xf_kernel make after a full
+// step, bit for bit (u + 1.0 d rounds once, as the fused multiply-add there does)
+template <typename S>
+__global__ void full_step_xf_kernel(int nv, const V4<S>* __restrict__ d, const double* __restrict__ X,
+                                    const double* __restrict__ u, float4* __restrict__ xf) {
+  const int v = blockIdx.x * SB + threadIdx.x;
+  if (v >= nv) return;
+  const V4<S> dv = d[v];
+  const double u0 = u[v * 3 + 0] + (double)dv.x;
+  const double u1 = u[v * 3 + 1] + (double)dv.y;
+  const double u2 = u[v * 3 + 2] + (double)dv.z;
+  xf[v] = make_float4((float)(X[v * 3 + 0] + u0), (float)(X[v * 3 + 1] + u1), (float)(X[v * 3 + 2] + u2), 0.f);
+}
+
 template <typename S>
 __global__ void axpy_update_kernel(int nv, double alpha, const V4<S>* __restrict__ d, const double* __restrict__ X,
                                    double* __restrict__ u, float4* __restrict__ xf) {
@@ -1675,6 +1689,16 @@ void launch_axpy_update(int nv, double alpha, const V4<S>* d, const double* X, d
   axpy_update_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, alpha, d, X, u, xf);
   after_launch("axpy_update");
 }
+
+template <typename S>
+void launch_full_step_xf(int nv, const V4<S>* d, const double* X, const double* u, float4* xf, cudaStream_t st) {
+  if (nv <= 0) return;
+  full_step_xf_kernel<S><<<div_up(nv, SB), SB, 0, st>>>(nv, d, X, u, xf);
+  after_launch("full_step_xf");
+}
+template void launch_full_step_xf<float>(int, const float4*, const double*, const double*, float4*, cudaStream_t);
+template void launch_full_step_xf<double>(int, const double4_32a*, const double*, const double*, float4*,
+                                          cudaStream_t);
 
 void launch_refresh_xf(int nv, const double* X, const double* u, float4* xf, cudaStream_t st) {
   if (nv <= 0) return;

@@ -156,6 +156,7 @@ void ssim_gb_default_params(ssim_gb_params* p) {
   p->half_matrix_min_rtol = 1e-2;
   p->half_hessian_blocks = 1;
   p->half_check_slack = 1.2;
+  p->speculative_hessian = 0;
   p->elem32_switch = 10.0;
 }
 
@@ -313,7 +314,7 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
       !(p->ls_energy_slack32 >= 0) || !(p->elem32_switch >= 1) || p->pcg_pipe_iters < 0 || (p->fused_assembly != 0 && p->fused_assembly != 1) ||
       (p->mixed_delta != 0 && p->mixed_delta != 1) || (p->pcg_half_matrix != 0 && p->pcg_half_matrix != 1) ||
       !(p->half_matrix_min_rtol >= 0) || (p->half_hessian_blocks != 0 && p->half_hessian_blocks != 1) ||
-      !(p->half_check_slack > 0) ||
+      !(p->half_check_slack > 0) || (p->speculative_hessian != 0 && p->speculative_hessian != 1) ||
       !(p->cg_rtol >= 0) || p->cg_check_every < 1 || p->lbfgs_history < 1)
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;

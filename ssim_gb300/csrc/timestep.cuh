@@ -133,6 +133,13 @@ struct TimeStep {
   long long nfs = 0;
   long long asm_count = 0, h16_count = -1;  // assemblies of the FP32 values; the one the copy was made from
   bool last_half = false;  // the last pcg() ran on the FP16 copy
+  // speculative assembly (speculative_hessian): the next Newton iteration's Hessian at the full step, built on
+  // a second stream while the line search runs on the handle's stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_dir = nullptr, ev_spec = nullptr, ev_xf = nullptr;
+  DBuf<float4> xf_spec;
+  bool spec_pending = false;
+  bool spec_k16 = false;  // the element-block precision of the speculative assembly
   bool half_off = false;   // a Newton solve on the copy missed its forcing on the FP32 values: not used again
                            // until reset() or new parameters
   DBuf<double> lf, csr_out;
@@ -311,6 +318,11 @@ struct TimeStep {
   double prof_bytes[PK_COUNT] = {0};
 
   ~TimeStep() {
+    if (side) cudaStreamSynchronize(side);
+    if (side) cudaStreamDestroy(side);
+    if (ev_dir) cudaEventDestroy(ev_dir);
+    if (ev_spec) cudaEventDestroy(ev_spec);
+    if (ev_xf) cudaEventDestroy(ev_xf);
     for (auto e : ev) cudaEventDestroy(e);
     if (hsc) cudaFreeHost(hsc);
     if (hscal) cudaFreeHost(hscal);
@@ -623,6 +635,8 @@ struct TimeStep {
     if (stepper_kind < 0 || stepper_kind > SSIM_GB_STEPPER_NCG_EXT) throw invalid_argument("unknown stepper");
     stepper = stepper_kind;
     half_off = false;
+    if (side) SSIM_CUDA(cudaStreamSynchronize(side));  // no speculative assembly outlives the buffers it writes
+    spec_pending = false;
     for (DBuf<double>* b : {&inertia, &next, &forces, &work}) b->zero(stream);
     if (!springs) upload_material();
     // consistent mass per slot (time_step.hpp:437-461) and the threshold (time_step.hpp:490-491):
@@ -840,13 +854,14 @@ struct TimeStep {
   // update_hessian (time_step.hpp:626-658)
   // k16: the element blocks in FP16 (tets, mixed precision; for assemblies whose solve runs on the FP16 copy)
   template <typename S>
-  void hessian(bool spsd, bool filter, bool k16 = false) {
+  void hessian(bool spsd, bool filter, bool k16 = false, const float4* xfp = nullptr) {
     Solver<S>& s = solver<S>();
     ++asm_count;
+    if (xfp == nullptr) xfp = xf.p;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profiling) prof_begin(e0, e1);
     if (!springs && !tri2d && params.fused_assembly && fused_ready()) {
-      launch_fused_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, A(), topo.nslices,
+      launch_fused_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xfp : nullptr, dt * dt, spsd, A(), topo.nslices,
                               fused_spc, fused_ncta, fptr.p, felem.p, fcode.p, s.slot_mass.p, mask.p, filter, s.vals.p,
                               s.dinv.p, params.precond, stream);
       if (profiling) prof_end(e0, e1, PK_HESS, 0);
@@ -855,7 +870,7 @@ struct TimeStep {
     if constexpr (std::is_same<S, float>::value) {
       if (k16 && !springs && !tri2d) {
         s.K16.alloc((size_t)30 * nt);
-        launch_elem_hessian16(e64(), e32(), dX.p, next.p, xf.p, dt * dt, spsd, s.K16.p, stream, shapes.hess);
+        launch_elem_hessian16(e64(), e32(), dX.p, next.p, xfp, dt * dt, spsd, s.K16.p, stream, shapes.hess);
         if (profiling) prof_end(e0, e1, PK_HESS, 0);
         if (profiling) prof_begin(e0, e1);
         launch_assemble16(A(), cptr.p, csrc.p, s.K16.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
@@ -871,13 +886,48 @@ struct TimeStep {
     else if (tri2d)
       launch_tri_hessian<S>(e64(), next.p, dt * dt, spsd, s.K.p, stream);
     else
-      launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xf.p : nullptr, dt * dt, spsd, s.K.p, stream,
+      launch_elem_hessian<S>(e64(), e32(), dX.p, next.p, mixed() ? xfp : nullptr, dt * dt, spsd, s.K.p, stream,
                              shapes.hess);
     if (profiling) prof_end(e0, e1, PK_HESS, 0);
     if (profiling) prof_begin(e0, e1);
     launch_assemble<S>(A(), cptr.p, csrc.p, s.K.p, s.slot_mass.p, mask.p, filter, s.vals.p, s.dinv.p,
                        params.precond, stream, shapes.assem);
     if (profiling) prof_end(e0, e1, PK_ASM, 0);
+  }
+
+  // the next Newton iteration's Hessian at u + d (the full step), on the side stream after the direction
+  // is final: the same FP32 positions as launch_axpy_update(alpha = 1) and refresh_xf would make, so a
+  // full step accepted by the line search finds its matrix assembled
+  template <typename S>
+  void spec_hessian(const V4<S>* d, bool k16) {
+    if (!side) {
+      SSIM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+      SSIM_CUDA(cudaEventCreateWithFlags(&ev_dir, cudaEventDisableTiming));
+      SSIM_CUDA(cudaEventCreateWithFlags(&ev_spec, cudaEventDisableTiming));
+      SSIM_CUDA(cudaEventCreateWithFlags(&ev_xf, cudaEventDisableTiming));
+    }
+    xf_spec.alloc(nv);
+    SSIM_CUDA(cudaEventRecord(ev_dir, stream));
+    SSIM_CUDA(cudaStreamWaitEvent(side, ev_dir, 0));
+    launch_full_step_xf<S>(nv, d, dX.p, next.p, xf_spec.p, side);
+    SSIM_CUDA(cudaEventRecord(ev_xf, side));  // the line search's update of u waits for this read of u
+    std::swap(stream, side);  // hessian() launches on `stream`
+    try {
+      hessian<S>(true, true, k16, xf_spec.p);
+    } catch (...) {
+      std::swap(stream, side);
+      throw;
+    }
+    std::swap(stream, side);
+    SSIM_CUDA(cudaEventRecord(ev_spec, side));
+    spec_pending = true;
+  }
+  // the handle's stream waits for a speculative assembly in flight (before anything reads or rewrites the
+  // system values, the element blocks or the positions it used)
+  void spec_join() {
+    if (!spec_pending) return;
+    SSIM_CUDA(cudaStreamWaitEvent(stream, ev_spec, 0));
+    spec_pending = false;
   }
 
   void hessian_any(bool spsd, bool filter) {
@@ -1324,6 +1374,10 @@ struct TimeStep {
       }
     };
     int it = 0;
+    // speculation: tets in mixed precision (the Hessian reads only the FP32 positions), not while profiling
+    const bool can_spec = params.speculative_hessian == 1 && std::is_same<S, float>::value && !springs && !tri2d &&
+                          !profiling;
+    bool spec_ready = false;  // this iteration's matrix was assembled ahead, at the accepted full step
     for (;; ++it) {
       st.grad_norm = gn;
       st.energy = E0;
@@ -1348,9 +1402,14 @@ struct TimeStep {
       if (it >= params.max_newton_iters) break;
       double eta = params.cg_rtol;
       if (params.cg_forcing == 1 && g0 > 0) eta = std::min(params.cg_rtol, std::max(params.cg_eta_min, gn / g0));
-      if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
       // a solve on the FP16 matrix copy can take FP16 element blocks too (half_hessian_blocks)
-      hessian<S>(true, true, std::is_same<S, float>::value && params.half_hessian_blocks == 1 && use_half(eta));
+      const bool k16 = std::is_same<S, float>::value && params.half_hessian_blocks == 1 && use_half(eta);
+      spec_join();
+      if (!(spec_ready && spec_k16 == k16)) {
+        if (mixed()) launch_refresh_xf(nv, dX.p, next.p, xf.p, stream);
+        hessian<S>(true, true, k16);
+      }
+      spec_ready = false;
       double rr = 0;
       st.cg_iters_total += pcg<S>(forces.p, true, eta, params.cg_max_iters, &rr);
       const bool checked = last_half;
@@ -1377,6 +1436,15 @@ struct TimeStep {
         launch_to_vec4<S>(nv, forces.p, s.x.p, true, stream);
         gd = -gn * gn;
       }
+      // the next iteration's matrix at the full step, on the side stream while the line search runs; its
+      // element-block precision is the one the next forcing term will ask for (FP16 blocks only when every
+      // possible next forcing term allows them)
+      const bool spec = can_spec && it + 1 < params.max_newton_iters;
+      if (spec) {
+        const double eta_lo = std::min(params.cg_rtol, params.cg_forcing == 1 ? params.cg_eta_min : params.cg_rtol);
+        spec_k16 = params.half_hessian_blocks == 1 && use_half(eta_lo);
+        if constexpr (std::is_same<S, float>::value) spec_hessian<S>(s.x.p, spec_k16);
+      }
       // backtracking line search; each trial evaluates energy and forces at u + alpha d in one element
       // pass, so the accepted trial's forces are the next gradient (no separate evaluation)
       double alpha = 1.0;
@@ -1402,6 +1470,7 @@ struct TimeStep {
         if (Et <= E0 + params.armijo * alpha * gd + slack) break;
         if (ls + 1 < params.max_ls_iters) alpha *= params.ls_shrink;
       }
+      if (spec) SSIM_CUDA(cudaStreamWaitEvent(stream, ev_xf, 0));
       launch_axpy_update<S>(nv, alpha, s.x.p, dX.p, next.p, nullptr, stream);
       if (delta)
         delta_gather();
@@ -1416,7 +1485,10 @@ struct TimeStep {
       gn = std::sqrt(hsc->gnorm2);
       stall = gn > 0.5 * gn_prev ? stall + 1 : 0;
       gn_prev = gn;
+      spec_ready = spec && alpha == 1.0;
+      st.spec_hits += spec_ready ? 1 : 0;
     }
+    spec_join();
     st.newton_iters = it;
   }
 
