@@ -256,6 +256,7 @@ def run_gpu_arm(args, scene):
     # ---- roofline of the dominant kernel (PCG SpMV), events around each launch, same workload
     _, _, _, _, prof, _ = timed_run("mixed", min(args.steps, 3), 1, profile=True)
     half_matrix = int(ts.params.pcg_half_matrix)  # the solves ran on the FP16 copy of the scaled matrix
+    pcg_variant = int(ts.params.pcg_persistent)
     # ---- plain FP64 on the same steps
     _, ms_fp64, st_fp64, _, _, first_fp64 = timed_run("fp64", args.steps, args.warmup)
     # ---- e2e through the reference-facing API: per step h2d of the Dirichlet targets (pinned), the step,
@@ -309,7 +310,7 @@ def run_gpu_arm(args, scene):
     result.update(
         ms_mixed=ms_mixed, ms_fp64=ms_fp64, st_mixed=st_mixed, st_fp64=st_fp64, launches=launches, prof=prof,
         clocks=clocks, e2e_s=e2e_s, h2d=fixed.size * 3 * 8 + fixed.size * 4, d2h=d.size * 8,
-        total_launches=g.launch_count() - launches0, nnz=ts.nnz, solve_log=solve_log, half_matrix=half_matrix,
+        total_launches=g.launch_count() - launches0, nnz=ts.nnz, solve_log=solve_log, half_matrix=half_matrix, pcg_variant=pcg_variant,
         first={"mixed": first_mixed, "fp64": first_fp64}, tuning=tuning,
     )
     if args.adjoint:
@@ -539,18 +540,23 @@ def main():
         p = prof["pcg_iteration"]
         avg_s = p["total_ms"] / p["launches"] / 1e3
         algo = spmv_algo + 7 * s_b * n
-        pipe = args.pcg_variant == 4
-        half = not pipe and r.get("half_matrix", 0) == 1
-        kname = "pipe_persistent" if pipe else "cgcg_half" if half else "cgcg_persistent"
-        roofline = {"kernel": ("pipe_persistent_kernel<float> (whole pipelined PCG solve in one cooperative launch; "
+        variant = r.get("pcg_variant", args.pcg_variant)
+        half = r.get("half_matrix", 0) == 1 and sum(s.get("half_solves", 0) for s in r["st_mixed"]) > 0
+        pipe = variant == 4 or (half and variant == 3)
+        kname = ("pipe_half" if pipe else "cgcg_half") if half else ("pipe_persistent" if pipe else "cgcg_persistent")
+        roofline = {"kernel": {
+            "pipe_half": "pipe_half_kernel (whole pipelined PCG solve in one cooperative launch on the FP16 copy of "
+                         "the Jacobi-scaled matrix, full block SELL-32; unit = one PCG iteration: SpMV of m = M w "
+                         "fused with the vector recurrences and dots, one reducing grid barrier)",
+            "cgcg_half": "cgcg_half_kernel (whole Chronopoulos-Gear PCG solve in one cooperative launch on the FP16 "
+                         "copy of the Jacobi-scaled matrix, full block SELL-32; unit = one PCG iteration: SpMV + "
+                         "dots, grid reduction, vector update, grid barrier)",
+            "pipe_persistent": "pipe_persistent_kernel<float> (whole pipelined PCG solve in one cooperative launch; "
                                "unit = one PCG iteration: symmetric SELL-32 SpMV of m = M w fused with the vector "
-                               "recurrences and dots, one reducing grid barrier)") if pipe else
-                              ("cgcg_half_kernel (whole Chronopoulos-Gear PCG solve in one cooperative launch on "
-                               "the FP16 copy of the Jacobi-scaled matrix, full block SELL-32; unit = one PCG "
-                               "iteration: SpMV + dots, grid reduction, vector update, grid barrier)") if half else
-                              ("cgcg_persistent_kernel<float> (whole Chronopoulos-Gear PCG solve in one cooperative "
+                               "recurrences and dots, one reducing grid barrier)",
+            "cgcg_persistent": "cgcg_persistent_kernel<float> (whole Chronopoulos-Gear PCG solve in one cooperative "
                                "launch; unit = one PCG iteration: symmetric SELL-32 SpMV + dots, grid reduction, "
-                               "vector update, grid barrier)"),
+                               "vector update, grid barrier)"}[kname],
                     "bound": "hbm", "achieved": round(algo / avg_s / 1e9, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(algo / avg_s / 1e9 / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_iteration": algo, "avg_iteration_us": round(avg_s * 1e6, 2),

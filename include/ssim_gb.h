@@ -109,7 +109,9 @@ typedef struct {
                              1: the same PCG in one cooperative launch per solve (grid barriers, no host
                              round trips; bitwise the iterates of 0); 2: Chronopoulos-Gear PCG in one
                              launch (one reduction per iteration; equal to 0 up to rounding);
-                             3 (default): 2 in mixed precision, 0 in FP64 (the faster on GB300);
+                             3 (default): in mixed precision 4 for the solves on the FP16 copy of the
+                             scaled matrix (pcg_half_matrix, whose true-residual check covers the drift
+                             below) and 2 on the FP32 values; 0 in FP64 (the faster on GB300);
                              4: pipelined PCG in one launch (one grid barrier per iteration, two more vertex
                              vectors, Chronopoulos-Gear after pcg_pipe_iters iterations; equal to 0 up to
                              rounding, but in FP32 its true residual drifts from the recursive one with the

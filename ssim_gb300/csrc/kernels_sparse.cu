@@ -1113,6 +1113,154 @@ __global__ void __launch_bounds__(SB, sizeof(S) == 4 ? 5 : 4)
   if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
 }
 
+// Pipelined PCG (pipe_persistent_kernel) on the FP16 copy, in its scaled space: the SpMV of m = M w reads the
+// full FP16 entries, the third dot is (r, r) of the unscaled residual, and every block unscales its own rows
+// of x after the last iteration.  After pipe_iters iterations it continues as Chronopoulos-Gear.
+__device__ __forceinline__ void pipe_half_row(const HalfMatrix& H, const float4* __restrict__ dinv, bool first,
+                                              float alpha, float beta, const float4* mk, float4* mn, float4* x,
+                                              float4* r, float4* z, float4* p, float4* sv, float4* w, int u,
+                                              int (*sidx)[32], float (&part)[3]) {
+  part[0] = part[1] = part[2] = 0.f;
+  if (u >= H.nv) return;
+  float n0, n1, n2;
+  half_row_product(H, u, mk, sidx, n0, n1, n2);
+  float4 ru = r[u], wu = w[u];
+  const float4 uu = block_jacobi<float>(dinv, u, ru.x, ru.y, ru.z);
+  float4 zu = make_float4(n0, n1, n2, 0.f), su = wu, pu = uu;
+  if (!first) {
+    const float4 zo = z[u], so = sv[u], po = p[u];
+    zu = make_float4(n0 + beta * zo.x, n1 + beta * zo.y, n2 + beta * zo.z, 0.f);
+    su = make_float4(wu.x + beta * so.x, wu.y + beta * so.y, wu.z + beta * so.z, 0.f);
+    pu = make_float4(uu.x + beta * po.x, uu.y + beta * po.y, uu.z + beta * po.z, 0.f);
+  }
+  float4 xu = x[u];
+  xu.x += alpha * pu.x;
+  xu.y += alpha * pu.y;
+  xu.z += alpha * pu.z;
+  ru.x -= alpha * su.x;
+  ru.y -= alpha * su.y;
+  ru.z -= alpha * su.z;
+  wu.x -= alpha * zu.x;
+  wu.y -= alpha * zu.y;
+  wu.z -= alpha * zu.z;
+  z[u] = zu;
+  sv[u] = su;
+  p[u] = pu;
+  x[u] = xu;
+  r[u] = ru;
+  w[u] = wu;
+  mn[u] = block_jacobi<float>(dinv, u, wu.x, wu.y, wu.z);
+  const float4 un = block_jacobi<float>(dinv, u, ru.x, ru.y, ru.z);
+  const float4 is = H.iscale[u];
+  const float t0 = ru.x * is.x, t1 = ru.y * is.y, t2 = ru.z * is.z;
+  part[0] = ru.x * un.x + ru.y * un.y + ru.z * un.z;
+  part[1] = wu.x * un.x + wu.y * un.y + wu.z * un.z;
+  part[2] = t0 * t0 + t1 * t1 + t2 * t2;
+}
+
+__global__ void __launch_bounds__(SB, 5)
+    pipe_half_kernel(HalfMatrix H, const float4* __restrict__ dinv, float4* x, float4* r, float4* z, float4* p,
+                     float4* sv, float4* w, float4* m, int max_iters, Reduce red, GridSync gs, int pipe_iters) {
+  __shared__ double shred[SB / 32][3];
+  __shared__ int sidx[SB / 32][ST_K][32];
+  __shared__ double s_alpha, s_beta;
+  __shared__ int s_done;
+  DevScalars* sc = red.sc;
+  if (threadIdx.x == 0) s_done = *(volatile int*)&sc->done;
+  __syncthreads();
+  if (s_done) return;
+  const int nv = H.nv;
+  const int nvb = (nv + SB - 1) / SB;
+  double* part = red.partials;
+  double* gsum = red.partials + 3 * (size_t)nvb;
+  auto publish = [&](int vb, float (&pr)[3]) {
+    double bs[3];
+    block_sum_s<3, SB, float>(pr, bs, shred);
+    if (threadIdx.x == 0) {
+      part[3 * vb] = bs[0];
+      part[3 * vb + 1] = bs[1];
+      part[3 * vb + 2] = bs[2];
+    }
+    __syncthreads();
+  };
+  // prologue: w = A u0 (u0 = z from the setup), m_0 = M w, the first dots
+  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    const int u = vb * SB + threadIdx.x;
+    float pr[3] = {0.f, 0.f, 0.f};
+    if (u < nv) {
+      float a0, a1, a2;
+      half_row_product(H, u, z, sidx[threadIdx.x >> 5], a0, a1, a2);
+      w[u] = make_float4(a0, a1, a2, 0.f);
+      m[u] = block_jacobi<float>(dinv, u, a0, a1, a2);
+      const float4 uu = z[u], ru = r[u], is = H.iscale[u];
+      const float t0 = ru.x * is.x, t1 = ru.y * is.y, t2 = ru.z * is.z;
+      pr[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
+      pr[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
+      pr[2] = t0 * t0 + t1 * t1 + t2 * t2;
+    }
+    publish(vb, pr);
+  }
+  bool ok = true;
+  for (int k = 0;; ++k) {
+    ok = reduce_barrier<3>(gs, (unsigned long long)k, part, gsum, nvb,
+                           [&](const double (&t)[3]) { cgcg_after(sc, t[0], t[1], t[2], max_iters); });
+    if (!ok) break;
+    if (threadIdx.x == 0) {
+      s_done = __ldcg(&sc->done);
+      s_alpha = __ldcg(&sc->alpha);
+      s_beta = __ldcg(&sc->beta);
+    }
+    __syncthreads();
+    if (s_done) break;
+    const float alpha = (float)s_alpha, beta = (float)s_beta;
+    if (k < pipe_iters) {
+      const float4* mk = m + (size_t)(k & 1) * nv;
+      float4* mn = m + (size_t)((k + 1) & 1) * nv;
+      for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+        float pr[3];
+        pipe_half_row(H, dinv, k == 0, alpha, beta, mk, mn, x, r, z, p, sv, w, vb * SB + threadIdx.x,
+                      sidx[threadIdx.x >> 5], pr);
+        publish(vb, pr);
+      }
+      continue;
+    }
+    // Chronopoulos-Gear from here on (as pipe_persistent_kernel)
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int u = vb * SB + threadIdx.x;
+      if (k == pipe_iters && u < nv) {
+        const float4 ru = r[u];
+        z[u] = block_jacobi<float>(dinv, u, ru.x, ru.y, ru.z);
+      }
+      cgcg_update_row<float>(nv, k == 0, alpha, beta, dinv, z, w, p, sv, x, r, u);
+    }
+    ok = plain_barrier(gs, (unsigned long long)(k - pipe_iters));
+    if (!ok) break;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int u = vb * SB + threadIdx.x;
+      float pr[3] = {0.f, 0.f, 0.f};
+      if (u < nv) {
+        float a0, a1, a2;
+        half_row_product(H, u, z, sidx[threadIdx.x >> 5], a0, a1, a2);
+        w[u] = make_float4(a0, a1, a2, 0.f);
+        const float4 uu = z[u], ru = r[u], is = H.iscale[u];
+        const float t0 = ru.x * is.x, t1 = ru.y * is.y, t2 = ru.z * is.z;
+        pr[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
+        pr[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
+        pr[2] = t0 * t0 + t1 * t1 + t2 * t2;
+      }
+      publish(vb, pr);
+    }
+  }
+  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    const int u = vb * SB + threadIdx.x;
+    if (u < nv) {
+      const float4 xv = x[u], s4 = H.scale[u];
+      x[u] = make_float4(xv.x * s4.x, xv.y * s4.y, xv.z * s4.z, 0.f);
+    }
+  }
+  if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
+}
+
 // Standard PCG in one launch: the two-launch loop's phases (SpMV forming p = z + beta p_old, then the
 // update) separated by reducing grid barriers; the last block runs the same reductions and epilogues as
 // the two-launch kernels, so the iterates are bitwise theirs.
@@ -1623,13 +1771,14 @@ void launch_half_spmv(const HalfMatrix& H, const float4* x, float4* xs, float4* 
 
 bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float4* r, float4* z, float4* p0,
                      float4* p1, float4* q, int max_iters, const Reduce& red, unsigned long long* gsync,
-                     long long spin_limit, int extra, int max_blocks, cudaStream_t st) {
+                     long long spin_limit, int extra, int max_blocks, cudaStream_t st, float4* pm, int pipe_iters) {
   int dev = 0, coop = 0, nsm = 0, per_sm = 0;
   SSIM_CUDA(cudaGetDevice(&dev));
   SSIM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return false;
   SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const void* fn = (const void*)cgcg_half_kernel;
+  const bool pipe = pm != nullptr;
+  const void* fn = pipe ? (const void*)pipe_half_kernel : (const void*)cgcg_half_kernel;
   SSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SB, 0));
   if (per_sm < 1) return false;
   int grid = std::min(div_up(H.nv, SB), per_sm * nsm);
@@ -1650,7 +1799,10 @@ bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float
   Reduce rd = red;
   void* args[] = {(void*)&h,  (void*)&dinv16, (void*)&x, (void*)&r,         (void*)&z,  (void*)&p0,
                   (void*)&p1, (void*)&q,      (void*)&max_iters, (void*)&rd, (void*)&gs};
-  SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), args, 0, st));
+  // pipelined: p = p0, s = p1, w = q, then the two m vectors
+  void* pargs[] = {(void*)&h,  (void*)&dinv16, (void*)&x,  (void*)&r,         (void*)&z,  (void*)&p0, (void*)&p1,
+                   (void*)&q,  (void*)&pm,     (void*)&max_iters, (void*)&rd, (void*)&gs, (void*)&pipe_iters};
+  SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), pipe ? pargs : args, 0, st));
   after_launch("pcg_half");
   return true;
 }

@@ -588,8 +588,8 @@ struct TimeStep {
   // solve would run the persistent Chronopoulos-Gear kernel, and the pattern fits
   bool use_half(double rtol) {
     if (half_off || !mixed() || params.pcg_half_matrix != 1 || !(rtol >= params.half_matrix_min_rtol)) return false;
-    const int variant = params.pcg_persistent == 3 ? 2 : params.pcg_persistent;
-    return variant == 2 && half_ready();
+    const int variant = params.pcg_persistent;
+    return (variant == 2 || variant == 3 || variant == 4) && half_ready();
   }
 
   // material: per element Lame parameters (basic_elast.hpp:10-20) and the stable Neo-Hookean constants
@@ -964,9 +964,14 @@ struct TimeStep {
     const HalfMatrix H = half_matrix();
     launch_pcg_setup_half(H, b, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
     if (profiling) SSIM_CUDA(cudaEventRecord(ev[0], stream));
+    // the automatic choice (3) on the copy is the pipelined iteration: one reducing barrier per iteration
+    // (21.1 against 23.8 us per iteration on the 1.02M-tet beam, the same iteration counts); its FP32
+    // recursive-residual drift is covered by the true-residual check that follows every Newton solve
+    const bool pipe = params.pcg_persistent == 3 || params.pcg_persistent == 4;
+    if (pipe && s.pm.n < 2 * (size_t)nv) s.pm.alloc(2 * (size_t)nv);
     const bool ran = launch_pcg_half(H, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters, red(),
                                      gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra, params.pcg_max_blocks,
-                                     stream);
+                                     stream, pipe ? s.pm.p : nullptr, params.pcg_pipe_iters);
     if (!ran) return false;
     if (profiling) SSIM_CUDA(cudaEventRecord(ev[1], stream));
     sync_scalars();
@@ -1831,7 +1836,9 @@ struct TimeStep {
     int nsm = 0, dev = 0;
     SSIM_CUDA(cudaGetDevice(&dev));
     SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const std::vector<int> variants = mixed() ? std::vector<int>{2, 1} : std::vector<int>{0, 2};
+    // mixed: Chronopoulos-Gear or standard PCG on the FP32 values, and on the FP16 copy (when enabled) the
+    // automatic choice (pipelined, variant 3) or Chronopoulos-Gear
+    const std::vector<int> variants = mixed() ? std::vector<int>{2, 1, 3} : std::vector<int>{0, 2};
     std::vector<int> grids = {0};
     if (4 * nsm < div_up(nv, 256)) grids.push_back(4 * nsm);
     const int keep_variant = params.pcg_persistent, keep_grid = params.pcg_max_blocks;
@@ -1846,7 +1853,8 @@ struct TimeStep {
         for (int half : {0, 1}) {
           if (v == 0 && gcap != 0) continue;  // the two-launch loop has no persistent grid
           // the FP16 copy serves only these, and only when enabled (the sweep may turn it off, never on)
-          if (half && (v != 2 || !mixed() || keep_half != 1 || !half_ready())) continue;
+          if (half && ((v != 2 && v != 3) || !mixed() || keep_half != 1 || !half_ready())) continue;
+          if (v == 3 && !half) continue;  // on the FP32 values variant 3 is variant 2
           params.pcg_persistent = v;
           params.pcg_max_blocks = gcap;
           params.pcg_half_matrix = half;

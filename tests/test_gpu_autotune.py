@@ -35,13 +35,14 @@ def test_autotune_choices_cache_and_states(precision):
     if precision == "mixed":
         assert t["elem_block"] in (64, 128, 256) and t["gather_block"] in (128, 256, 512)
         assert t["elem_regcap"] in (0, 1)
-        assert t["pcg_persistent"] in (1, 2)
+        assert t["pcg_persistent"] in (1, 2, 3)
+        assert t["pcg_persistent"] != 3 or t["pcg_half_matrix"] == 1
     else:
         assert t["pcg_persistent"] in (0, 2)
     assert t["hessian_block"] in (32, 64, 128) and t["assembly_block"] in (128, 256, 512)
     assert t["fused_assembly"] in (0, 1) and t["pcg_solve_ms"] > 0 and t["pcg_iterations"] > 0
     if precision == "mixed":
-        assert t["pcg_half_matrix"] in (0, 1) and (t["pcg_half_matrix"] == 0 or t["pcg_persistent"] == 2)
+        assert t["pcg_half_matrix"] in (0, 1) and (t["pcg_half_matrix"] == 0 or t["pcg_persistent"] in (2, 3))
     assert np.array_equal(ts.get("deformation"), u) and np.array_equal(ts.get("forces"), f)
     p = ts.params
     assert (p.pcg_persistent, p.pcg_max_blocks, p.fused_assembly) == (t["pcg_persistent"], t["pcg_max_blocks"],

@@ -185,3 +185,26 @@ def test_half_fallback_to_fp32_values():
     ts.reset("newton")
     ts.step()
     assert ts.stats()["half_solves"] == 1
+
+
+@pytest.mark.parametrize("pipelined", [3, 4])
+def test_pipelined_pcg_on_half_matrix(pipelined):
+    """pcg_persistent = 3 (automatic, the default) or 4 with the FP16 copy: the pipelined iteration (one
+    reducing barrier per iteration) in the copy's scaled space.  Newton steps converge like the
+    Chronopoulos-Gear solves on the copy (variant 2): states within 1e-5, Newton iterations per step within 1,
+    every solve on the copy."""
+    scene = scenes.beam(40, 20, 14, h=0.05)
+    runs = {}
+    for variant in (pipelined, 2):
+        params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2,
+                                  precond=2, pcg_persistent=variant)
+        ts = scenes.build_timestep(scene, precision="mixed", params=params)
+        newton = []
+        for _ in range(3):
+            ts.step()
+            st = ts.stats()
+            assert st["converged"] == 1 and st["half_solves"] == st["newton_iters"], (variant, st)
+            newton.append(st["newton_iters"])
+        runs[variant] = (ts.get("deformation"), newton)
+    assert rel(runs[pipelined][0], runs[2][0]) <= 1e-5
+    assert all(abs(a - b) <= 1 for a, b in zip(runs[pipelined][1], runs[2][1])), runs
