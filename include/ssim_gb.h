@@ -157,10 +157,9 @@ typedef struct {
   int32_t half_hessian_blocks; /* tets: 1 (default) writes the element Hessian blocks of the assemblies whose solve
                              runs on the FP16 copy in FP16 (a power-of-two scale per 3x3 block, 24 bytes a block
                              instead of 36, three 8-byte loads in the assembly, FP32 sums); 0 keeps FP32 blocks */
-  double half_check_slack; /* after the first four Newton solves on the FP16 copy since reset(), the first solve
-                             of every step and any solve that follows a backtracked line search, the true
-                             residual |g + K d| on the FP32 values is computed with g . d; above
-                             half_check_slack (1.2) times the forcing eta
+  double half_check_slack; /* after every Newton solve on the FP16 copy the true residual |g + K d| on the FP32
+                             values is computed with g . d (one fused kernel, about 25 us more than g . d alone
+                             at 1M tets); above half_check_slack (1.2) times the forcing eta
                              times |g| the copy is too coarse for the system's conditioning and the handle's
                              later solves use the FP32 values (until reset() or ssim_gb_set_params).  Measured
                              ratios: 0.8-1.05 on the beams, bar and cube, up to 1.46 (2.7 with FP32 element

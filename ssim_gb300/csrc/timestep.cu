@@ -319,7 +319,6 @@ ssim_gb_status ssim_gb_set_params(ssim_gb_timestep* h, const ssim_gb_params* p) 
     return fail(h, SSIM_GB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
   h->ts.params = *p;
   h->ts.half_off = false;
-  h->ts.half_checks = 0;
   return SSIM_GB_OK;
 }
 

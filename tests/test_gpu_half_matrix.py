@@ -154,9 +154,8 @@ def test_newton_with_half_hessian_blocks(name):
 
 
 def test_half_solves_reported_and_checked():
-    """Newton solves on the copy are followed by their true residual on the FP32 values (fused with g . d; the
-    first four after reset(), the first of every step, any after a backtracked line search): on a
-    well-conditioned beam every step's solves stay on the copy (half_solves = Newton iterations) and the
+    """Every Newton solve on the copy is followed by its true residual on the FP32 values (fused with g . d):
+    on a well-conditioned beam every step's solves stay on the copy (half_solves = Newton iterations) and the
     checked ratio |g + K d| / (eta |g|) stays near 1."""
     scene = scenes.beam(40, 20, 14, h=0.05)
     params = g.default_params(stop_mode=1, rel_tol=1e-6, cg_forcing=1, cg_rtol=1e-1, cg_eta_min=5e-2, precond=2)
