@@ -280,6 +280,8 @@ SSIM_GB_API ssim_gb_status ssim_gb_set_material(ssim_gb_timestep* h, const doubl
                                     const double* poisson_per_cell);
 
 /* ---- boundary conditions (fem_cuda.cu:115-150, boundary.hpp:13-106) ---- */
+/* The arrays are copied before the call returns (the caller may reuse them at once); the upload and the
+ * marking run on the handle's stream ahead of its next work, without a host wait. */
 SSIM_GB_API ssim_gb_status ssim_gb_mark_dirichlet_batched(ssim_gb_timestep* h, const int32_t* verts, int32_t n,
                                               const double* targ_deform /* [n,3] */);
 SSIM_GB_API ssim_gb_status ssim_gb_mark_general_batched(ssim_gb_timestep* h, const int32_t* verts, int32_t n);

@@ -361,11 +361,15 @@ ssim_gb_status ssim_gb_mark_dirichlet_batched(ssim_gb_timestep* h, const int32_t
   if (n == 0) return SSIM_GB_OK;
   if (t.mark_verts.n < (size_t)n) t.mark_verts.alloc(n);
   if (t.mark_targ.n < 3 * (size_t)n) t.mark_targ.alloc(3 * (size_t)n);
-  SSIM_CUDA(cudaMemcpyAsync(t.mark_verts.p, verts, sizeof(int32_t) * n, cudaMemcpyHostToDevice, t.stream));
-  SSIM_CUDA(cudaMemcpyAsync(t.mark_targ.p, targ, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, t.stream));
+  // the caller's arrays are copied before the return; the upload and the marking run on the handle's
+  // stream ahead of the next step without a host wait
+  t.stage_marks(verts, targ, n);
+  SSIM_CUDA(cudaMemcpyAsync(t.mark_verts.p, t.mark_verts_h, sizeof(int32_t) * n, cudaMemcpyHostToDevice, t.stream));
+  SSIM_CUDA(cudaMemcpyAsync(t.mark_targ.p, t.mark_targ_h, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, t.stream));
+  SSIM_CUDA(cudaEventRecord(t.ev_mark, t.stream));
+  t.mark_in_flight = true;
   ssim_gb::launch_mark_dofs(n, t.mark_verts.p, t.mark_targ.p, 1, t.dof_type.p, t.dbc_values.p, t.stream);
   ssim_gb::launch_build_mask(t.nv, t.dof_type.p, t.mask.p, t.stream);
-  SSIM_CUDA(cudaStreamSynchronize(t.stream));
   API_CATCH(h)
 }
 

@@ -91,6 +91,30 @@ struct TimeStep {
   double mass_third = 0;  // sum |M_ij| / 3, the reference threshold's scale (abs_tol = rtol * mass_third)
   DBuf<int32_t> mark_verts;  // scratch of the mark_* calls (grown, never shrunk)
   DBuf<double> mark_targ;
+  // pinned staging of the Dirichlet marks: the call copies the caller's arrays here and returns without
+  // waiting for the upload (the next upload waits for this one's event before it reuses the staging)
+  int32_t* mark_verts_h = nullptr;
+  double* mark_targ_h = nullptr;
+  size_t mark_cap_h = 0;
+  cudaEvent_t ev_mark = nullptr;
+  bool mark_in_flight = false;
+  void stage_marks(const int32_t* verts, const double* targ, int n) {
+    if (mark_in_flight) SSIM_CUDA(cudaEventSynchronize(ev_mark));
+    mark_in_flight = false;
+    if ((size_t)n > mark_cap_h) {
+      if (mark_verts_h) cudaFreeHost(mark_verts_h);
+      if (mark_targ_h) cudaFreeHost(mark_targ_h);
+      mark_verts_h = nullptr;
+      mark_targ_h = nullptr;
+      mark_cap_h = 0;
+      SSIM_CUDA(cudaMallocHost((void**)&mark_verts_h, sizeof(int32_t) * n));
+      SSIM_CUDA(cudaMallocHost((void**)&mark_targ_h, sizeof(double) * 3 * n));
+      mark_cap_h = n;
+    }
+    if (!ev_mark) SSIM_CUDA(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming));
+    std::memcpy(mark_verts_h, verts, sizeof(int32_t) * n);
+    std::memcpy(mark_targ_h, targ, sizeof(double) * 3 * n);
+  }
   int precision = SSIM_GB_FP64;
   int stepper = SSIM_GB_STEPPER_NONE;
   ssim_gb_params params{};
@@ -318,6 +342,10 @@ struct TimeStep {
   double prof_bytes[PK_COUNT] = {0};
 
   ~TimeStep() {
+    if (mark_in_flight && ev_mark) cudaEventSynchronize(ev_mark);  // the staging is not freed under the upload
+    if (mark_verts_h) cudaFreeHost(mark_verts_h);
+    if (mark_targ_h) cudaFreeHost(mark_targ_h);
+    if (ev_mark) cudaEventDestroy(ev_mark);
     if (side) cudaStreamSynchronize(side);
     if (side) cudaStreamDestroy(side);
     if (ev_dir) cudaEventDestroy(ev_dir);
