@@ -301,12 +301,25 @@ void launch_pcg_setup_half(const HalfMatrix& H, const double* b, const float4* d
                            float4* p0, double rtol, int max_iters, bool negate, const Reduce& red, cudaStream_t st);
 // Chronopoulos-Gear PCG on the FP16 copy in one cooperative launch (as launch_pcg_persistent variant 2);
 // x holds the unscaled solution on return.  false if the device cannot launch it cooperatively.
-// pm non-null: pipelined PCG (pipe_persistent_kernel's scheme, 2 nv vectors of scratch in pm) for pipe_iters
-// iterations, then Chronopoulos-Gear
+// the pipelined solve on the copy does its own set-up and, with check set, the solve's check on the FP32
+// symmetric store (A32, vals32): g . x, |x|^2, |sign b - K x|^2, |b|^2 into sc->gd, dnorm2, true_rr, true_bb
+struct HalfSolveArgs {
+  const double* b;  // right-hand side sign * b (the Newton gradient g with negate = 1)
+  int negate;
+  double rtol;
+  int max_iters;
+  int pipe_iters;  // pipelined iterations before Chronopoulos-Gear
+  int check;
+  SellMatrix A32;
+  const float* vals32;
+};
+// pm and pa non-null: the pipelined solve (pipe_persistent_kernel's scheme, 2 nv vectors of scratch in pm)
+// with its set-up and check in the same launch (no launch_pcg_setup_half before it); otherwise
+// Chronopoulos-Gear after launch_pcg_setup_half
 bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float4* r, float4* z, float4* p0,
                      float4* p1, float4* q, int max_iters, const Reduce& red, unsigned long long* gsync,
                      long long spin_limit, int extra, int max_blocks, cudaStream_t st, float4* pm = nullptr,
-                     int pipe_iters = 0);
+                     const HalfSolveArgs* pa = nullptr);
 // after a solve on the FP16 copy: g . d, |d|^2 (as launch_dot_gd) and the solve's true residual on the FP32
 // symmetric values, |-g - K d|^2 and |g|^2 (sc->true_rr, sc->true_bb)
 void launch_dot_gd_check(const SellMatrix& A, const float* vals, const double* g, const float4* d, const Reduce& red,

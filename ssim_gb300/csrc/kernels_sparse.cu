@@ -1158,21 +1158,26 @@ __device__ __forceinline__ void pipe_half_row(const HalfMatrix& H, const float4*
   part[2] = t0 * t0 + t1 * t1 + t2 * t2;
 }
 
+// The whole solve on the copy in one launch: the set-up (x = 0, r~ = S (sign b), u0 = M r~; a plain
+// barrier orders u0 before the prologue's SpMV), the pipelined iterations (Chronopoulos-Gear after
+// pipe_iters), x unscaled, and, when a.check is set, the solve's check on the FP32 symmetric store: g . x,
+// |x|^2, |sign b - K x|^2 and |b|^2 (b = the Newton gradient g, sign = -1) into sc->gd, dnorm2, true_rr,
+// true_bb.  Barriers are numbered by their own counters (the plain ones, the reducing ones) in the order
+// every block meets them.
 __global__ void __launch_bounds__(SB, 5)
     pipe_half_kernel(HalfMatrix H, const float4* __restrict__ dinv, float4* x, float4* r, float4* z, float4* p,
-                     float4* sv, float4* w, float4* m, int max_iters, Reduce red, GridSync gs, int pipe_iters) {
+                     float4* sv, float4* w, float4* m, HalfSolveArgs a, Reduce red, GridSync gs) {
   __shared__ double shred[SB / 32][3];
+  __shared__ double shred4[SB / 32][4];
   __shared__ int sidx[SB / 32][ST_K][32];
   __shared__ double s_alpha, s_beta;
   __shared__ int s_done;
   DevScalars* sc = red.sc;
-  if (threadIdx.x == 0) s_done = *(volatile int*)&sc->done;
-  __syncthreads();
-  if (s_done) return;
   const int nv = H.nv;
   const int nvb = (nv + SB - 1) / SB;
   double* part = red.partials;
   double* gsum = red.partials + 3 * (size_t)nvb;
+  double* gsum4 = red.partials + 4 * (size_t)nvb;
   auto publish = [&](int vb, float (&pr)[3]) {
     double bs[3];
     block_sum_s<3, SB, float>(pr, bs, shred);
@@ -1183,27 +1188,55 @@ __global__ void __launch_bounds__(SB, 5)
     }
     __syncthreads();
   };
-  // prologue: w = A u0 (u0 = z from the setup), m_0 = M w, the first dots
+  const double sg = a.negate ? -1.0 : 1.0;
+  unsigned long long npb = 0, nrb = 0;
+  // set-up (pcg_setup_half_kernel's per-row work)
   for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
     const int u = vb * SB + threadIdx.x;
-    float pr[3] = {0.f, 0.f, 0.f};
     if (u < nv) {
-      float a0, a1, a2;
-      half_row_product(H, u, z, sidx[threadIdx.x >> 5], a0, a1, a2);
-      w[u] = make_float4(a0, a1, a2, 0.f);
-      m[u] = block_jacobi<float>(dinv, u, a0, a1, a2);
-      const float4 uu = z[u], ru = r[u], is = H.iscale[u];
-      const float t0 = ru.x * is.x, t1 = ru.y * is.y, t2 = ru.z * is.z;
-      pr[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
-      pr[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
-      pr[2] = t0 * t0 + t1 * t1 + t2 * t2;
+      const float r0 = (float)(sg * a.b[u * 3 + 0]), r1 = (float)(sg * a.b[u * 3 + 1]),
+                  r2 = (float)(sg * a.b[u * 3 + 2]);
+      const float4 s4 = H.scale[u];
+      const float t0 = r0 * s4.x, t1 = r1 * s4.y, t2 = r2 * s4.z;
+      x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      r[u] = make_float4(t0, t1, t2, 0.f);
+      z[u] = block_jacobi<float>(dinv, u, t0, t1, t2);
+      p[u] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    publish(vb, pr);
   }
-  bool ok = true;
-  for (int k = 0;; ++k) {
-    ok = reduce_barrier<3>(gs, (unsigned long long)k, part, gsum, nvb,
-                           [&](const double (&t)[3]) { cgcg_after(sc, t[0], t[1], t[2], max_iters); });
+  bool ok = plain_barrier(gs, npb++);
+  // prologue: w = A u0, m_0 = M w, the first dots
+  if (ok) {
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int u = vb * SB + threadIdx.x;
+      float pr[3] = {0.f, 0.f, 0.f};
+      if (u < nv) {
+        float a0, a1, a2;
+        half_row_product(H, u, z, sidx[threadIdx.x >> 5], a0, a1, a2);
+        w[u] = make_float4(a0, a1, a2, 0.f);
+        m[u] = block_jacobi<float>(dinv, u, a0, a1, a2);
+        const float4 uu = z[u], ru = r[u], is = H.iscale[u];
+        const float t0 = ru.x * is.x, t1 = ru.y * is.y, t2 = ru.z * is.z;
+        pr[0] = ru.x * uu.x + ru.y * uu.y + ru.z * uu.z;
+        pr[1] = a0 * uu.x + a1 * uu.y + a2 * uu.z;
+        pr[2] = t0 * t0 + t1 * t1 + t2 * t2;
+      }
+      publish(vb, pr);
+    }
+  }
+  for (int k = 0; ok; ++k) {
+    const bool first = k == 0;
+    ok = reduce_barrier<3>(gs, nrb++, part, gsum, nvb, [&](const double (&t)[3]) {
+      if (first) {  // the set-up's scalars: the stop test is relative to this residual
+        sc->done = 0;
+        sc->rz_old = 1.0;
+        sc->rr0 = t[2];
+        sc->tol2 = a.rtol * a.rtol * t[2];
+        sc->iters = 0;
+        sc->status = 0;
+      }
+      cgcg_after(sc, t[0], t[1], t[2], a.max_iters);
+    });
     if (!ok) break;
     if (threadIdx.x == 0) {
       s_done = __ldcg(&sc->done);
@@ -1213,7 +1246,7 @@ __global__ void __launch_bounds__(SB, 5)
     __syncthreads();
     if (s_done) break;
     const float alpha = (float)s_alpha, beta = (float)s_beta;
-    if (k < pipe_iters) {
+    if (k < a.pipe_iters) {
       const float4* mk = m + (size_t)(k & 1) * nv;
       float4* mn = m + (size_t)((k + 1) & 1) * nv;
       for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
@@ -1227,13 +1260,13 @@ __global__ void __launch_bounds__(SB, 5)
     // Chronopoulos-Gear from here on (as pipe_persistent_kernel)
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       const int u = vb * SB + threadIdx.x;
-      if (k == pipe_iters && u < nv) {
+      if (k == a.pipe_iters && u < nv) {
         const float4 ru = r[u];
         z[u] = block_jacobi<float>(dinv, u, ru.x, ru.y, ru.z);
       }
       cgcg_update_row<float>(nv, k == 0, alpha, beta, dinv, z, w, p, sv, x, r, u);
     }
-    ok = plain_barrier(gs, (unsigned long long)(k - pipe_iters));
+    ok = plain_barrier(gs, npb++);
     if (!ok) break;
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       const int u = vb * SB + threadIdx.x;
@@ -1251,12 +1284,44 @@ __global__ void __launch_bounds__(SB, 5)
       publish(vb, pr);
     }
   }
+  // x = S x~ (rows of this block only)
   for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
     const int u = vb * SB + threadIdx.x;
     if (u < nv) {
       const float4 xv = x[u], s4 = H.scale[u];
       x[u] = make_float4(xv.x * s4.x, xv.y * s4.y, xv.z * s4.z, 0.f);
     }
+  }
+  // the check on the FP32 values: every block's x is final after a plain barrier
+  if (ok && a.check) ok = plain_barrier(gs, npb++);
+  if (ok && a.check) {
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int u = vb * SB + threadIdx.x;
+      double pr[4] = {0, 0, 0, 0};
+      if (u < nv) {
+        float a0, a1, a2;
+        row_product_t<float, true>(a.A32, a.vals32, u, x, nullptr, 0.f, sidx[threadIdx.x >> 5], a0, a1, a2);
+        const float4 dv = x[u];
+        const double g0 = a.b[u * 3 + 0], g1 = a.b[u * 3 + 1], g2 = a.b[u * 3 + 2];
+        pr[0] = g0 * (double)dv.x + g1 * (double)dv.y + g2 * (double)dv.z;
+        pr[1] = (double)dv.x * dv.x + (double)dv.y * dv.y + (double)dv.z * dv.z;
+        const double q0 = sg * g0 - (double)a0, q1 = sg * g1 - (double)a1, q2 = sg * g2 - (double)a2;
+        pr[2] = q0 * q0 + q1 * q1 + q2 * q2;
+        pr[3] = g0 * g0 + g1 * g1 + g2 * g2;
+      }
+      block_sum<4, SB>(pr, shred4);
+      if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) part[4 * vb + c] = pr[c];
+      }
+      __syncthreads();
+    }
+    ok = reduce_barrier<4>(gs, nrb++, part, gsum4, nvb, [&](const double (&t)[4]) {
+      sc->gd = t[0];
+      sc->dnorm2 = t[1];
+      sc->true_rr = t[2];
+      sc->true_bb = t[3];
+    });
   }
   if (!ok && threadIdx.x == 0) atomicExch(&sc->wait_failed, 1);
 }
@@ -1771,13 +1836,14 @@ void launch_half_spmv(const HalfMatrix& H, const float4* x, float4* xs, float4* 
 
 bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float4* r, float4* z, float4* p0,
                      float4* p1, float4* q, int max_iters, const Reduce& red, unsigned long long* gsync,
-                     long long spin_limit, int extra, int max_blocks, cudaStream_t st, float4* pm, int pipe_iters) {
+                     long long spin_limit, int extra, int max_blocks, cudaStream_t st, float4* pm,
+                     const HalfSolveArgs* pa) {
   int dev = 0, coop = 0, nsm = 0, per_sm = 0;
   SSIM_CUDA(cudaGetDevice(&dev));
   SSIM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return false;
   SSIM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const bool pipe = pm != nullptr;
+  const bool pipe = pm != nullptr && pa != nullptr;
   const void* fn = pipe ? (const void*)pipe_half_kernel : (const void*)cgcg_half_kernel;
   SSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SB, 0));
   if (per_sm < 1) return false;
@@ -1800,8 +1866,10 @@ bool launch_pcg_half(const HalfMatrix& H, const float4* dinv16, float4* x, float
   void* args[] = {(void*)&h,  (void*)&dinv16, (void*)&x, (void*)&r,         (void*)&z,  (void*)&p0,
                   (void*)&p1, (void*)&q,      (void*)&max_iters, (void*)&rd, (void*)&gs};
   // pipelined: p = p0, s = p1, w = q, then the two m vectors
-  void* pargs[] = {(void*)&h,  (void*)&dinv16, (void*)&x,  (void*)&r,         (void*)&z,  (void*)&p0, (void*)&p1,
-                   (void*)&q,  (void*)&pm,     (void*)&max_iters, (void*)&rd, (void*)&gs, (void*)&pipe_iters};
+  HalfSolveArgs ha{};
+  if (pa) ha = *pa;
+  void* pargs[] = {(void*)&h, (void*)&dinv16, (void*)&x,  (void*)&r,  (void*)&z, (void*)&p0,
+                   (void*)&p1, (void*)&q,     (void*)&pm, (void*)&ha, (void*)&rd, (void*)&gs};
   SSIM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(SB), pipe ? pargs : args, 0, st));
   after_launch("pcg_half");
   return true;

@@ -157,6 +157,7 @@ struct TimeStep {
   long long nfs = 0;
   long long asm_count = 0, h16_count = -1;  // assemblies of the FP32 values; the one the copy was made from
   bool last_half = false;  // the last pcg() ran on the FP16 copy
+  bool half_checked = false;  // ... and its kernel left g . d, |d|^2 and the true residual in the scalars
   // speculative assembly (speculative_hessian): the next Newton iteration's Hessian at the full step, built on
   // a second stream while the line search runs on the handle's stream
   cudaStream_t side = nullptr;
@@ -990,17 +991,24 @@ struct TimeStep {
     Solver<float>& s = sf;
     half_refresh();
     const HalfMatrix H = half_matrix();
-    launch_pcg_setup_half(H, b, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
-    if (profiling) SSIM_CUDA(cudaEventRecord(ev[0], stream));
     // the automatic choice (3) on the copy is the pipelined iteration: one reducing barrier per iteration
     // (21.1 against 23.8 us per iteration on the 1.02M-tet beam, the same iteration counts); its FP32
-    // recursive-residual drift is covered by the true-residual check that follows every Newton solve
-    const bool pipe = params.pcg_persistent == 3 || params.pcg_persistent == 4;
-    if (pipe && s.pm.n < 2 * (size_t)nv) s.pm.alloc(2 * (size_t)nv);
+    // recursive-residual drift is covered by the true-residual check of every Newton solve, which that
+    // kernel runs itself after the solve (with its set-up before it: one launch, one host wait)
+    const bool pipe = (params.pcg_persistent == 3 || params.pcg_persistent == 4) && max_iters > 0;
+    half_checked = false;
+    HalfSolveArgs ha{b, negate ? 1 : 0, eta, max_iters, params.pcg_pipe_iters, negate ? 1 : 0, A(), s.vals.p};
+    if (pipe) {
+      if (s.pm.n < 2 * (size_t)nv) s.pm.alloc(2 * (size_t)nv);
+    } else {
+      launch_pcg_setup_half(H, b, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, eta, max_iters, negate, red(), stream);
+    }
+    if (profiling) SSIM_CUDA(cudaEventRecord(ev[0], stream));
     const bool ran = launch_pcg_half(H, h16dinv.p, s.x.p, s.r.p, s.z.p, s.p0.p, s.p1.p, s.q.p, max_iters, red(),
                                      gsync.p, params.pcg_spin_limit, params.pcg_barrier_extra, params.pcg_max_blocks,
-                                     stream, pipe ? s.pm.p : nullptr, params.pcg_pipe_iters);
+                                     stream, pipe ? s.pm.p : nullptr, pipe ? &ha : nullptr);
     if (!ran) return false;
+    half_checked = pipe && ha.check;
     if (profiling) SSIM_CUDA(cudaEventRecord(ev[1], stream));
     sync_scalars();
     if (hsc->wait_failed) throw device_timeout("a grid-barrier wait of the persistent PCG kernel gave up");
@@ -1450,15 +1458,17 @@ struct TimeStep {
       // after reset(), the first of each step) let the copy cost it a fifth more Newton iterations
       const bool checked = last_half;
       st.half_solves += last_half ? 1 : 0;
-      if constexpr (std::is_same<S, float>::value) {
-        if (checked)
-          launch_dot_gd_check(A(), s.vals.p, forces.p, s.x.p, red(), stream);
-        else
+      if (!(checked && half_checked)) {  // the pipelined solve on the copy did this in its own launch
+        if constexpr (std::is_same<S, float>::value) {
+          if (checked)
+            launch_dot_gd_check(A(), s.vals.p, forces.p, s.x.p, red(), stream);
+          else
+            launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
+        } else {
           launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
-      } else {
-        launch_dot_gd<S>(nv, forces.p, s.x.p, red(), stream);
+        }
+        sync_scalars();
       }
-      sync_scalars();
       // a solve on the FP16 copy whose true residual (FP32 values) misses the forcing by the slack: the copy's
       // rounding is too coarse for this system's conditioning; later solves use the FP32 values
       const double tr_max = params.half_check_slack * eta;
