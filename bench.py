@@ -431,8 +431,10 @@ def bench_config(scene, stepper, world):
     return {
         "workload": scene["name"], cells_key: T, "vertices": V, "dofs": 3 * V, "stepper": stepper,
         "solver": SOLVER_TEXT.get(stepper, f"{stepper}, stop |g| <= 1e-6 |g0| (per instance for batches)"),
-        "precision": "GPU value: FP32 Hessian/assembly/PCG vectors with FP64 energy/gradient/state/dots; "
-                     "fp64_plain and the CPU reference: FP64 throughout",
+        "precision": "GPU value: FP32 arithmetic for the Hessian, assembly and PCG (the Newton solves on an FP16 "
+                     "copy of the Jacobi-scaled matrix, each checked on the FP32 values; FP16 element blocks for "
+                     "their assemblies) with FP64 energy/gradient/state/dots; fp64_plain and the CPU reference: "
+                     "FP64 throughout",
         "parallelism": "replicas" if world > 1 else "1 GPU",
         "l2": "working set per step ~1 GB > L2 (no explicit flush)",
     }
