@@ -217,6 +217,9 @@ typedef struct ssim_gb_timestep ssim_gb_timestep;
 SSIM_GB_API const char* ssim_gb_version(void);
 /* count of CUDA kernels this library has launched in this process */
 SSIM_GB_API uint64_t ssim_gb_launch_count(void);
+/* ABI check for bindings that mirror the public structs: sizeof of ssim_gb_params (0), ssim_gb_step_stats (1)
+ * and ssim_gb_tuning (2); 0 for anything else.  Needs no GPU. */
+SSIM_GB_API size_t ssim_gb_struct_size(int32_t which);
 SSIM_GB_API void ssim_gb_default_params(ssim_gb_params* p);
 SSIM_GB_API const char* ssim_gb_last_error(const ssim_gb_timestep* h);
 

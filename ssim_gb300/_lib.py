@@ -144,6 +144,7 @@ _I = C.POINTER(C.c_int32)
 _SIGS = {
     "ssim_gb_version": (C.c_char_p, []),
     "ssim_gb_launch_count": (C.c_uint64, []),
+    "ssim_gb_struct_size": (C.c_size_t, [C.c_int32]),
     "ssim_gb_default_params": (None, [C.POINTER(Params)]),
     "ssim_gb_last_error": (C.c_char_p, [_H]),
     "ssim_gb_mesh_csr_nnz": (C.c_int, [_I, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),

@@ -119,6 +119,15 @@ const char* ssim_gb_version(void) { return "ssim_gb300 0.1.0 (sm_103a)"; }
 
 uint64_t ssim_gb_launch_count(void) { return ssim_gb::g_launches.load(); }
 
+size_t ssim_gb_struct_size(int32_t which) {
+  switch (which) {
+    case 0: return sizeof(ssim_gb_params);
+    case 1: return sizeof(ssim_gb_step_stats);
+    case 2: return sizeof(ssim_gb_tuning);
+    default: return 0;
+  }
+}
+
 void ssim_gb_default_params(ssim_gb_params* p) {
   if (!p) return;
   p->max_newton_iters = 1000;

@@ -123,11 +123,16 @@ def _header_struct_fields(name):
     return re.findall(r"^\s*(int32_t|int64_t|double)\s+(\w+);", m.group(1), flags=re.M)
 
 
-@pytest.mark.parametrize("cname, pycls", [("ssim_gb_params", _lib.Params), ("ssim_gb_step_stats", _lib.StepStats)])
-def test_ctypes_structs_mirror_header(cname, pycls):
+@pytest.mark.parametrize("cname, pycls, which", [("ssim_gb_params", _lib.Params, 0),
+                                                 ("ssim_gb_step_stats", _lib.StepStats, 1),
+                                                 ("ssim_gb_tuning", _lib.Tuning, 2)])
+def test_ctypes_structs_mirror_header(cname, pycls, which):
     ctype = {"int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64, "double": ctypes.c_double}
     hdr = [(f, ctype[t]) for t, f in _header_struct_fields(cname)]
     assert hdr == list(pycls._fields_)
+    # the compiled library's layout (padding included) is the ctypes one
+    assert _lib.lib().ssim_gb_struct_size(which) == ctypes.sizeof(pycls)
+    assert _lib.lib().ssim_gb_struct_size(7) == 0
     # the library's defaults round-trip through the Python struct
     p = g.default_params()
     assert p.pcg_persistent == 3 and p.pcg_barrier_extra == 0 and p.pcg_spin_limit == 0
