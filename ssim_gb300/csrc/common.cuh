@@ -167,6 +167,15 @@ __device__ __forceinline__ void warp_top_sum(const double* gsums, int ngroups, d
   }
 }
 
+// one block's arrival at the end-of-kernel reductions: an acquire-release atomic at GPU scope publishes the
+// block's partials (release) and lets the last arrival see every earlier block's (acquire; the atomics on
+// the counter chain them), with no separate fences
+__device__ __forceinline__ unsigned int atom_inc_acq_rel_gpu(unsigned int* p) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
 // grid_sum_last with the tree order above: the last block's warps sum the groups (group sums in gscratch,
 // ceil(grid / 32) * NV doubles), then warp 0 the group sums.  true in thread 0 of the last block.
 template <int NV, int BLOCK>
@@ -176,13 +185,10 @@ __device__ __forceinline__ bool grid_sum_last_tree(const double (&blockval)[NV],
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) partials[blockIdx.x * NV + k] = blockval[k];
-    __threadfence();
-    const unsigned int t = atomicAdd(counter, 1u);
-    am_last = (t == gridDim.x - 1);
+    am_last = (atom_inc_acq_rel_gpu(counter) == gridDim.x - 1);
   }
   __syncthreads();
   if (!am_last) return false;
-  __threadfence();
   const int nparts = (int)gridDim.x, ngroups = (nparts + 31) / 32, warp = threadIdx.x >> 5;
   for (int g = warp; g < ngroups; g += BLOCK / 32) {
     double v[NV];
@@ -215,13 +221,10 @@ __device__ __forceinline__ bool grid_sum_last(const double (&blockval)[NV], doub
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) partials[blockIdx.x * NV + k] = blockval[k];
-    __threadfence();
-    const unsigned int t = atomicAdd(counter, 1u);
-    am_last = (t == gridDim.x - 1);
+    am_last = (atom_inc_acq_rel_gpu(counter) == gridDim.x - 1);
   }
   __syncthreads();
   if (!am_last) return false;
-  __threadfence();
   double acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) acc[k] = 0;

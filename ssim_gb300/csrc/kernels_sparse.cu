@@ -500,10 +500,18 @@ __device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long
 __device__ __forceinline__ void st_release_gpu(unsigned long long* p, unsigned long long v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-// The barriers' fences: acquire-release at GPU scope (a release pattern before each arrival, an acquire
-// pattern after each observed completion), lighter than the sequentially consistent __threadfence: 9.4
-// against 10.0 us per reducing + plain barrier pair on 705 blocks of a GB300 (micro-benchmark)
-__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+// The barriers' ordering: every arrival is one acquire-release atomic at GPU scope (its release half
+// publishes the block's writes and partials, its acquire half lets the arrival that completes a count see
+// every earlier arrival's writes: the atomics on one counter chain them in observation order), the
+// completion is one release store and the waiters poll with acquire loads.  No separate fences: 6.3 against
+// 8.1 us per reducing barrier on 705 blocks of a GB300 with fence.acq_rel around relaxed atomics, and 7.3
+// with release atomics plus a fence in the completing arrival (micro-benchmark; each fence waits for a
+// round trip to L2)
+__device__ __forceinline__ unsigned long long atom_add_acq_rel_gpu(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
 
 // thread 0 polls *p until it reaches target (at most spin_limit polls); true if it did
 __device__ __forceinline__ bool wait_at_least(const unsigned long long* p, unsigned long long target,
@@ -513,7 +521,6 @@ __device__ __forceinline__ bool wait_at_least(const unsigned long long* p, unsig
     if (++n > spin_limit) return false;
     __nanosleep(32);
   }
-  fence_acq_rel_gpu();
   return true;
 }
 
@@ -523,12 +530,8 @@ __device__ __forceinline__ bool plain_barrier(const GridSync& gs, unsigned long 
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    fence_acq_rel_gpu();
     const unsigned long long target = (k + 1) * (unsigned long long)(gridDim.x + gs.extra);
-    if (atomicAdd(gs.arrive, 1ull) == target - 1) {
-      fence_acq_rel_gpu();
-      st_release_gpu(gs.prelease, k + 1);
-    }
+    if (atom_add_acq_rel_gpu(gs.arrive, 1ull) == target - 1) st_release_gpu(gs.prelease, k + 1);
     ok = wait_at_least(gs.prelease, k + 1, gs.spin_limit);
   }
   __syncthreads();
@@ -550,11 +553,9 @@ __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long
     for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       const int g = vb >> 5, gsize = min(32, nvb - 32 * g);
       int last = 0;
-      if (lane == 0) {
-        fence_acq_rel_gpu();
-        last = atomicAdd(gs.group + (size_t)g * kSyncStride, 1ull) == (kr + 1) * (unsigned long long)gsize - 1;
-        if (last) fence_acq_rel_gpu();
-      }
+      if (lane == 0)
+        last = atom_add_acq_rel_gpu(gs.group + (size_t)g * kSyncStride, 1ull) ==
+               (kr + 1) * (unsigned long long)gsize - 1;
       last = __shfl_sync(0xffffffffu, last, 0);
       __syncwarp();
       if (!last) continue;
@@ -564,9 +565,7 @@ __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long
       if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) gsum[g * NV + k] = v[k];
-        fence_acq_rel_gpu();
-        top = atomicAdd(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
-        if (top) fence_acq_rel_gpu();
+        top = atom_add_acq_rel_gpu(gs.top, 1ull) == (kr + 1) * (unsigned long long)(gs.ngroups + gs.extra) - 1;
       }
       top = __shfl_sync(0xffffffffu, top, 0);
       __syncwarp();
@@ -575,7 +574,6 @@ __device__ __forceinline__ bool reduce_barrier(const GridSync& gs, unsigned long
       warp_top_sum<NV>(gsum, gs.ngroups, tot);
       if (lane == 0) {
         epi(tot);
-        fence_acq_rel_gpu();
         st_release_gpu(gs.release, kr + 1);
       }
     }
