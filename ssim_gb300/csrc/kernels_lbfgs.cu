@@ -185,17 +185,15 @@ __global__ void __launch_bounds__(LB)
     for (int w = 0; w < LB / 32; ++w) b += shred[w][threadIdx.x];
     partials[(size_t)blockIdx.x * NV + threadIdx.x] = b;
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();  // orders the partials before thread 0's release
+  if (threadIdx.x == 0) am_last = (atom_inc_acq_rel_gpu(counter) == gridDim.x - 1);
   __syncthreads();
   if (!am_last) return;
-  __threadfence();
   {  // LB / NV groups of threads each sum every (LB / NV)-th block's partials, then the groups in order
     constexpr int G = LB / NV;
     const int k = threadIdx.x % NV, grp = threadIdx.x / NV;
     double t = 0;
-    for (int b = grp; b < (int)gridDim.x; b += G) t += partials[(size_t)b * NV + k];
+    for (int b = grp; b < (int)gridDim.x; b += G) t += __ldcg(partials + (size_t)b * NV + k);
     shred[grp][k] = t;
     __syncthreads();
     if (threadIdx.x < NV) {
