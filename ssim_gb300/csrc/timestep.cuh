@@ -1195,11 +1195,17 @@ struct TimeStep {
     double gamma = 0.0;     // s.y / y.y of the newest pair
     int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
     // mixed precision: FP32 element / spring arithmetic until the residual is within elem32_switch times
-    // the target or a line search runs out, FP64 after that and for the stopping test
+    // the target, a line search runs out or the residual stops falling (its best value not halved in
+    // kLbfgsStall32 iterations: the FP32 rounding floor of the O(|g0|) forces can lie above the switch, where
+    // the trials' energy slack keeps accepting steps), FP64 after that and for the stopping test
+    constexpr int kLbfgsStall32 = 100;
     bool e32 = mixed() && params.mixed_elem32 != 0, e32_stall = false;
+    double best32 = 0.0;
+    int since32 = 0;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
+    best32 = gn;
     st.grad_norm0 = g0;
     start_instances();
     SSIM_CUDA(cudaMemcpyAsync(gprev.p, forces.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
@@ -1322,6 +1328,14 @@ struct TimeStep {
       gn = std::sqrt(hsc->gnorm2);
       if (!std::isfinite(E0) || !std::isfinite(gn))
         throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
+      if (e32) {
+        if (gn < 0.5 * best32) {
+          best32 = gn;
+          since32 = 0;
+        } else if (++since32 >= kLbfgsStall32) {
+          e32_stall = true;
+        }
+      }
       const double sy = hsc->pair_sy, yy = hsc->pair_yy;
       if (sy > 1e-300) {
         rho_h[head] = 1.0 / sy;

@@ -422,6 +422,27 @@ def test_lbfgs_mixed_reaches_residual():
         assert st["converged"] == 1 and st["grad_norm"] <= 1e-6 * st["grad_norm0"]
 
 
+def test_lbfgs_mixed_leaves_a_stalled_fp32_phase():
+    """Mixed L-BFGS with a target (1e-8 |g0|) below what FP32 element arithmetic resolves and the FP32 phase
+    allowed down to the target itself (elem32_switch = 1): the phase ends once its residual stops falling
+    (the best |g| not halved in 100 iterations), FP64 evaluations finish, every step converges (the
+    relative target or the absolute floor stop_floor, whichever is larger) in far fewer than the iteration
+    cap, and the state matches the all-FP64-evaluation run's."""
+    scene = scenes.cube10()
+    states = []
+    for e32 in (1, 0):
+        params = g.default_params(stop_mode=1, rel_tol=1e-8, max_lbfgs_iters=20000, mixed_elem32=e32,
+                                  elem32_switch=1.0)
+        ts = scenes.build_timestep(scene, precision="mixed", stepper="lbfgs", params=params)
+        for _ in range(2):
+            ts.step()
+            st = ts.stats()
+            assert st["converged"] == 1 and st["grad_norm"] <= 1e-7 * st["grad_norm0"], (e32, st)
+            assert st["newton_iters"] < 5000, (e32, st)
+        states.append(ts.get("deformation"))
+    assert rel(states[0], states[1]) <= 1e-6
+
+
 def test_forward_euler_matches_oracle():
     """time_step_solver_forward_euler (time_step.hpp:717-736) restated: one explicit update per step."""
     from oracle import pyoracle
