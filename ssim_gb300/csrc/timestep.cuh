@@ -1195,13 +1195,16 @@ struct TimeStep {
     double gamma = 0.0;     // s.y / y.y of the newest pair
     int hsize = 0, head = 0;  // ring: entries head-hsize .. head-1 (mod m), oldest first
     // mixed precision: FP32 element / spring arithmetic until the residual is within elem32_switch times
-    // the target, a line search runs out or the residual stops falling (its best value not halved in
-    // kLbfgsStall32 iterations: the FP32 rounding floor of the O(|g0|) forces can lie above the switch, where
-    // the trials' energy slack keeps accepting steps), FP64 after that and for the stopping test
+    // the target, a line search runs out or the residual stalls within kLbfgsStallBand times the target
+    // (its best value not halved in max(kLbfgsStall32, 3 x the longest halving interval of the phase so far)
+    // iterations: the FP32 rounding floor of the O(|g0|) forces can lie above the switch, where the trials'
+    // energy slack keeps accepting steps; the band and the phase's own pace keep slow but steady progress,
+    // as on the cloth, in FP32), FP64 after that and for the stopping test
     constexpr int kLbfgsStall32 = 100;
+    constexpr double kLbfgsStallBand = 1e3;
     bool e32 = mixed() && params.mixed_elem32 != 0, e32_stall = false;
     double best32 = 0.0;
-    int since32 = 0;
+    int since32 = 0, longest32 = 0;
     double E0 = e32 ? energy_grad32() : energy_grad();
     double gn = std::sqrt(hsc->gnorm2);
     const double g0 = gn;
@@ -1329,10 +1332,12 @@ struct TimeStep {
       if (!std::isfinite(E0) || !std::isfinite(gn))
         throw numerical_error("non-finite energy or gradient (inverted or degenerate element?)");
       if (e32) {
+        const double tgt32 = params.stop_mode == 0 ? abs_tol : params.rel_tol * g0;
         if (gn < 0.5 * best32) {
+          longest32 = std::max(longest32, since32 + 1);
           best32 = gn;
           since32 = 0;
-        } else if (++since32 >= kLbfgsStall32) {
+        } else if (++since32 >= std::max(kLbfgsStall32, 3 * longest32) && best32 <= kLbfgsStallBand * tgt32) {
           e32_stall = true;
         }
       }

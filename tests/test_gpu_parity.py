@@ -425,7 +425,8 @@ def test_lbfgs_mixed_reaches_residual():
 def test_lbfgs_mixed_leaves_a_stalled_fp32_phase():
     """Mixed L-BFGS with a target (1e-8 |g0|) below what FP32 element arithmetic resolves and the FP32 phase
     allowed down to the target itself (elem32_switch = 1): the phase ends once its residual stops falling
-    (the best |g| not halved in 100 iterations), FP64 evaluations finish, every step converges (the
+    near the target (the best |g|, within 1e3 times the target, not halved in max(100, 3 x the phase's
+    longest halving interval) iterations), FP64 evaluations finish, every step converges (the
     relative target or the absolute floor stop_floor, whichever is larger) in far fewer than the iteration
     cap, and the state matches the all-FP64-evaluation run's."""
     scene = scenes.cube10()
