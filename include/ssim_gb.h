@@ -129,9 +129,12 @@ typedef struct {
   double stop_floor;      /* stop_mode 1 also stops when |g| <= stop_floor * sum|M| / 3 (the reference's absolute
                              rule with rtol = stop_floor; default 1e-12), so a step starting at rest, whose
                              gradient is round-off, does not chase a fraction of it */
-  int32_t mixed_elem32;   /* mixed precision, Newton: 1 (default) evaluates energy and forces with FP32 element
-                             arithmetic while the residual is above elem32_switch times the target, then in
-                             FP64 (the stopping test always sees an FP64 residual); 0 keeps every evaluation FP64 */
+  int32_t mixed_elem32;   /* mixed precision, Newton and L-BFGS: 1 (default) evaluates energy and forces with FP32
+                             element arithmetic while the residual is above elem32_switch times the target, then
+                             in FP64 (the stopping test always sees an FP64 residual); the FP32 phase also ends
+                             when its residual stalls (Newton: two iterations without halving; L-BFGS: within 1e3
+                             times the target, no halving in max(100, 3 x the phase's longest halving interval)
+                             iterations, or a line search that runs out); 0 keeps every evaluation FP64 */
   double ls_energy_slack32; /* Armijo round-off slack of the FP32 evaluations, times their term-magnitude sum */
   double elem32_switch;   /* residual / target below which the FP32 phase ends (10) */
   int32_t pcg_pipe_iters; /* pipelined PCG (pcg_persistent 4) continues as Chronopoulos-Gear PCG after this many
