@@ -220,6 +220,9 @@ def run_gpu_arm(args, scene):
             tuning[precision] = dict(args.tuning, pinned=True)
         elif args.autotune:  # launch shapes for this precision (swept once, then from the process cache)
             tuning[precision] = ts.autotune()
+            if args.pcg_variant != 3:  # an explicit PCG variant outranks the sweep's choice
+                ts.set_params(pcg_persistent=args.pcg_variant)
+                tuning[precision]["pcg_persistent"] = args.pcg_variant
         first = None
         for i in range(warmup):
             ts.step()
